@@ -1,0 +1,364 @@
+"""Python front end of ``libbwacuda.so`` (ctypes over the C ABI in include/bwacuda.h).
+
+This module is plumbing for tests, the benchmark and Python callers: it lays out
+jobs in numpy arrays, calls the C entry points and returns numpy structured
+arrays.  All computation happens in the CUDA library; if the library is missing
+or no GPU is visible the calls raise instead of falling back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(_PKG, "libbwacuda.so")
+SYNTH_PATH = os.path.join(_PKG, "libbwasynth.so")
+
+OK, EINVAL, EBASE, ENOMEM, ECUDA, ETIMEOUT, EUNSUPPORTED, EBUSY, EAGAIN = 0, -1, -2, -3, -4, -5, -6, -7, -8
+OPT_EXT_PATH, OPT_CHUNK_JOBS = 1, 2
+PATH_PLAIN, PATH_BATCHED = 0, 1
+INT_MAX = 2**31 - 1
+
+# ---------------------------------------------------------------- struct layouts (include/bwacuda.h)
+EXT_JOB = np.dtype([("query", "u8"), ("target", "u8"), ("qlen", "i4"), ("tlen", "i4"), ("h0", "i4")],
+                   align=True)
+RES_JOB = np.dtype([("query", "u8"), ("target", "u8"), ("qlen", "i4"), ("tlen", "i4")], align=True)
+FWD_JOB = np.dtype([("query", "u8"), ("target", "u8"), ("qlen", "i4"), ("tlen", "i4"), ("minsc", "i4"),
+                    ("endsc", "i4")], align=True)
+DEV_EXT_JOB = np.dtype([("q_off", "u8"), ("t_off", "u8"), ("qlen", "i4"), ("tlen", "i4"), ("h0", "i4"),
+                        ("w", "i4")], align=True)
+DEV_RES_JOB = np.dtype([("q_off", "u8"), ("t_off", "u8"), ("qlen", "i4"), ("tlen", "i4"), ("minsc", "i4"),
+                        ("endsc", "i4")], align=True)
+EXT_RES = np.dtype([(n, "i4") for n in ("score", "qle", "tle", "gtle", "gscore", "max_off")])
+ALN_RES = np.dtype([(n, "i4") for n in ("score", "qb", "qe", "tb", "te", "score2", "te2")])
+FWD_RES = np.dtype([(n, "i4") for n in ("score", "te", "qe", "score2", "te2")])
+assert EXT_JOB.itemsize == 32 and RES_JOB.itemsize == 24 and FWD_JOB.itemsize == 32
+assert DEV_EXT_JOB.itemsize == 32 and DEV_RES_JOB.itemsize == 32
+
+
+class Scoring(C.Structure):
+    _fields_ = [("m", C.c_int32), ("mat", C.c_int8 * 64), ("o_del", C.c_int32), ("e_del", C.c_int32),
+                ("o_ins", C.c_int32), ("e_ins", C.c_int32)]
+
+
+STAT_FIELDS = ("ext_jobs", "ext_cells", "ext_bin_u8", "ext_bin_i16", "ext_bin_i32", "rescue_jobs",
+               "rescue_cells", "rescue_width_u8", "rescue_width_i16", "rescue_width_i32",
+               "kernel_launches", "h2d_bytes", "d2h_bytes")
+
+
+class Stats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in STAT_FIELDS]
+
+
+# Every symbol include/bwacuda.h declares.
+EXPORTS = ("bwacuda_ctx_create", "bwacuda_ctx_destroy", "bwacuda_set_option", "bwacuda_strerror",
+           "bwacuda_backend_name", "bwacuda_extend", "bwacuda_extend_batch", "bwacuda_ksw_align2_batch",
+           "bwacuda_ksw_align2_scalar_batch", "bwacuda_ksw_local_fwd_batch", "bwacuda_extend_device",
+           "bwacuda_ksw_align2_device", "bwacuda_ctx_sync", "bwacuda_get_stats", "bwacuda_reset_stats")
+
+_lib = None
+_synth = None
+
+
+class BwaCudaError(RuntimeError):
+    def __init__(self, code, what=""):
+        self.code = code
+        msg = lib().bwacuda_strerror(code).decode() if _lib is not None else str(code)
+        super().__init__(f"{what}: {msg} ({code})")
+
+
+def lib():
+    """Load libbwacuda.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} missing: build it with `python bwa-mem4_gb300/build.py`")
+    L = C.CDLL(LIB_PATH)
+    vp, I, sz = C.c_void_p, C.c_int, C.c_size_t
+    L.bwacuda_ctx_create.argtypes = [I, C.POINTER(vp)]
+    L.bwacuda_ctx_destroy.argtypes = [vp]
+    L.bwacuda_ctx_destroy.restype = None
+    L.bwacuda_set_option.argtypes = [vp, I, C.c_int64]
+    L.bwacuda_strerror.argtypes = [I]
+    L.bwacuda_strerror.restype = C.c_char_p
+    L.bwacuda_backend_name.restype = C.c_char_p
+    L.bwacuda_extend.argtypes = [vp, vp, C.c_int32, vp, C.c_int32, I, vp, I, I, I, I, I, I, I, I, vp]
+    L.bwacuda_extend_batch.argtypes = [vp, vp, sz, I, vp, I, I, I, I, I, I, I, vp]
+    L.bwacuda_ksw_align2_batch.argtypes = [vp, vp, sz, I, vp, I, I, I, I, I, I, vp]
+    L.bwacuda_ksw_align2_scalar_batch.argtypes = [vp, vp, sz, I, vp, I, I, I, I, I, I, I, vp]
+    L.bwacuda_ksw_local_fwd_batch.argtypes = [vp, vp, sz, I, vp, I, I, I, I, I, I, vp]
+    L.bwacuda_extend_device.argtypes = [vp, vp, vp, sz, C.POINTER(Scoring), I, I, I, vp, vp]
+    L.bwacuda_ksw_align2_device.argtypes = [vp, vp, vp, sz, C.POINTER(Scoring), I, I, I, I, vp, vp]
+    L.bwacuda_ctx_sync.argtypes = [vp]
+    L.bwacuda_get_stats.argtypes = [vp, C.POINTER(Stats)]
+    L.bwacuda_reset_stats.argtypes = [vp]
+    _lib = L
+    return L
+
+
+def synth_lib():
+    global _synth
+    if _synth is None:
+        if not os.path.exists(SYNTH_PATH):
+            raise RuntimeError(f"{SYNTH_PATH} missing: build it with `python bwa-mem4_gb300/build.py`")
+        S = C.CDLL(SYNTH_PATH)
+        u64, i64, vp, I = C.c_uint64, C.c_int64, C.c_void_p, C.c_int
+        S.synth_ext1_sizes.argtypes = [u64, i64, vp, vp, vp, vp]
+        S.synth_ext1_fill.argtypes = [u64, i64, vp, vp, vp, vp, vp]
+        S.synth_ext2_sizes.argtypes = [u64, i64, I, vp, vp, vp, vp]
+        S.synth_ext2_fill.argtypes = [u64, i64, I, vp, vp, vp, vp, vp]
+        S.synth_res4_sizes.argtypes = [u64, i64, vp, vp]
+        S.synth_res4_fill.argtypes = [u64, i64, vp, vp, vp, vp, vp]
+        _synth = S
+    return _synth
+
+
+def _ptr(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+def scmat(a: int = 1, b: int = 4) -> np.ndarray:
+    """bwa_fill_scmat (crates/bwa-core/src/opt.rs:445-482)."""
+    m = np.full(25, -1, dtype=np.int8)
+    for r in range(4):
+        for c in range(4):
+            m[r * 5 + c] = a if r == c else -b
+    return m
+
+
+# ---------------------------------------------------------------- job sets
+
+@dataclass
+class JobSet:
+    """Jobs laid out flat: all bases in ``seq``, per-job byte offsets and lengths."""
+    seq: np.ndarray
+    q_off: np.ndarray
+    t_off: np.ndarray
+    qlen: np.ndarray
+    tlen: np.ndarray
+    h0: np.ndarray
+    w: np.ndarray
+
+    def __len__(self):
+        return len(self.qlen)
+
+    @staticmethod
+    def from_lists(queries, targets, h0=None, w=None) -> "JobSet":
+        n = len(queries)
+        ql = np.array([len(q) for q in queries], dtype=np.int32)
+        tl = np.array([len(t) for t in targets], dtype=np.int32)
+        parts = []
+        for q, t in zip(queries, targets):
+            parts.append(np.asarray(q, dtype=np.uint8))
+            parts.append(np.asarray(t, dtype=np.uint8))
+        seq = np.concatenate(parts) if parts else np.zeros(0, np.uint8)
+        sizes = np.empty(2 * n, dtype=np.int64)
+        sizes[0::2] = ql
+        sizes[1::2] = tl
+        offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64) if n else np.zeros(0, np.int64)
+        h0a = np.full(n, 1, np.int32) if h0 is None else np.ascontiguousarray(np.broadcast_to(np.asarray(h0, np.int32), (n,)))
+        wa = np.full(n, 100, np.int32) if w is None else np.ascontiguousarray(np.broadcast_to(np.asarray(w, np.int32), (n,)))
+        return JobSet(seq, offs[0::2].copy(), offs[1::2].copy(), ql, tl, h0a, wa)
+
+    def query(self, k):
+        return self.seq[self.q_off[k]:self.q_off[k] + self.qlen[k]]
+
+    def target(self, k):
+        return self.seq[self.t_off[k]:self.t_off[k] + self.tlen[k]]
+
+    def take(self, idx) -> "JobSet":
+        idx = np.asarray(idx)
+        return JobSet.from_lists([self.query(k) for k in idx], [self.target(k) for k in idx],
+                                 self.h0[idx], self.w[idx])
+
+    def dev_ext_jobs(self) -> np.ndarray:
+        d = np.zeros(len(self), dtype=DEV_EXT_JOB)
+        d["q_off"], d["t_off"], d["qlen"], d["tlen"], d["h0"], d["w"] = (
+            self.q_off, self.t_off, self.qlen, self.tlen, self.h0, self.w)
+        return d
+
+    def dev_res_jobs(self, minsc=0, endsc=0) -> np.ndarray:
+        d = np.zeros(len(self), dtype=DEV_RES_JOB)
+        d["q_off"], d["t_off"], d["qlen"], d["tlen"] = self.q_off, self.t_off, self.qlen, self.tlen
+        d["minsc"], d["endsc"] = minsc, endsc
+        return d
+
+
+def _layout(qlen, tlen):
+    sizes = np.empty(2 * len(qlen), dtype=np.int64)
+    sizes[0::2] = qlen
+    sizes[1::2] = tlen
+    offs = np.zeros(len(sizes) + 1, dtype=np.int64)
+    np.cumsum(sizes, out=offs[1:])
+    return offs[0:-1:2].copy(), offs[1:-1:2].copy(), int(offs[-1])
+
+
+def synth_ext(config: int, n: int, seed: int = 0) -> JobSet:
+    """Extension workloads: 1 = 20k-job style, 2 = 2x150 read pairs, 3 = mixed read lengths / bands."""
+    S = synth_lib()
+    ql, tl, h0, w = (np.zeros(n, np.int32) for _ in range(4))
+    if config == 1:
+        S.synth_ext1_sizes(seed, n, _ptr(ql), _ptr(tl), _ptr(h0), _ptr(w))
+    else:
+        S.synth_ext2_sizes(seed, n, 1 if config == 3 else 0, _ptr(ql), _ptr(tl), _ptr(h0), _ptr(w))
+    qo, to, total = _layout(ql, tl)
+    seq = np.zeros(max(total, 1), np.uint8)
+    if config == 1:
+        S.synth_ext1_fill(seed, n, _ptr(qo), _ptr(to), _ptr(ql), _ptr(tl), _ptr(seq))
+    else:
+        S.synth_ext2_fill(seed, n, 1 if config == 3 else 0, _ptr(qo), _ptr(to), _ptr(ql), _ptr(tl), _ptr(seq))
+    return JobSet(seq, qo, to, ql, tl, h0, w)
+
+
+def synth_rescue(n: int, seed: int = 0) -> JobSet:
+    """Mate-rescue workload: 150 bp query vs 750 bp window (10% without the true mate)."""
+    S = synth_lib()
+    ql, tl = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    S.synth_res4_sizes(seed, n, _ptr(ql), _ptr(tl))
+    qo, to, total = _layout(ql, tl)
+    seq = np.zeros(max(total, 1), np.uint8)
+    S.synth_res4_fill(seed, n, _ptr(qo), _ptr(to), _ptr(ql), _ptr(tl), _ptr(seq))
+    return JobSet(seq, qo, to, ql, tl, np.ones(n, np.int32), np.zeros(n, np.int32))
+
+
+# ---------------------------------------------------------------- context
+
+class Context:
+    """One bwacuda_ctx on a CUDA device."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        rc = lib().bwacuda_ctx_create(device, C.byref(h))
+        if rc != OK:
+            raise BwaCudaError(rc, "bwacuda_ctx_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().bwacuda_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != OK:
+            raise BwaCudaError(rc, what)
+
+    def set_option(self, opt, value):
+        self._check(lib().bwacuda_set_option(self.h, opt, value), "bwacuda_set_option")
+
+    def stats(self) -> dict:
+        s = Stats()
+        self._check(lib().bwacuda_get_stats(self.h, C.byref(s)), "bwacuda_get_stats")
+        return {n: getattr(s, n) for n in STAT_FIELDS}
+
+    def reset_stats(self):
+        self._check(lib().bwacuda_reset_stats(self.h), "bwacuda_reset_stats")
+
+    # -- host-buffer entry points (pointers into js.seq) --
+    @staticmethod
+    def _host_jobs(js: JobSet, dtype, minsc=None, endsc=None):
+        base = js.seq.ctypes.data
+        a = np.zeros(len(js), dtype=dtype)
+        a["query"] = base + js.q_off.astype(np.uint64)
+        a["target"] = base + js.t_off.astype(np.uint64)
+        a["qlen"], a["tlen"] = js.qlen, js.tlen
+        if "h0" in dtype.names:
+            a["h0"] = js.h0
+        if "minsc" in dtype.names:
+            a["minsc"], a["endsc"] = minsc, endsc
+        return a
+
+    def extend_batch(self, js: JobSet, mat=None, o_del=6, e_del=1, o_ins=6, e_ins=1, w=100, end_bonus=5,
+                     zdrop=100, m=5) -> np.ndarray:
+        mat = np.ascontiguousarray(scmat() if mat is None else mat, dtype=np.int8)
+        jobs = self._host_jobs(js, EXT_JOB)
+        out = np.zeros(len(js), dtype=EXT_RES)
+        rc = lib().bwacuda_extend_batch(self.h, _ptr(jobs), len(js), m, _ptr(mat), o_del, e_del, o_ins, e_ins,
+                                        w, end_bonus, zdrop, _ptr(out))
+        self._check(rc, "bwacuda_extend_batch")
+        return out
+
+    def extend(self, q, t, h0, mat=None, o_del=6, e_del=1, o_ins=6, e_ins=1, w=100, end_bonus=5, zdrop=100, m=5):
+        mat = np.ascontiguousarray(scmat() if mat is None else mat, dtype=np.int8)
+        q = np.ascontiguousarray(q, dtype=np.uint8)
+        t = np.ascontiguousarray(t, dtype=np.uint8)
+        out = np.zeros(1, dtype=EXT_RES)
+        rc = lib().bwacuda_extend(self.h, _ptr(q), len(q), _ptr(t), len(t), m, _ptr(mat), o_del, e_del, o_ins,
+                                  e_ins, w, end_bonus, zdrop, h0, _ptr(out))
+        self._check(rc, "bwacuda_extend")
+        return tuple(int(x) for x in out[0])
+
+    def ksw_align2_batch(self, js: JobSet, mat=None, o_del=6, e_del=1, o_ins=6, e_ins=1, minsc=19, max_sc=1,
+                         m=5) -> np.ndarray:
+        mat = np.ascontiguousarray(scmat() if mat is None else mat, dtype=np.int8)
+        jobs = self._host_jobs(js, RES_JOB)
+        out = np.zeros(len(js), dtype=ALN_RES)
+        rc = lib().bwacuda_ksw_align2_batch(self.h, _ptr(jobs), len(js), m, _ptr(mat), o_del, e_del, o_ins,
+                                            e_ins, minsc, max_sc, _ptr(out))
+        self._check(rc, "bwacuda_ksw_align2_batch")
+        return out
+
+    def ksw_align2_scalar_batch(self, js: JobSet, mat=None, o_del=6, e_del=1, o_ins=6, e_ins=1, minsc=19,
+                                max_sc=1, lanes=0, m=5) -> np.ndarray:
+        mat = np.ascontiguousarray(scmat() if mat is None else mat, dtype=np.int8)
+        jobs = self._host_jobs(js, RES_JOB)
+        out = np.zeros(len(js), dtype=ALN_RES)
+        rc = lib().bwacuda_ksw_align2_scalar_batch(self.h, _ptr(jobs), len(js), m, _ptr(mat), o_del, e_del,
+                                                   o_ins, e_ins, minsc, max_sc, lanes, _ptr(out))
+        self._check(rc, "bwacuda_ksw_align2_scalar_batch")
+        return out
+
+    def ksw_local_fwd_batch(self, js: JobSet, minsc, endsc, mat=None, o_del=6, e_del=1, o_ins=6, e_ins=1,
+                            max_sc=1, lanes=0, m=5) -> np.ndarray:
+        mat = np.ascontiguousarray(scmat() if mat is None else mat, dtype=np.int8)
+        jobs = self._host_jobs(js, FWD_JOB, minsc, endsc)
+        out = np.zeros(len(js), dtype=FWD_RES)
+        rc = lib().bwacuda_ksw_local_fwd_batch(self.h, _ptr(jobs), len(js), m, _ptr(mat), o_del, e_del, o_ins,
+                                               e_ins, max_sc, lanes, _ptr(out))
+        self._check(rc, "bwacuda_ksw_local_fwd_batch")
+        return out
+
+    # -- device-resident entry points (torch tensors or raw device pointers) --
+    @staticmethod
+    def scoring(mat=None, o_del=6, e_del=1, o_ins=6, e_ins=1, m=5) -> Scoring:
+        mat = np.asarray(scmat() if mat is None else mat, dtype=np.int8)
+        s = Scoring()
+        s.m = m
+        for k in range(m * m):
+            s.mat[k] = int(mat[k])
+        s.o_del, s.e_del, s.o_ins, s.e_ins = o_del, e_del, o_ins, e_ins
+        return s
+
+    def extend_device(self, d_seq, d_jobs, n, d_out, sc: Scoring = None, end_bonus=5, zdrop=100,
+                      path=PATH_PLAIN, stream=None):
+        sc = sc or self.scoring()
+        rc = lib().bwacuda_extend_device(self.h, C.c_void_p(d_seq), C.c_void_p(d_jobs), n, C.byref(sc),
+                                         end_bonus, zdrop, path, C.c_void_p(d_out),
+                                         C.c_void_p(stream) if stream else None)
+        self._check(rc, "bwacuda_extend_device")
+
+    def ksw_align2_device(self, d_seq, d_jobs, n, d_out, sc: Scoring = None, minsc=19, max_sc=1, mode=0,
+                          lanes=0, stream=None):
+        sc = sc or self.scoring()
+        rc = lib().bwacuda_ksw_align2_device(self.h, C.c_void_p(d_seq), C.c_void_p(d_jobs), n, C.byref(sc),
+                                             minsc, max_sc, mode, lanes, C.c_void_p(d_out),
+                                             C.c_void_p(stream) if stream else None)
+        self._check(rc, "bwacuda_ksw_align2_device")
+
+    def sync(self):
+        self._check(lib().bwacuda_ctx_sync(self.h), "bwacuda_ctx_sync")

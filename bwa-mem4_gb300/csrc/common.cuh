@@ -1,0 +1,75 @@
+// common.cuh -- shared device-side definitions of the bwa-cuda engine.
+//
+// Score lookup.  Every kernel scores a cell with one byte permute: for target
+// code tc the 8-byte "profile row" holds mat[tc*m + qc] in byte qc (qc < m) and
+// 0 in the unused bytes, so a query column whose code is PAD_CODE (7) scores 0.
+// That zero column is exactly ksw's query-profile padding
+// (crates/bwa-neon/src/matesw.rs:591-607, ksw_qinit's `k >= qlen ? 0`).
+#pragma once
+#include <cstdint>
+
+#include "../../include/bwacuda.h"
+
+namespace bwacuda {
+
+constexpr int PAD_CODE = 7;
+
+// Per-launch scoring parameters, passed by value (kernel parameter space).
+struct Scoring {
+    int32_t m;
+    int32_t o_del, e_del, o_ins, e_ins;
+    int32_t max_sc;     // largest matrix entry (band clamp, score2 window)
+    uint32_t prof[8][2]; // profile rows, see above; rows >= m unused
+};
+
+struct ExtParams {
+    Scoring sc;
+    int32_t end_bonus, zdrop;
+};
+
+// Device error flags (OR-ed into ctx->d_err).
+constexpr uint32_t ERR_BASE = 1u;      // a base code >= m
+constexpr uint32_t ERR_RANGE = 2u;     // a score left the kernel's storage range
+constexpr uint32_t ERR_SCRATCH = 4u;   // tracker scratch overflow (never expected)
+
+__host__ __device__ inline uint32_t prof_lo(const Scoring &s, int tc) { return s.prof[tc][0]; }
+__host__ __device__ inline uint32_t prof_hi(const Scoring &s, int tc) { return s.prof[tc][1]; }
+
+// PTX prmt in its generic mode: a selector nibble with bit 3 set replicates the
+// sign of the selected byte (the __byte_perm intrinsic ignores that bit).
+__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel)
+{
+    uint32_t r;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(sel));
+    return r;
+}
+
+// Sign-extended byte `qc` of the 8-byte profile row {lo, hi}.
+__device__ __forceinline__ int prof_score(uint32_t lo, uint32_t hi, uint32_t qc)
+{
+    // selector nibbles: byte 0 <- qc, bytes 1..3 <- sign of byte qc
+    return (int)prmt(lo, hi, qc * 0x1111u | 0x8880u);
+}
+
+// Band clamp, crates/bwa-neon/src/batched.rs:1305-1329: double division, then a
+// truncating (toward zero, saturating) conversion exactly like `f64 as i32`.
+__host__ __device__ inline int clamp_band(int w, int qlen, int max_sc, int end_bonus, int o_ins,
+                                          int e_ins, int o_del, int e_del)
+{
+    double di = ((double)qlen * max_sc + end_bonus - o_ins) / e_ins + 1.0;
+    double dd = ((double)qlen * max_sc + end_bonus - o_del) / e_del + 1.0;
+#ifdef __CUDA_ARCH__
+    int max_ins = __double2int_rz(di);
+    int max_del = __double2int_rz(dd);
+#else
+    int max_ins = di != di ? 0 : (di >= 2147483647.0 ? 2147483647 : (di <= -2147483648.0 ? (-2147483647 - 1) : (int)di));
+    int max_del = dd != dd ? 0 : (dd >= 2147483647.0 ? 2147483647 : (dd <= -2147483648.0 ? (-2147483647 - 1) : (int)dd));
+#endif
+    if (max_ins < 1) max_ins = 1;
+    if (max_del < 1) max_del = 1;
+    if (w > max_ins) w = max_ins;
+    if (w > max_del) w = max_del;
+    return w;
+}
+
+}  // namespace bwacuda

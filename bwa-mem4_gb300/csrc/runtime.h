@@ -1,0 +1,108 @@
+// runtime.h -- host runtime of the bwa-cuda engine: buffers, worker pool, context.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <condition_variable>
+#include <cstddef>
+#include <cstdint>
+#include <functional>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "../../include/bwacuda.h"
+#include "common.cuh"
+
+namespace bwacuda {
+
+// Grow-only device buffer.
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes);
+    void release();
+};
+
+// Grow-only pinned host buffer.
+struct HostBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes);
+    void release();
+};
+
+// Fixed pool of host threads; run(fn) calls fn(id) once on every worker
+// (id 0 on the caller's thread) and returns when all are done.
+class WorkerPool {
+public:
+    explicit WorkerPool(int n);
+    ~WorkerPool();
+    void run(const std::function<void(int)> &fn);
+    int size() const { return nthreads_; }
+
+private:
+    void loop(int id);
+    std::vector<std::thread> threads_;
+    std::mutex mu_;
+    std::condition_variable cv_, done_cv_;
+    std::function<void(int)> *fn_ = nullptr;
+    uint64_t gen_ = 0;
+    int pending_ = 0;
+    int nthreads_ = 1;
+    bool stop_ = false;
+};
+
+// One staging slot of the host-buffer pipeline.
+struct Slot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    HostBuf h_seq, h_jobs, h_out, h_aux;
+    DevBuf d_seq, d_jobs, d_out, d_aux, d_scratch;
+};
+
+struct BatchedState;  // batched path (batched.cu)
+struct ServerState;   // serving loop (server.cu)
+
+int cuda_status(cudaError_t e);
+Scoring make_scoring(int m, const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins);
+int validate_scoring(int m, const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins);
+int ext_bin_label(int qlen, int tlen, int h0, int m, const int8_t *mat);
+
+}  // namespace bwacuda
+
+struct bwacuda_ctx {
+    explicit bwacuda_ctx(int dev);
+    int device;
+    std::mutex mu;
+    cudaStream_t stream = nullptr;  // default stream of device-resident calls
+    cudaStream_t dev_pending_stream = nullptr;
+    bwacuda::Slot slot[2];
+    bwacuda::DevBuf d_misc;   // error flags, counters
+    bwacuda::HostBuf h_misc;
+    bwacuda::DevBuf d_dev_aux, d_dev_scratch;
+    bwacuda::WorkerPool pool;
+    bwacuda_stats stats{};
+    int ext_path = BWACUDA_PATH_PLAIN;
+    size_t chunk_jobs = 262144;
+    bwacuda::BatchedState *batched = nullptr;
+    bwacuda::ServerState *server = nullptr;
+};
+
+namespace bwacuda {
+
+int collect_device_status(bwacuda_ctx *c, cudaStream_t s, uint64_t *cells);
+int extend_batch_host(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int m, const int8_t *mat,
+                      int o_del, int e_del, int o_ins, int e_ins, int w, int end_bonus, int zdrop,
+                      bwacuda_ext_result *out);
+
+// batched.cu
+int extend_batch_host_batched(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, const ExtParams &P,
+                              int w, bwacuda_ext_result *out);
+int extend_device_batched(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_dev_ext_job *d_jobs, size_t n,
+                          const ExtParams &P, bwacuda_ext_result *d_out, cudaStream_t s);
+void batched_release(bwacuda_ctx *c);
+
+// server.cu
+void server_shutdown(bwacuda_ctx *c);
+
+}  // namespace bwacuda

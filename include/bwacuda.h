@@ -1,0 +1,196 @@
+/*
+ * bwacuda.h -- C ABI of the GB300 (sm_103a) Smith-Waterman engine for the
+ * bwa-mem4 seed-extension and mate-rescue hot path.
+ *
+ * The entry points replace, one for one, the reference's Rust interfaces
+ * (paths relative to the reference project root):
+ *
+ *   bwacuda_backend_name        SwBackend::name            crates/bwa-extend/src/lib.rs:85
+ *   bwacuda_extend              SwBackend::extend          crates/bwa-extend/src/lib.rs:115-129
+ *   bwacuda_extend_batch        SwBackend::extend_batch    crates/bwa-extend/src/lib.rs:154-175
+ *   bwacuda_ksw_align2_batch    bwa_neon::batched_ksw_align2  crates/bwa-neon/src/matesw.rs:299-309
+ *   bwacuda_ksw_align2_scalar_batch  bwa_extend::ksw_align2 (per job)  crates/bwa-extend/src/sw.rs:1108-1185
+ *   bwacuda_ksw_local_fwd_batch bwa_extend::ksw_local_fwd (per job)  crates/bwa-extend/src/sw.rs:921-1075
+ *
+ * Conventions (all entry points):
+ *  - Plain pointers and sizes only.  The caller owns every input and output
+ *    buffer; the library copies inputs into its own pinned staging memory and
+ *    copies results back before returning.
+ *  - Bases are one byte per base, codes 0..m-1 (bwa: 0=A 1=C 2=G 3=T 4=N).
+ *  - Return 0 on success or a negative BWACUDA_E* code; nothing throws across
+ *    the ABI.  On error the output buffer contents are unspecified.
+ *  - There is no CPU fallback: every job runs on the GPU or the call fails.
+ *  - A context may be shared between threads: calls on one context are
+ *    serialised by an internal lock.  Use one context per thread for overlap.
+ *  - Results are bit-identical to the reference's integer semantics for every
+ *    field.
+ */
+#ifndef BWACUDA_H
+#define BWACUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BWACUDA_OK 0
+#define BWACUDA_EINVAL (-1)       /* bad argument: m, gap extends <= 0, w < 0, h0 <= 0, max_sc <= 0, negative length */
+#define BWACUDA_EBASE (-2)        /* a base code >= m in some query or target */
+#define BWACUDA_ENOMEM (-3)       /* device or pinned host allocation failed */
+#define BWACUDA_ECUDA (-4)        /* a CUDA runtime call failed */
+#define BWACUDA_ETIMEOUT (-5)     /* a bounded device wait gave up */
+#define BWACUDA_EUNSUPPORTED (-6) /* input beyond the kernels' limits (e.g. score range) */
+#define BWACUDA_EBUSY (-7)        /* serving queue full / request not admitted */
+#define BWACUDA_EAGAIN (-8)       /* serving request not finished yet */
+
+/* Largest alphabet the kernels' score profile holds. */
+#define BWACUDA_MAX_M 7
+
+/* crates/bwa-extend/src/lib.rs:181-195 ExtendJob */
+typedef struct {
+    const uint8_t *query;
+    const uint8_t *target;
+    int32_t qlen;
+    int32_t tlen;
+    int32_t h0;
+} bwacuda_ext_job;
+
+/* crates/bwa-extend/src/sw.rs:139-162 ExtendResult */
+typedef struct {
+    int32_t score, qle, tle, gtle, gscore, max_off;
+} bwacuda_ext_result;
+
+/* crates/bwa-neon/src/matesw.rs:104-116 KswJob */
+typedef struct {
+    const uint8_t *query;
+    const uint8_t *target;
+    int32_t qlen;
+    int32_t tlen;
+} bwacuda_rescue_job;
+
+/* crates/bwa-extend/src/sw.rs:750-774 KswAlignResult */
+typedef struct {
+    int32_t score, qb, qe, tb, te, score2, te2;
+} bwacuda_rescue_result;
+
+/* crates/bwa-neon/src/matesw.rs:131-142 FwdJob (per-job minsc / endsc) */
+typedef struct {
+    const uint8_t *query;
+    const uint8_t *target;
+    int32_t qlen;
+    int32_t tlen;
+    int32_t minsc;
+    int32_t endsc;
+} bwacuda_fwd_job;
+
+/* Return tuple of ksw_local_fwd, crates/bwa-extend/src/sw.rs:921-934 */
+typedef struct {
+    int32_t score, te, qe, score2, te2;
+} bwacuda_fwd_result;
+
+typedef struct bwacuda_ctx bwacuda_ctx;
+
+/* Kernel family used for extension batches (bwacuda_set_option). */
+#define BWACUDA_OPT_EXT_PATH 1
+#define BWACUDA_PATH_PLAIN 0   /* one launch per chunk, jobs in caller order */
+#define BWACUDA_PATH_BATCHED 1 /* length-bucketed, persistent, graph-replayed */
+/* Jobs per device chunk (pipelining granularity of the host-buffer calls). */
+#define BWACUDA_OPT_CHUNK_JOBS 2
+
+int bwacuda_ctx_create(int device, bwacuda_ctx **out);
+void bwacuda_ctx_destroy(bwacuda_ctx *ctx);
+int bwacuda_set_option(bwacuda_ctx *ctx, int option, int64_t value);
+const char *bwacuda_strerror(int code);
+/* SwBackend::name, crates/bwa-extend/src/lib.rs:85 */
+const char *bwacuda_backend_name(void);
+
+/* SwBackend::extend: one banded seed extension (ksw_extend2). */
+int bwacuda_extend(bwacuda_ctx *ctx, const uint8_t *query, int32_t qlen, const uint8_t *target,
+                   int32_t tlen, int m, const int8_t *mat, int o_del, int e_del, int o_ins,
+                   int e_ins, int w, int end_bonus, int zdrop, int h0, bwacuda_ext_result *out);
+
+/* SwBackend::extend_batch: n extensions sharing scoring / band; out[k] is the
+ * ksw_extend2 result of jobs[k].  A job with qlen == 0 yields the production
+ * batched path's answer (crates/bwa-neon/src/batched.rs:1025-1039). */
+int bwacuda_extend_batch(bwacuda_ctx *ctx, const bwacuda_ext_job *jobs, size_t n, int m,
+                         const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins, int w,
+                         int end_bonus, int zdrop, bwacuda_ext_result *out);
+
+/* batched_ksw_align2: forward pass with bwa's padding rule, then the reverse
+ * start-recovery pass over the truncated reversed prefixes. */
+int bwacuda_ksw_align2_batch(bwacuda_ctx *ctx, const bwacuda_rescue_job *jobs, size_t n, int m,
+                             const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins,
+                             int minsc, int max_sc, bwacuda_rescue_result *out);
+
+/* ksw_align2 per job: the reverse pass scans the whole target with only
+ * target[..=te] reversed.  lanes = 16 or 8 (query padding width), or 0 for
+ * bwa's rule per job (qlen * max_sc < 250 ? 16 : 8). */
+int bwacuda_ksw_align2_scalar_batch(bwacuda_ctx *ctx, const bwacuda_rescue_job *jobs, size_t n,
+                                    int m, const int8_t *mat, int o_del, int e_del, int o_ins,
+                                    int e_ins, int minsc, int max_sc, int lanes,
+                                    bwacuda_rescue_result *out);
+
+/* ksw_local_fwd per job with its own minsc / endsc (lanes as above). */
+int bwacuda_ksw_local_fwd_batch(bwacuda_ctx *ctx, const bwacuda_fwd_job *jobs, size_t n, int m,
+                                const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins,
+                                int max_sc, int lanes, bwacuda_fwd_result *out);
+
+/* ------------------------------------------------------------------------
+ * Device-resident form.  Inputs already in device memory: `d_seq` holds all
+ * bases, each job addresses its query and target by byte offset.  Results are
+ * written to device memory; the call is asynchronous on `stream` (a
+ * cudaStream_t, NULL = the context's own stream) and returns after enqueueing.
+ * bwacuda_ctx_sync() waits and reports device-side errors (bad base codes).
+ * These calls carry no counterpart in the reference (which has no device);
+ * they expose the same computation for callers that keep data in HBM.
+ * ------------------------------------------------------------------------ */
+typedef struct {
+    uint64_t q_off, t_off;
+    int32_t qlen, tlen;
+    int32_t h0; /* extension: seed score */
+    int32_t w;  /* extension: band half-width for this job */
+} bwacuda_dev_ext_job;
+
+typedef struct {
+    uint64_t q_off, t_off;
+    int32_t qlen, tlen;
+    int32_t minsc, endsc; /* used by the forward-pass-only entry */
+} bwacuda_dev_rescue_job;
+
+typedef struct {
+    int32_t m;
+    int8_t mat[64]; /* m*m row-major, mat[t*m + q] */
+    int32_t o_del, e_del, o_ins, e_ins;
+} bwacuda_scoring;
+
+int bwacuda_extend_device(bwacuda_ctx *ctx, const uint8_t *d_seq, const bwacuda_dev_ext_job *d_jobs,
+                          size_t n, const bwacuda_scoring *sc, int end_bonus, int zdrop,
+                          int path, bwacuda_ext_result *d_out, void *stream);
+
+/* mode 0 = batched_ksw_align2 semantics, 1 = scalar ksw_align2 (lanes as above). */
+int bwacuda_ksw_align2_device(bwacuda_ctx *ctx, const uint8_t *d_seq,
+                              const bwacuda_dev_rescue_job *d_jobs, size_t n,
+                              const bwacuda_scoring *sc, int minsc, int max_sc, int mode,
+                              int lanes, bwacuda_rescue_result *d_out, void *stream);
+
+int bwacuda_ctx_sync(bwacuda_ctx *ctx);
+
+/* Counters accumulated since the context was created (or last reset). */
+typedef struct {
+    uint64_t ext_jobs, ext_cells;       /* cells = sum over rows of (end - beg) */
+    uint64_t ext_bin_u8, ext_bin_i16, ext_bin_i32; /* reference 8/16-bit bin labels */
+    uint64_t rescue_jobs, rescue_cells; /* cells = qlen * tlen of the forward pass */
+    uint64_t rescue_width_u8, rescue_width_i16, rescue_width_i32; /* per call */
+    uint64_t kernel_launches;
+    uint64_t h2d_bytes, d2h_bytes;
+} bwacuda_stats;
+
+int bwacuda_get_stats(bwacuda_ctx *ctx, bwacuda_stats *out);
+int bwacuda_reset_stats(bwacuda_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BWACUDA_H */

@@ -1,0 +1,171 @@
+"""Seed-extension parity: the CUDA kernels through the C ABI against the oracle.
+
+Bit-exact on every field of every job (score, qle, tle, gtle, gscore, max_off).
+Inputs are the reference's own test streams (replayed bit for bit), the
+benchmark workloads at sizes the oracle finishes in seconds, and edge cases.
+"""
+import numpy as np
+import pytest
+
+import bwacuda as B
+import oracle
+import refstreams as R
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("score", "qle", "tle", "gtle", "gscore", "max_off")
+
+
+def _tuples(res):
+    return [tuple(int(r[f]) for f in FIELDS) for r in res]
+
+
+def _check_batch(ctx, qs, ts, h0s, a=1, b=4, o_del=6, e_del=1, o_ins=6, e_ins=1, w=100, end_bonus=5,
+                 zdrop=100, path=B.PATH_PLAIN, what=""):
+    mat = oracle.scmat(a, b)
+    js = B.JobSet.from_lists(qs, ts, h0s, w)
+    ctx.set_option(B.OPT_EXT_PATH, path)
+    got = _tuples(ctx.extend_batch(js, mat, o_del, e_del, o_ins, e_ins, w, end_bonus, zdrop))
+    want = [oracle.extend2(q, t, h, mat, o_del, e_del, o_ins, e_ins, w, end_bonus, zdrop)
+            for q, t, h in zip(qs, ts, h0s)]
+    for k, (g, x) in enumerate(zip(got, want)):
+        assert g == x, f"{what} job {k}: qlen={len(qs[k])} tlen={len(ts[k])} h0={h0s[k]} got {g} want {x}"
+
+
+def test_known_answers(ctx):
+    s = [0, 1, 2, 3] * 4
+    assert ctx.extend(s, s, 1, oracle.scmat(1, 4), 6, 1, 6, 1, 100, 0, 100) == (17, 16, 16, 16, 17, 0)
+    q = [0] * 10 + [1] * 40
+    t = [0] * 10 + [2] * 40
+    r = ctx.extend(q, t, 1, oracle.scmat(1, 4), 6, 1, 6, 1, 100, 0, 100)
+    assert r[0] == 11 and r[2] == 10
+
+
+def test_gate_stream_scoring_swept(ctx):
+    # crates/bwa-extend/src/lib.rs:283-354: 2000 cases, scoring swept; batched per scoring.
+    groups = {}
+    for c in R.backend_matches_scalar():
+        key = (c["a"], c["b"], c["o_del"], c["e_del"], c["o_ins"], c["e_ins"], c["w"], c["end_bonus"], c["zdrop"])
+        groups.setdefault(key, []).append(c)
+    for key, cs in groups.items():
+        a, b, od, ed, oi, ei, w, eb, zd = key
+        _check_batch(ctx, [c["q"] for c in cs], [c["t"] for c in cs], [c["h0"] for c in cs], a, b, od, ed, oi,
+                     ei, w, eb, zd, what=f"gate {key}")
+
+
+@pytest.mark.parametrize("stream", ["batch", "read_sized", "ungapped", "simd_verify"])
+def test_reference_batch_streams(ctx, stream):
+    gen = {"batch": R.backend_batch_matches_scalar, "read_sized": R.read_sized, "ungapped": R.ungapped,
+           "simd_verify": R.simd_verify}[stream]
+    for k, c in enumerate(gen()):
+        _check_batch(ctx, c["qs"], c["ts"], c["h0s"], c["a"], c["b"], c["o_del"], c["e_del"], c["o_ins"],
+                     c["e_ins"], c["w"], c["end_bonus"], c["zdrop"], what=f"{stream} round {k}")
+
+
+def _check_jobset(ctx, js, w=100, path=B.PATH_PLAIN, **kw):
+    ctx.set_option(B.OPT_EXT_PATH, path)
+    # per-job band: group by w (the host ABI shares w per call, as the reference does)
+    want, _ = oracle.extend_batch(js, **kw)
+    for wv in np.unique(js.w):
+        idx = np.nonzero(js.w == wv)[0]
+        sub = js.take(idx) if len(idx) != len(js) else js
+        got = ctx.extend_batch(sub, w=int(wv), **kw)
+        bad = np.nonzero(got != want[idx])[0]
+        assert len(bad) == 0, f"{len(bad)} mismatches, first job {idx[bad[0]]}: {got[bad[0]]} vs {want[idx[bad[0]]]}"
+
+
+def test_workload_20k_jobs(ctx):
+    js = B.synth_ext(1, 20000, seed=0)
+    _check_jobset(ctx, js)
+
+
+def test_workload_read_pairs(ctx):
+    js = B.synth_ext(2, 200000, seed=1)
+    _check_jobset(ctx, js)
+
+
+def test_workload_mixed_lengths_and_bands(ctx):
+    js = B.synth_ext(3, 60000, seed=2)
+    _check_jobset(ctx, js)
+
+
+def test_device_entry_equals_host_entry(ctx):
+    import torch
+
+    js = B.synth_ext(3, 50000, seed=3)
+    want, _ = oracle.extend_batch(js)
+    d_seq = torch.from_numpy(js.seq).cuda()
+    d_jobs = torch.from_numpy(js.dev_ext_jobs().view(np.uint8)).cuda()
+    d_out = torch.zeros(len(js) * 24, dtype=torch.uint8, device="cuda")
+    ctx.extend_device(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), d_out.data_ptr())
+    ctx.sync()
+    got = d_out.cpu().numpy().view(B.EXT_RES)
+    assert np.array_equal(got, want)
+
+
+def test_edge_cases(ctx):
+    mat = oracle.scmat(1, 4)
+    qs = [[], [0, 1, 2], [], [1] * 5, [0, 4, 4, 1], [2] * 300, [3] * 7]
+    ts = [[1, 2, 3], [], [], [1] * 5, [4, 0, 1, 1], [2] * 300, [3] * 7]
+    h0s = [10, 5, 3, 1, 20, 40, 250]
+    for w in (0, 1, 2, 100):
+        for zd in (0, 1, 100):
+            _check_batch(ctx, qs, ts, h0s, w=w, zdrop=zd, what=f"edge w={w} zdrop={zd}")
+    # a single job, and empty batches
+    assert ctx.extend([], [1, 2, 3], 10) == (10, 0, 0, 1, 3, 0)
+    empty = B.JobSet.from_lists([], [])
+    assert len(ctx.extend_batch(empty)) == 0
+
+
+def test_wide_cells_for_large_scores(ctx):
+    # h0 + min(q,t)*a >= 32768 needs int32 cells (the reference's scalar bin)
+    rng = np.random.default_rng(5)
+    qs, ts, h0s = [], [], []
+    for k in range(40):
+        q = rng.integers(0, 4, 60 + k).tolist()
+        t = list(q) + rng.integers(0, 4, 30).tolist()
+        qs.append(q)
+        ts.append(t)
+        h0s.append(32760 + k if k % 2 else 100 + k)
+    _check_batch(ctx, qs, ts, h0s, what="wide")
+
+
+def test_non_uniform_matrix_is_exact(ctx):
+    rng = np.random.default_rng(7)
+    mat = rng.integers(-5, 4, 25).astype(np.int8)
+    mat[0] = 3
+    qs = [rng.integers(0, 5, rng.integers(1, 80)).tolist() for _ in range(300)]
+    ts = [list(q[: len(q) // 2]) + rng.integers(0, 5, 40).tolist() for q in qs]
+    h0s = rng.integers(1, 60, 300).tolist()
+    js = B.JobSet.from_lists(qs, ts, h0s)
+    got = _tuples(ctx.extend_batch(js, mat, 5, 2, 4, 1, 30, 3, 40))
+    want = [oracle.extend2(q, t, h, mat, 5, 2, 4, 1, 30, 3, 40) for q, t, h in zip(qs, ts, h0s)]
+    assert got == want
+
+
+def test_invalid_inputs_fail_loudly(ctx):
+    js = B.JobSet.from_lists([[0, 1, 5]], [[0, 1, 2]], [10])
+    with pytest.raises(B.BwaCudaError) as e:
+        ctx.extend_batch(js)
+    assert e.value.code == B.EBASE
+    js = B.JobSet.from_lists([[0, 1]], [[0, 1, 2]], [0])
+    with pytest.raises(B.BwaCudaError) as e:
+        ctx.extend_batch(js)
+    assert e.value.code == B.EINVAL
+    js = B.JobSet.from_lists([[0, 1]], [[0, 1, 2]], [3])
+    with pytest.raises(B.BwaCudaError) as e:
+        ctx.extend_batch(js, e_del=0)
+    assert e.value.code == B.EINVAL
+    # the context stays usable after an error
+    assert ctx.extend([0, 1, 2], [0, 1, 2], 5) == oracle.extend2([0, 1, 2], [0, 1, 2], 5)
+
+
+def test_cell_counter_matches_oracle(ctx):
+    js = B.synth_ext(2, 30000, seed=9)
+    ctx.reset_stats()
+    ctx.extend_batch(js)
+    _, cells = oracle.extend_batch(js)
+    st = ctx.stats()
+    assert st["ext_cells"] == cells
+    assert st["ext_jobs"] == len(js)
+    assert st["ext_bin_u8"] + st["ext_bin_i16"] + st["ext_bin_i32"] == len(js)
