@@ -1,0 +1,326 @@
+"""Benchmark: bit-exact banded seed-extension GCUPS on one GB300.
+
+Workload (one "step"): 8,388,608 seed-extension jobs drawn as left/right
+extension pairs of 2x150 bp reads (seed 19-60 bp, qlen 0..131, tlen = qlen +
+100, w = 100, 0.1% SNV / 0.01% indel divergence, 2% of jobs with a 5%-error
+tail), bwa default scoring.  Inputs are larger than L2 (about 2.1 GB of bases
+and descriptors), so no flush is needed between steps.
+
+value    : GCUPS of the batched path (length-sorted buckets, persistent
+           kernels, graph replay) with the inputs resident in HBM.
+e2e      : the same metric through bwacuda_extend_batch with HOST buffers
+           (packing, host->device and device->host copies inside the timed region).
+plain    : the plain path (one launch per 256k-job chunk, caller order).
+GCUPS    = extension cells (one inner-loop iteration of ksw_extend2, counted by
+           the kernels themselves and equal to the oracle's count) / time.
+
+--impl reference times the CPU restatement of the reference algorithm (the
+reference is Rust and no Rust toolchain exists on these hosts) on every host
+core, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "bwa-mem4_gb300")
+sys.path.insert(0, PKG)
+sys.path.insert(0, ROOT)
+
+METRIC = "bit-exact SW extension GCUPS: batched/served vs plain on 1 GB300; p50/p99 latency"
+N_JOBS = 8 * 1024 * 1024
+OPS_PER_CELL = 9  # minimal fused integer op count of one extension cell (see the design doc roofline)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--jobs", type=int, default=N_JOBS)
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": mx or None, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def int_peak_gops(nsm, mhz):
+    # 128 INT32 lanes per SM per clock (one warp instruction per SMSP per clock, 4 SMSPs)
+    return nsm * 128 * mhz * 1e6 / 1e9
+
+
+def cpu_baseline(js_sample, nthreads=0):
+    import oracle
+
+    t0 = time.perf_counter()
+    _, cells = oracle.extend_batch(js_sample, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return cells, dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import bwacuda as B
+
+    cores = os.cpu_count() or 1
+    n = min(args.jobs, 1_000_000)
+    js = B.synth_ext(2, n, seed=0)
+    for _ in range(max(args.warmup, 0)):
+        cpu_baseline(js.head(min(n, 20000)))
+    tot_cells, tot_t = 0, 0.0
+    for _ in range(args.steps):
+        cells, dt = cpu_baseline(js)
+        tot_cells += cells
+        tot_t += dt
+    g = tot_cells / tot_t / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(g, 3), "unit": "GCUPS", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(tot_t / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": f"ksw_extend2 read-pair extensions, {n} of the {args.jobs}-job step per sample",
+                   "jobs_per_step": n, "parallelism": "host threads"},
+        "cpu_baseline": {"value": round(g, 3), "unit": "GCUPS", "cores": cores, "kind": "port",
+                         "sample": f"{n} jobs per step ({tot_cells // args.steps} cells), all host threads; "
+                                   "restatement of the reference (no Rust toolchain on the host)"},
+        "e2e": {"value": round(g, 3), "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import numpy as np
+    import torch
+
+    import bwacuda as B
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    ctx = B.Context(local)
+    n = args.jobs
+    # each rank extends its own shard of reads (weak scaling: per-GPU work fixed)
+    js = B.synth_ext(2, n, seed=1000 + rank)
+    d_seq = torch.from_numpy(js.seq).cuda()
+    d_jobs = torch.from_numpy(js.dev_ext_jobs().view(np.uint8)).cuda()
+    d_out = torch.zeros(n * 24, dtype=torch.uint8, device="cuda")
+    # a dedicated (non-default) stream: the library's kernels and the timing
+    # events must be ordered on the same stream
+    st = torch.cuda.Stream()
+    torch.cuda.set_stream(st)
+    stream = st.cuda_stream
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    def timed_device(path, steps, warmup):
+        for _ in range(warmup):
+            ctx.extend_device(d_seq.data_ptr(), d_jobs.data_ptr(), n, d_out.data_ptr(), path=path, stream=stream)
+        ctx.sync()
+        ctx.reset_stats()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(steps):
+            ctx.extend_device(d_seq.data_ptr(), d_jobs.data_ptr(), n, d_out.data_ptr(), path=path, stream=stream)
+        e1.record(st)
+        ctx.sync()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        stt = ctx.stats()
+        return ms, stt
+
+    # plain path: one launch per 256k-job chunk, caller order
+    plain_res = None
+    CH = 262144
+
+    def timed_plain(steps, warmup):
+        def one_step():
+            for c0 in range(0, n, CH):
+                cn = min(CH, n - c0)
+                ctx.extend_device(d_seq.data_ptr(), d_jobs.data_ptr() + c0 * 32, cn, d_out.data_ptr() + c0 * 24,
+                                  path=B.PATH_PLAIN, stream=stream)
+        for _ in range(warmup):
+            one_step()
+        ctx.sync()
+        ctx.reset_stats()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            one_step()
+        ctx.sync()
+        barrier()
+        return (time.perf_counter() - t0) * 1e3, ctx.stats()
+
+    with ClockSampler(local) as clk:
+        ms_b, st_b = timed_device(B.PATH_BATCHED, args.steps, args.warmup)
+    clocks = clk.summary()
+    ms_b = max_over_ranks(ms_b)
+    cells_step = st_b["ext_cells"] / args.steps
+    gcups_b = cells_step * world / (ms_b / args.steps / 1e3) / 1e9
+    launches = st_b["kernel_launches"]
+    batched_out = d_out.cpu().numpy().view(B.EXT_RES).copy()
+
+    psteps = max(1, min(args.steps, 3))
+    ms_p, st_p = timed_plain(psteps, 1)
+    ms_p = max_over_ranks(ms_p)
+    gcups_p = (st_p["ext_cells"] / psteps) * world / (ms_p / psteps / 1e3) / 1e9
+    same = bool(np.array_equal(batched_out, d_out.cpu().numpy().view(B.EXT_RES)))
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        ctx.set_option(B.OPT_EXT_PATH, B.PATH_BATCHED)
+        ctx.set_option(B.OPT_CHUNK_JOBS, 1 << 20)
+        ctx.extend_batch(js)  # warm-up (pinned staging allocation)
+        ctx.reset_stats()
+        barrier()
+        lat = []
+        t0 = time.perf_counter()
+        esteps = max(1, min(args.steps, 3))
+        for _ in range(esteps):
+            t1 = time.perf_counter()
+            host_out = ctx.extend_batch(js)
+            lat.append(time.perf_counter() - t1)
+        barrier()
+        et = max_over_ranks(time.perf_counter() - t0)
+        ste = ctx.stats()
+        e2e = {"value": round(ste["ext_cells"] / esteps * world / (et / esteps) / 1e9, 2), "unit": "GCUPS",
+               "h2d_bytes_per_step": int(ste["h2d_bytes"] / esteps), "d2h_bytes_per_step": int(ste["d2h_bytes"] / esteps),
+               "ms_per_step": round(et / esteps * 1e3, 2), "bit_identical_to_device_path":
+                   bool(np.array_equal(host_out, batched_out))}
+
+    # roofline: integer-ALU bound (no tensor cores, about 0.03 B of HBM per cell)
+    pk, kind = peaks()
+    nsm = torch.cuda.get_device_properties(local).multi_processor_count
+    mhz = clocks["sm_mhz"] or pk.get("sm_max_mhz", 2070.0)
+    peak_g = int_peak_gops(nsm, mhz)
+    achieved = gcups_b / world * OPS_PER_CELL
+    line = {
+        "metric": METRIC, "value": round(gcups_b, 2), "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_b / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": f"ksw_extend2 read-pair extensions (2x150 bp reads, w=100), {n} jobs per GPU per step",
+                   "jobs_per_step": n * world, "cells_per_step": int(cells_step * world),
+                   "parallelism": f"shard{world}", "l2": "inputs larger than L2 (about 2.1 GB per GPU)",
+                   "path": "batched: length-sorted buckets, persistent kernels, CUDA graph replay"},
+        "jobs_per_s": round(n * world / (ms_b / args.steps / 1e3), 1),
+        "plain": {"value": round(gcups_p, 2), "unit": "GCUPS", "ms_per_step": round(ms_p / psteps, 3),
+                  "note": "one launch per 262144-job chunk, jobs in caller order"},
+        "batched_over_plain": round(gcups_b / gcups_p, 3) if gcups_p else None,
+        "plain_equals_batched": same,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "roofline": {"bound": "alu", "achieved": round(achieved, 1), "peak": round(peak_g, 1), "unit": "Gop/s",
+                     "frac": round(achieved / peak_g, 4),
+                     "traffic": None,
+                     "note": f"integer ops = GCUPS x {OPS_PER_CELL} ops/cell; peak = {nsm} SMs x 128 INT32 lanes x "
+                             f"median SM clock under load ({kind} peaks file has no integer figure)"},
+    }
+    if e2e:
+        line["e2e"] = e2e
+    if rank == 0:
+        # CPU baseline: the oracle port on a bounded sample of the same workload
+        sample = js.head(min(n, 400_000))
+        cells, dt = cpu_baseline(sample)
+        line["cpu_baseline"] = {"value": round(cells / dt / 1e9, 3), "unit": "GCUPS", "cores": os.cpu_count(),
+                                "kind": "port", "sample": f"first {len(sample)} jobs of the step ({cells} cells)"}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

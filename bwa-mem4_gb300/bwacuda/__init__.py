@@ -18,7 +18,8 @@ LIB_PATH = os.path.join(_PKG, "libbwacuda.so")
 SYNTH_PATH = os.path.join(_PKG, "libbwasynth.so")
 
 OK, EINVAL, EBASE, ENOMEM, ECUDA, ETIMEOUT, EUNSUPPORTED, EBUSY, EAGAIN = 0, -1, -2, -3, -4, -5, -6, -7, -8
-OPT_EXT_PATH, OPT_CHUNK_JOBS = 1, 2
+OPT_EXT_PATH, OPT_CHUNK_JOBS, OPT_GRAPHS, OPT_PERSIST_BLOCK, OPT_RESCUE_KERNEL = 1, 2, 3, 4, 5
+RESCUE_AUTO, RESCUE_TPJ = 0, 1
 PATH_PLAIN, PATH_BATCHED = 0, 1
 INT_MAX = 2**31 - 1
 
@@ -169,6 +170,11 @@ class JobSet:
 
     def target(self, k):
         return self.seq[self.t_off[k]:self.t_off[k] + self.tlen[k]]
+
+    def head(self, k: int) -> "JobSet":
+        """The first k jobs, sharing this set's base buffer."""
+        return JobSet(self.seq, self.q_off[:k], self.t_off[:k], self.qlen[:k], self.tlen[:k], self.h0[:k],
+                      self.w[:k])
 
     def take(self, idx) -> "JobSet":
         idx = np.asarray(idx)

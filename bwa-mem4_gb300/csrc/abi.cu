@@ -254,6 +254,16 @@ extern "C" int bwacuda_set_option(bwacuda_ctx *c, int option, int64_t value)
         if (value < 1) return BWACUDA_EINVAL;
         c->chunk_jobs = (size_t)value;
         return BWACUDA_OK;
+    case BWACUDA_OPT_RESCUE_KERNEL:
+        if (value != BWACUDA_RESCUE_AUTO && value != BWACUDA_RESCUE_TPJ) return BWACUDA_EINVAL;
+        c->rescue_kernel = (int)value;
+        return BWACUDA_OK;
+    case BWACUDA_OPT_GRAPHS:
+        c->use_graphs = value != 0;
+        return BWACUDA_OK;
+    case BWACUDA_OPT_PERSIST_BLOCK:
+        if (value != 32 && value != 64 && value != 128 && value != 256) return BWACUDA_EINVAL;
+        return batched_set_block(c, (int)value);
     default:
         return BWACUDA_EINVAL;
     }
@@ -411,8 +421,9 @@ ExtChunk pack_ext_chunk(bwacuda_ctx *c, Slot &sl, const bwacuda_ext_job *jobs, s
     return ch;
 }
 
-int run_ext_chunk(bwacuda_ctx *c, Slot &sl, const ExtChunk &ch, const ExtParams &P)
+int run_ext_chunk(bwacuda_ctx *c, int slot_i, const ExtChunk &ch, const ExtParams &P, const ExtRunner &run)
 {
+    Slot &sl = c->slot[slot_i];
     cudaError_t e;
     const size_t jb = ch.cn * sizeof(bwacuda_dev_ext_job);
     if ((e = sl.d_seq.ensure(ch.bytes + 16)) != cudaSuccess) return cuda_status(e);
@@ -423,32 +434,52 @@ int run_ext_chunk(bwacuda_ctx *c, Slot &sl, const ExtChunk &ch, const ExtParams 
     if (ch.bytes && (e = cudaMemcpyAsync(sl.d_seq.p, sl.h_seq.p, ch.bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess) return cuda_status(e);
     if ((e = cudaMemcpyAsync(sl.d_jobs.p, sl.h_jobs.p, jb + (size_t)ch.nwide * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess) return cuda_status(e);
     c->stats.h2d_bytes += ch.bytes + jb + (size_t)ch.nwide * 4;
-    ExtLaunch L;
-    L.seq = static_cast<const uint8_t *>(sl.d_seq.p);
-    L.jobs = static_cast<const bwacuda_dev_ext_job *>(sl.d_jobs.p);
-    L.order = nullptr;
-    L.count_ptr = nullptr;
-    L.n = ch.cn;
-    L.P = P;
-    L.qcap = ch.qmax + 1;
-    L.only_wide = 0;
-    L.out = static_cast<bwacuda_ext_result *>(sl.d_out.p);
-    L.err = d_err(c);
-    L.cells = d_cells(c);
-    L.stream = s;
-    if (ch.cn > ch.nwide) {
-        if ((e = ext_tpj_launch(L, false)) != cudaSuccess) return cuda_status(e);
-        c->stats.kernel_launches++;
-    }
-    if (ch.nwide) {
-        L.order = reinterpret_cast<const uint32_t *>(static_cast<const bwacuda_dev_ext_job *>(sl.d_jobs.p) + ch.cn);
-        L.n = ch.nwide;
-        if ((e = ext_tpj_launch(L, true)) != cudaSuccess) return cuda_status(e);
-        c->stats.kernel_launches++;
-    }
+    ExtChunkInfo info;
+    info.d_seq = static_cast<const uint8_t *>(sl.d_seq.p);
+    info.d_jobs = static_cast<const bwacuda_dev_ext_job *>(sl.d_jobs.p);
+    info.d_wide = reinterpret_cast<const uint32_t *>(info.d_jobs + ch.cn);
+    info.n = ch.cn;
+    info.nwide = ch.nwide;
+    info.qmax = ch.qmax;
+    info.P = P;
+    info.d_out = static_cast<bwacuda_ext_result *>(sl.d_out.p);
+    int rc = run(slot_i, info, s);
+    if (rc) return rc;
     if ((e = cudaMemcpyAsync(sl.h_out.p, sl.d_out.p, ch.cn * sizeof(bwacuda_ext_result), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_status(e);
     c->stats.d2h_bytes += ch.cn * sizeof(bwacuda_ext_result);
     if ((e = cudaEventRecord(sl.done, s)) != cudaSuccess) return cuda_status(e);
+    return BWACUDA_OK;
+}
+
+// The plain path: narrow launch over the chunk in caller order, wide jobs from
+// the host-built list.
+int run_plain(bwacuda_ctx *c, const ExtChunkInfo &I, cudaStream_t s)
+{
+    if ((size_t)I.qmax + 1 > ext_tpj_smem_limit_qcap(I.nwide > 0)) return BWACUDA_EUNSUPPORTED;
+    ExtLaunch L;
+    L.seq = I.d_seq;
+    L.jobs = I.d_jobs;
+    L.order = nullptr;
+    L.count_ptr = nullptr;
+    L.n = I.n;
+    L.P = I.P;
+    L.qcap = I.qmax + 1;
+    L.only_wide = 0;
+    L.out = I.d_out;
+    L.err = d_err(c);
+    L.cells = d_cells(c);
+    L.stream = s;
+    cudaError_t e;
+    if (I.n > I.nwide) {
+        if ((e = ext_tpj_launch(L, false)) != cudaSuccess) return cuda_status(e);
+        c->stats.kernel_launches++;
+    }
+    if (I.nwide) {
+        L.order = I.d_wide;
+        L.n = I.nwide;
+        if ((e = ext_tpj_launch(L, true)) != cudaSuccess) return cuda_status(e);
+        c->stats.kernel_launches++;
+    }
     return BWACUDA_OK;
 }
 
@@ -456,27 +487,14 @@ int run_ext_chunk(bwacuda_ctx *c, Slot &sl, const ExtChunk &ch, const ExtParams 
 
 namespace bwacuda {
 
-int extend_batch_host(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int m, const int8_t *mat,
-                      int o_del, int e_del, int o_ins, int e_ins, int w, int end_bonus, int zdrop,
-                      bwacuda_ext_result *out)
+int extend_host_pipeline(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int m, const int8_t *mat,
+                         const ExtParams &P, int w, bwacuda_ext_result *out, const ExtRunner &run)
 {
-    int rc = validate_scoring(m, mat, o_del, e_del, o_ins, e_ins);
-    if (rc) return rc;
-    if (w < 0 || (n && (!jobs || !out))) return BWACUDA_EINVAL;
-    if (n == 0) return BWACUDA_OK;
-    if (cudaSetDevice(c->device) != cudaSuccess) return BWACUDA_ECUDA;
-    ExtParams P;
-    P.sc = make_scoring(m, mat, o_del, e_del, o_ins, e_ins);
-    P.end_bonus = end_bonus;
-    P.zdrop = zdrop;
-    if (c->ext_path == BWACUDA_PATH_BATCHED)
-        return extend_batch_host_batched(c, jobs, n, P, w, out);
-
     const size_t CH = c->chunk_jobs;
     ExtChunk pend[2] = {};
     bool busy[2] = {false, false};
     int slot_i = 0;
-    rc = BWACUDA_OK;
+    int rc = BWACUDA_OK;
     auto drain = [&](int s) -> int {
         if (!busy[s]) return BWACUDA_OK;
         busy[s] = false;
@@ -492,8 +510,7 @@ int extend_batch_host(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int
         int prc;
         ExtChunk ch = pack_ext_chunk(c, sl, jobs, c0, cn, w, P.sc.max_sc, m, mat, &prc);
         if (prc) { rc = prc; break; }
-        if ((size_t)ch.qmax + 1 > ext_tpj_smem_limit_qcap(ch.nwide > 0)) { rc = BWACUDA_EUNSUPPORTED; break; }
-        if ((rc = run_ext_chunk(c, sl, ch, P)) != BWACUDA_OK) break;
+        if ((rc = run_ext_chunk(c, slot_i, ch, P, run)) != BWACUDA_OK) break;
         pend[slot_i] = ch;
         busy[slot_i] = true;
         slot_i ^= 1;
@@ -507,6 +524,24 @@ int extend_batch_host(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int
     c->stats.ext_jobs += n;
     c->stats.ext_cells += cells;
     return rc;
+}
+
+int extend_batch_host(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int m, const int8_t *mat,
+                      int o_del, int e_del, int o_ins, int e_ins, int w, int end_bonus, int zdrop,
+                      bwacuda_ext_result *out)
+{
+    int rc = validate_scoring(m, mat, o_del, e_del, o_ins, e_ins);
+    if (rc) return rc;
+    if (w < 0 || (n && (!jobs || !out))) return BWACUDA_EINVAL;
+    if (n == 0) return BWACUDA_OK;
+    if (cudaSetDevice(c->device) != cudaSuccess) return BWACUDA_ECUDA;
+    ExtParams P;
+    P.sc = make_scoring(m, mat, o_del, e_del, o_ins, e_ins);
+    P.end_bonus = end_bonus;
+    P.zdrop = zdrop;
+    if (c->ext_path == BWACUDA_PATH_BATCHED) return extend_batch_host_batched(c, jobs, n, m, mat, P, w, out);
+    return extend_host_pipeline(c, jobs, n, m, mat, P, w, out,
+                                [c](int, const ExtChunkInfo &I, cudaStream_t s) { return run_plain(c, I, s); });
 }
 
 }  // namespace bwacuda
@@ -534,6 +569,20 @@ extern "C" int bwacuda_extend(bwacuda_ctx *c, const uint8_t *query, int32_t qlen
 }
 
 // ------------------------------------------------------------------ rescue
+
+namespace bwacuda {
+
+// Narrow-cell rescue jobs: the register wavefront when the padded query fits
+// 16 lanes x 32 columns (and the kernel choice allows it), else the
+// shared-memory thread-per-job kernel.  Wide jobs always go to the latter.
+cudaError_t rescue_narrow_launch(bwacuda_ctx *c, const RescueLaunch &L)
+{
+    if (c->rescue_kernel == BWACUDA_RESCUE_AUTO && L.qcap <= rescue_wf_max_qpad() && L.only_wide != 2)
+        return rescue_wf_launch(L, L.qcap);
+    return rescue_tpj_launch(L, false);
+}
+
+}  // namespace bwacuda
 
 namespace {
 
@@ -687,7 +736,7 @@ int run_res_chunk(bwacuda_ctx *c, Slot &sl, const ResChunk &ch, const Scoring &s
     L.err = d_err(c);
     L.stream = s;
     if (ch.cn > ch.nwide) {
-        if ((e = rescue_tpj_launch(L, false)) != cudaSuccess) return cuda_status(e);
+        if ((e = rescue_narrow_launch(c, L)) != cudaSuccess) return cuda_status(e);
         c->stats.kernel_launches++;
     }
     if (ch.nwide) {
@@ -938,7 +987,7 @@ extern "C" int bwacuda_ksw_align2_device(bwacuda_ctx *c, const uint8_t *d_seq,
     L.stream = s;
     const bool wide_fits = (size_t)qcap <= rescue_tpj_smem_limit_qcap(true);
     L.only_wide = wide_fits ? 0 : 2;
-    if ((e = rescue_tpj_launch(L, false)) != cudaSuccess) return cuda_status(e);
+    if ((e = rescue_narrow_launch(c, L)) != cudaSuccess) return cuda_status(e);
     if (wide_fits) {
         L.only_wide = 1;
         if ((e = rescue_tpj_launch(L, true)) != cudaSuccess) return cuda_status(e);

@@ -1,24 +1,203 @@
-// batched.cu -- the batched extension path (length buckets, persistent kernel,
-// graph replay).  Built out in steps; until the persistent kernel lands the
-// batched path reports BWACUDA_EUNSUPPORTED rather than silently running the
-// plain one.
+// batched.cu -- host orchestration of the batched extension path: buffers,
+// the bucket fan-out over several streams, CUDA-graph capture and replay of the
+// whole device sequence, and the host-buffer pipeline that feeds it.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "kernels.h"
+#include "persist.h"
 #include "runtime.h"
 
 namespace bwacuda {
 
-int extend_batch_host_batched(bwacuda_ctx *, const bwacuda_ext_job *, size_t, const ExtParams &, int,
-                              bwacuda_ext_result *)
+constexpr int FAN = 4;  // bucket streams
+
+// Device work buffers of one in-flight batch.
+struct BatchBufs {
+    DevBuf keys_in, keys_out, idx_in, idx_out, tmp, table;
+    cudaStream_t fan[FAN] = {};
+    cudaEvent_t fork = nullptr, join[FAN] = {};
+    // graph cache for device-resident replays
+    cudaGraphExec_t graph = nullptr;
+    const void *g_seq = nullptr, *g_jobs = nullptr, *g_out = nullptr;
+    const void *g_bufs[6] = {};  // work buffers the graph was captured with
+    int g_tb = 0;
+    size_t g_n = 0;
+    cudaStream_t g_stream = nullptr;
+    ExtParams g_P{};
+};
+
+struct BatchedState {
+    int nsm = 0;
+    int nb = 0;
+    int tb = 128;  // block size picked by the autotuner (bwacuda_autotune)
+    ExtBucketDef defs[EXT_MAX_BUCKETS];
+    DevBuf d_defs;
+    BatchBufs bufs[3];  // [0], [1]: host-pipeline slots; [2]: device-resident calls
+};
+
+static int batched_init(bwacuda_ctx *c)
 {
-    return BWACUDA_EUNSUPPORTED;
+    if (c->batched) return BWACUDA_OK;
+    BatchedState *B = new (std::nothrow) BatchedState();
+    if (!B) return BWACUDA_ENOMEM;
+    cudaError_t e = cudaDeviceGetAttribute(&B->nsm, cudaDevAttrMultiProcessorCount, c->device);
+    if (e != cudaSuccess) { delete B; return cuda_status(e); }
+    B->nb = ext_bucket_defs(B->defs, EXT_MAX_BUCKETS);
+    if ((e = B->d_defs.ensure(sizeof(B->defs))) != cudaSuccess) { delete B; return cuda_status(e); }
+    if ((e = cudaMemcpy(B->d_defs.p, B->defs, sizeof(ExtBucketDef) * B->nb, cudaMemcpyHostToDevice)) != cudaSuccess) {
+        delete B;
+        return cuda_status(e);
+    }
+    for (auto &bb : B->bufs) {
+        for (int f = 0; f < FAN; ++f) {
+            if ((e = cudaStreamCreateWithFlags(&bb.fan[f], cudaStreamNonBlocking)) != cudaSuccess) break;
+            if ((e = cudaEventCreateWithFlags(&bb.join[f], cudaEventDisableTiming)) != cudaSuccess) break;
+        }
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&bb.fork, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = bb.table.ensure(EXT_MAX_BUCKETS * 4 * sizeof(uint32_t));
+        if (e != cudaSuccess) break;
+    }
+    c->batched = B;
+    return cuda_status(e);
 }
 
-int extend_device_batched(bwacuda_ctx *, const uint8_t *, const bwacuda_dev_ext_job *, size_t,
-                          const ExtParams &, bwacuda_ext_result *, cudaStream_t)
+void batched_release(bwacuda_ctx *c)
 {
-    return BWACUDA_EUNSUPPORTED;
+    BatchedState *B = c->batched;
+    if (!B) return;
+    for (auto &bb : B->bufs) {
+        if (bb.graph) cudaGraphExecDestroy(bb.graph);
+        for (int f = 0; f < FAN; ++f) {
+            if (bb.fan[f]) cudaStreamSynchronize(bb.fan[f]);
+        }
+        for (int f = 0; f < FAN; ++f) {
+            if (bb.fan[f]) cudaStreamDestroy(bb.fan[f]);
+            if (bb.join[f]) cudaEventDestroy(bb.join[f]);
+        }
+        if (bb.fork) cudaEventDestroy(bb.fork);
+        bb.keys_in.release(); bb.keys_out.release(); bb.idx_in.release(); bb.idx_out.release();
+        bb.tmp.release(); bb.table.release();
+    }
+    B->d_defs.release();
+    delete B;
+    c->batched = nullptr;
 }
 
-void batched_release(bwacuda_ctx *) {}
+int batched_set_block(bwacuda_ctx *c, int tb)
+{
+    int rc = batched_init(c);
+    if (rc) return rc;
+    c->batched->tb = tb;
+    return BWACUDA_OK;
+}
+
+static cudaError_t ensure_bufs(BatchBufs &bb, size_t n)
+{
+    cudaError_t e;
+    if ((e = bb.keys_in.ensure(n * 2 + 16)) != cudaSuccess) return e;
+    if ((e = bb.keys_out.ensure(n * 2 + 16)) != cudaSuccess) return e;
+    if ((e = bb.idx_in.ensure(n * 4 + 16)) != cudaSuccess) return e;
+    if ((e = bb.idx_out.ensure(n * 4 + 16)) != cudaSuccess) return e;
+    return bb.tmp.ensure(ext_sort_temp_bytes(n) + 256);
+}
+
+// Enqueue the batched sequence for n device-resident jobs on stream s.
+static cudaError_t enqueue_batched(bwacuda_ctx *c, BatchBufs &bb, const uint8_t *d_seq,
+                                   const bwacuda_dev_ext_job *d_jobs, size_t n, const ExtParams &P,
+                                   bwacuda_ext_result *d_out, cudaStream_t s)
+{
+    BatchedState *B = c->batched;
+    cudaError_t e = ext_sort_and_bucket(d_jobs, n, P.sc.max_sc, static_cast<uint16_t *>(bb.keys_in.p),
+                                        static_cast<uint16_t *>(bb.keys_out.p), static_cast<uint32_t *>(bb.idx_in.p),
+                                        static_cast<uint32_t *>(bb.idx_out.p), bb.tmp.p, bb.tmp.cap,
+                                        static_cast<const ExtBucketDef *>(B->d_defs.p), B->nb,
+                                        static_cast<uint32_t *>(bb.table.p), s);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaEventRecord(bb.fork, s)) != cudaSuccess) return e;
+    for (int f = 0; f < FAN; ++f)
+        if ((e = cudaStreamWaitEvent(bb.fan[f], bb.fork, 0)) != cudaSuccess) return e;
+    PersistLaunch L;
+    L.seq = d_seq;
+    L.jobs = d_jobs;
+    L.order = static_cast<const uint32_t *>(bb.idx_out.p);
+    L.P = P;
+    L.out = d_out;
+    L.err = reinterpret_cast<uint32_t *>(c->d_misc.p);
+    L.cells = reinterpret_cast<unsigned long long *>((char *)c->d_misc.p + 8);
+    // largest buckets first: they hold the long jobs
+    for (int b = B->nb - 1, k = 0; b >= 0; --b, ++k) {
+        L.stream = bb.fan[k % FAN];
+        uint32_t *tab = static_cast<uint32_t *>(bb.table.p) + 4 * b;
+        if ((e = ext_persist_launch(L, B->defs[b], tab, B->nsm, B->tb)) != cudaSuccess) return e;
+    }
+    for (int f = 0; f < FAN; ++f) {
+        if ((e = cudaEventRecord(bb.join[f], bb.fan[f])) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(s, bb.join[f], 0)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+int extend_device_batched(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_dev_ext_job *d_jobs, size_t n,
+                          const ExtParams &P, bwacuda_ext_result *d_out, cudaStream_t s)
+{
+    int rc = batched_init(c);
+    if (rc) return rc;
+    BatchBufs &bb = c->batched->bufs[2];
+    cudaError_t e = ensure_bufs(bb, n);
+    if (e != cudaSuccess) return cuda_status(e);
+    // Replay a captured graph when the same batch comes back (same buffers, size,
+    // scoring and stream); otherwise capture a new one.
+    const void *bufs[6] = {bb.keys_in.p, bb.keys_out.p, bb.idx_in.p, bb.idx_out.p, bb.tmp.p, bb.table.p};
+    const bool same = bb.graph && bb.g_seq == d_seq && bb.g_jobs == d_jobs && bb.g_out == d_out && bb.g_n == n &&
+                      bb.g_stream == s && bb.g_tb == c->batched->tb && memcmp(bb.g_bufs, bufs, sizeof(bufs)) == 0 &&
+                      memcmp(&bb.g_P, &P, sizeof(P)) == 0;
+    if (!same && c->use_graphs) {
+        if (bb.graph) {
+            cudaGraphExecDestroy(bb.graph);
+            bb.graph = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return cuda_status(e);
+        cudaError_t e2 = enqueue_batched(c, bb, d_seq, d_jobs, n, P, d_out, s);
+        e = cudaStreamEndCapture(s, &g);
+        if (e2 != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_status(e2); }
+        if (e != cudaSuccess) return cuda_status(e);
+        e = cudaGraphInstantiate(&bb.graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { bb.graph = nullptr; return cuda_status(e); }
+        bb.g_seq = d_seq; bb.g_jobs = d_jobs; bb.g_out = d_out; bb.g_n = n; bb.g_stream = s; bb.g_P = P;
+        bb.g_tb = c->batched->tb;
+        memcpy(bb.g_bufs, bufs, sizeof(bufs));
+    }
+    if (c->use_graphs) {
+        if ((e = cudaGraphLaunch(bb.graph, s)) != cudaSuccess) return cuda_status(e);
+    } else if ((e = enqueue_batched(c, bb, d_seq, d_jobs, n, P, d_out, s)) != cudaSuccess) {
+        return cuda_status(e);
+    }
+    c->stats.kernel_launches += 3 + c->batched->nb;
+    c->stats.ext_jobs += n;
+    c->dev_pending_stream = s;
+    return BWACUDA_OK;
+}
+
+// Host-buffer form: the plain path's packing pipeline, each chunk run batched.
+int extend_batch_host_batched(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int m, const int8_t *mat,
+                              const ExtParams &P, int w, bwacuda_ext_result *out)
+{
+    int rc = batched_init(c);
+    if (rc) return rc;
+    return extend_host_pipeline(c, jobs, n, m, mat, P, w, out, [c](int slot, const ExtChunkInfo &I, cudaStream_t s) {
+        BatchBufs &bb = c->batched->bufs[slot];
+        cudaError_t e = ensure_bufs(bb, I.n);
+        if (e == cudaSuccess) e = enqueue_batched(c, bb, I.d_seq, I.d_jobs, I.n, I.P, I.d_out, s);
+        c->stats.kernel_launches += 3 + c->batched->nb;
+        return cuda_status(e);
+    });
+}
 
 void server_shutdown(bwacuda_ctx *) {}
 

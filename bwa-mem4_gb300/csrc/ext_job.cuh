@@ -1,0 +1,202 @@
+// ext_job.cuh -- one banded seed extension (ksw_extend2) run by one thread,
+// shared by the plain launch (extend_tpj.cu) and the persistent bucketed
+// launch (ext_persist.cu).
+//
+// Semantics: crates/bwa-extend/src/sw.rs:203-493 integer for integer, with the
+// qlen == 0 convention of crates/bwa-neon/src/batched.rs:1025-1039.
+//
+// The thread's persistent DP row lives in shared memory: column j (H(i-1, j-1)
+// and E(i, j), j = 0..qlen) at cell[j * TB], so any mix of columns across a
+// warp hits distinct banks.  Cells outside the live window [beg, end) are never
+// written and keep the stale values of earlier rows exactly as the scalar code
+// does (sw.rs:465-482 can grow `end` by two and read them back).  Query codes
+// are four per shared word at qw[(j / 4) * TB].
+#pragma once
+#include "common.cuh"
+
+namespace bwacuda {
+
+// H (low 16 bits) and E (high 16 bits): exact whenever every DP value < 32768.
+struct FmtI16 {
+    using T = uint32_t;
+    using Key = int32_t;
+    static constexpr int bytes = 4;
+    __device__ static __forceinline__ T pack(int h, int e) { return __byte_perm((uint32_t)h, (uint32_t)e, 0x5410); }
+    __device__ static __forceinline__ int h(T c) { return (int)(c & 0xffffu); }
+    __device__ static __forceinline__ int e(T c) { return (int)(c >> 16); }
+    __device__ static __forceinline__ bool dead(T c) { return c == 0u; }
+    // row max with ties going to the later column: max of (h << 16 | j)
+    __device__ static __forceinline__ Key key(int h, int j) { return (h << 16) | j; }
+    __device__ static __forceinline__ int key_h(Key k) { return k >> 16; }
+    __device__ static __forceinline__ int key_j(Key k) { return k & 0xffff; }
+};
+
+// Two int32: the reference's scalar bin (values >= 32768).
+struct FmtI32 {
+    using T = int2;
+    using Key = long long;
+    static constexpr int bytes = 8;
+    __device__ static __forceinline__ T pack(int h, int e) { return make_int2(h, e); }
+    __device__ static __forceinline__ int h(T c) { return c.x; }
+    __device__ static __forceinline__ int e(T c) { return c.y; }
+    __device__ static __forceinline__ bool dead(T c) { return c.x == 0 && c.y == 0; }
+    __device__ static __forceinline__ Key key(int h, int j) { return ((long long)h << 32) | (unsigned)j; }
+    __device__ static __forceinline__ int key_h(Key k) { return (int)(k >> 32); }
+    __device__ static __forceinline__ int key_j(Key k) { return (int)(k & 0xffffffffLL); }
+};
+
+// Upper bound of every H, E, F value of a job: a path gains at most max_sc per
+// diagonal step and gaps never add (opens and extends are validated >= 0).
+__host__ __device__ inline long long ext_value_bound(int qlen, int tlen, int h0, int max_sc)
+{
+    long long mn = qlen < tlen ? qlen : tlen;
+    return (long long)h0 + mn * (max_sc > 0 ? max_sc : 0);
+}
+
+__host__ __device__ inline bool ext_fits_i16(int qlen, int tlen, int h0, int max_sc)
+{
+    return ext_value_bound(qlen, tlen, h0, max_sc) < 32768 && qlen < 65535;
+}
+
+// Runs job J; returns the ExtendResult, adds the inner-loop iterations to ncells.
+template <class F, int TB>
+__device__ __forceinline__ bwacuda_ext_result ext_run_job(typename F::T *__restrict__ cell,
+                                                          uint32_t *__restrict__ qw,
+                                                          const uint8_t *__restrict__ seq,
+                                                          const bwacuda_dev_ext_job &J, const ExtParams &P,
+                                                          bool &bad, unsigned long long &ncells)
+{
+    using CellT = typename F::T;
+    const int qlen = J.qlen, tlen = J.tlen, h0 = J.h0, m = P.sc.m;
+    const uint8_t *q = seq + J.q_off;
+    const uint8_t *t = seq + J.t_off;
+    const int o_del = P.sc.o_del, e_del = P.sc.e_del, o_ins = P.sc.o_ins, e_ins = P.sc.e_ins;
+    const int oe_del = o_del + e_del, oe_ins = o_ins + e_ins;
+
+    // Query codes, four per shared word (one word past the end stays readable).
+    for (int jw = 0; jw * 4 <= qlen; ++jw) {
+        uint32_t v = 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int j = jw * 4 + u;
+            uint32_t c = j < qlen ? (uint32_t)q[j] : 0u;
+            bad |= c >= (uint32_t)m;
+            v |= (c & 7u) << (8 * u);
+        }
+        qw[jw * TB] = v;
+    }
+    // Row -1 (sw.rs:269-279): h0, then the insertion chain while > e_ins; E = 0.
+    {
+        int hv = h0;
+        cell[0] = F::pack(h0, 0);
+        if (qlen >= 1) {
+            hv = h0 > oe_ins ? h0 - oe_ins : 0;
+            cell[TB] = F::pack(hv, 0);
+        }
+        for (int j = 2; j <= qlen; ++j) {
+            hv = hv > e_ins ? hv - e_ins : 0;
+            cell[(size_t)j * TB] = F::pack(hv, 0);
+        }
+    }
+    const int w = clamp_band(J.w < 0 ? 0 : J.w, qlen, P.sc.max_sc, P.end_bonus, o_ins, e_ins, o_del, e_del);
+    int best = h0, best_i = -1, best_j = -1, best_ie = -1, gscore = -1, max_off = 0;
+    int beg = 0, end = qlen;
+    uint32_t tnext = tlen > 0 ? t[0] : 0u;
+    for (int i = 0; i < tlen; ++i) {
+        uint32_t tc = tnext;
+        if (i + 1 < tlen) tnext = t[i + 1];
+        bad |= tc >= (uint32_t)m;
+        tc &= 7u;
+        const uint32_t plo = P.sc.prof[tc][0], phi = P.sc.prof[tc][1];
+        if (beg < i - w) beg = i - w;
+        if (end > i + w + 1) end = i + w + 1;
+        if (end > qlen) end = qlen;
+        int h1 = 0;
+        if (beg == 0) {
+            h1 = h0 - (o_del + e_del * (i + 1));
+            h1 = h1 > 0 ? h1 : 0;
+        }
+        int f = 0;
+        typename F::Key rowkey = 0;
+        if (beg < end) {
+            // Software pipelined: the cell and query word for column j+1 are loaded
+            // while column j computes.  cell[end] (end <= qlen) and the query word
+            // holding column end are always allocated, so the look-ahead is in bounds.
+            int j = beg;
+            CellT cn = cell[(size_t)j * TB];
+            uint32_t qn = qw[(j >> 2) * TB] >> ((j & 3) * 8);
+            for (; j < end; ++j) {
+                const CellT c = cn;
+                cn = cell[(size_t)(j + 1) * TB];
+                const uint32_t qc = qn & 0xffu;
+                qn = ((j & 3) == 3) ? qw[((j >> 2) + 1) * TB] : (qn >> 8);
+                const int hd = F::h(c);
+                const int e = F::e(c);
+                const int s = prof_score(plo, phi, qc);
+                const int M = hd != 0 ? hd + s : 0;  // a zero diagonal is never extended
+                int h = M > e ? M : e;
+                h = h > f ? h : f;
+                int od = M - oe_del;
+                od = od > 0 ? od : 0;
+                int en = e - e_del;
+                en = en > od ? en : od;
+                cell[(size_t)j * TB] = F::pack(h1, en);  // H(i, j-1) for the next row, E(i+1, j)
+                h1 = h;
+                const typename F::Key kk = F::key(h, j);  // ties -> later column
+                rowkey = rowkey > kk ? rowkey : kk;
+                int oi = M - oe_ins;
+                oi = oi > 0 ? oi : 0;
+                f -= e_ins;
+                f = f > oi ? f : oi;
+            }
+            ncells += (unsigned long long)(end - beg);
+        }
+        cell[(size_t)end * TB] = F::pack(h1, 0);  // sentinel column (sw.rs:418-419)
+        const int jf = end > beg ? end : beg;
+        if (jf == qlen && gscore <= h1) {  // later row wins ties (sw.rs:424-427)
+            best_ie = i;
+            gscore = h1;
+        }
+        const int rmax = F::key_h(rowkey);
+        const int mj = F::key_j(rowkey);
+        if (rmax == 0) break;
+        if (rmax > best) {
+            best = rmax;
+            best_i = i;
+            best_j = mj;
+            const int off = mj > i ? mj - i : i - mj;
+            if (off > max_off) max_off = off;
+        } else if (P.zdrop > 0) {  // sw.rs:440-456
+            if (i - best_i > mj - best_j) {
+                if (best - rmax - ((i - best_i) - (mj - best_j)) * e_del > P.zdrop) break;
+            } else if (best - rmax - ((mj - best_j) - (i - best_i)) * e_ins > P.zdrop) {
+                break;
+            }
+        }
+        // adaptive band (sw.rs:465-482)
+        int lo = beg;
+        while (lo < end && F::dead(cell[(size_t)lo * TB])) ++lo;
+        beg = lo;
+        int hi = end;
+        while (hi >= beg && F::dead(cell[(size_t)hi * TB])) --hi;
+        end = hi + 2 < qlen ? hi + 2 : qlen;
+    }
+    bwacuda_ext_result r;
+    r.score = best;
+    r.qle = best_j + 1;
+    r.tle = best_i + 1;
+    r.gtle = best_ie + 1;
+    r.gscore = gscore;
+    r.max_off = max_off;
+    return r;
+}
+
+// Shared-memory bytes of a block: TB threads, qcap cell columns each, plus the
+// query words (one spare word for the look-ahead).
+__host__ __device__ inline size_t ext_block_smem(int qcap, int tb, int cell_bytes)
+{
+    size_t qwords = (size_t)qcap / 4 + 1;
+    return (size_t)qcap * tb * cell_bytes + qwords * tb * 4;
+}
+
+}  // namespace bwacuda

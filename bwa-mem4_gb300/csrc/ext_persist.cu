@@ -1,0 +1,209 @@
+// ext_persist.cu -- the batched extension path: jobs are length-sorted on the
+// device, cut into buckets by query length and cell width, and each bucket is
+// run by a persistent kernel sized to fill the GPU at that bucket's shared
+// memory footprint.  Warps pull 32 consecutive sorted jobs at a time from the
+// bucket's work counter, so the jobs that share a warp have near-equal row
+// counts and window widths (the SIMT analogue of the reference's length-sorted
+// lane groups, crates/bwa-neon/src/matesw.rs:176-183).  Bucket kernels go out
+// on several streams so one bucket's tail overlaps the next bucket's start.
+// The whole sequence (keys, sort, bucket bounds, launches) depends only on
+// device data, so it can be captured once into a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <cub/device/device_radix_sort.cuh>
+
+#include "common.cuh"
+#include "ext_job.cuh"
+#include "kernels.h"
+#include "persist.h"
+
+namespace bwacuda {
+
+namespace {
+
+// 16-bit sort key: cell width (i16 before i32), query length descending
+// (clamped at 1023), target length descending in 16-row steps.
+__device__ __forceinline__ uint16_t ext_sort_key(const bwacuda_dev_ext_job &J, int max_sc)
+{
+    const uint32_t wide = ext_fits_i16(J.qlen, J.tlen, J.h0, max_sc) ? 0u : 1u;
+    const uint32_t ql = J.qlen < 0 ? 0u : (J.qlen > 1023 ? 1023u : (uint32_t)J.qlen);
+    const uint32_t tb = J.tlen < 0 ? 0u : ((uint32_t)J.tlen >> 4 > 31u ? 31u : (uint32_t)J.tlen >> 4);
+    return (uint16_t)((wide << 15) | ((1023u - ql) << 5) | (31u - tb));
+}
+
+__global__ void ext_keys_kernel(const bwacuda_dev_ext_job *__restrict__ jobs, uint32_t n, int max_sc,
+                                uint16_t *__restrict__ keys, uint32_t *__restrict__ idx)
+{
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        keys[k] = ext_sort_key(jobs[k], max_sc);
+        idx[k] = k;
+    }
+}
+
+__device__ __forceinline__ uint32_t lower_bound16(const uint16_t *a, uint32_t n, uint32_t v)
+{
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (a[mid] < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Bucket b covers sorted keys [key_lo, key_hi]; writes its [start, end) and
+// clears its work counter.
+__global__ void ext_bucket_bounds_kernel(const uint16_t *__restrict__ keys, uint32_t n,
+                                         const ExtBucketDef *__restrict__ defs, int nb,
+                                         uint32_t *__restrict__ table)
+{
+    const int b = threadIdx.x;
+    if (b >= nb) return;
+    const ExtBucketDef d = defs[b];
+    const uint32_t ql_hi = d.qhi > 1023 ? 1023u : (uint32_t)d.qhi;
+    const uint32_t ql_lo = d.qlo > 1023 ? 1023u : (uint32_t)d.qlo;
+    const uint32_t key_lo = ((uint32_t)d.wide << 15) | ((1023u - ql_hi) << 5);
+    const uint32_t key_hi = ((uint32_t)d.wide << 15) | ((1023u - ql_lo) << 5) | 31u;
+    table[b * 4 + 0] = lower_bound16(keys, n, key_lo);
+    table[b * 4 + 1] = lower_bound16(keys, n, key_hi + 1);
+    table[b * 4 + 2] = 0;  // work counter
+}
+
+template <class F, int TB>
+__global__ void __launch_bounds__(TB)
+ext_persist_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *__restrict__ jobs,
+                   const uint32_t *__restrict__ order, uint32_t *__restrict__ table,
+                   const __grid_constant__ ExtParams P, int qcap, bwacuda_ext_result *__restrict__ out,
+                   uint32_t *__restrict__ err, unsigned long long *__restrict__ cells_total)
+{
+    using CellT = typename F::T;
+    constexpr bool WIDE = sizeof(CellT) == 8;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int tid = threadIdx.x, lane = tid & 31;
+    CellT *cell = reinterpret_cast<CellT *>(smem_raw) + tid;
+    uint32_t *qw = reinterpret_cast<uint32_t *>(reinterpret_cast<CellT *>(smem_raw) + (size_t)qcap * TB) + tid;
+    const uint32_t start = table[0], stop = table[1];
+    uint32_t *counter = table + 2;
+    unsigned long long ncells = 0;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(counter, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0) + start;
+        if (base >= stop) break;
+        const uint32_t k = base + lane;
+        if (k < stop) {
+            const uint32_t jid = order[k];
+            const bwacuda_dev_ext_job J = jobs[jid];
+            const bool narrow = ext_fits_i16(J.qlen, J.tlen, J.h0, P.sc.max_sc);
+            if (J.qlen < 0 || J.qlen + 1 > qcap || (!WIDE && !narrow)) {
+                atomicOr(err, ERR_RANGE);
+            } else {
+                bool bad = false;
+                const bwacuda_ext_result r = ext_run_job<F, TB>(cell, qw, seq, J, P, bad, ncells);
+                if (bad) atomicOr(err, ERR_BASE);
+                out[jid] = r;
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ncells += __shfl_xor_sync(0xffffffffu, ncells, o);
+    if (lane == 0 && ncells) atomicAdd(cells_total, ncells);
+}
+
+constexpr size_t SMEM_MAX = 227u * 1024u;
+
+template <class F, int TB>
+cudaError_t launch_persist_tb(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm)
+{
+    const size_t smem = ext_block_smem(d.qcap, TB, sizeof(typename F::T));
+    if (smem > SMEM_MAX) return cudaErrorInvalidValue;
+    auto kern = ext_persist_kernel<F, TB>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TB, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidValue;
+    const int grid = per_sm * nsm;
+    kern<<<grid, TB, smem, L.stream>>>(L.seq, L.jobs, L.order, table, L.P, d.qcap, L.out, L.err, L.cells);
+    return cudaGetLastError();
+}
+
+template <class F>
+cudaError_t launch_persist(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm, int tb)
+{
+    const int cb = sizeof(typename F::T);
+    // requested block size if it fits, else the largest that does
+    if (tb >= 256 && ext_block_smem(d.qcap, 256, cb) <= SMEM_MAX) return launch_persist_tb<F, 256>(L, d, table, nsm);
+    if (tb >= 128 && ext_block_smem(d.qcap, 128, cb) <= SMEM_MAX) return launch_persist_tb<F, 128>(L, d, table, nsm);
+    if (tb >= 64 && ext_block_smem(d.qcap, 64, cb) <= SMEM_MAX) return launch_persist_tb<F, 64>(L, d, table, nsm);
+    return launch_persist_tb<F, 32>(L, d, table, nsm);
+}
+
+}  // namespace
+
+// Query-length buckets: cap of each class (qlen <= cap - 1), per cell width.
+static const int kQcapI16[] = {33, 65, 97, 129, 161, 193, 257, 385, 513, 769, 1023};
+static const int kQcapI32[] = {33, 65, 97, 129, 161, 193, 257, 385, 513, 769};
+
+int ext_bucket_defs(ExtBucketDef *defs, int max_defs)
+{
+    int nb = 0;
+    for (int wide = 0; wide < 2; ++wide) {
+        const int *caps = wide ? kQcapI32 : kQcapI16;
+        const int nc = wide ? (int)(sizeof(kQcapI32) / sizeof(int)) : (int)(sizeof(kQcapI16) / sizeof(int));
+        int lo = 0;
+        for (int c = 0; c < nc && nb < max_defs; ++c) {
+            ExtBucketDef d;
+            d.wide = wide;
+            d.qlo = lo;
+            d.qhi = caps[c] - 1;
+            d.qcap = caps[c];
+            defs[nb++] = d;
+            lo = caps[c];
+        }
+        // the open-ended last class: every longer query up to the shared-memory limit
+        if (nb < max_defs) {
+            ExtBucketDef d;
+            d.wide = wide;
+            d.qlo = lo;
+            d.qhi = 1 << 30;
+            d.qcap = (int)ext_tpj_smem_limit_qcap(wide != 0);
+            defs[nb++] = d;
+        }
+    }
+    return nb;
+}
+
+size_t ext_sort_temp_bytes(size_t n)
+{
+    size_t bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, bytes, (const uint16_t *)nullptr, (uint16_t *)nullptr,
+                                    (const uint32_t *)nullptr, (uint32_t *)nullptr, (int)n, 0, 16);
+    return bytes;
+}
+
+cudaError_t ext_sort_and_bucket(const bwacuda_dev_ext_job *jobs, size_t n, int max_sc, uint16_t *keys_in,
+                                uint16_t *keys_out, uint32_t *idx_in, uint32_t *idx_out, void *tmp,
+                                size_t tmp_bytes, const ExtBucketDef *d_defs, int nb, uint32_t *d_table,
+                                cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    uint32_t grid = (uint32_t)((n + 255) / 256);
+    if (grid > 8192) grid = 8192;
+    ext_keys_kernel<<<grid, 256, 0, s>>>(jobs, (uint32_t)n, max_sc, keys_in, idx_in);
+    cudaError_t e = cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys_in, keys_out, idx_in, idx_out, (int)n, 0,
+                                                    16, s);
+    if (e != cudaSuccess) return e;
+    ext_bucket_bounds_kernel<<<1, 64, 0, s>>>(keys_out, (uint32_t)n, d_defs, nb, d_table);
+    return cudaGetLastError();
+}
+
+cudaError_t ext_persist_launch(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *d_bucket_table, int nsm,
+                               int tb)
+{
+    return d.wide ? launch_persist<FmtI32>(L, d, d_bucket_table, nsm, tb)
+                  : launch_persist<FmtI16>(L, d, d_bucket_table, nsm, tb);
+}
+
+}  // namespace bwacuda

@@ -51,6 +51,8 @@ struct RescueLaunch {
 };
 
 cudaError_t rescue_tpj_launch(const RescueLaunch &L, bool wide);
+cudaError_t rescue_wf_launch(const RescueLaunch &L, int qcap);
+int rescue_wf_max_qpad();
 size_t rescue_tpj_smem_limit_qcap(bool wide);
 // Entries the suboptimal tracker may need for a target of tlen rows.
 __host__ __device__ inline uint64_t rescue_scratch_entries(int tlen) { return (uint64_t)(tlen / 2 + 2); }

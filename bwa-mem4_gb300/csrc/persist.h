@@ -1,0 +1,44 @@
+// persist.h -- interface of the batched (sorted, bucketed, persistent) extension path.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace bwacuda {
+
+// One bucket: jobs whose cell width is `wide` and qlen in [qlo, qhi], run with
+// qcap cell columns per thread.
+struct ExtBucketDef {
+    int32_t wide;
+    int32_t qlo, qhi;
+    int32_t qcap;
+};
+
+constexpr int EXT_MAX_BUCKETS = 32;
+
+struct PersistLaunch {
+    const uint8_t *seq;
+    const bwacuda_dev_ext_job *jobs;
+    const uint32_t *order;  // sorted job indices
+    ExtParams P;
+    bwacuda_ext_result *out;
+    uint32_t *err;
+    unsigned long long *cells;
+    cudaStream_t stream;
+};
+
+int ext_bucket_defs(ExtBucketDef *defs, int max_defs);
+size_t ext_sort_temp_bytes(size_t n);
+// keys + radix sort + bucket bounds; d_table holds 4 words per bucket
+// (start, end, work counter, spare).
+cudaError_t ext_sort_and_bucket(const bwacuda_dev_ext_job *jobs, size_t n, int max_sc, uint16_t *keys_in,
+                                uint16_t *keys_out, uint32_t *idx_in, uint32_t *idx_out, void *tmp,
+                                size_t tmp_bytes, const ExtBucketDef *d_defs, int nb, uint32_t *d_table,
+                                cudaStream_t s);
+cudaError_t ext_persist_launch(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *d_bucket_table, int nsm,
+                               int tb);
+
+}  // namespace bwacuda

@@ -83,6 +83,8 @@ struct bwacuda_ctx {
     bwacuda::WorkerPool pool;
     bwacuda_stats stats{};
     int ext_path = BWACUDA_PATH_PLAIN;
+    bool use_graphs = true;
+    int rescue_kernel = BWACUDA_RESCUE_AUTO;
     size_t chunk_jobs = 262144;
     bwacuda::BatchedState *batched = nullptr;
     bwacuda::ServerState *server = nullptr;
@@ -91,16 +93,34 @@ struct bwacuda_ctx {
 namespace bwacuda {
 
 int collect_device_status(bwacuda_ctx *c, cudaStream_t s, uint64_t *cells);
+struct RescueLaunch;
+cudaError_t rescue_narrow_launch(bwacuda_ctx *c, const RescueLaunch &L);
+
+// One packed chunk of extension jobs, resident on the device.
+struct ExtChunkInfo {
+    const uint8_t *d_seq;
+    const bwacuda_dev_ext_job *d_jobs;
+    const uint32_t *d_wide;  // indices of jobs needing int32 cells (plain path)
+    size_t n;
+    uint32_t nwide;
+    int qmax;
+    ExtParams P;
+    bwacuda_ext_result *d_out;
+};
+using ExtRunner = std::function<int(int slot, const ExtChunkInfo &info, cudaStream_t s)>;
+int extend_host_pipeline(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int m, const int8_t *mat,
+                         const ExtParams &P, int w, bwacuda_ext_result *out, const ExtRunner &run);
 int extend_batch_host(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int m, const int8_t *mat,
                       int o_del, int e_del, int o_ins, int e_ins, int w, int end_bonus, int zdrop,
                       bwacuda_ext_result *out);
 
 // batched.cu
-int extend_batch_host_batched(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, const ExtParams &P,
-                              int w, bwacuda_ext_result *out);
+int extend_batch_host_batched(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int m, const int8_t *mat,
+                              const ExtParams &P, int w, bwacuda_ext_result *out);
 int extend_device_batched(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_dev_ext_job *d_jobs, size_t n,
                           const ExtParams &P, bwacuda_ext_result *d_out, cudaStream_t s);
 void batched_release(bwacuda_ctx *c);
+int batched_set_block(bwacuda_ctx *c, int tb);
 
 // server.cu
 void server_shutdown(bwacuda_ctx *c);

@@ -98,6 +98,14 @@ typedef struct bwacuda_ctx bwacuda_ctx;
 #define BWACUDA_PATH_BATCHED 1 /* length-bucketed, persistent, graph-replayed */
 /* Jobs per device chunk (pipelining granularity of the host-buffer calls). */
 #define BWACUDA_OPT_CHUNK_JOBS 2
+/* Batched device calls: replay a captured CUDA graph (1, default) or enqueue every call (0). */
+#define BWACUDA_OPT_GRAPHS 3
+/* Threads per block of the persistent extension kernels (32, 64, 128 or 256). */
+#define BWACUDA_OPT_PERSIST_BLOCK 4
+/* Mate-rescue kernel: register wavefront where it fits (AUTO) or thread-per-job (TPJ). */
+#define BWACUDA_OPT_RESCUE_KERNEL 5
+#define BWACUDA_RESCUE_AUTO 0
+#define BWACUDA_RESCUE_TPJ 1
 
 int bwacuda_ctx_create(int device, bwacuda_ctx **out);
 void bwacuda_ctx_destroy(bwacuda_ctx *ctx);

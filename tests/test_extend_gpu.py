@@ -74,50 +74,105 @@ def _check_jobset(ctx, js, w=100, path=B.PATH_PLAIN, **kw):
         assert len(bad) == 0, f"{len(bad)} mismatches, first job {idx[bad[0]]}: {got[bad[0]]} vs {want[idx[bad[0]]]}"
 
 
-def test_workload_20k_jobs(ctx):
+PATHS = [pytest.param(B.PATH_PLAIN, id="plain"), pytest.param(B.PATH_BATCHED, id="batched")]
+
+
+@pytest.mark.parametrize("path", PATHS)
+def test_workload_20k_jobs(ctx, path):
     js = B.synth_ext(1, 20000, seed=0)
-    _check_jobset(ctx, js)
+    _check_jobset(ctx, js, path=path)
 
 
-def test_workload_read_pairs(ctx):
+@pytest.mark.parametrize("path", PATHS)
+def test_workload_read_pairs(ctx, path):
     js = B.synth_ext(2, 200000, seed=1)
-    _check_jobset(ctx, js)
+    _check_jobset(ctx, js, path=path)
 
 
-def test_workload_mixed_lengths_and_bands(ctx):
+@pytest.mark.parametrize("path", PATHS)
+def test_workload_mixed_lengths_and_bands(ctx, path):
     js = B.synth_ext(3, 60000, seed=2)
-    _check_jobset(ctx, js)
+    _check_jobset(ctx, js, path=path)
 
 
-def test_device_entry_equals_host_entry(ctx):
+@pytest.mark.parametrize("path", PATHS)
+def test_batch_streams_through_both_paths(ctx, path):
+    # the reference's lane-cross-talk stream, every batch through the chosen path
+    for k, c in enumerate(R.backend_batch_matches_scalar()):
+        if k >= 60:
+            break
+        _check_batch(ctx, c["qs"], c["ts"], c["h0s"], c["a"], c["b"], c["o_del"], c["e_del"], c["o_ins"],
+                     c["e_ins"], c["w"], c["end_bonus"], c["zdrop"], path=path, what=f"batch round {k}")
+
+
+def test_chunked_pipeline_boundaries(ctx):
+    # chunks smaller than the batch exercise both staging slots and the tail chunk
+    js = B.synth_ext(3, 5000, seed=12)
+    want, _ = oracle.extend_batch(js)
+    try:
+        for path in (B.PATH_PLAIN, B.PATH_BATCHED):
+            ctx.set_option(B.OPT_EXT_PATH, path)
+            ctx.set_option(B.OPT_CHUNK_JOBS, 777)
+            for wv in np.unique(js.w):
+                idx = np.nonzero(js.w == wv)[0]
+                got = ctx.extend_batch(js.take(idx), w=int(wv))
+                assert np.array_equal(got, want[idx])
+    finally:
+        ctx.set_option(B.OPT_CHUNK_JOBS, 262144)
+
+
+def _device_run(ctx, js, path, reps=1):
     import torch
 
-    js = B.synth_ext(3, 50000, seed=3)
-    want, _ = oracle.extend_batch(js)
     d_seq = torch.from_numpy(js.seq).cuda()
     d_jobs = torch.from_numpy(js.dev_ext_jobs().view(np.uint8)).cuda()
     d_out = torch.zeros(len(js) * 24, dtype=torch.uint8, device="cuda")
-    ctx.extend_device(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), d_out.data_ptr())
-    ctx.sync()
-    got = d_out.cpu().numpy().view(B.EXT_RES)
+    outs = []
+    for _ in range(reps):
+        d_out.zero_()
+        ctx.extend_device(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), d_out.data_ptr(), path=path)
+        ctx.sync()
+        outs.append(d_out.cpu().numpy().view(B.EXT_RES).copy())
+    return outs
+
+
+@pytest.mark.parametrize("path", PATHS)
+def test_device_entry_equals_oracle(ctx, path):
+    js = B.synth_ext(3, 50000, seed=3)
+    want, _ = oracle.extend_batch(js)
+    for got in _device_run(ctx, js, path, reps=3):  # batched: capture, then two graph replays
+        assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("block", [32, 64, 128, 256])
+def test_persistent_block_sizes(ctx, block):
+    js = B.synth_ext(2, 20000, seed=13)
+    want, _ = oracle.extend_batch(js)
+    ctx.set_option(B.OPT_PERSIST_BLOCK, block)
+    try:
+        got = _device_run(ctx, js, B.PATH_BATCHED)[0]
+    finally:
+        ctx.set_option(B.OPT_PERSIST_BLOCK, 128)
     assert np.array_equal(got, want)
 
 
-def test_edge_cases(ctx):
+@pytest.mark.parametrize("path", PATHS)
+def test_edge_cases(ctx, path):
     mat = oracle.scmat(1, 4)
-    qs = [[], [0, 1, 2], [], [1] * 5, [0, 4, 4, 1], [2] * 300, [3] * 7]
-    ts = [[1, 2, 3], [], [], [1] * 5, [4, 0, 1, 1], [2] * 300, [3] * 7]
-    h0s = [10, 5, 3, 1, 20, 40, 250]
+    qs = [[], [0, 1, 2], [], [1] * 5, [0, 4, 4, 1], [2] * 300, [3] * 7, [0, 1] * 600]
+    ts = [[1, 2, 3], [], [], [1] * 5, [4, 0, 1, 1], [2] * 300, [3] * 7, [0, 1] * 700]
+    h0s = [10, 5, 3, 1, 20, 40, 250, 30]
     for w in (0, 1, 2, 100):
         for zd in (0, 1, 100):
-            _check_batch(ctx, qs, ts, h0s, w=w, zdrop=zd, what=f"edge w={w} zdrop={zd}")
+            _check_batch(ctx, qs, ts, h0s, w=w, zdrop=zd, path=path, what=f"edge w={w} zdrop={zd}")
     # a single job, and empty batches
     assert ctx.extend([], [1, 2, 3], 10) == (10, 0, 0, 1, 3, 0)
     empty = B.JobSet.from_lists([], [])
     assert len(ctx.extend_batch(empty)) == 0
 
 
-def test_wide_cells_for_large_scores(ctx):
+@pytest.mark.parametrize("path", PATHS)
+def test_wide_cells_for_large_scores(ctx, path):
     # h0 + min(q,t)*a >= 32768 needs int32 cells (the reference's scalar bin)
     rng = np.random.default_rng(5)
     qs, ts, h0s = [], [], []
@@ -127,7 +182,7 @@ def test_wide_cells_for_large_scores(ctx):
         qs.append(q)
         ts.append(t)
         h0s.append(32760 + k if k % 2 else 100 + k)
-    _check_batch(ctx, qs, ts, h0s, what="wide")
+    _check_batch(ctx, qs, ts, h0s, path=path, what="wide")
 
 
 def test_non_uniform_matrix_is_exact(ctx):

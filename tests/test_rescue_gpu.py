@@ -9,70 +9,80 @@ import refstreams as R
 
 pytestmark = pytest.mark.gpu
 
+KERNELS = [pytest.param(B.RESCUE_AUTO, id="wavefront"), pytest.param(B.RESCUE_TPJ, id="tpj")]
+
+
+@pytest.fixture(params=KERNELS)
+def rctx(ctx, request):
+    """The context with the rescue kernel family under test selected."""
+    ctx.set_option(B.OPT_RESCUE_KERNEL, request.param)
+    yield ctx
+    ctx.set_option(B.OPT_RESCUE_KERNEL, B.RESCUE_AUTO)
+
 
 def _js(pairs):
     return B.JobSet.from_lists([p[0] for p in pairs], [p[1] for p in pairs])
 
 
-def test_known_answers(ctx):
+def test_known_answers(rctx):
     js = _js([([0, 1, 2, 3, 0, 1, 2, 3], [0, 1, 2, 3, 0, 1, 2, 3])])
-    r = ctx.ksw_align2_scalar_batch(js, oracle.scmat(1, 4), 6, 1, 6, 1, 4, 1, 16)[0]
+    r = rctx.ksw_align2_scalar_batch(js, oracle.scmat(1, 4), 6, 1, 6, 1, 4, 1, 16)[0]
     assert tuple(int(x) for x in r)[:5] == (8, 0, 7, 0, 7)
     js = _js([([3, 3, 0, 0, 1, 1, 3, 3], [2, 0, 0, 1, 1, 2])])
-    r = ctx.ksw_align2_scalar_batch(js, oracle.scmat(1, 4), 6, 1, 6, 1, 1, 1, 16)[0]
+    r = rctx.ksw_align2_scalar_batch(js, oracle.scmat(1, 4), 6, 1, 6, 1, 1, 1, 16)[0]
     assert tuple(int(x) for x in r)[:5] == (4, 2, 5, 1, 4)
 
 
 @pytest.mark.parametrize("a,b,minsc", [(1, 4, 19), (10, 40, 190)])
-def test_matesw_stream_batched_and_scalar(ctx, a, b, minsc):
+def test_matesw_stream_batched_and_scalar(rctx, a, b, minsc):
     # crates/bwa-neon/src/matesw.rs:5045-5139
     pairs = R.matesw_jobs()
     js = _js(pairs)
     mat = oracle.scmat(a, b)
     want_b, _ = oracle.align2_batch(js, mat, 6, 1, 6, 1, minsc, a, mode=0)
-    got_b = ctx.ksw_align2_batch(js, mat, 6, 1, 6, 1, minsc, a)
+    got_b = rctx.ksw_align2_batch(js, mat, 6, 1, 6, 1, minsc, a)
     assert np.array_equal(got_b, want_b)
     want_s, _ = oracle.align2_batch(js, mat, 6, 1, 6, 1, minsc, a, mode=1)
-    got_s = ctx.ksw_align2_scalar_batch(js, mat, 6, 1, 6, 1, minsc, a, 0)
+    got_s = rctx.ksw_align2_scalar_batch(js, mat, 6, 1, 6, 1, minsc, a, 0)
     assert np.array_equal(got_s, want_s)
 
 
-def test_pad_columns_stream(ctx):
+def test_pad_columns_stream(rctx):
     js = _js(R.matesw_pad_columns())
     want = oracle.local_fwd_batch(js, 19, oracle.INT_MAX)
-    got = ctx.ksw_local_fwd_batch(js, 19, B.INT_MAX)
+    got = rctx.ksw_local_fwd_batch(js, 19, B.INT_MAX)
     assert np.array_equal(got, want)
     assert int((got["score2"] >= 0).sum()) >= 8
 
 
-def test_ragged_tlen_endsc_stream(ctx):
+def test_ragged_tlen_endsc_stream(rctx):
     js = _js(R.matesw_ragged())
     want = oracle.local_fwd_batch(js, 19, 60)
-    got = ctx.ksw_local_fwd_batch(js, 19, 60)
+    got = rctx.ksw_local_fwd_batch(js, 19, 60)
     assert np.array_equal(got, want)
 
 
-def test_bench_jobs_stream(ctx):
+def test_bench_jobs_stream(rctx):
     js = _js(R.rescue_bench_jobs(2048))
     want, _ = oracle.align2_batch(js, minsc=19)
-    assert np.array_equal(ctx.ksw_align2_batch(js, minsc=19), want)
+    assert np.array_equal(rctx.ksw_align2_batch(js, minsc=19), want)
 
 
 @pytest.mark.parametrize("lanes", [8, 16])
-def test_fixed_lanes(ctx, lanes):
+def test_fixed_lanes(rctx, lanes):
     js = _js(R.matesw_jobs()[:500])
     want, _ = oracle.align2_batch(js, minsc=19, mode=1, lanes=lanes)
-    assert np.array_equal(ctx.ksw_align2_scalar_batch(js, minsc=19, lanes=lanes), want)
+    assert np.array_equal(rctx.ksw_align2_scalar_batch(js, minsc=19, lanes=lanes), want)
 
 
-def test_workload_windows(ctx):
+def test_workload_windows(rctx):
     js = B.synth_rescue(20000, seed=4)
     want, _ = oracle.align2_batch(js, minsc=20)
-    got = ctx.ksw_align2_batch(js, minsc=20)
+    got = rctx.ksw_align2_batch(js, minsc=20)
     assert np.array_equal(got, want)
 
 
-def test_device_entry(ctx):
+def test_device_entry(rctx):
     import torch
 
     js = B.synth_rescue(5000, seed=6)
@@ -80,23 +90,23 @@ def test_device_entry(ctx):
     d_seq = torch.from_numpy(js.seq).cuda()
     d_jobs = torch.from_numpy(js.dev_res_jobs().view(np.uint8)).cuda()
     d_out = torch.zeros(len(js) * 28, dtype=torch.uint8, device="cuda")
-    ctx.ksw_align2_device(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), d_out.data_ptr(), minsc=20)
-    ctx.sync()
+    rctx.ksw_align2_device(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), d_out.data_ptr(), minsc=20)
+    rctx.sync()
     assert np.array_equal(d_out.cpu().numpy().view(B.ALN_RES), want)
 
 
-def test_edge_cases(ctx):
+def test_edge_cases(rctx):
     pairs = [([], [0, 1, 2]), ([0, 1], []), ([], []), ([4, 4, 4], [4, 4, 4]), ([0] * 300, [0] * 400),
              ([1, 2, 3, 0] * 70, [1, 2, 3, 0] * 100), ([2], [2])]
     js = _js(pairs)
     for minsc in (0, 1, 19):
         want, _ = oracle.align2_batch(js, minsc=minsc)
-        assert np.array_equal(ctx.ksw_align2_batch(js, minsc=minsc), want)
+        assert np.array_equal(rctx.ksw_align2_batch(js, minsc=minsc), want)
         want, _ = oracle.align2_batch(js, minsc=minsc, mode=1)
-        assert np.array_equal(ctx.ksw_align2_scalar_batch(js, minsc=minsc), want)
+        assert np.array_equal(rctx.ksw_align2_scalar_batch(js, minsc=minsc), want)
 
 
-def test_wide_scores(ctx):
+def test_wide_scores(rctx):
     # min(q,t) * max_sc >= 32768 needs int32 cells
     rng = np.random.default_rng(3)
     q = rng.integers(0, 4, 400).tolist()
@@ -104,7 +114,7 @@ def test_wide_scores(ctx):
     mat = oracle.scmat(100, 120)
     js = _js([(q, t), (q[:50], t)])
     want, _ = oracle.align2_batch(js, mat, 6, 1, 6, 1, 500, 100)
-    assert np.array_equal(ctx.ksw_align2_batch(js, mat, 6, 1, 6, 1, 500, 100), want)
+    assert np.array_equal(rctx.ksw_align2_batch(js, mat, 6, 1, 6, 1, 500, 100), want)
 
 
 def test_invalid_inputs(ctx):
