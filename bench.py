@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--jobs", type=int, default=N_JOBS)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-graphs", action="store_true", help="enqueue the batched path every step (profiling)")
     return ap.parse_args()
 
 
@@ -180,6 +181,8 @@ def main():
 
         dist.init_process_group("nccl")
     ctx = B.Context(local)
+    if args.no_graphs:
+        ctx.set_option(B.OPT_GRAPHS, 0)
     n = args.jobs
     # each rank extends its own shard of reads (weak scaling: per-GPU work fixed)
     js = B.synth_ext(2, n, seed=1000 + rank)
