@@ -41,12 +41,14 @@ OPS_PER_CELL = 9  # minimal fused integer op count of one extension cell (see DE
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--jobs", type=int, default=N_JOBS)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-graphs", action="store_true", help="enqueue the batched path every step (profiling)")
+    ap.add_argument("--case", choices=["ext-batched", "ext-plain", "rescue"],
+                    help="profiling case: run the small workload twice through one path, no timing")
     return ap.parse_args()
 
 
@@ -164,9 +166,41 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_case(args):
+    """Small fixed case for ncu captures: two calls of one path, nothing timed."""
+    import numpy as np
+    import torch
+
+    import bwacuda as B
+
+    ctx = B.Context(0)
+    ctx.set_option(B.OPT_GRAPHS, 0)  # plain stream launches (no graph nodes) under the profiler
+    if args.case.startswith("ext"):
+        js = B.synth_ext(2, args.jobs, seed=0)
+        d_seq = torch.from_numpy(js.seq).cuda()
+        d_jobs = torch.from_numpy(js.dev_ext_jobs().view(np.uint8)).cuda()
+        d_out = torch.zeros(len(js) * 24, dtype=torch.uint8, device="cuda")
+        path = B.PATH_BATCHED if args.case == "ext-batched" else B.PATH_PLAIN
+        for _ in range(2):
+            ctx.extend_device(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), d_out.data_ptr(), path=path)
+            ctx.sync()
+    else:
+        js = B.synth_rescue(args.jobs, seed=0)
+        d_seq = torch.from_numpy(js.seq).cuda()
+        d_jobs = torch.from_numpy(js.dev_res_jobs().view(np.uint8)).cuda()
+        d_out = torch.zeros(len(js) * 28, dtype=torch.uint8, device="cuda")
+        for _ in range(2):
+            ctx.ksw_align2_device(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), d_out.data_ptr(), minsc=20)
+            ctx.sync()
+    ctx.close()
+    print("ok")
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.case:
+        return run_case(args)
     if args.impl == "reference":
         return run_reference(args, rank, world)
 
