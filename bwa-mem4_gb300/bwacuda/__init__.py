@@ -58,7 +58,8 @@ class Stats(C.Structure):
 EXPORTS = ("bwacuda_ctx_create", "bwacuda_ctx_destroy", "bwacuda_set_option", "bwacuda_strerror",
            "bwacuda_backend_name", "bwacuda_extend", "bwacuda_extend_batch", "bwacuda_ksw_align2_batch",
            "bwacuda_ksw_align2_scalar_batch", "bwacuda_ksw_local_fwd_batch", "bwacuda_extend_device",
-           "bwacuda_ksw_align2_device", "bwacuda_ctx_sync", "bwacuda_get_stats", "bwacuda_reset_stats")
+           "bwacuda_ksw_align2_device", "bwacuda_ctx_sync", "bwacuda_get_stats", "bwacuda_reset_stats",
+           "bwacuda_ksw_align2_device_noalloc")
 
 _lib = None
 _synth = None
@@ -94,6 +95,7 @@ def lib():
     L.bwacuda_ksw_local_fwd_batch.argtypes = [vp, vp, sz, I, vp, I, I, I, I, I, I, vp]
     L.bwacuda_extend_device.argtypes = [vp, vp, vp, sz, C.POINTER(Scoring), I, I, I, vp, vp]
     L.bwacuda_ksw_align2_device.argtypes = [vp, vp, vp, sz, C.POINTER(Scoring), I, I, I, I, vp, vp]
+    L.bwacuda_ksw_align2_device_noalloc.argtypes = [vp, vp, vp, sz, C.POINTER(Scoring), I, I, I, I, vp, vp]
     L.bwacuda_ctx_sync.argtypes = [vp]
     L.bwacuda_get_stats.argtypes = [vp, C.POINTER(Stats)]
     L.bwacuda_reset_stats.argtypes = [vp]
@@ -365,6 +367,15 @@ class Context:
                                              minsc, max_sc, mode, lanes, C.c_void_p(d_out),
                                              C.c_void_p(stream) if stream else None)
         self._check(rc, "bwacuda_ksw_align2_device")
+
+    def ksw_align2_device_noalloc(self, d_seq, d_jobs, n, d_out, sc: Scoring = None, minsc=19, max_sc=1, mode=0,
+                                 lanes=0, stream=None):
+        """The allocation-free variant (synchronous); see include/bwacuda.h."""
+        sc = sc or self.scoring()
+        rc = lib().bwacuda_ksw_align2_device_noalloc(self.h, C.c_void_p(d_seq), C.c_void_p(d_jobs), n, C.byref(sc),
+                                                     minsc, max_sc, mode, lanes, C.c_void_p(d_out),
+                                                     C.c_void_p(stream) if stream else None)
+        self._check(rc, "bwacuda_ksw_align2_device_noalloc")
 
     def sync(self):
         self._check(lib().bwacuda_ctx_sync(self.h), "bwacuda_ctx_sync")

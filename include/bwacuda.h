@@ -185,6 +185,23 @@ int bwacuda_ksw_align2_device(bwacuda_ctx *ctx, const uint8_t *d_seq,
 
 int bwacuda_ctx_sync(bwacuda_ctx *ctx);
 
+/* bwacuda_ksw_align2_device for callers that cannot allocate device memory (a
+ * pool allocator owns the whole device budget, or cudaMalloc/cudaFree would
+ * synchronise a latency-critical stream).  No counterpart in the reference.
+ * Same inputs, outputs and results as bwacuda_ksw_align2_device; the tracker
+ * scratch lives in a static device array of this library (128 MiB of entries,
+ * 4 MiB of offsets, held by every GPU that loads the library until exit).
+ * A call may hold at most 524288 jobs and n * (max tlen / 2 + 2) <= 16 Mi
+ * tracker entries, else it returns BWACUDA_EUNSUPPORTED without launching.
+ * Synchronous: returns after the results are written (errors included).
+ * Calls share the static array: calls that overlap on the GPU race.  The first
+ * call on a device resolves the array's address (cudaGetSymbolAddress) and must
+ * come before any stream capture. */
+int bwacuda_ksw_align2_device_noalloc(bwacuda_ctx *ctx, const uint8_t *d_seq,
+                                      const bwacuda_dev_rescue_job *d_jobs, size_t n,
+                                      const bwacuda_scoring *sc, int minsc, int max_sc, int mode,
+                                      int lanes, bwacuda_rescue_result *d_out, void *stream);
+
 /* Counters accumulated since the context was created (or last reset). */
 typedef struct {
     uint64_t ext_jobs, ext_cells;       /* cells = sum over rows of (end - beg) */
