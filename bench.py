@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--jobs", type=int, default=N_JOBS)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-chunk", type=int, default=1 << 20, help="jobs per pipelined chunk of the host-buffer call")
     ap.add_argument("--no-graphs", action="store_true", help="enqueue the batched path every step (profiling)")
     ap.add_argument("--case", choices=["ext-batched", "ext-plain", "rescue"],
                     help="profiling case: run the small workload twice through one path, no timing")
@@ -123,8 +124,10 @@ def peaks():
 
 
 def int_peak_gops(nsm, mhz):
-    # 128 INT32 lanes per SM per clock (one warp instruction per SMSP per clock, 4 SMSPs)
-    return nsm * 128 * mhz * 1e6 / 1e9
+    # integer ALU pipe (min/max/compare/select/permute): half a warp-instruction per cycle per
+    # scheduler, i.e. 64 lanes per SM per clock (ncu: the rescue kernel's ALU pipe at 84.6% of
+    # peak while issuing 0.80 warp-instructions per cycle per scheduler)
+    return nsm * 64 * mhz * 1e6 / 1e9
 
 
 def cpu_baseline(js_sample, nthreads=0):
@@ -298,18 +301,31 @@ def main():
     # end to end through the C ABI with host buffers
     e2e = None
     if not args.no_e2e:
+        import ctypes
+
         ctx.set_option(B.OPT_EXT_PATH, B.PATH_BATCHED)
-        ctx.set_option(B.OPT_CHUNK_JOBS, 1 << 20)
-        ctx.extend_batch(js)  # warm-up (pinned staging allocation)
+        ctx.set_option(B.OPT_CHUNK_JOBS, args.e2e_chunk)
+        # the caller's ExtendJob array (pointers into its own host buffers), built
+        # once like a Rust or C caller's; the timed call is the C ABI itself
+        host_jobs = ctx._host_jobs(js, B.EXT_JOB)
+        host_out = np.zeros(n, dtype=B.EXT_RES)
+        mat = B.scmat()
+        L = B.lib()
+
+        def call():
+            rc = L.bwacuda_extend_batch(ctx.h, ctypes.c_void_p(host_jobs.ctypes.data), n, 5,
+                                        ctypes.c_void_p(mat.ctypes.data), 6, 1, 6, 1, 100, 5, 100,
+                                        ctypes.c_void_p(host_out.ctypes.data))
+            if rc != B.OK:
+                raise B.BwaCudaError(rc, "bwacuda_extend_batch")
+
+        call()  # warm-up (pinned staging allocation)
         ctx.reset_stats()
         barrier()
-        lat = []
         t0 = time.perf_counter()
-        esteps = max(1, min(args.steps, 3))
+        esteps = max(1, min(args.steps, 5))
         for _ in range(esteps):
-            t1 = time.perf_counter()
-            host_out = ctx.extend_batch(js)
-            lat.append(time.perf_counter() - t1)
+            call()
         barrier()
         et = max_over_ranks(time.perf_counter() - t0)
         ste = ctx.stats()
@@ -342,8 +358,9 @@ def main():
         "roofline": {"bound": "alu", "achieved": round(achieved, 1), "peak": round(peak_g, 1), "unit": "Gop/s",
                      "frac": round(achieved / peak_g, 4),
                      "traffic": None,
-                     "note": f"integer ops = GCUPS x {OPS_PER_CELL} ops/cell; peak = {nsm} SMs x 128 INT32 lanes x "
-                             f"median SM clock under load ({kind} peaks file has no integer figure)"},
+                     "note": f"integer ops = GCUPS x {OPS_PER_CELL} ops/cell (minimal fused count); peak = {nsm} SMs x "
+                             f"64 ALU-pipe lanes x median SM clock under load (the {kind} peaks file has HBM and bf16 "
+                             "figures only; this path touches ~0.05 B of HBM per cell and no tensor core)"},
     }
     if e2e:
         line["e2e"] = e2e

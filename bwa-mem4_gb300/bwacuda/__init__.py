@@ -50,6 +50,10 @@ STAT_FIELDS = ("ext_jobs", "ext_cells", "ext_bin_u8", "ext_bin_i16", "ext_bin_i3
                "kernel_launches", "h2d_bytes", "d2h_bytes")
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_waves", C.c_int32), ("max_requests", C.c_int32)]
+
+
 class Stats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in STAT_FIELDS]
 
@@ -59,7 +63,9 @@ EXPORTS = ("bwacuda_ctx_create", "bwacuda_ctx_destroy", "bwacuda_set_option", "b
            "bwacuda_backend_name", "bwacuda_extend", "bwacuda_extend_batch", "bwacuda_ksw_align2_batch",
            "bwacuda_ksw_align2_scalar_batch", "bwacuda_ksw_local_fwd_batch", "bwacuda_extend_device",
            "bwacuda_ksw_align2_device", "bwacuda_ctx_sync", "bwacuda_get_stats", "bwacuda_reset_stats",
-           "bwacuda_ksw_align2_device_noalloc")
+           "bwacuda_ksw_align2_device_noalloc", "bwacuda_server_start", "bwacuda_server_stop",
+           "bwacuda_server_submit_extend", "bwacuda_server_submit_rescue", "bwacuda_server_wait",
+           "bwacuda_server_stats")
 
 _lib = None
 _synth = None
@@ -96,6 +102,12 @@ def lib():
     L.bwacuda_extend_device.argtypes = [vp, vp, vp, sz, C.POINTER(Scoring), I, I, I, vp, vp]
     L.bwacuda_ksw_align2_device.argtypes = [vp, vp, vp, sz, C.POINTER(Scoring), I, I, I, I, vp, vp]
     L.bwacuda_ksw_align2_device_noalloc.argtypes = [vp, vp, vp, sz, C.POINTER(Scoring), I, I, I, I, vp, vp]
+    L.bwacuda_server_start.argtypes = [vp, C.POINTER(ServerConfig)]
+    L.bwacuda_server_stop.argtypes = [vp]
+    L.bwacuda_server_submit_extend.argtypes = [vp, vp, sz, C.POINTER(Scoring), I, I, I, C.POINTER(C.c_uint64)]
+    L.bwacuda_server_submit_rescue.argtypes = [vp, vp, sz, C.POINTER(Scoring), I, I, C.POINTER(C.c_uint64)]
+    L.bwacuda_server_wait.argtypes = [vp, C.c_uint64, vp, C.c_int64, C.POINTER(C.c_int64)]
+    L.bwacuda_server_stats.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     L.bwacuda_ctx_sync.argtypes = [vp]
     L.bwacuda_get_stats.argtypes = [vp, C.POINTER(Stats)]
     L.bwacuda_reset_stats.argtypes = [vp]
@@ -376,6 +388,54 @@ class Context:
                                                      minsc, max_sc, mode, lanes, C.c_void_p(d_out),
                                                      C.c_void_p(stream) if stream else None)
         self._check(rc, "bwacuda_ksw_align2_device_noalloc")
+
+    # -- serving loop --
+    def server_start(self, hbm_budget_bytes=1 << 30, max_waves=3, max_requests=4096):
+        cfg = ServerConfig(hbm_budget_bytes, max_waves, max_requests)
+        self._check(lib().bwacuda_server_start(self.h, C.byref(cfg)), "bwacuda_server_start")
+        self._held = {}
+
+    def server_stop(self):
+        self._check(lib().bwacuda_server_stop(self.h), "bwacuda_server_stop")
+        self._held = {}
+
+    def submit_extend(self, js: JobSet, sc: Scoring = None, w=100, end_bonus=5, zdrop=100) -> int:
+        """Queue an extension request; js must stay alive until wait() (kept here)."""
+        jobs = self._host_jobs(js, EXT_JOB)
+        rid = C.c_uint64()
+        sc = sc or self.scoring()
+        rc = lib().bwacuda_server_submit_extend(self.h, _ptr(jobs), len(js), C.byref(sc), w, end_bonus, zdrop,
+                                                C.byref(rid))
+        self._check(rc, "bwacuda_server_submit_extend")
+        self._held[rid.value] = (js, jobs, EXT_RES)
+        return rid.value
+
+    def submit_rescue(self, js: JobSet, sc: Scoring = None, minsc=19, max_sc=1) -> int:
+        jobs = self._host_jobs(js, RES_JOB)
+        rid = C.c_uint64()
+        sc = sc or self.scoring()
+        rc = lib().bwacuda_server_submit_rescue(self.h, _ptr(jobs), len(js), C.byref(sc), minsc, max_sc,
+                                                C.byref(rid))
+        self._check(rc, "bwacuda_server_submit_rescue")
+        self._held[rid.value] = (js, jobs, ALN_RES)
+        return rid.value
+
+    def wait(self, rid, timeout_us=-1):
+        """Results of a request and its submit-to-completion latency in seconds."""
+        js, jobs, dt = self._held[rid]
+        out = np.zeros(len(js), dtype=dt)
+        lat = C.c_int64()
+        rc = lib().bwacuda_server_wait(self.h, rid, _ptr(out), timeout_us, C.byref(lat))
+        if rc == EAGAIN or rc == ETIMEOUT:
+            raise BwaCudaError(rc, "bwacuda_server_wait")
+        del self._held[rid]
+        self._check(rc, "bwacuda_server_wait")
+        return out, lat.value * 1e-9
+
+    def server_stats(self):
+        a, b, q = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        self._check(lib().bwacuda_server_stats(self.h, C.byref(a), C.byref(b), C.byref(q)), "bwacuda_server_stats")
+        return {"served_jobs": a.value, "waves": b.value, "queued": q.value}
 
     def sync(self):
         self._check(lib().bwacuda_ctx_sync(self.h), "bwacuda_ctx_sync")

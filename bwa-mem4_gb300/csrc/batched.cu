@@ -108,7 +108,8 @@ static cudaError_t ensure_bufs(BatchBufs &bb, size_t n)
 // Enqueue the batched sequence for n device-resident jobs on stream s.
 static cudaError_t enqueue_batched(bwacuda_ctx *c, BatchBufs &bb, const uint8_t *d_seq,
                                    const bwacuda_dev_ext_job *d_jobs, size_t n, const ExtParams &P,
-                                   bwacuda_ext_result *d_out, cudaStream_t s)
+                                   bwacuda_ext_result *d_out, cudaStream_t s, uint32_t *err = nullptr,
+                                   unsigned long long *cells = nullptr)
 {
     BatchedState *B = c->batched;
     cudaError_t e = ext_sort_and_bucket(d_jobs, n, P.sc.max_sc, static_cast<uint16_t *>(bb.keys_in.p),
@@ -126,8 +127,8 @@ static cudaError_t enqueue_batched(bwacuda_ctx *c, BatchBufs &bb, const uint8_t 
     L.order = static_cast<const uint32_t *>(bb.idx_out.p);
     L.P = P;
     L.out = d_out;
-    L.err = reinterpret_cast<uint32_t *>(c->d_misc.p);
-    L.cells = reinterpret_cast<unsigned long long *>((char *)c->d_misc.p + 8);
+    L.err = err ? err : reinterpret_cast<uint32_t *>(c->d_misc.p);
+    L.cells = cells ? cells : reinterpret_cast<unsigned long long *>((char *)c->d_misc.p + 8);
     // largest buckets first: they hold the long jobs
     for (int b = B->nb - 1, k = 0; b >= 0; --b, ++k) {
         L.stream = bb.fan[k % FAN];
@@ -184,6 +185,56 @@ int extend_device_batched(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_de
     return BWACUDA_OK;
 }
 
+int batched_prepare(bwacuda_ctx *c) { return batched_init(c); }
+
+static cudaError_t bufs_streams(BatchBufs &bb)
+{
+    cudaError_t e = cudaSuccess;
+    for (int f = 0; f < FAN && e == cudaSuccess; ++f) {
+        e = cudaStreamCreateWithFlags(&bb.fan[f], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&bb.join[f], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&bb.fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = bb.table.ensure(EXT_MAX_BUCKETS * 4 * sizeof(uint32_t));
+    return e;
+}
+
+BatchBufs *batchbufs_create()
+{
+    BatchBufs *bb = new (std::nothrow) BatchBufs();
+    if (!bb) return nullptr;
+    if (bufs_streams(*bb) != cudaSuccess) {
+        batchbufs_destroy(bb);
+        return nullptr;
+    }
+    return bb;
+}
+
+void batchbufs_destroy(BatchBufs *bb)
+{
+    if (!bb) return;
+    for (int f = 0; f < FAN; ++f) {
+        if (bb->fan[f]) cudaStreamSynchronize(bb->fan[f]);
+        if (bb->fan[f]) cudaStreamDestroy(bb->fan[f]);
+        if (bb->join[f]) cudaEventDestroy(bb->join[f]);
+    }
+    if (bb->fork) cudaEventDestroy(bb->fork);
+    if (bb->graph) cudaGraphExecDestroy(bb->graph);
+    bb->keys_in.release(); bb->keys_out.release(); bb->idx_in.release(); bb->idx_out.release();
+    bb->tmp.release(); bb->table.release();
+    delete bb;
+}
+
+// The batched sequence on the caller's buffers (batched_prepare must have run).
+cudaError_t batched_enqueue(bwacuda_ctx *c, BatchBufs *bb, const uint8_t *d_seq, const bwacuda_dev_ext_job *d_jobs,
+                            size_t n, const ExtParams &P, bwacuda_ext_result *d_out, cudaStream_t s, uint32_t *err,
+                            unsigned long long *cells)
+{
+    cudaError_t e = ensure_bufs(*bb, n);
+    if (e != cudaSuccess) return e;
+    return enqueue_batched(c, *bb, d_seq, d_jobs, n, P, d_out, s, err, cells);
+}
+
 // Host-buffer form: the plain path's packing pipeline, each chunk run batched.
 int extend_batch_host_batched(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int m, const int8_t *mat,
                               const ExtParams &P, int w, bwacuda_ext_result *out)
@@ -199,6 +250,5 @@ int extend_batch_host_batched(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_
     });
 }
 
-void server_shutdown(bwacuda_ctx *) {}
 
 }  // namespace bwacuda

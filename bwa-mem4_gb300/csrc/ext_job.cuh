@@ -199,4 +199,210 @@ __host__ __device__ inline size_t ext_block_smem(int qcap, int tb, int cell_byte
     return (size_t)qcap * tb * cell_bytes + qwords * tb * 4;
 }
 
+// ---------------------------------------------------------------------------
+// 8-bit pair cells: word k of a thread holds columns 2k and 2k+1 as the bytes
+// (H_2k, E_2k, H_2k+1, E_2k+1).  Exact whenever every DP value < 256, i.e. for
+// the jobs the reference routes to its 8-bit kernels
+// (crates/bwa-neon/src/batched.rs:850-864).  Half the row footprint of FmtI16,
+// so twice the jobs per SM; each word access serves two columns.
+// ---------------------------------------------------------------------------
+
+__host__ __device__ inline bool ext_fits_u8(int qlen, int tlen, int h0, int max_sc)
+{
+    return ext_value_bound(qlen, tlen, h0, max_sc) < 256;
+}
+
+// Cell words of a block for the pair format (one spare word for the look-ahead).
+__host__ __device__ inline size_t ext_block_smem_u8p(int qcap, int tb)
+{
+    size_t cwords = (size_t)qcap / 2 + 2;
+    size_t qwords = (size_t)qcap / 4 + 1;
+    return (cwords + qwords) * tb * 4;
+}
+
+// One extension cell (sw.rs:363-414): in hd = H(i-1, j-1), e = E(i, j) and the
+// carried f = F(i, j); out h = H(i, j), en = E(i+1, j), f = F(i, j+1).
+__device__ __forceinline__ void ext_cell(int hd, int e, uint32_t qc, uint32_t plo, uint32_t phi, int oe_del,
+                                         int e_del, int oe_ins, int e_ins, int &f, int &h, int &en)
+{
+    const int s = prof_score(plo, phi, qc);
+    const int M = hd != 0 ? hd + s : 0;  // a zero diagonal is never extended
+    h = M > e ? M : e;
+    h = h > f ? h : f;
+    int od = M - oe_del;
+    od = od > 0 ? od : 0;
+    en = e - e_del;
+    en = en > od ? en : od;
+    int oi = M - oe_ins;
+    oi = oi > 0 ? oi : 0;
+    f -= e_ins;
+    f = f > oi ? f : oi;
+}
+
+template <int TB>
+__device__ __forceinline__ bool u8p_dead(const uint32_t *cellw, int x)
+{
+    return ((cellw[(x >> 1) * TB] >> ((x & 1) * 16)) & 0xffffu) == 0u;
+}
+
+template <int TB>
+__device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restrict__ cellw, uint32_t *__restrict__ qw,
+                                                              const uint8_t *__restrict__ seq,
+                                                              const bwacuda_dev_ext_job &J, const ExtParams &P,
+                                                              bool &bad, unsigned long long &ncells)
+{
+    const int qlen = J.qlen, tlen = J.tlen, h0 = J.h0, m = P.sc.m;
+    const uint8_t *q = seq + J.q_off;
+    const uint8_t *t = seq + J.t_off;
+    const int o_del = P.sc.o_del, e_del = P.sc.e_del, o_ins = P.sc.o_ins, e_ins = P.sc.e_ins;
+    const int oe_del = o_del + e_del, oe_ins = o_ins + e_ins;
+
+    // Query codes as prmt selector bytes 0x80 | c * 0x11 (nibbles c, c|8): two
+    // consecutive bytes select two sign-extended 16-bit scores in one prmt.
+    for (int jw = 0; jw * 4 <= qlen; ++jw) {
+        uint32_t v = 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int j = jw * 4 + u;
+            uint32_t c = j < qlen ? (uint32_t)q[j] : 0u;
+            bad |= c >= (uint32_t)m;
+            v |= (0x80u | (c & 7u) * 0x11u) << (8 * u);
+        }
+        qw[jw * TB] = v;
+    }
+    // Row -1 (sw.rs:269-279): H(-1, j-1) = h0, h0 - oe_ins, then - e_ins while > e_ins; E = 0.
+    {
+        int hv = h0;
+        for (int k = 0; 2 * k <= qlen; ++k) {
+            const int a = hv;  // column 2k
+            if (2 * k == 0) hv = h0 > oe_ins ? h0 - oe_ins : 0;
+            else hv = hv > e_ins ? hv - e_ins : 0;
+            const int b = 2 * k + 1 <= qlen ? hv : 0;  // column 2k+1
+            if (2 * k + 1 <= qlen) hv = hv > e_ins ? hv - e_ins : 0;
+            cellw[k * TB] = (uint32_t)a | ((uint32_t)b << 16);
+        }
+    }
+    const int w = clamp_band(J.w < 0 ? 0 : J.w, qlen, P.sc.max_sc, P.end_bonus, o_ins, e_ins, o_del, e_del);
+    int best = h0, best_i = -1, best_j = -1, best_ie = -1, gscore = -1, max_off = 0;
+    int beg = 0, end = qlen;
+    uint32_t tnext = tlen > 0 ? t[0] : 0u;
+    // 16x2 broadcasts of the negated gap costs
+    const uint32_t noe_ins2 = (uint32_t)(-oe_ins & 0xffff) * 0x10001u;
+    const uint32_t noe_del2 = (uint32_t)(-oe_del & 0xffff) * 0x10001u;
+    const uint32_t ne_del2 = (uint32_t)(-e_del & 0xffff) * 0x10001u;
+    for (int i = 0; i < tlen; ++i) {
+        uint32_t tc = tnext;
+        if (i + 1 < tlen) tnext = t[i + 1];
+        bad |= tc >= (uint32_t)m;
+        tc &= 7u;
+        const uint32_t plo = P.sc.prof[tc][0], phi = P.sc.prof[tc][1];
+        if (beg < i - w) beg = i - w;
+        if (end > i + w + 1) end = i + w + 1;
+        if (end > qlen) end = qlen;
+        int h1 = 0;
+        if (beg == 0) {
+            h1 = h0 - (o_del + e_del * (i + 1));
+            h1 = h1 > 0 ? h1 : 0;
+        }
+        int f = 0;
+        int32_t rowkey = 0;
+        if (beg < end) {
+            int j = beg;
+            if (j & 1) {  // odd first column: the high half of its word
+                uint32_t wv = cellw[(j >> 1) * TB];
+                const uint32_t qc = (qw[(j >> 2) * TB] >> ((j & 3) * 8)) & 7u;
+                int h, en;
+                ext_cell((int)((wv >> 16) & 0xffu), (int)(wv >> 24), qc, plo, phi, oe_del, e_del, oe_ins, e_ins, f, h,
+                         en);
+                cellw[(j >> 1) * TB] = (wv & 0xffffu) | ((uint32_t)h1 << 16) | ((uint32_t)en << 24);
+                h1 = h;
+                const int32_t kk = (h << 16) | j;
+                rowkey = rowkey > kk ? rowkey : kk;
+                ++j;
+            }
+            uint32_t wn = cellw[(j >> 1) * TB];  // j <= end <= qlen: allocated
+            for (; j + 1 < end; j += 2) {
+                // columns j, j+1 of one word as 16x2 lanes; only F runs column by column
+                const uint32_t wv = wn;
+                wn = cellw[((j >> 1) + 1) * TB];  // spare word keeps this in bounds
+                const uint32_t sel = qw[(j >> 2) * TB] >> ((j & 2) * 8);
+                const uint32_t s2 = prmt(plo, phi, sel);   // (s_j, s_j+1)
+                const uint32_t hd2 = prmt(wv, 0u, 0x4240u);  // (H(i-1,j-1), H(i-1,j))
+                const uint32_t e2 = prmt(wv, 0u, 0x4341u);   // (E(i,j), E(i,j+1))
+                // M = hd ? hd + s : 0, as min(hd + s, 128 hd): hd <= 255 and s >= -128, so
+                // the minimum is hd + s whenever hd >= 1 and <= 0 when hd == 0, and a
+                // non-positive M acts as 0 below (E, F >= 0)
+                const uint32_t M2 = __viaddmin_s16x2(hd2, s2, hd2 << 7);
+                const uint32_t ti2 = __viaddmax_s16x2_relu(M2, noe_ins2, 0u);  // max(M - oe_ins, 0)
+                const uint32_t td2 = __viaddmax_s16x2_relu(M2, noe_del2, 0u);  // max(M - oe_del, 0)
+                const uint32_t en2 = __viaddmax_s16x2(e2, ne_del2, td2);       // E(i+1, .)
+                const int f0 = f;
+                const int f1 = __viaddmax_s32(f0, -e_ins, (int)(ti2 & 0xffffu));
+                f = __viaddmax_s32(f1, -e_ins, (int)(ti2 >> 16));
+                const uint32_t f2 = prmt((uint32_t)f0, (uint32_t)f1, 0x5410u);
+                const uint32_t h2 = __vimax3_s16x2(M2, e2, f2);  // (H(i,j), H(i,j+1))
+                // stored bytes: H(i,j-1), E(i+1,j), H(i,j), E(i+1,j+1)
+                const uint32_t lo = prmt((uint32_t)h1, h2, 0x4040u);
+                cellw[(j >> 1) * TB] = prmt(lo, en2, 0x6140u);
+                h1 = (int)(h2 >> 16);
+                const int32_t ka = (int32_t)(h2 << 16) | j;              // ties -> later column
+                const int32_t kb = (int32_t)(h2 & 0xffff0000u) | (j + 1);
+                rowkey = __vimax3_s32(rowkey, ka, kb);
+            }
+            if (j < end) {  // even last column: the low half of its word
+                const uint32_t wv = wn;
+                const uint32_t qc = (qw[(j >> 2) * TB] >> ((j & 3) * 8)) & 7u;
+                int h, en;
+                ext_cell((int)(wv & 0xffu), (int)((wv >> 8) & 0xffu), qc, plo, phi, oe_del, e_del, oe_ins, e_ins, f,
+                         h, en);
+                cellw[(j >> 1) * TB] = (wv & 0xffff0000u) | (uint32_t)h1 | ((uint32_t)en << 8);
+                h1 = h;
+                const int32_t kk = (h << 16) | j;
+                rowkey = rowkey > kk ? rowkey : kk;
+            }
+            ncells += (unsigned long long)(end - beg);
+        }
+        {   // sentinel column end (sw.rs:418-419): H = h1, E = 0
+            const uint32_t wv = cellw[(end >> 1) * TB];
+            cellw[(end >> 1) * TB] =
+                (end & 1) ? ((wv & 0xffffu) | ((uint32_t)h1 << 16)) : ((wv & 0xffff0000u) | (uint32_t)h1);
+        }
+        const int jf = end > beg ? end : beg;
+        if (jf == qlen && gscore <= h1) {
+            best_ie = i;
+            gscore = h1;
+        }
+        const int rmax = rowkey >> 16;
+        const int mj = rowkey & 0xffff;
+        if (rmax == 0) break;
+        if (rmax > best) {
+            best = rmax;
+            best_i = i;
+            best_j = mj;
+            const int off = mj > i ? mj - i : i - mj;
+            if (off > max_off) max_off = off;
+        } else if (P.zdrop > 0) {
+            if (i - best_i > mj - best_j) {
+                if (best - rmax - ((i - best_i) - (mj - best_j)) * e_del > P.zdrop) break;
+            } else if (best - rmax - ((mj - best_j) - (i - best_i)) * e_ins > P.zdrop) {
+                break;
+            }
+        }
+        int lo = beg;
+        while (lo < end && u8p_dead<TB>(cellw, lo)) ++lo;
+        beg = lo;
+        int hi = end;
+        while (hi >= beg && u8p_dead<TB>(cellw, hi)) --hi;
+        end = hi + 2 < qlen ? hi + 2 : qlen;
+    }
+    bwacuda_ext_result r;
+    r.score = best;
+    r.qle = best_j + 1;
+    r.tle = best_i + 1;
+    r.gtle = best_ie + 1;
+    r.gscore = gscore;
+    r.max_off = max_off;
+    return r;
+}
+
 }  // namespace bwacuda

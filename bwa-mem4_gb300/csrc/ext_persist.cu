@@ -21,14 +21,21 @@ namespace bwacuda {
 
 namespace {
 
-// 16-bit sort key: cell width (i16 before i32), query length descending
-// (clamped at 1023), target length descending in 16-row steps.
+// Cell class of a job: 0 = 8-bit pairs, 1 = 16-bit, 2 = 32-bit cells.
+__device__ __forceinline__ uint32_t ext_cell_class(const bwacuda_dev_ext_job &J, int max_sc)
+{
+    if (ext_fits_u8(J.qlen, J.tlen, J.h0, max_sc)) return 0u;
+    return ext_fits_i16(J.qlen, J.tlen, J.h0, max_sc) ? 1u : 2u;
+}
+
+// 16-bit sort key: cell class, query length descending (clamped at 1023),
+// target length descending in 32-row steps.
 __device__ __forceinline__ uint16_t ext_sort_key(const bwacuda_dev_ext_job &J, int max_sc)
 {
-    const uint32_t wide = ext_fits_i16(J.qlen, J.tlen, J.h0, max_sc) ? 0u : 1u;
+    const uint32_t cls = ext_cell_class(J, max_sc);
     const uint32_t ql = J.qlen < 0 ? 0u : (J.qlen > 1023 ? 1023u : (uint32_t)J.qlen);
-    const uint32_t tb = J.tlen < 0 ? 0u : ((uint32_t)J.tlen >> 4 > 31u ? 31u : (uint32_t)J.tlen >> 4);
-    return (uint16_t)((wide << 15) | ((1023u - ql) << 5) | (31u - tb));
+    const uint32_t tb = J.tlen < 0 ? 0u : ((uint32_t)J.tlen >> 5 > 15u ? 15u : (uint32_t)J.tlen >> 5);
+    return (uint16_t)((cls << 14) | ((1023u - ql) << 4) | (15u - tb));
 }
 
 __global__ void ext_keys_kernel(const bwacuda_dev_ext_job *__restrict__ jobs, uint32_t n, int max_sc,
@@ -62,8 +69,8 @@ __global__ void ext_bucket_bounds_kernel(const uint16_t *__restrict__ keys, uint
     const ExtBucketDef d = defs[b];
     const uint32_t ql_hi = d.qhi > 1023 ? 1023u : (uint32_t)d.qhi;
     const uint32_t ql_lo = d.qlo > 1023 ? 1023u : (uint32_t)d.qlo;
-    const uint32_t key_lo = ((uint32_t)d.wide << 15) | ((1023u - ql_hi) << 5);
-    const uint32_t key_hi = ((uint32_t)d.wide << 15) | ((1023u - ql_lo) << 5) | 31u;
+    const uint32_t key_lo = ((uint32_t)d.cls << 14) | ((1023u - ql_hi) << 4);
+    const uint32_t key_hi = ((uint32_t)d.cls << 14) | ((1023u - ql_lo) << 4) | 15u;
     table[b * 4 + 0] = lower_bound16(keys, n, key_lo);
     table[b * 4 + 1] = lower_bound16(keys, n, key_hi + 1);
     table[b * 4 + 2] = 0;  // work counter
@@ -94,12 +101,51 @@ ext_persist_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *_
         if (k < stop) {
             const uint32_t jid = order[k];
             const bwacuda_dev_ext_job J = jobs[jid];
-            const bool narrow = ext_fits_i16(J.qlen, J.tlen, J.h0, P.sc.max_sc);
-            if (J.qlen < 0 || J.qlen + 1 > qcap || (!WIDE && !narrow)) {
+            const bool fits = WIDE || ext_fits_i16(J.qlen, J.tlen, J.h0, P.sc.max_sc);
+            if (J.qlen < 0 || J.qlen + 1 > qcap || !fits) {
                 atomicOr(err, ERR_RANGE);
             } else {
                 bool bad = false;
                 const bwacuda_ext_result r = ext_run_job<F, TB>(cell, qw, seq, J, P, bad, ncells);
+                if (bad) atomicOr(err, ERR_BASE);
+                out[jid] = r;
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ncells += __shfl_xor_sync(0xffffffffu, ncells, o);
+    if (lane == 0 && ncells) atomicAdd(cells_total, ncells);
+}
+
+// The same persistent loop over 8-bit pair cells.
+template <int TB>
+__global__ void __launch_bounds__(TB)
+ext_persist_u8p_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *__restrict__ jobs,
+                       const uint32_t *__restrict__ order, uint32_t *__restrict__ table,
+                       const __grid_constant__ ExtParams P, int qcap, bwacuda_ext_result *__restrict__ out,
+                       uint32_t *__restrict__ err, unsigned long long *__restrict__ cells_total)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int tid = threadIdx.x, lane = tid & 31;
+    uint32_t *cellw = reinterpret_cast<uint32_t *>(smem_raw) + tid;
+    uint32_t *qw = reinterpret_cast<uint32_t *>(smem_raw) + ((size_t)qcap / 2 + 2) * TB + tid;
+    const uint32_t start = table[0], stop = table[1];
+    uint32_t *counter = table + 2;
+    unsigned long long ncells = 0;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(counter, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0) + start;
+        if (base >= stop) break;
+        const uint32_t k = base + lane;
+        if (k < stop) {
+            const uint32_t jid = order[k];
+            const bwacuda_dev_ext_job J = jobs[jid];
+            if (J.qlen < 0 || J.qlen + 1 > qcap || !ext_fits_u8(J.qlen, J.tlen, J.h0, P.sc.max_sc)) {
+                atomicOr(err, ERR_RANGE);
+            } else {
+                bool bad = false;
+                const bwacuda_ext_result r = ext_run_job_u8p<TB>(cellw, qw, seq, J, P, bad, ncells);
                 if (bad) atomicOr(err, ERR_BASE);
                 out[jid] = r;
             }
@@ -129,6 +175,30 @@ cudaError_t launch_persist_tb(const PersistLaunch &L, const ExtBucketDef &d, uin
     return cudaGetLastError();
 }
 
+template <int TB>
+cudaError_t launch_persist_u8p_tb(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm)
+{
+    const size_t smem = ext_block_smem_u8p(d.qcap, TB);
+    if (smem > SMEM_MAX) return cudaErrorInvalidValue;
+    auto kern = ext_persist_u8p_kernel<TB>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TB, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidValue;
+    kern<<<per_sm * nsm, TB, smem, L.stream>>>(L.seq, L.jobs, L.order, table, L.P, d.qcap, L.out, L.err, L.cells);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_persist_u8p(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm, int tb)
+{
+    if (tb >= 256 && ext_block_smem_u8p(d.qcap, 256) <= SMEM_MAX) return launch_persist_u8p_tb<256>(L, d, table, nsm);
+    if (tb >= 128 && ext_block_smem_u8p(d.qcap, 128) <= SMEM_MAX) return launch_persist_u8p_tb<128>(L, d, table, nsm);
+    if (tb >= 64 && ext_block_smem_u8p(d.qcap, 64) <= SMEM_MAX) return launch_persist_u8p_tb<64>(L, d, table, nsm);
+    return launch_persist_u8p_tb<32>(L, d, table, nsm);
+}
+
 template <class F>
 cudaError_t launch_persist(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm, int tb)
 {
@@ -142,33 +212,42 @@ cudaError_t launch_persist(const PersistLaunch &L, const ExtBucketDef &d, uint32
 
 }  // namespace
 
-// Query-length buckets: cap of each class (qlen <= cap - 1), per cell width.
+// Query-length buckets: cap of each class (qlen <= cap - 1), per cell class.
+// 8-bit jobs have h0 + min(qlen, tlen) * max_sc < 256, so their queries are short.
+static const int kQcapU8[] = {33, 65, 97, 129, 161, 193, 257};
 static const int kQcapI16[] = {33, 65, 97, 129, 161, 193, 257, 385, 513, 769, 1023};
 static const int kQcapI32[] = {33, 65, 97, 129, 161, 193, 257, 385, 513, 769};
+
+static int max_qcap_of_class(int cls)
+{
+    if (cls == 0) return 257;  // bound < 256 forces min(qlen, tlen) < 256; longer queries meet short targets
+    return (int)ext_tpj_smem_limit_qcap(cls == 2);
+}
 
 int ext_bucket_defs(ExtBucketDef *defs, int max_defs)
 {
     int nb = 0;
-    for (int wide = 0; wide < 2; ++wide) {
-        const int *caps = wide ? kQcapI32 : kQcapI16;
-        const int nc = wide ? (int)(sizeof(kQcapI32) / sizeof(int)) : (int)(sizeof(kQcapI16) / sizeof(int));
+    for (int cls = 0; cls < 3; ++cls) {
+        const int *caps = cls == 0 ? kQcapU8 : (cls == 1 ? kQcapI16 : kQcapI32);
+        const int nc = cls == 0 ? (int)(sizeof(kQcapU8) / sizeof(int))
+                                : (cls == 1 ? (int)(sizeof(kQcapI16) / sizeof(int)) : (int)(sizeof(kQcapI32) / sizeof(int)));
         int lo = 0;
         for (int c = 0; c < nc && nb < max_defs; ++c) {
             ExtBucketDef d;
-            d.wide = wide;
+            d.cls = cls;
             d.qlo = lo;
             d.qhi = caps[c] - 1;
             d.qcap = caps[c];
             defs[nb++] = d;
             lo = caps[c];
         }
-        // the open-ended last class: every longer query up to the shared-memory limit
+        // the open-ended last class: every longer query up to the class's limit
         if (nb < max_defs) {
             ExtBucketDef d;
-            d.wide = wide;
+            d.cls = cls;
             d.qlo = lo;
             d.qhi = 1 << 30;
-            d.qcap = (int)ext_tpj_smem_limit_qcap(wide != 0);
+            d.qcap = cls == 0 ? (int)ext_tpj_smem_limit_qcap(false) : max_qcap_of_class(cls);
             defs[nb++] = d;
         }
     }
@@ -202,8 +281,9 @@ cudaError_t ext_sort_and_bucket(const bwacuda_dev_ext_job *jobs, size_t n, int m
 cudaError_t ext_persist_launch(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *d_bucket_table, int nsm,
                                int tb)
 {
-    return d.wide ? launch_persist<FmtI32>(L, d, d_bucket_table, nsm, tb)
-                  : launch_persist<FmtI16>(L, d, d_bucket_table, nsm, tb);
+    if (d.cls == 0) return launch_persist_u8p(L, d, d_bucket_table, nsm, tb);
+    return d.cls == 2 ? launch_persist<FmtI32>(L, d, d_bucket_table, nsm, tb)
+                      : launch_persist<FmtI16>(L, d, d_bucket_table, nsm, tb);
 }
 
 }  // namespace bwacuda

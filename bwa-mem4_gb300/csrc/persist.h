@@ -9,15 +9,15 @@
 
 namespace bwacuda {
 
-// One bucket: jobs whose cell width is `wide` and qlen in [qlo, qhi], run with
-// qcap cell columns per thread.
+// One bucket: jobs of cell class `cls` (0 = 8-bit pairs, 1 = 16-bit, 2 = 32-bit)
+// with qlen in [qlo, qhi], run with qcap cell columns per thread.
 struct ExtBucketDef {
-    int32_t wide;
+    int32_t cls;
     int32_t qlo, qhi;
     int32_t qcap;
 };
 
-constexpr int EXT_MAX_BUCKETS = 32;
+constexpr int EXT_MAX_BUCKETS = 40;
 
 struct PersistLaunch {
     const uint8_t *seq;

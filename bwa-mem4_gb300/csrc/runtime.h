@@ -122,6 +122,14 @@ int extend_device_batched(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_de
 void batched_release(bwacuda_ctx *c);
 int batched_set_block(bwacuda_ctx *c, int tb);
 
+struct BatchBufs;
+int batched_prepare(bwacuda_ctx *c);
+BatchBufs *batchbufs_create();
+void batchbufs_destroy(BatchBufs *bb);
+cudaError_t batched_enqueue(bwacuda_ctx *c, BatchBufs *bb, const uint8_t *d_seq, const bwacuda_dev_ext_job *d_jobs,
+                            size_t n, const ExtParams &P, bwacuda_ext_result *d_out, cudaStream_t s, uint32_t *err,
+                            unsigned long long *cells);
+
 // server.cu
 void server_shutdown(bwacuda_ctx *c);
 

@@ -202,6 +202,40 @@ int bwacuda_ksw_align2_device_noalloc(bwacuda_ctx *ctx, const uint8_t *d_seq,
                                       const bwacuda_scoring *sc, int minsc, int max_sc, int mode,
                                       int lanes, bwacuda_rescue_result *d_out, void *stream);
 
+/* ------------------------------------------------------------------------
+ * Serving loop.  Requests (a batch of extension or rescue jobs each) are
+ * submitted at any time and admitted to the GPU as space in a fixed HBM budget
+ * frees up; admitted requests that share a scoring run together in the next
+ * "wave" (continuous batching) and several waves overlap on the device.
+ * Results stay in device memory until bwacuda_server_wait copies them out.
+ * The job arrays and base buffers passed to a submit call must stay valid
+ * until its wait returns.  No counterpart in the reference, which has no
+ * device; each result equals what the batch calls return for the same jobs.
+ * ------------------------------------------------------------------------ */
+typedef struct {
+    uint64_t hbm_budget_bytes; /* device arena for admitted requests (0 = 4 GiB); a pinned host arena of the same size mirrors it */
+    int32_t max_waves;         /* waves in flight (0 = 3) */
+    int32_t max_requests;      /* requests held (queued, running or unread; 0 = 4096) */
+} bwacuda_server_config;
+
+int bwacuda_server_start(bwacuda_ctx *ctx, const bwacuda_server_config *cfg);
+/* Finishes waves in flight; requests not yet launched end with BWACUDA_EBUSY. */
+int bwacuda_server_stop(bwacuda_ctx *ctx);
+/* BWACUDA_EBUSY when max_requests are held; BWACUDA_ENOMEM when the request
+ * alone exceeds the HBM budget. */
+int bwacuda_server_submit_extend(bwacuda_ctx *ctx, const bwacuda_ext_job *jobs, size_t n,
+                                 const bwacuda_scoring *sc, int w, int end_bonus, int zdrop,
+                                 uint64_t *req_id);
+int bwacuda_server_submit_rescue(bwacuda_ctx *ctx, const bwacuda_rescue_job *jobs, size_t n,
+                                 const bwacuda_scoring *sc, int minsc, int max_sc, uint64_t *req_id);
+/* Waits up to timeout_us (0 = poll: BWACUDA_EAGAIN if not done; < 0 = no
+ * limit, BWACUDA_ETIMEOUT when the limit passes), copies the n results into
+ * out (bwacuda_ext_result or bwacuda_rescue_result) and releases the request.
+ * latency_ns (may be NULL) receives submit-to-completion time. */
+int bwacuda_server_wait(bwacuda_ctx *ctx, uint64_t req_id, void *out, int64_t timeout_us,
+                        int64_t *latency_ns);
+int bwacuda_server_stats(bwacuda_ctx *ctx, uint64_t *served_jobs, uint64_t *waves, uint64_t *queued);
+
 /* Counters accumulated since the context was created (or last reset). */
 typedef struct {
     uint64_t ext_jobs, ext_cells;       /* cells = sum over rows of (end - beg) */
