@@ -8,8 +8,12 @@ and descriptors), so no flush is needed between steps.
 
 value    : GCUPS of the batched path (length-sorted buckets, persistent
            kernels, graph replay) with the inputs resident in HBM.
-e2e      : the same metric through bwacuda_extend_batch with HOST buffers
-           (packing, host->device and device->host copies inside the timed region).
+e2e      : the same metric through bwacuda_extend_batch with HOST buffers, every
+           transfer inside the timed region.  Two routes are timed: "device-gather"
+           (GPU kernels load the caller's job array and sequence slices from host
+           memory over NVLink-C2C and store the results into the caller's array)
+           and "host-pack" (worker threads pack pinned staging, copy-engine
+           transfers); the headline is device-gather where the device supports it.
 plain    : the plain path (one launch per 256k-job chunk, caller order).
 GCUPS    = extension cells (one inner-loop iteration of ksw_extend2, counted by
            the kernels themselves and equal to the oracle's count) / time.
@@ -319,20 +323,46 @@ def main():
             if rc != B.OK:
                 raise B.BwaCudaError(rc, "bwacuda_extend_batch")
 
-        call()  # warm-up (pinned staging allocation)
-        ctx.reset_stats()
-        barrier()
-        t0 = time.perf_counter()
-        esteps = max(1, min(args.steps, 5))
-        for _ in range(esteps):
-            call()
-        barrier()
-        et = max_over_ranks(time.perf_counter() - t0)
-        ste = ctx.stats()
-        e2e = {"value": round(ste["ext_cells"] / esteps * world / (et / esteps) / 1e9, 2), "unit": "GCUPS",
-               "h2d_bytes_per_step": int(ste["h2d_bytes"] / esteps), "d2h_bytes_per_step": int(ste["d2h_bytes"] / esteps),
-               "ms_per_step": round(et / esteps * 1e3, 2), "bit_identical_to_device_path":
-                   bool(np.array_equal(host_out, batched_out))}
+        seq_bytes = int(js.qlen.astype(np.int64).sum() + js.tlen.astype(np.int64).sum())
+
+        def timed_route(gather):
+            ctx.set_option(B.OPT_HOST_GATHER, gather)
+            host_out[:] = 0
+            call()  # warm-up (staging allocation)
+            ctx.reset_stats()
+            barrier()
+            t0 = time.perf_counter()
+            esteps = max(1, min(args.steps, 5))
+            for _ in range(esteps):
+                call()
+            barrier()
+            et = max_over_ranks(time.perf_counter() - t0)
+            ste = ctx.stats()
+            r = {"value": round(ste["ext_cells"] / esteps * world / (et / esteps) / 1e9, 2), "unit": "GCUPS",
+                 "ms_per_step": round(et / esteps * 1e3, 2),
+                 "bit_identical_to_device_path": bool(np.array_equal(host_out, batched_out))}
+            if ste["h2d_bytes"]:
+                r["h2d_bytes_per_step"] = int(ste["h2d_bytes"] / esteps)
+                r["d2h_bytes_per_step"] = int(ste["d2h_bytes"] / esteps)
+            else:
+                # device gather: the GPU loads the job array and the sequence slices from host memory
+                # and stores the results into the caller's array (no copy engine involved)
+                r["h2d_bytes_per_step"] = n * B.EXT_JOB.itemsize + seq_bytes
+                r["d2h_bytes_per_step"] = n * B.EXT_RES.itemsize
+            return r
+
+        routes = {}
+        try:
+            routes["device-gather"] = timed_route(B.GATHER_DEVICE)
+        except B.BwaCudaError as err:
+            if err.code != B.EUNSUPPORTED:
+                raise
+        routes["host-pack"] = timed_route(B.GATHER_HOST)
+        ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_AUTO)
+        best = "device-gather" if "device-gather" in routes else "host-pack"
+        e2e = dict(routes[best])
+        e2e["route"] = best
+        e2e["routes"] = {k: {"value": v["value"], "ms_per_step": v["ms_per_step"]} for k, v in routes.items()}
 
     # roofline: integer-ALU bound (no tensor cores, about 0.03 B of HBM per cell)
     pk, kind = peaks()

@@ -20,6 +20,8 @@ SYNTH_PATH = os.path.join(_PKG, "libbwasynth.so")
 OK, EINVAL, EBASE, ENOMEM, ECUDA, ETIMEOUT, EUNSUPPORTED, EBUSY, EAGAIN = 0, -1, -2, -3, -4, -5, -6, -7, -8
 OPT_EXT_PATH, OPT_CHUNK_JOBS, OPT_GRAPHS, OPT_PERSIST_BLOCK, OPT_RESCUE_KERNEL = 1, 2, 3, 4, 5
 RESCUE_AUTO, RESCUE_TPJ = 0, 1
+OPT_HOST_GATHER = 6
+GATHER_AUTO, GATHER_HOST, GATHER_DEVICE = 0, 1, 2
 PATH_PLAIN, PATH_BATCHED = 0, 1
 INT_MAX = 2**31 - 1
 

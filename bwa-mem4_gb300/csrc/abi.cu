@@ -162,21 +162,7 @@ int validate_scoring(int m, const int8_t *mat, int o_del, int e_del, int o_ins, 
 // bwa-mem's 8/16-bit bin label, crates/bwa-neon/src/batched.rs:817-865 (statistics only).
 int ext_bin_label(int qlen, int tlen, int h0, int m, const int8_t *mat)
 {
-    const int a = mat[0], mm = mat[1], npen = mat[m - 1];
-    bool uniform = m >= 2;
-    for (int i = 0; i < m && uniform; ++i)
-        for (int j = 0; j < m; ++j) {
-            int want = (i == m - 1 || j == m - 1) ? npen : (i == j ? a : mm);
-            if (mat[i * m + j] != want) { uniform = false; break; }
-        }
-    if (!uniform) return 2;
-    int mx = mat[0];
-    for (int k = 0; k < m * m; ++k) mx = mat[k] > mx ? mat[k] : mx;
-    int head = std::max(std::max(-(int)mat[1], -(int)mat[m - 1]), 0) + mx;
-    long long bound = (long long)h0 + (long long)std::min(qlen, tlen) * std::max(mx, 0);
-    if (qlen < 256 && tlen < 256 && bound + head < 256) return 0;
-    if (qlen < 32768 && tlen < 32768 && bound + head < 32768) return 1;
-    return 2;
+    return bin_label(bin_rule(m, mat), qlen, tlen, h0);
 }
 
 }  // namespace bwacuda
@@ -194,6 +180,9 @@ static int ctx_init(bwacuda_ctx *c)
         if ((e = cudaEventCreateWithFlags(&c->slot[s].done, cudaEventDisableTiming)) != cudaSuccess) return cuda_status(e);
     }
     c->stream = c->slot[0].stream;
+    int pageable = 0;
+    if ((e = cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, c->device)) != cudaSuccess) return cuda_status(e);
+    c->pageable_access = pageable != 0;
     if ((e = c->d_misc.ensure(4096)) != cudaSuccess) return cuda_status(e);
     if ((e = c->h_misc.ensure(4096)) != cudaSuccess) return cuda_status(e);
     if ((e = cudaMemset(c->d_misc.p, 0, 4096)) != cudaSuccess) return cuda_status(e);
@@ -237,6 +226,7 @@ extern "C" void bwacuda_ctx_destroy(bwacuda_ctx *c)
     c->h_misc.release();
     c->d_dev_aux.release();
     c->d_dev_scratch.release();
+    ats_release(c);
     batched_release(c);
     delete c;
 }
@@ -260,6 +250,11 @@ extern "C" int bwacuda_set_option(bwacuda_ctx *c, int option, int64_t value)
         return BWACUDA_OK;
     case BWACUDA_OPT_GRAPHS:
         c->use_graphs = value != 0;
+        return BWACUDA_OK;
+    case BWACUDA_OPT_HOST_GATHER:
+        if (value != BWACUDA_GATHER_AUTO && value != BWACUDA_GATHER_HOST && value != BWACUDA_GATHER_DEVICE)
+            return BWACUDA_EINVAL;
+        c->host_gather = (int)value;
         return BWACUDA_OK;
     case BWACUDA_OPT_PERSIST_BLOCK:
         if (value != 32 && value != 64 && value != 128 && value != 256) return BWACUDA_EINVAL;
@@ -349,6 +344,7 @@ ExtChunk pack_ext_chunk(bwacuda_ctx *c, Slot &sl, const bwacuda_ext_job *jobs, s
     std::vector<int> part_qmax(P, 0), part_bad(P, 0);
     std::vector<std::vector<uint32_t>> part_wide(P);
     std::vector<uint64_t> part_bins((size_t)P * 3, 0);
+    const BinRule br = bin_rule(m, mat);
     auto range = [&](int id, size_t &b, size_t &e) {
         b = cn * (size_t)id / P;
         e = cn * (size_t)(id + 1) / P;
@@ -369,7 +365,7 @@ ExtChunk pack_ext_chunk(bwacuda_ctx *c, Slot &sl, const bwacuda_ext_job *jobs, s
             qm = std::max(qm, J.qlen);
             long long bound = (long long)J.h0 + (long long)std::min(J.qlen, J.tlen) * std::max(max_sc, 0);
             if (bound >= 32768) part_wide[id].push_back((uint32_t)k);
-            part_bins[(size_t)id * 3 + ext_bin_label(J.qlen, J.tlen, J.h0, m, mat)]++;
+            part_bins[(size_t)id * 3 + bin_label(br, J.qlen, J.tlen, J.h0)]++;
         }
         part_bytes[id] = sum;
         part_qmax[id] = qm;
@@ -539,7 +535,12 @@ int extend_batch_host(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int
     P.sc = make_scoring(m, mat, o_del, e_del, o_ins, e_ins);
     P.end_bonus = end_bonus;
     P.zdrop = zdrop;
-    if (c->ext_path == BWACUDA_PATH_BATCHED) return extend_batch_host_batched(c, jobs, n, m, mat, P, w, out);
+    if (c->ext_path == BWACUDA_PATH_BATCHED) {
+        const bool device_gather = c->host_gather == BWACUDA_GATHER_DEVICE ||
+                                   (c->host_gather == BWACUDA_GATHER_AUTO && c->pageable_access);
+        if (device_gather) return extend_batch_ats(c, jobs, n, m, mat, P, w, out);
+        return extend_batch_host_batched(c, jobs, n, m, mat, P, w, out);
+    }
     return extend_host_pipeline(c, jobs, n, m, mat, P, w, out,
                                 [c](int, const ExtChunkInfo &I, cudaStream_t s) { return run_plain(c, I, s); });
 }

@@ -186,6 +186,9 @@ int extend_device_batched(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_de
 }
 
 int batched_prepare(bwacuda_ctx *c) { return batched_init(c); }
+BatchBufs *batched_slot_bufs(bwacuda_ctx *c, int slot) { return &c->batched->bufs[slot & 1]; }
+int batched_nsm(bwacuda_ctx *c) { return c->batched->nsm; }
+int batched_bucket_count(bwacuda_ctx *c) { return c->batched->nb; }
 
 static cudaError_t bufs_streams(BatchBufs &bb)
 {

@@ -72,4 +72,44 @@ __host__ __device__ inline int clamp_band(int w, int qlen, int max_sc, int end_b
     return w;
 }
 
+// bwa-mem's 8/16-bit bin label of an extension job, the rule of
+// crates/bwa-neon/src/batched.rs:817-865 split in two: bin_rule() summarises
+// the matrix once per call, bin_label() classifies one job (statistics only).
+struct BinRule {
+    int32_t uniform;  // matrix is match / mismatch / N-penalty shaped
+    int32_t mx;       // largest entry
+    int32_t head;     // max(-mismatch, -N penalty, 0) + mx
+};
+
+inline BinRule bin_rule(int m, const int8_t *mat)
+{
+    BinRule r;
+    const int a = mat[0], mm = mat[1], npen = mat[m - 1];
+    bool uniform = m >= 2;
+    for (int i = 0; i < m && uniform; ++i)
+        for (int j = 0; j < m; ++j) {
+            int want = (i == m - 1 || j == m - 1) ? npen : (i == j ? a : mm);
+            if (mat[i * m + j] != want) { uniform = false; break; }
+        }
+    int mx = mat[0];
+    for (int k = 0; k < m * m; ++k) mx = mat[k] > mx ? mat[k] : mx;
+    int head = -(int)mat[1];
+    if (-(int)mat[m - 1] > head) head = -(int)mat[m - 1];
+    if (head < 0) head = 0;
+    r.uniform = uniform;
+    r.mx = mx;
+    r.head = head + mx;
+    return r;
+}
+
+__host__ __device__ inline int bin_label(const BinRule &r, int qlen, int tlen, int h0)
+{
+    if (!r.uniform) return 2;
+    const int mn = qlen < tlen ? qlen : tlen;
+    const long long bound = (long long)h0 + (long long)mn * (r.mx > 0 ? r.mx : 0);
+    if (qlen < 256 && tlen < 256 && bound + r.head < 256) return 0;
+    if (qlen < 32768 && tlen < 32768 && bound + r.head < 32768) return 1;
+    return 2;
+}
+
 }  // namespace bwacuda

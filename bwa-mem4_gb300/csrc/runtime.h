@@ -62,6 +62,7 @@ struct Slot {
 
 struct BatchedState;  // batched path (batched.cu)
 struct ServerState;   // serving loop (server.cu)
+struct AtsState;      // device-side gather of host buffers (ats.cu)
 
 int cuda_status(cudaError_t e);
 Scoring make_scoring(int m, const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins);
@@ -86,7 +87,10 @@ struct bwacuda_ctx {
     bool use_graphs = true;
     int rescue_kernel = BWACUDA_RESCUE_AUTO;
     size_t chunk_jobs = 262144;
+    int host_gather = BWACUDA_GATHER_AUTO;
+    bool pageable_access = false;  // the device reads pageable host memory (host page tables)
     bwacuda::BatchedState *batched = nullptr;
+    bwacuda::AtsState *ats = nullptr;
     bwacuda::ServerState *server = nullptr;
 };
 
@@ -129,6 +133,14 @@ void batchbufs_destroy(BatchBufs *bb);
 cudaError_t batched_enqueue(bwacuda_ctx *c, BatchBufs *bb, const uint8_t *d_seq, const bwacuda_dev_ext_job *d_jobs,
                             size_t n, const ExtParams &P, bwacuda_ext_result *d_out, cudaStream_t s, uint32_t *err,
                             unsigned long long *cells);
+BatchBufs *batched_slot_bufs(bwacuda_ctx *c, int slot);  // work buffers of host-pipeline slot 0 or 1
+int batched_nsm(bwacuda_ctx *c);
+int batched_bucket_count(bwacuda_ctx *c);
+
+// ats.cu
+int extend_batch_ats(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int m, const int8_t *mat,
+                     const ExtParams &P, int w, bwacuda_ext_result *out);
+void ats_release(bwacuda_ctx *c);
 
 // server.cu
 void server_shutdown(bwacuda_ctx *c);

@@ -106,6 +106,18 @@ typedef struct bwacuda_ctx bwacuda_ctx;
 #define BWACUDA_OPT_RESCUE_KERNEL 5
 #define BWACUDA_RESCUE_AUTO 0
 #define BWACUDA_RESCUE_TPJ 1
+/* How host-buffer extension batches on the batched path reach the device.
+ * DEVICE: GPU kernels read the caller's job array and sequence slices through
+ * the host page tables (devices reporting cudaDevAttrPageableMemoryAccess, e.g.
+ * Grace-Blackwell over NVLink-C2C) and write results straight into out[].
+ * HOST: worker threads pack into pinned staging, then H2D/D2H copies.
+ * AUTO (default): DEVICE where the device supports it, else HOST.  Asking for
+ * DEVICE on a device without pageable access makes the calls fail with
+ * BWACUDA_EUNSUPPORTED. */
+#define BWACUDA_OPT_HOST_GATHER 6
+#define BWACUDA_GATHER_AUTO 0
+#define BWACUDA_GATHER_HOST 1
+#define BWACUDA_GATHER_DEVICE 2
 
 int bwacuda_ctx_create(int device, bwacuda_ctx **out);
 void bwacuda_ctx_destroy(bwacuda_ctx *ctx);

@@ -63,3 +63,14 @@ def test_synthetic_workloads_are_deterministic():
     digest = hashlib.sha256(js.seq.tobytes() + js.h0.tobytes()).hexdigest()[:16]
     from golden_digests import SYNTH_EXT2_2000_SEED11
     assert digest == SYNTH_EXT2_2000_SEED11
+
+
+def test_header_constants_match_binding():
+    src = open(os.path.join(ROOT, "include", "bwacuda.h")).read()
+    defs = dict((k, int(v)) for k, v in re.findall(r"#define BWACUDA_([A-Z0-9_]+) (-?\d+)", src))
+    for name, val in defs.items():
+        if hasattr(B, name):
+            assert getattr(B, name) == val, name
+    for name in ("OPT_EXT_PATH", "OPT_CHUNK_JOBS", "OPT_GRAPHS", "OPT_PERSIST_BLOCK", "OPT_RESCUE_KERNEL",
+                 "OPT_HOST_GATHER", "GATHER_AUTO", "GATHER_HOST", "GATHER_DEVICE", "PATH_PLAIN", "PATH_BATCHED"):
+        assert getattr(B, name) == defs[name], name

@@ -20,11 +20,39 @@ def _tuples(res):
     return [tuple(int(r[f]) for f in FIELDS) for r in res]
 
 
+_GATHER_OK = {}
+
+
+def _device_gather_supported(ctx):
+    """Whether this device reads pageable host memory (the device-gather route)."""
+    if ctx.h not in _GATHER_OK:
+        ctx.set_option(B.OPT_EXT_PATH, B.PATH_BATCHED)
+        ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_DEVICE)
+        try:
+            ctx.extend_batch(B.JobSet.from_lists([[0, 1, 2]], [[0, 1, 2]], [5]))
+            _GATHER_OK[ctx.h] = True
+        except B.BwaCudaError as e:
+            assert e.code == B.EUNSUPPORTED
+            _GATHER_OK[ctx.h] = False
+        finally:
+            ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_AUTO)
+    return _GATHER_OK[ctx.h]
+
+
+def _set_path(ctx, path):
+    """path: PATH_PLAIN / PATH_BATCHED (host-buffer route AUTO) or a (path, gather) pair."""
+    path, gather = path if isinstance(path, tuple) else (path, B.GATHER_AUTO)
+    if gather == B.GATHER_DEVICE and not _device_gather_supported(ctx):
+        pytest.skip("device cannot read pageable host memory")
+    ctx.set_option(B.OPT_EXT_PATH, path)
+    ctx.set_option(B.OPT_HOST_GATHER, gather)
+
+
 def _check_batch(ctx, qs, ts, h0s, a=1, b=4, o_del=6, e_del=1, o_ins=6, e_ins=1, w=100, end_bonus=5,
                  zdrop=100, path=B.PATH_PLAIN, what=""):
     mat = oracle.scmat(a, b)
     js = B.JobSet.from_lists(qs, ts, h0s, w)
-    ctx.set_option(B.OPT_EXT_PATH, path)
+    _set_path(ctx, path)
     got = _tuples(ctx.extend_batch(js, mat, o_del, e_del, o_ins, e_ins, w, end_bonus, zdrop))
     want = [oracle.extend2(q, t, h, mat, o_del, e_del, o_ins, e_ins, w, end_bonus, zdrop)
             for q, t, h in zip(qs, ts, h0s)]
@@ -63,7 +91,7 @@ def test_reference_batch_streams(ctx, stream):
 
 
 def _check_jobset(ctx, js, w=100, path=B.PATH_PLAIN, **kw):
-    ctx.set_option(B.OPT_EXT_PATH, path)
+    _set_path(ctx, path)
     # per-job band: group by w (the host ABI shares w per call, as the reference does)
     want, _ = oracle.extend_batch(js, **kw)
     for wv in np.unique(js.w):
@@ -74,7 +102,10 @@ def _check_jobset(ctx, js, w=100, path=B.PATH_PLAIN, **kw):
         assert len(bad) == 0, f"{len(bad)} mismatches, first job {idx[bad[0]]}: {got[bad[0]]} vs {want[idx[bad[0]]]}"
 
 
-PATHS = [pytest.param(B.PATH_PLAIN, id="plain"), pytest.param(B.PATH_BATCHED, id="batched")]
+# host-buffer routes: plain kernels; batched kernels fed by host packing or by the device's own gather
+PATHS = [pytest.param(B.PATH_PLAIN, id="plain"),
+         pytest.param((B.PATH_BATCHED, B.GATHER_HOST), id="batched-hostpack"),
+         pytest.param((B.PATH_BATCHED, B.GATHER_DEVICE), id="batched-devgather")]
 
 
 @pytest.mark.parametrize("path", PATHS)
@@ -109,9 +140,12 @@ def test_chunked_pipeline_boundaries(ctx):
     # chunks smaller than the batch exercise both staging slots and the tail chunk
     js = B.synth_ext(3, 5000, seed=12)
     want, _ = oracle.extend_batch(js)
+    routes = [B.PATH_PLAIN, (B.PATH_BATCHED, B.GATHER_HOST)]
+    if _device_gather_supported(ctx):
+        routes.append((B.PATH_BATCHED, B.GATHER_DEVICE))
     try:
-        for path in (B.PATH_PLAIN, B.PATH_BATCHED):
-            ctx.set_option(B.OPT_EXT_PATH, path)
+        for path in routes:
+            _set_path(ctx, path)
             ctx.set_option(B.OPT_CHUNK_JOBS, 777)
             for wv in np.unique(js.w):
                 idx = np.nonzero(js.w == wv)[0]
@@ -119,6 +153,7 @@ def test_chunked_pipeline_boundaries(ctx):
                 assert np.array_equal(got, want[idx])
     finally:
         ctx.set_option(B.OPT_CHUNK_JOBS, 262144)
+        ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_AUTO)
 
 
 def _device_run(ctx, js, path, reps=1):
@@ -136,7 +171,10 @@ def _device_run(ctx, js, path, reps=1):
     return outs
 
 
-@pytest.mark.parametrize("path", PATHS)
+DEVICE_PATHS = [pytest.param(B.PATH_PLAIN, id="plain"), pytest.param(B.PATH_BATCHED, id="batched")]
+
+
+@pytest.mark.parametrize("path", DEVICE_PATHS)
 def test_device_entry_equals_oracle(ctx, path):
     js = B.synth_ext(3, 50000, seed=3)
     want, _ = oracle.extend_batch(js)
@@ -198,21 +236,80 @@ def test_non_uniform_matrix_is_exact(ctx):
     assert got == want
 
 
-def test_invalid_inputs_fail_loudly(ctx):
-    js = B.JobSet.from_lists([[0, 1, 5]], [[0, 1, 2]], [10])
-    with pytest.raises(B.BwaCudaError) as e:
-        ctx.extend_batch(js)
-    assert e.value.code == B.EBASE
-    js = B.JobSet.from_lists([[0, 1]], [[0, 1, 2]], [0])
-    with pytest.raises(B.BwaCudaError) as e:
-        ctx.extend_batch(js)
-    assert e.value.code == B.EINVAL
-    js = B.JobSet.from_lists([[0, 1]], [[0, 1, 2]], [3])
-    with pytest.raises(B.BwaCudaError) as e:
-        ctx.extend_batch(js, e_del=0)
-    assert e.value.code == B.EINVAL
-    # the context stays usable after an error
-    assert ctx.extend([0, 1, 2], [0, 1, 2], 5) == oracle.extend2([0, 1, 2], [0, 1, 2], 5)
+def _raw_extend(ctx, jobs, out, m=5, mat=None):
+    mat = np.ascontiguousarray(oracle.scmat() if mat is None else mat, dtype=np.int8)
+    return B.lib().bwacuda_extend_batch(ctx.h, jobs.ctypes.data, len(jobs), m, mat.ctypes.data, 6, 1, 6, 1, 100, 5,
+                                        100, out.ctypes.data)
+
+
+@pytest.mark.parametrize("path", PATHS)
+def test_invalid_inputs_fail_loudly(ctx, path):
+    _set_path(ctx, path)
+    try:
+        js = B.JobSet.from_lists([[0, 1, 5]], [[0, 1, 2]], [10])
+        with pytest.raises(B.BwaCudaError) as e:
+            ctx.extend_batch(js)
+        assert e.value.code == B.EBASE
+        js = B.JobSet.from_lists([[0, 1]], [[0, 1, 2]], [0])
+        with pytest.raises(B.BwaCudaError) as e:
+            ctx.extend_batch(js)
+        assert e.value.code == B.EINVAL
+        js = B.JobSet.from_lists([[0, 1]], [[0, 1, 2]], [3])
+        with pytest.raises(B.BwaCudaError) as e:
+            ctx.extend_batch(js, e_del=0)
+        assert e.value.code == B.EINVAL
+        # null sequence pointers with non-zero lengths, and negative lengths, among valid jobs:
+        # rejected before anything reads them
+        js = B.synth_ext(2, 3000, seed=21)
+        out = np.zeros(len(js), dtype=B.EXT_RES)
+        for field, val in (("query", 0), ("target", 0), ("qlen", -1), ("tlen", -5)):
+            jobs = ctx._host_jobs(js, B.EXT_JOB)
+            jobs[1234][field] = val
+            assert _raw_extend(ctx, jobs, out) == B.EINVAL, field
+        # null pointers are fine where the length is zero
+        jobs = ctx._host_jobs(js, B.EXT_JOB)
+        jobs[7]["qlen"], jobs[7]["query"] = 0, 0
+        jobs[8]["tlen"], jobs[8]["target"] = 0, 0
+        assert _raw_extend(ctx, jobs, out) == B.OK
+        t7 = js.seq[js.t_off[7]:js.t_off[7] + js.tlen[7]]
+        q8 = js.seq[js.q_off[8]:js.q_off[8] + js.qlen[8]]
+        assert _tuples(out[7:9]) == [oracle.extend2([], t7, int(js.h0[7])), oracle.extend2(q8, [], int(js.h0[8]))]
+        # the context stays usable after an error
+        assert ctx.extend([0, 1, 2], [0, 1, 2], 5) == oracle.extend2([0, 1, 2], [0, 1, 2], 5)
+        want, _ = oracle.extend_batch(js)
+        assert np.array_equal(ctx.extend_batch(js), want)
+    finally:
+        ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_AUTO)
+
+
+def test_device_gather_equals_host_packing(ctx):
+    # the two feeds of the batched kernels agree on results, cell counts and bin statistics,
+    # and the device gather writes every result word of the caller's array
+    if not _device_gather_supported(ctx):
+        pytest.skip("device cannot read pageable host memory")
+    js = B.synth_ext(3, 40000, seed=22)
+    runs = {}
+    try:
+        for gather in (B.GATHER_HOST, B.GATHER_DEVICE):
+            _set_path(ctx, (B.PATH_BATCHED, gather))
+            for chunk in (262144, 4099):
+                ctx.set_option(B.OPT_CHUNK_JOBS, chunk)
+                sub = js.take(np.nonzero(js.w == 100)[0])
+                jobs = ctx._host_jobs(sub, B.EXT_JOB)
+                out = np.full(len(sub), -7, dtype=B.EXT_RES)
+                ctx.reset_stats()
+                assert _raw_extend(ctx, jobs, out) == B.OK
+                st = ctx.stats()
+                runs[(gather, chunk)] = (out, {k: st[k] for k in ("ext_jobs", "ext_cells", "ext_bin_u8",
+                                                                  "ext_bin_i16", "ext_bin_i32")})
+    finally:
+        ctx.set_option(B.OPT_CHUNK_JOBS, 262144)
+        ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_AUTO)
+    want, _ = oracle.extend_batch(sub)
+    for key, (out, st) in runs.items():
+        assert np.array_equal(out, want), key
+        assert st == runs[(B.GATHER_HOST, 262144)][1], key
+    assert runs[(B.GATHER_HOST, 262144)][1]["ext_bin_u8"] > 0
 
 
 def test_cell_counter_matches_oracle(ctx):
