@@ -43,6 +43,19 @@ __device__ __forceinline__ bool job_ok(const bwacuda_ext_job &J)
            (J.tlen == 0 || J.target != nullptr);
 }
 
+// Slices are copied as whole aligned 16-byte words: a slice of len bytes at
+// host address src covers words [src >> 4, (src + len - 1) >> 4], and lands at
+// a 16-byte aligned HBM base plus (src & 15), so every word maps to one aligned
+// word of HBM.  The bytes of a covering word outside the slice lie in the same
+// page as bytes of the slice (a 16-byte word never straddles a page), so the
+// widened reads touch only mapped memory; in HBM they land in the slice's own
+// reserve.
+__device__ __forceinline__ uint32_t slice_words(const uint8_t *src, int len)
+{
+    const uint64_t a = reinterpret_cast<uint64_t>(src);
+    return len > 0 ? (uint32_t)(((a + (uint64_t)len - 1) >> 4) - (a >> 4) + 1) : 0u;
+}
+
 __global__ void ats_lengths_kernel(const bwacuda_ext_job *__restrict__ hjobs, uint32_t n, BinRule br,
                                    uint64_t *__restrict__ sizes, uint32_t *__restrict__ flags)
 {
@@ -52,7 +65,8 @@ __global__ void ats_lengths_kernel(const bwacuda_ext_job *__restrict__ hjobs, ui
         const bool ok = job_ok(J);
         bad |= !ok;
         if (ok) bins[bin_label(br, J.qlen, J.tlen, J.h0)]++;
-        sizes[k] = ok ? (uint64_t)J.qlen + (uint64_t)J.tlen : 0u;
+        // reserve, in bytes (a multiple of 16, so every job's base stays aligned)
+        sizes[k] = ok ? 16ull * (slice_words(J.query, J.qlen) + slice_words(J.target, J.tlen)) : 0u;
     }
     // every thread of the warp reaches this point
     bad = __reduce_or_sync(0xffffffffu, bad);
@@ -68,9 +82,11 @@ __global__ void ats_lengths_kernel(const bwacuda_ext_job *__restrict__ hjobs, ui
     }
 }
 
-// One warp per job.  Each lane keeps four byte loads in flight (128 bytes per
-// warp step); lane 0 writes the descriptor.  An invalid job becomes an empty
-// one (qlen = tlen = 0, h0 = 1) whose result is discarded by the error return.
+// A warp takes 32 consecutive jobs: lane i loads job i's descriptor (one
+// coalesced read of the caller's array) and writes its device descriptor; then
+// the warp copies the 32 jobs one after the other, lane l moving words l,
+// l + 32, ... of the job's query words followed by its target words.  An invalid
+// job becomes an empty one (qlen = tlen = 0, h0 = 1); the call then fails.
 __global__ void __launch_bounds__(256) ats_gather_kernel(const bwacuda_ext_job *__restrict__ hjobs, uint32_t n,
                                                          const uint64_t *__restrict__ offs, int w,
                                                          uint8_t *__restrict__ seq,
@@ -79,34 +95,40 @@ __global__ void __launch_bounds__(256) ats_gather_kernel(const bwacuda_ext_job *
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t k = warp; k < n; k += nwarps) {
-        const bwacuda_ext_job J = hjobs[k];
-        const bool ok = job_ok(J);
-        const uint64_t base = offs[k];
-        const int ql = ok ? J.qlen : 0, tl = ok ? J.tlen : 0;
-        const int len = ql + tl;
-        for (int x0 = 0; x0 < len; x0 += 128) {
-            uint8_t v[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int x = x0 + u * 32 + (int)lane;
-                v[u] = x < ql ? J.query[x] : (x < len ? J.target[x - ql] : 0u);
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int x = x0 + u * 32 + (int)lane;
-                if (x < len) seq[base + (uint64_t)x] = v[u];
-            }
-        }
-        if (lane == 0) {
+    for (uint32_t k0 = warp * 32; k0 < n; k0 += nwarps * 32) {
+        const uint32_t k = k0 + lane;
+        uint64_t qa = 0, ta = 0, base = 0;
+        uint32_t qw = 0, tw = 0;
+        if (k < n) {
+            const bwacuda_ext_job J = hjobs[k];
+            const bool ok = job_ok(J);
+            base = offs[k];
+            qa = reinterpret_cast<uint64_t>(J.query);
+            ta = reinterpret_cast<uint64_t>(J.target);
+            qw = ok ? slice_words(J.query, J.qlen) : 0u;
+            tw = ok ? slice_words(J.target, J.tlen) : 0u;
             bwacuda_dev_ext_job D;
-            D.q_off = base;
-            D.t_off = base + (uint64_t)ql;
-            D.qlen = ql;
-            D.tlen = tl;
+            D.q_off = base + (qa & 15);
+            D.t_off = base + 16ull * qw + (ta & 15);
+            D.qlen = ok ? J.qlen : 0;
+            D.tlen = ok ? J.tlen : 0;
             D.h0 = ok ? J.h0 : 1;
             D.w = w;
             djobs[k] = D;
+        }
+        const uint32_t cnt = min(32u, n - k0);
+        for (uint32_t j = 0; j < cnt; ++j) {
+            const uint64_t jqa = __shfl_sync(0xffffffffu, qa, j) & ~15ull;
+            const uint64_t jta = __shfl_sync(0xffffffffu, ta, j) & ~15ull;
+            const uint64_t jb = __shfl_sync(0xffffffffu, base, j);
+            const uint32_t jqw = __shfl_sync(0xffffffffu, qw, j);
+            const uint32_t jtw = __shfl_sync(0xffffffffu, tw, j);
+            uint4 *dst = reinterpret_cast<uint4 *>(seq + jb);
+            for (uint32_t x = lane; x < jqw + jtw; x += 32) {
+                const uint4 *src = x < jqw ? reinterpret_cast<const uint4 *>(jqa) + x
+                                           : reinterpret_cast<const uint4 *>(jta) + (x - jqw);
+                dst[x] = *src;
+            }
         }
     }
 }
@@ -194,7 +216,7 @@ cudaError_t ats_enqueue_chunk(bwacuda_ctx *c, int si, const bwacuda_ext_job *hj,
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
     const uint64_t total = *static_cast<const uint64_t *>(S.h_total.p);
     if ((e = S.seq.ensure(total + 16)) != cudaSuccess) return e;
-    grid = (uint32_t)std::min<size_t>((cn + 7) / 8, (size_t)nsm * 8);
+    grid = (uint32_t)std::min<size_t>((cn + 255) / 256, (size_t)nsm * 8);
     ats_gather_kernel<<<grid, 256, 0, s>>>(hj, (uint32_t)cn, offs, w, static_cast<uint8_t *>(S.seq.p),
                                           static_cast<bwacuda_dev_ext_job *>(S.djobs.p));
     if ((e = cudaGetLastError()) != cudaSuccess) return e;

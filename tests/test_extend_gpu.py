@@ -25,18 +25,18 @@ _GATHER_OK = {}
 
 def _device_gather_supported(ctx):
     """Whether this device reads pageable host memory (the device-gather route)."""
-    if ctx.h not in _GATHER_OK:
+    if id(ctx) not in _GATHER_OK:
         ctx.set_option(B.OPT_EXT_PATH, B.PATH_BATCHED)
         ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_DEVICE)
         try:
             ctx.extend_batch(B.JobSet.from_lists([[0, 1, 2]], [[0, 1, 2]], [5]))
-            _GATHER_OK[ctx.h] = True
+            _GATHER_OK[id(ctx)] = True
         except B.BwaCudaError as e:
             assert e.code == B.EUNSUPPORTED
-            _GATHER_OK[ctx.h] = False
+            _GATHER_OK[id(ctx)] = False
         finally:
             ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_AUTO)
-    return _GATHER_OK[ctx.h]
+    return _GATHER_OK[id(ctx)]
 
 
 def _set_path(ctx, path):
