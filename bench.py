@@ -15,6 +15,11 @@ e2e      : the same metric through bwacuda_extend_batch with HOST buffers, every
            and "host-pack" (worker threads pack pinned staging, copy-engine
            transfers); the headline is device-gather where the device supports it.
 plain    : the plain path (one launch per 256k-job chunk, caller order).
+configs  : the mixed-length extension workload (32M jobs, per-job bands) and
+           mate rescue (2M jobs), device-resident.
+served   : the serving loop replaying Poisson arrivals of mixed extension and
+           rescue requests, p50/p99 latency and jobs/s against a FIFO of
+           synchronous plain-path calls on the same arrivals.
 GCUPS    = extension cells (one inner-loop iteration of ksw_extend2, counted by
            the kernels themselves and equal to the oracle's count) / time.
 
@@ -31,6 +36,8 @@ import subprocess
 import sys
 import threading
 import time
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "bwa-mem4_gb300")
@@ -52,9 +59,244 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-chunk", type=int, default=1 << 20, help="jobs per pipelined chunk of the host-buffer call")
     ap.add_argument("--no-graphs", action="store_true", help="enqueue the batched path every step (profiling)")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving-loop measurement")
+    ap.add_argument("--no-configs", action="store_true", help="skip the mixed-length and rescue workloads")
+    ap.add_argument("--mixed-jobs", type=int, default=32 * 1024 * 1024)
+    ap.add_argument("--rescue-jobs", type=int, default=2 * 1024 * 1024)
+    ap.add_argument("--serve-rates", default="100,500,2000", help="Poisson arrival rates (requests/s)")
+    ap.add_argument("--serve-requests", type=int, default=600, help="requests per arrival rate")
     ap.add_argument("--case", choices=["ext-batched", "ext-plain", "rescue"],
                     help="profiling case: run the small workload twice through one path, no timing")
     return ap.parse_args()
+
+
+# ---------------------------------------------------------------- serving (continuous batching)
+
+SERVE_EXT_MAX, SERVE_RES_MAX, SERVE_MIN = 262144, 65536, 1000
+
+
+class ServePools:
+    """Job pools the requests are windows of, with their caller-side job arrays built once."""
+
+    def __init__(self, B, seed):
+        self.B = B
+        self.ext = {2: B.synth_ext(2, 1 << 21, seed=seed + 1), 3: B.synth_ext(3, 1 << 21, seed=seed + 2)}
+        self.res = B.synth_rescue(1 << 18, seed=seed + 3)
+        self.ext_jobs = {k: B.Context._host_jobs(js, B.EXT_JOB) for k, js in self.ext.items()}
+        self.res_jobs = B.Context._host_jobs(self.res, B.RES_JOB, minsc=20, endsc=0)
+
+
+def serve_trace(rate, count, seed):
+    """Poisson arrivals; 80% extension requests (read-pair or mixed-length pools, one band per
+    request), 20% rescue; sizes log-uniform in [1k, 256k] jobs (rescue [1k, 64k])."""
+    rng = np.random.default_rng(seed)
+    t, trace = 0.0, []
+    for _ in range(count):
+        t += rng.exponential(1.0 / rate)
+        if rng.random() < 0.2:
+            n = int(np.exp(rng.uniform(np.log(SERVE_MIN), np.log(SERVE_RES_MAX))))
+            trace.append((t, "rescue", 0, int(rng.integers(0, (1 << 18) - n)), n, 0))
+        else:
+            cfg = int(rng.choice([2, 3]))
+            n = int(np.exp(rng.uniform(np.log(SERVE_MIN), np.log(SERVE_EXT_MAX))))
+            w = 100 if cfg == 2 else int(rng.choice([50, 100, 200]))
+            trace.append((t, "extend", cfg, int(rng.integers(0, (1 << 21) - n)), n, w))
+    return trace
+
+
+def _out_layout(B, trace):
+    offs, tot = [], 0
+    for _, kind, _, _, n, _ in trace:
+        offs.append(tot)
+        tot += n * (B.EXT_RES.itemsize if kind == "extend" else B.ALN_RES.itemsize)
+    return offs, tot
+
+
+def run_served(B, pools, trace, budget):
+    """Real-time replay through the serving loop: a submitter thread submits each request at its
+    arrival time; the caller's thread waits on them in order.  Latency = completion - arrival."""
+    import ctypes as C
+
+    L = B.lib()
+    ctx = B.Context(0)
+    ctx.server_start(hbm_budget_bytes=budget, max_waves=3, max_requests=8192)
+    sc = ctx.scoring()
+    offs, tot = _out_layout(B, trace)
+    out = np.zeros(max(tot, 1), np.uint8)
+    rids, submit_t = [None] * len(trace), [0.0] * len(trace)
+    ready = threading.Semaphore(0)
+    err = []
+
+    def submitter(t0):
+        for i, (ta, kind, cfg, start, n, w) in enumerate(trace):
+            d = t0 + ta - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            rid = C.c_uint64()
+            submit_t[i] = time.perf_counter() - t0
+            if kind == "extend":
+                jp = pools.ext_jobs[cfg].ctypes.data + start * B.EXT_JOB.itemsize
+                rc = L.bwacuda_server_submit_extend(ctx.h, C.c_void_p(jp), n, C.byref(sc), w, 5, 100, C.byref(rid))
+            else:
+                jp = pools.res_jobs.ctypes.data + start * B.RES_JOB.itemsize
+                rc = L.bwacuda_server_submit_rescue(ctx.h, C.c_void_p(jp), n, C.byref(sc), 20, 1, C.byref(rid))
+            if rc != B.OK:
+                err.append(rc)
+            rids[i] = rid.value
+            ready.release()
+
+    lat = np.zeros(len(trace))
+    t0 = time.perf_counter() + 0.05
+    th = threading.Thread(target=submitter, args=(t0,), daemon=True)
+    th.start()
+    last = 0.0
+    for i in range(len(trace)):
+        ready.acquire()
+        if err:
+            break
+        ns = C.c_int64()
+        rc = L.bwacuda_server_wait(ctx.h, rids[i], C.c_void_p(out.ctypes.data + offs[i]), -1, C.byref(ns))
+        if rc != B.OK:
+            err.append(rc)
+            break
+        done = submit_t[i] + ns.value * 1e-9
+        lat[i] = done - trace[i][0]
+        last = max(last, done)
+    th.join()
+    ctx.server_stop()
+    ctx.close()
+    if err:
+        raise B.BwaCudaError(err[0], "serving replay")
+    return lat, last, out
+
+
+def run_plain_fifo(B, pools, trace):
+    """The same arrivals served one request at a time in arrival order by synchronous plain-path
+    calls (host packing, one launch per 256k-job chunk).  Latency = completion - arrival."""
+    import ctypes as C
+
+    L = B.lib()
+    ctx = B.Context(0)
+    ctx.set_option(B.OPT_EXT_PATH, B.PATH_PLAIN)
+    ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_HOST)
+    mat = B.scmat()
+    offs, tot = _out_layout(B, trace)
+    out = np.zeros(max(tot, 1), np.uint8)
+    lat = np.zeros(len(trace))
+    t0 = time.perf_counter()
+    now = 0.0
+    for i, (ta, kind, cfg, start, n, w) in enumerate(trace):
+        now = time.perf_counter() - t0
+        if ta > now:
+            time.sleep(ta - now)
+        op = C.c_void_p(out.ctypes.data + offs[i])
+        if kind == "extend":
+            jp = C.c_void_p(pools.ext_jobs[cfg].ctypes.data + start * B.EXT_JOB.itemsize)
+            rc = L.bwacuda_extend_batch(ctx.h, jp, n, 5, C.c_void_p(mat.ctypes.data), 6, 1, 6, 1, w, 5, 100, op)
+        else:
+            jp = C.c_void_p(pools.res_jobs.ctypes.data + start * B.RES_JOB.itemsize)
+            rc = L.bwacuda_ksw_align2_batch(ctx.h, jp, n, 5, C.c_void_p(mat.ctypes.data), 6, 1, 6, 1, 20, 1, op)
+        if rc != B.OK:
+            raise B.BwaCudaError(rc, "plain replay")
+        now = time.perf_counter() - t0
+        lat[i] = now - ta
+    ctx.close()
+    return lat, now, out
+
+
+def serve_bench(B, rates, count, seed=5, budget=8 << 30):
+    pools = ServePools(B, seed)
+    # warm both sides (allocations, module loading) on a short trace
+    warm = serve_trace(1000.0, 8, seed + 99)
+    run_served(B, pools, warm, budget)
+    run_plain_fifo(B, pools, warm)
+    rows = []
+    for rate in rates:
+        trace = serve_trace(rate, count, seed + int(rate))
+        jobs = sum(r[4] for r in trace)
+        ls, end_s, out_s = run_served(B, pools, trace, budget)
+        lp, end_p, out_p = run_plain_fifo(B, pools, trace)
+        pct = lambda a, q: round(float(np.percentile(a, q)) * 1e3, 3)
+        rows.append({"rate_req_s": rate, "requests": len(trace), "jobs": jobs,
+                     "served": {"p50_ms": pct(ls, 50), "p99_ms": pct(ls, 99), "jobs_per_s": round(jobs / end_s, 1)},
+                     "plain": {"p50_ms": pct(lp, 50), "p99_ms": pct(lp, 99), "jobs_per_s": round(jobs / end_p, 1)},
+                     "identical": bool(np.array_equal(out_s, out_p))})
+    return {"workload": "Poisson arrivals; 80% extension requests (read-pair or mixed-length/band pools), 20% "
+                        "rescue (150 bp vs 750 bp windows, minsc 20); request sizes log-uniform 1k-256k jobs "
+                        "(rescue 1k-64k); latency = completion - arrival",
+            "hbm_budget_bytes": budget, "plain": "FIFO, one synchronous plain-path call per request",
+            "rates": rows}
+
+
+def other_configs(args, B, ctx, st, barrier, max_over_ranks, world, rank):
+    """The mixed-length extension workload (one batched call over all jobs, per-job bands) and
+    the mate-rescue workload, both device-resident, each timed with CUDA events over 3 steps."""
+    import torch
+
+    res = {}
+    stream = st.cuda_stream
+
+    def timed(fn, steps=3, warmup=1):
+        for _ in range(warmup):
+            fn()
+        ctx.sync()
+        ctx.reset_stats()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(steps):
+            fn()
+        e1.record(st)
+        ctx.sync()
+        barrier()
+        return max_over_ranks(e0.elapsed_time(e1)) / steps, ctx.stats()
+
+    # mixed read lengths 100/150/250 bp, w in {50, 100, 200} per job, h0 up to 250
+    n = args.mixed_jobs
+    js = B.synth_ext(3, n, seed=2000 + rank)
+    d_seq = torch.from_numpy(js.seq).cuda()
+    d_jobs = torch.from_numpy(js.dev_ext_jobs().view(np.uint8)).cuda()
+    d_out = torch.zeros(n * 24, dtype=torch.uint8, device="cuda")
+    ms, stt = timed(lambda: ctx.extend_device(d_seq.data_ptr(), d_jobs.data_ptr(), n, d_out.data_ptr(),
+                                              path=B.PATH_BATCHED, stream=stream))
+    batched = d_out.cpu().numpy().copy()
+    cells = stt["ext_cells"] / 3
+    # the plain path on the same jobs (one pass, 256k-job launches) must give the same results
+    ctx.reset_stats()
+    t0 = time.perf_counter()
+    for c0 in range(0, n, 262144):
+        cn = min(262144, n - c0)
+        ctx.extend_device(d_seq.data_ptr(), d_jobs.data_ptr() + c0 * 32, cn, d_out.data_ptr() + c0 * 24,
+                          path=B.PATH_PLAIN, stream=stream)
+    ctx.sync()
+    tp = time.perf_counter() - t0
+    res["mixed_lengths"] = {
+        "workload": f"ksw_extend2, {n} jobs per GPU: reads 30% 100 / 50% 150 / 20% 250 bp, per-job w in "
+                    "{50, 100, 200}, h0 <= 250; one batched call",
+        "value": round(cells * world / (ms / 1e3) / 1e9, 2), "unit": "GCUPS", "ms_per_step": round(ms, 2),
+        "plain": {"value": round(ctx.stats()["ext_cells"] * world / tp / 1e9, 2), "unit": "GCUPS"},
+        "plain_equals_batched": bool(np.array_equal(batched, d_out.cpu().numpy()))}
+    del d_seq, d_jobs, d_out, js
+    torch.cuda.empty_cache()
+
+    # mate rescue: 150 bp query vs 750 bp window, minsc 20
+    n = args.rescue_jobs
+    js = B.synth_rescue(n, seed=3000 + rank)
+    d_seq = torch.from_numpy(js.seq).cuda()
+    d_jobs = torch.from_numpy(js.dev_res_jobs().view(np.uint8)).cuda()
+    d_out = torch.zeros(n * 28, dtype=torch.uint8, device="cuda")
+    rcells = int((js.qlen.astype(np.int64) * js.tlen.astype(np.int64)).sum())
+    ms, stt = timed(lambda: ctx.ksw_align2_device(d_seq.data_ptr(), d_jobs.data_ptr(), n, d_out.data_ptr(),
+                                                  minsc=20, max_sc=1, mode=0, stream=stream))
+    res["rescue"] = {
+        "workload": f"batched_ksw_align2, {n} jobs per GPU: 150 bp query (0.5% error) vs 750 bp window, "
+                    "10% without the true mate, minsc 20",
+        "value": round(rcells * world / (ms / 1e3) / 1e9, 2), "unit": "GCUPS",
+        "cells": "qlen x tlen of the forward pass per job (padding and reverse pass not counted)",
+        "ms_per_step": round(ms, 2), "jobs_per_s": round(n * world / (ms / 1e3), 1)}
+    del d_seq, d_jobs, d_out
+    torch.cuda.empty_cache()
+    return res
 
 
 def dist_env():
@@ -394,6 +636,11 @@ def main():
     }
     if e2e:
         line["e2e"] = e2e
+    if not args.no_configs:
+        line["configs"] = other_configs(args, B, ctx, st, barrier, max_over_ranks, world, rank)
+    if not args.no_serve and world == 1:
+        rates = [float(r) for r in args.serve_rates.split(",") if r]
+        line["served"] = serve_bench(B, rates, args.serve_requests)
     if rank == 0:
         # CPU baseline: the oracle port on a bounded sample of the same workload
         sample = js.head(min(n, 400_000))
