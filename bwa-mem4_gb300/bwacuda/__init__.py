@@ -22,6 +22,7 @@ OPT_EXT_PATH, OPT_CHUNK_JOBS, OPT_GRAPHS, OPT_PERSIST_BLOCK, OPT_RESCUE_KERNEL =
 RESCUE_AUTO, RESCUE_TPJ = 0, 1
 OPT_HOST_GATHER = 6
 GATHER_AUTO, GATHER_HOST, GATHER_DEVICE = 0, 1, 2
+OPT_GRAB, OPT_BUCKET_STEP, OPT_RESCUE_LANES = 7, 8, 9
 PATH_PLAIN, PATH_BATCHED = 0, 1
 INT_MAX = 2**31 - 1
 
@@ -56,6 +57,15 @@ class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_waves", C.c_int32), ("max_requests", C.c_int32)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("persist_block", C.c_int32), ("grab", C.c_int32), ("bucket_step", C.c_int32),
+                ("rescue_lanes", C.c_int32), ("rescue_kernel", C.c_int32), ("candidates", C.c_int32),
+                ("ext_gcups", C.c_double), ("rescue_gcups", C.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 class Stats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in STAT_FIELDS]
 
@@ -67,7 +77,8 @@ EXPORTS = ("bwacuda_ctx_create", "bwacuda_ctx_destroy", "bwacuda_set_option", "b
            "bwacuda_ksw_align2_device", "bwacuda_ctx_sync", "bwacuda_get_stats", "bwacuda_reset_stats",
            "bwacuda_ksw_align2_device_noalloc", "bwacuda_server_start", "bwacuda_server_stop",
            "bwacuda_server_submit_extend", "bwacuda_server_submit_rescue", "bwacuda_server_wait",
-           "bwacuda_server_stats")
+           "bwacuda_server_stats", "bwacuda_measure_alu_peak", "bwacuda_get_tuning", "bwacuda_autotune_extend",
+           "bwacuda_autotune_rescue")
 
 _lib = None
 _synth = None
@@ -90,6 +101,10 @@ def lib():
     L = C.CDLL(LIB_PATH)
     vp, I, sz = C.c_void_p, C.c_int, C.c_size_t
     L.bwacuda_ctx_create.argtypes = [I, C.POINTER(vp)]
+    L.bwacuda_measure_alu_peak.argtypes = [vp, C.POINTER(C.c_double)]
+    L.bwacuda_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
+    L.bwacuda_autotune_extend.argtypes = [vp, vp, vp, sz, C.POINTER(Scoring), I, I, sz, C.POINTER(Tuning)]
+    L.bwacuda_autotune_rescue.argtypes = [vp, vp, vp, sz, C.POINTER(Scoring), I, I, sz, C.POINTER(Tuning)]
     L.bwacuda_ctx_destroy.argtypes = [vp]
     L.bwacuda_ctx_destroy.restype = None
     L.bwacuda_set_option.argtypes = [vp, I, C.c_int64]
@@ -441,3 +456,32 @@ class Context:
 
     def sync(self):
         self._check(lib().bwacuda_ctx_sync(self.h), "bwacuda_ctx_sync")
+
+    def tuning(self) -> dict:
+        t = Tuning()
+        self._check(lib().bwacuda_get_tuning(self.h, C.byref(t)), "bwacuda_get_tuning")
+        return t.as_dict()
+
+    def autotune_extend(self, d_seq, d_jobs, n, sc: Scoring = None, end_bonus=5, zdrop=100, sample=0) -> dict:
+        """Pick the batched extension launch shape on a sample of a device-resident batch."""
+        t = Tuning()
+        sc = sc or self.scoring()
+        rc = lib().bwacuda_autotune_extend(self.h, C.c_void_p(d_seq), C.c_void_p(d_jobs), n, C.byref(sc), end_bonus,
+                                           zdrop, sample, C.byref(t))
+        self._check(rc, "bwacuda_autotune_extend")
+        return t.as_dict()
+
+    def autotune_rescue(self, d_seq, d_jobs, n, sc: Scoring = None, minsc=19, max_sc=1, sample=0) -> dict:
+        """Pick the rescue kernel (wavefront lanes per job, or thread-per-job) on a sample."""
+        t = Tuning()
+        sc = sc or self.scoring()
+        rc = lib().bwacuda_autotune_rescue(self.h, C.c_void_p(d_seq), C.c_void_p(d_jobs), n, C.byref(sc), minsc,
+                                           max_sc, sample, C.byref(t))
+        self._check(rc, "bwacuda_autotune_rescue")
+        return t.as_dict()
+
+    def measure_alu_peak(self) -> float:
+        """Measured integer ALU-pipe rate of the device, 1e9 fused add-max ops per second."""
+        g = C.c_double()
+        self._check(lib().bwacuda_measure_alu_peak(self.h, C.byref(g)), "bwacuda_measure_alu_peak")
+        return g.value

@@ -259,6 +259,17 @@ extern "C" int bwacuda_set_option(bwacuda_ctx *c, int option, int64_t value)
     case BWACUDA_OPT_PERSIST_BLOCK:
         if (value != 32 && value != 64 && value != 128 && value != 256) return BWACUDA_EINVAL;
         return batched_set_block(c, (int)value);
+    case BWACUDA_OPT_GRAB:
+        if (value != 1 && value != 2 && value != 4) return BWACUDA_EINVAL;
+        return batched_set_grab(c, (int)value);
+    case BWACUDA_OPT_BUCKET_STEP:
+        if (value != 16 && value != 32 && value != 64) return BWACUDA_EINVAL;
+        if (cudaSetDevice(c->device) != cudaSuccess) return BWACUDA_ECUDA;
+        return batched_set_bucket_step(c, (int)value);
+    case BWACUDA_OPT_RESCUE_LANES:
+        if (value != 8 && value != 16 && value != 32) return BWACUDA_EINVAL;
+        c->rescue_lanes = (int)value;
+        return BWACUDA_OK;
     default:
         return BWACUDA_EINVAL;
     }
@@ -579,7 +590,7 @@ namespace bwacuda {
 cudaError_t rescue_narrow_launch(bwacuda_ctx *c, const RescueLaunch &L)
 {
     if (c->rescue_kernel == BWACUDA_RESCUE_AUTO && L.qcap <= rescue_wf_max_qpad() && L.only_wide != 2)
-        return rescue_wf_launch(L, L.qcap);
+        return rescue_wf_launch(L, L.qcap, c->rescue_lanes);
     return rescue_tpj_launch(L, false);
 }
 
@@ -939,6 +950,16 @@ extern "C" int bwacuda_ksw_align2_device(bwacuda_ctx *c, const uint8_t *d_seq,
 {
     if (!c || !scp) return BWACUDA_EINVAL;
     std::lock_guard<std::mutex> g(c->mu);
+    return bwacuda::ksw_align2_device_locked(c, d_seq, d_jobs, n, scp, minsc, max_sc, mode, lanes, d_out, stream);
+}
+
+namespace bwacuda {
+
+// bwacuda_ksw_align2_device with the context lock already held.
+int ksw_align2_device_locked(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_dev_rescue_job *d_jobs, size_t n,
+                             const bwacuda_scoring *scp, int minsc, int max_sc, int mode, int lanes,
+                             bwacuda_rescue_result *d_out, void *stream)
+{
     int rc = validate_scoring(scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
     if (rc) return rc;
     if (max_sc < 1 || (mode != 0 && mode != 1) || (lanes != 0 && lanes != 8 && lanes != 16)) return BWACUDA_EINVAL;
@@ -999,6 +1020,8 @@ extern "C" int bwacuda_ksw_align2_device(bwacuda_ctx *c, const uint8_t *d_seq,
     c->dev_pending_stream = s;
     return BWACUDA_OK;
 }
+
+}  // namespace bwacuda
 
 extern "C" int bwacuda_ctx_sync(bwacuda_ctx *c)
 {

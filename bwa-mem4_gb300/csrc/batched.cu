@@ -24,7 +24,7 @@ struct BatchBufs {
     cudaGraphExec_t graph = nullptr;
     const void *g_seq = nullptr, *g_jobs = nullptr, *g_out = nullptr;
     const void *g_bufs[6] = {};  // work buffers the graph was captured with
-    int g_tb = 0;
+    uint64_t g_gen = 0;          // tuning generation the graph was captured with
     size_t g_n = 0;
     cudaStream_t g_stream = nullptr;
     ExtParams g_P{};
@@ -33,7 +33,11 @@ struct BatchBufs {
 struct BatchedState {
     int nsm = 0;
     int nb = 0;
-    int tb = 128;  // block size picked by the autotuner (bwacuda_autotune)
+    // tuning (set by bwacuda_autotune_extend or the options); gen changes with every setting
+    int tb = 128;    // threads per block of the persistent kernels
+    int grab = 1;    // 32-job rounds per work-counter grab
+    int step = 32;   // query-length bucket width below 257 columns
+    uint64_t gen = 1;
     ExtBucketDef defs[EXT_MAX_BUCKETS];
     DevBuf d_defs;
     BatchBufs bufs[3];  // [0], [1]: host-pipeline slots; [2]: device-resident calls
@@ -46,7 +50,7 @@ static int batched_init(bwacuda_ctx *c)
     if (!B) return BWACUDA_ENOMEM;
     cudaError_t e = cudaDeviceGetAttribute(&B->nsm, cudaDevAttrMultiProcessorCount, c->device);
     if (e != cudaSuccess) { delete B; return cuda_status(e); }
-    B->nb = ext_bucket_defs(B->defs, EXT_MAX_BUCKETS);
+    B->nb = ext_bucket_defs(B->defs, EXT_MAX_BUCKETS, B->step);
     if ((e = B->d_defs.ensure(sizeof(B->defs))) != cudaSuccess) { delete B; return cuda_status(e); }
     if ((e = cudaMemcpy(B->d_defs.p, B->defs, sizeof(ExtBucketDef) * B->nb, cudaMemcpyHostToDevice)) != cudaSuccess) {
         delete B;
@@ -92,7 +96,42 @@ int batched_set_block(bwacuda_ctx *c, int tb)
     int rc = batched_init(c);
     if (rc) return rc;
     c->batched->tb = tb;
+    c->batched->gen++;
     return BWACUDA_OK;
+}
+
+int batched_set_grab(bwacuda_ctx *c, int grab)
+{
+    int rc = batched_init(c);
+    if (rc) return rc;
+    c->batched->grab = grab;
+    c->batched->gen++;
+    return BWACUDA_OK;
+}
+
+// New bucket boundaries; waits for in-flight batches (they read the old table).
+int batched_set_bucket_step(bwacuda_ctx *c, int step)
+{
+    int rc = batched_init(c);
+    if (rc) return rc;
+    BatchedState *B = c->batched;
+    if (B->step == step) return BWACUDA_OK;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_status(e);
+    B->step = step;
+    B->nb = ext_bucket_defs(B->defs, EXT_MAX_BUCKETS, step);
+    if ((e = cudaMemcpy(B->d_defs.p, B->defs, sizeof(ExtBucketDef) * B->nb, cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cuda_status(e);
+    B->gen++;
+    return BWACUDA_OK;
+}
+
+void batched_get_tuning(bwacuda_ctx *c, int *tb, int *grab, int *step)
+{
+    BatchedState *B = c->batched;
+    *tb = B ? B->tb : 128;
+    *grab = B ? B->grab : 1;
+    *step = B ? B->step : 32;
 }
 
 static cudaError_t ensure_bufs(BatchBufs &bb, size_t n)
@@ -129,6 +168,7 @@ static cudaError_t enqueue_batched(bwacuda_ctx *c, BatchBufs &bb, const uint8_t 
     L.out = d_out;
     L.err = err ? err : reinterpret_cast<uint32_t *>(c->d_misc.p);
     L.cells = cells ? cells : reinterpret_cast<unsigned long long *>((char *)c->d_misc.p + 8);
+    L.grab = B->grab;
     // largest buckets first: they hold the long jobs
     for (int b = B->nb - 1, k = 0; b >= 0; --b, ++k) {
         L.stream = bb.fan[k % FAN];
@@ -154,7 +194,7 @@ int extend_device_batched(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_de
     // scoring and stream); otherwise capture a new one.
     const void *bufs[6] = {bb.keys_in.p, bb.keys_out.p, bb.idx_in.p, bb.idx_out.p, bb.tmp.p, bb.table.p};
     const bool same = bb.graph && bb.g_seq == d_seq && bb.g_jobs == d_jobs && bb.g_out == d_out && bb.g_n == n &&
-                      bb.g_stream == s && bb.g_tb == c->batched->tb && memcmp(bb.g_bufs, bufs, sizeof(bufs)) == 0 &&
+                      bb.g_stream == s && bb.g_gen == c->batched->gen && memcmp(bb.g_bufs, bufs, sizeof(bufs)) == 0 &&
                       memcmp(&bb.g_P, &P, sizeof(P)) == 0;
     if (!same && c->use_graphs) {
         if (bb.graph) {
@@ -171,7 +211,7 @@ int extend_device_batched(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_de
         cudaGraphDestroy(g);
         if (e != cudaSuccess) { bb.graph = nullptr; return cuda_status(e); }
         bb.g_seq = d_seq; bb.g_jobs = d_jobs; bb.g_out = d_out; bb.g_n = n; bb.g_stream = s; bb.g_P = P;
-        bb.g_tb = c->batched->tb;
+        bb.g_gen = c->batched->gen;
         memcpy(bb.g_bufs, bufs, sizeof(bufs));
     }
     if (c->use_graphs) {

@@ -80,7 +80,7 @@ template <class F, int TB>
 __global__ void __launch_bounds__(TB)
 ext_persist_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *__restrict__ jobs,
                    const uint32_t *__restrict__ order, uint32_t *__restrict__ table,
-                   const __grid_constant__ ExtParams P, int qcap, bwacuda_ext_result *__restrict__ out,
+                   const __grid_constant__ ExtParams P, int qcap, int grab, bwacuda_ext_result *__restrict__ out,
                    uint32_t *__restrict__ err, unsigned long long *__restrict__ cells_total)
 {
     using CellT = typename F::T;
@@ -94,10 +94,11 @@ ext_persist_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *_
     unsigned long long ncells = 0;
     for (;;) {
         uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(counter, 32u);
+        if (lane == 0) base = atomicAdd(counter, 32u * (uint32_t)grab);
         base = __shfl_sync(0xffffffffu, base, 0) + start;
         if (base >= stop) break;
-        const uint32_t k = base + lane;
+        for (int g = 0; g < grab; ++g) {
+        const uint32_t k = base + 32u * (uint32_t)g + lane;
         if (k < stop) {
             const uint32_t jid = order[k];
             const bwacuda_dev_ext_job J = jobs[jid];
@@ -111,6 +112,7 @@ ext_persist_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *_
                 out[jid] = r;
             }
         }
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) ncells += __shfl_xor_sync(0xffffffffu, ncells, o);
@@ -122,7 +124,7 @@ template <int TB>
 __global__ void __launch_bounds__(TB)
 ext_persist_u8p_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *__restrict__ jobs,
                        const uint32_t *__restrict__ order, uint32_t *__restrict__ table,
-                       const __grid_constant__ ExtParams P, int qcap, bwacuda_ext_result *__restrict__ out,
+                       const __grid_constant__ ExtParams P, int qcap, int grab, bwacuda_ext_result *__restrict__ out,
                        uint32_t *__restrict__ err, unsigned long long *__restrict__ cells_total)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -134,10 +136,11 @@ ext_persist_u8p_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_jo
     unsigned long long ncells = 0;
     for (;;) {
         uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(counter, 32u);
+        if (lane == 0) base = atomicAdd(counter, 32u * (uint32_t)grab);
         base = __shfl_sync(0xffffffffu, base, 0) + start;
         if (base >= stop) break;
-        const uint32_t k = base + lane;
+        for (int g = 0; g < grab; ++g) {
+        const uint32_t k = base + 32u * (uint32_t)g + lane;
         if (k < stop) {
             const uint32_t jid = order[k];
             const bwacuda_dev_ext_job J = jobs[jid];
@@ -149,6 +152,7 @@ ext_persist_u8p_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_jo
                 if (bad) atomicOr(err, ERR_BASE);
                 out[jid] = r;
             }
+        }
         }
     }
 #pragma unroll
@@ -171,7 +175,7 @@ cudaError_t launch_persist_tb(const PersistLaunch &L, const ExtBucketDef &d, uin
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidValue;
     const int grid = per_sm * nsm;
-    kern<<<grid, TB, smem, L.stream>>>(L.seq, L.jobs, L.order, table, L.P, d.qcap, L.out, L.err, L.cells);
+    kern<<<grid, TB, smem, L.stream>>>(L.seq, L.jobs, L.order, table, L.P, d.qcap, L.grab, L.out, L.err, L.cells);
     return cudaGetLastError();
 }
 
@@ -187,7 +191,8 @@ cudaError_t launch_persist_u8p_tb(const PersistLaunch &L, const ExtBucketDef &d,
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TB, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidValue;
-    kern<<<per_sm * nsm, TB, smem, L.stream>>>(L.seq, L.jobs, L.order, table, L.P, d.qcap, L.out, L.err, L.cells);
+    kern<<<per_sm * nsm, TB, smem, L.stream>>>(L.seq, L.jobs, L.order, table, L.P, d.qcap, L.grab, L.out, L.err,
+                                               L.cells);
     return cudaGetLastError();
 }
 
@@ -212,11 +217,11 @@ cudaError_t launch_persist(const PersistLaunch &L, const ExtBucketDef &d, uint32
 
 }  // namespace
 
-// Query-length buckets: cap of each class (qlen <= cap - 1), per cell class.
-// 8-bit jobs have h0 + min(qlen, tlen) * max_sc < 256, so their queries are short.
-static const int kQcapU8[] = {33, 65, 97, 129, 161, 193, 257};
-static const int kQcapI16[] = {33, 65, 97, 129, 161, 193, 257, 385, 513, 769, 1023};
-static const int kQcapI32[] = {33, 65, 97, 129, 161, 193, 257, 385, 513, 769};
+// Query-length buckets of each cell class.  Below 257 columns the caps step by
+// `step` (16, 32 or 64: the autotuner's bucket granularity); longer queries
+// (16/32-bit cells only: an 8-bit job has h0 + min(qlen, tlen) * max_sc < 256)
+// take fixed caps; the last bucket of a class is open-ended.
+static const int kQcapLong[] = {385, 513, 769, 1023};
 
 static int max_qcap_of_class(int cls)
 {
@@ -224,13 +229,15 @@ static int max_qcap_of_class(int cls)
     return (int)ext_tpj_smem_limit_qcap(cls == 2);
 }
 
-int ext_bucket_defs(ExtBucketDef *defs, int max_defs)
+int ext_bucket_defs(ExtBucketDef *defs, int max_defs, int step)
 {
+    if (step != 16 && step != 32 && step != 64) step = 32;
     int nb = 0;
     for (int cls = 0; cls < 3; ++cls) {
-        const int *caps = cls == 0 ? kQcapU8 : (cls == 1 ? kQcapI16 : kQcapI32);
-        const int nc = cls == 0 ? (int)(sizeof(kQcapU8) / sizeof(int))
-                                : (cls == 1 ? (int)(sizeof(kQcapI16) / sizeof(int)) : (int)(sizeof(kQcapI32) / sizeof(int)));
+        int caps[32], nc = 0;
+        for (int c = step + 1; c <= 257; c += step) caps[nc++] = c;
+        const int nlong = cls == 0 ? 0 : (cls == 1 ? 4 : 3);  // 32-bit cells: up to 769 columns in one block
+        for (int k = 0; k < nlong; ++k) caps[nc++] = kQcapLong[k];
         int lo = 0;
         for (int c = 0; c < nc && nb < max_defs; ++c) {
             ExtBucketDef d;
@@ -274,7 +281,7 @@ cudaError_t ext_sort_and_bucket(const bwacuda_dev_ext_job *jobs, size_t n, int m
     cudaError_t e = cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys_in, keys_out, idx_in, idx_out, (int)n, 0,
                                                     16, s);
     if (e != cudaSuccess) return e;
-    ext_bucket_bounds_kernel<<<1, 64, 0, s>>>(keys_out, (uint32_t)n, d_defs, nb, d_table);
+    ext_bucket_bounds_kernel<<<1, EXT_MAX_BUCKETS, 0, s>>>(keys_out, (uint32_t)n, d_defs, nb, d_table);
     return cudaGetLastError();
 }
 

@@ -51,7 +51,7 @@ struct RescueLaunch {
 };
 
 cudaError_t rescue_tpj_launch(const RescueLaunch &L, bool wide);
-cudaError_t rescue_wf_launch(const RescueLaunch &L, int qcap);
+cudaError_t rescue_wf_launch(const RescueLaunch &L, int qcap, int lanes);  // lanes per job: 8, 16 or 32
 int rescue_wf_max_qpad();
 size_t rescue_tpj_smem_limit_qcap(bool wide);
 // Entries the suboptimal tracker may need for a target of tlen rows.

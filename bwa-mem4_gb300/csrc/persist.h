@@ -17,7 +17,7 @@ struct ExtBucketDef {
     int32_t qcap;
 };
 
-constexpr int EXT_MAX_BUCKETS = 40;
+constexpr int EXT_MAX_BUCKETS = 64;  // one thread each in the bucket-bounds kernel
 
 struct PersistLaunch {
     const uint8_t *seq;
@@ -27,10 +27,11 @@ struct PersistLaunch {
     bwacuda_ext_result *out;
     uint32_t *err;
     unsigned long long *cells;
+    int grab;  // 32-job rounds a warp takes per work-counter grab
     cudaStream_t stream;
 };
 
-int ext_bucket_defs(ExtBucketDef *defs, int max_defs);
+int ext_bucket_defs(ExtBucketDef *defs, int max_defs, int step);
 size_t ext_sort_temp_bytes(size_t n);
 // keys + radix sort + bucket bounds; d_table holds 4 words per bucket
 // (start, end, work counter, spare).

@@ -86,6 +86,10 @@ struct bwacuda_ctx {
     int ext_path = BWACUDA_PATH_PLAIN;
     bool use_graphs = true;
     int rescue_kernel = BWACUDA_RESCUE_AUTO;
+    int rescue_lanes = 16;  // lanes per job of the register wavefront (8, 16, 32)
+    int tune_candidates = 0;        // last autotune call
+    double tuned_ext_gcups = 0.0;   // best candidates' rates on their samples
+    double tuned_rescue_gcups = 0.0;
     size_t chunk_jobs = 262144;
     int host_gather = BWACUDA_GATHER_AUTO;
     bool pageable_access = false;  // the device reads pageable host memory (host page tables)
@@ -125,6 +129,9 @@ int extend_device_batched(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_de
                           const ExtParams &P, bwacuda_ext_result *d_out, cudaStream_t s);
 void batched_release(bwacuda_ctx *c);
 int batched_set_block(bwacuda_ctx *c, int tb);
+int batched_set_grab(bwacuda_ctx *c, int grab);
+int batched_set_bucket_step(bwacuda_ctx *c, int step);
+void batched_get_tuning(bwacuda_ctx *c, int *tb, int *grab, int *step);
 
 struct BatchBufs;
 int batched_prepare(bwacuda_ctx *c);
@@ -144,5 +151,10 @@ void ats_release(bwacuda_ctx *c);
 
 // server.cu
 void server_shutdown(bwacuda_ctx *c);
+
+// abi.cu (device-resident rescue with the context lock held)
+int ksw_align2_device_locked(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_dev_rescue_job *d_jobs, size_t n,
+                             const bwacuda_scoring *scp, int minsc, int max_sc, int mode, int lanes,
+                             bwacuda_rescue_result *d_out, void *stream);
 
 }  // namespace bwacuda

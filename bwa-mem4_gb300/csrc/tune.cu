@@ -1,0 +1,248 @@
+// tune.cu -- the autotuner: picks the launch shape of the batched extension
+// path (threads per block, 32-job rounds per work grab, length-bucket width)
+// and of the rescue kernels (wavefront lanes per job, or thread-per-job) by
+// timing every candidate with CUDA events on a strided sample of the caller's
+// device-resident batch.  The DP results do not depend on any of these knobs.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "kernels.h"
+#include "runtime.h"
+
+namespace bwacuda {
+namespace {
+
+// dst[k] = src[k * stride]: a sample spread over the whole batch (both job
+// descriptor types are 32 bytes and address the caller's base buffer).
+__global__ void tune_sample_kernel(const uint4 *__restrict__ src, uint64_t stride, uint32_t count,
+                                   uint4 *__restrict__ dst)
+{
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        dst[2 * k] = src[2 * (uint64_t)k * stride];
+        dst[2 * k + 1] = src[2 * (uint64_t)k * stride + 1];
+    }
+}
+
+// Forward-pass rescue cells (qlen x tlen) of the sample.
+__global__ void tune_rescue_cells_kernel(const bwacuda_dev_rescue_job *__restrict__ jobs, uint32_t n,
+                                         unsigned long long *__restrict__ cells)
+{
+    unsigned long long s = 0;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        s += (unsigned long long)max(jobs[k].qlen, 0) * (unsigned long long)max(jobs[k].tlen, 0);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0 && s) atomicAdd(cells, s);
+}
+
+struct Timer {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ~Timer()
+    {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    }
+    cudaError_t init()
+    {
+        cudaError_t e = cudaEventCreate(&e0);
+        return e == cudaSuccess ? cudaEventCreate(&e1) : e;
+    }
+};
+
+// Time `reps` runs of fn after one warm-up run; returns ms per run (or a negative BWACUDA code).
+template <class Fn>
+double time_runs(Timer &T, cudaStream_t s, int reps, const Fn &fn)
+{
+    int rc = fn();
+    if (rc) return rc;
+    cudaError_t e = cudaEventRecord(T.e0, s);
+    for (int r = 0; r < reps && e == cudaSuccess; ++r) {
+        rc = fn();
+        if (rc) return rc;
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(T.e1, s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(T.e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, T.e0, T.e1);
+    if (e != cudaSuccess) return cuda_status(e);
+    return (double)ms / reps;
+}
+
+// The sample's descriptors: the batch itself, or every stride-th job copied to tmp.
+cudaError_t take_sample(const void *d_jobs, size_t n, size_t count, DevBuf &tmp, const void **jp, cudaStream_t s)
+{
+    if (count == n) {
+        *jp = d_jobs;
+        return cudaSuccess;
+    }
+    cudaError_t e = tmp.ensure(count * 32);
+    if (e != cudaSuccess) return e;
+    const uint32_t grid = (uint32_t)std::min<size_t>((count + 255) / 256, 4096);
+    tune_sample_kernel<<<grid, 256, 0, s>>>(static_cast<const uint4 *>(d_jobs), (uint64_t)(n / count), (uint32_t)count,
+                                            static_cast<uint4 *>(tmp.p));
+    *jp = tmp.p;
+    return cudaGetLastError();
+}
+
+}  // namespace
+}  // namespace bwacuda
+
+using namespace bwacuda;
+
+extern "C" int bwacuda_get_tuning(bwacuda_ctx *c, bwacuda_tuning *out)
+{
+    if (!c || !out) return BWACUDA_EINVAL;
+    std::lock_guard<std::mutex> g(c->mu);
+    int tb, grab, step;
+    batched_get_tuning(c, &tb, &grab, &step);
+    out->persist_block = tb;
+    out->grab = grab;
+    out->bucket_step = step;
+    out->rescue_lanes = c->rescue_lanes;
+    out->rescue_kernel = c->rescue_kernel;
+    out->candidates = c->tune_candidates;
+    out->ext_gcups = c->tuned_ext_gcups;
+    out->rescue_gcups = c->tuned_rescue_gcups;
+    return BWACUDA_OK;
+}
+
+extern "C" int bwacuda_autotune_extend(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_dev_ext_job *d_jobs,
+                                       size_t n, const bwacuda_scoring *scp, int end_bonus, int zdrop, size_t sample,
+                                       bwacuda_tuning *out)
+{
+    if (!c || !scp || !d_seq || !d_jobs || n == 0) return BWACUDA_EINVAL;
+    {
+        std::lock_guard<std::mutex> g(c->mu);
+        int rc = validate_scoring(scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
+        if (rc) return rc;
+        if (cudaSetDevice(c->device) != cudaSuccess) return BWACUDA_ECUDA;
+        if ((rc = batched_prepare(c)) != BWACUDA_OK) return rc;
+        const size_t count = std::min(n, sample ? sample : (size_t)1 << 20);
+        cudaStream_t s = c->stream;
+        DevBuf tmp, dout;
+        const void *jp = nullptr;
+        cudaError_t e = take_sample(d_jobs, n, count, tmp, &jp, s);
+        if (e == cudaSuccess) e = dout.ensure(count * sizeof(bwacuda_ext_result));
+        Timer T;
+        if (e == cudaSuccess) e = T.init();
+        if (e != cudaSuccess) { tmp.release(); dout.release(); return cuda_status(e); }
+        ExtParams P;
+        P.sc = make_scoring(scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
+        P.end_bonus = end_bonus;
+        P.zdrop = zdrop;
+        const bwacuda_stats saved = c->stats;
+        const bool graphs = c->use_graphs;
+        c->use_graphs = false;
+        auto run = [&]() {
+            return extend_device_batched(c, d_seq, static_cast<const bwacuda_dev_ext_job *>(jp), count, P,
+                                         static_cast<bwacuda_ext_result *>(dout.p), s);
+        };
+        // one checked run: bad inputs fail here, and its cell count prices every candidate
+        uint64_t cells = 0;
+        rc = run();
+        if (!rc) rc = collect_device_status(c, s, &cells);
+        double best_ms = 0;
+        int best[3] = {128, 1, 32}, ncand = 0;
+        static const int kSteps[] = {16, 32, 64}, kBlocks[] = {32, 64, 128, 256}, kGrabs[] = {1, 2, 4};
+        for (int st : kSteps) {
+            if (rc) break;
+            if ((rc = batched_set_bucket_step(c, st)) != BWACUDA_OK) break;
+            for (int tb : kBlocks) {
+                if (rc) break;
+                batched_set_block(c, tb);
+                for (int gr : kGrabs) {
+                    batched_set_grab(c, gr);
+                    const double ms = time_runs(T, s, 2, run);
+                    if (ms < 0) { rc = (int)ms; break; }
+                    ++ncand;
+                    if (best_ms == 0 || ms < best_ms) {
+                        best_ms = ms;
+                        best[0] = tb; best[1] = gr; best[2] = st;
+                    }
+                }
+            }
+        }
+        uint64_t dummy = 0;
+        const int st = collect_device_status(c, s, &dummy);
+        if (!rc) rc = st;
+        if (!rc) rc = batched_set_bucket_step(c, best[2]);
+        if (!rc) rc = batched_set_block(c, best[0]);
+        if (!rc) rc = batched_set_grab(c, best[1]);
+        c->use_graphs = graphs;
+        c->stats = saved;
+        tmp.release();
+        dout.release();
+        if (rc) return rc;
+        c->tune_candidates = ncand;
+        c->tuned_ext_gcups = best_ms > 0 ? (double)cells / (best_ms * 1e-3) / 1e9 : 0.0;
+    }
+    return out ? bwacuda_get_tuning(c, out) : BWACUDA_OK;
+}
+
+extern "C" int bwacuda_autotune_rescue(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_dev_rescue_job *d_jobs,
+                                       size_t n, const bwacuda_scoring *scp, int minsc, int max_sc, size_t sample,
+                                       bwacuda_tuning *out)
+{
+    if (!c || !scp || !d_seq || !d_jobs || n == 0) return BWACUDA_EINVAL;
+    {
+        std::lock_guard<std::mutex> g(c->mu);
+        if (cudaSetDevice(c->device) != cudaSuccess) return BWACUDA_ECUDA;
+        const size_t count = std::min(n, sample ? sample : (size_t)262144);
+        cudaStream_t s = c->stream;
+        DevBuf tmp, dout, dcells;
+        const void *jp = nullptr;
+        cudaError_t e = take_sample(d_jobs, n, count, tmp, &jp, s);
+        if (e == cudaSuccess) e = dout.ensure(count * sizeof(bwacuda_rescue_result));
+        if (e == cudaSuccess) e = dcells.ensure(16);
+        if (e == cudaSuccess) e = cudaMemsetAsync(dcells.p, 0, 8, s);
+        if (e == cudaSuccess) {
+            const uint32_t grid = (uint32_t)std::min<size_t>((count + 255) / 256, 1024);
+            tune_rescue_cells_kernel<<<grid, 256, 0, s>>>(static_cast<const bwacuda_dev_rescue_job *>(jp),
+                                                         (uint32_t)count, static_cast<unsigned long long *>(dcells.p));
+            e = cudaGetLastError();
+        }
+        unsigned long long cells = 0;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&cells, dcells.p, 8, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        Timer T;
+        if (e == cudaSuccess) e = T.init();
+        if (e != cudaSuccess) { tmp.release(); dout.release(); dcells.release(); return cuda_status(e); }
+        const bwacuda_stats saved = c->stats;
+        const int kern0 = c->rescue_kernel, lanes0 = c->rescue_lanes;
+        auto run = [&]() {
+            return ksw_align2_device_locked(c, d_seq, static_cast<const bwacuda_dev_rescue_job *>(jp), count, scp,
+                                            minsc, max_sc, 0, 0, static_cast<bwacuda_rescue_result *>(dout.p), s);
+        };
+        // one checked run (errors surface here)
+        uint64_t dummy = 0;
+        int rc = run();
+        if (!rc) rc = collect_device_status(c, s, &dummy);
+        struct Cand { int kernel, lanes; } cands[] = {
+            {BWACUDA_RESCUE_AUTO, 8}, {BWACUDA_RESCUE_AUTO, 16}, {BWACUDA_RESCUE_AUTO, 32}, {BWACUDA_RESCUE_TPJ, 16}};
+        double best_ms = 0;
+        Cand best = {kern0, lanes0};
+        int ncand = 0;
+        for (const Cand &cd : cands) {
+            if (rc) break;
+            c->rescue_kernel = cd.kernel;
+            c->rescue_lanes = cd.lanes;
+            const double ms = time_runs(T, s, 2, run);
+            if (ms < 0) { rc = (int)ms; break; }
+            ++ncand;
+            if (best_ms == 0 || ms < best_ms) { best_ms = ms; best = cd; }
+        }
+        const int st = collect_device_status(c, s, &dummy);
+        if (!rc) rc = st;
+        c->rescue_kernel = rc ? kern0 : best.kernel;
+        c->rescue_lanes = rc ? lanes0 : best.lanes;
+        c->stats = saved;
+        tmp.release();
+        dout.release();
+        dcells.release();
+        if (rc) return rc;
+        c->tune_candidates = ncand;
+        c->tuned_rescue_gcups = best_ms > 0 ? (double)cells / (best_ms * 1e-3) / 1e9 : 0.0;
+    }
+    return out ? bwacuda_get_tuning(c, out) : BWACUDA_OK;
+}

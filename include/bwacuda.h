@@ -14,8 +14,9 @@
  *
  * Conventions (all entry points):
  *  - Plain pointers and sizes only.  The caller owns every input and output
- *    buffer; the library copies inputs into its own pinned staging memory and
- *    copies results back before returning.
+ *    buffer; host-buffer calls bring the inputs to device memory (pinned
+ *    staging and copies, or device loads from host memory, see
+ *    BWACUDA_OPT_HOST_GATHER) and store every result before returning.
  *  - Bases are one byte per base, codes 0..m-1 (bwa: 0=A 1=C 2=G 3=T 4=N).
  *  - Return 0 on success or a negative BWACUDA_E* code; nothing throws across
  *    the ABI.  On error the output buffer contents are unspecified.
@@ -118,6 +119,12 @@ typedef struct bwacuda_ctx bwacuda_ctx;
 #define BWACUDA_GATHER_AUTO 0
 #define BWACUDA_GATHER_HOST 1
 #define BWACUDA_GATHER_DEVICE 2
+/* Batched extension: 32-job rounds a warp takes per work-counter grab (1, 2 or 4). */
+#define BWACUDA_OPT_GRAB 7
+/* Batched extension: query-length bucket width below 257 columns (16, 32 or 64). */
+#define BWACUDA_OPT_BUCKET_STEP 8
+/* Rescue register wavefront: lanes per job (8, 16 or 32). */
+#define BWACUDA_OPT_RESCUE_LANES 9
 
 int bwacuda_ctx_create(int device, bwacuda_ctx **out);
 void bwacuda_ctx_destroy(bwacuda_ctx *ctx);
@@ -260,6 +267,41 @@ typedef struct {
 
 int bwacuda_get_stats(bwacuda_ctx *ctx, bwacuda_stats *out);
 int bwacuda_reset_stats(bwacuda_ctx *ctx);
+
+/* Measured integer ALU-pipe throughput of the context's device, in 1e9 fused
+ * add-max operations per second (one ALU-pipe instruction per lane each): the
+ * roofline denominator of the DP kernels.  Runs a few short kernels (~5 ms
+ * each) on the context's stream; synchronous.  A measurement helper with no
+ * counterpart in the reference. */
+int bwacuda_measure_alu_peak(bwacuda_ctx *ctx, double *gops);
+
+/* ------------------------------------------------------------------------
+ * Autotuner.  No counterpart in the reference (its NEON kernels have fixed
+ * lane counts).  The launch shape of the batched extension path (threads per
+ * block, jobs per warp grab, length-bucket width) and of the rescue kernels
+ * (register wavefront with 8, 16 or 32 lanes per job, or thread-per-job) is
+ * picked by timing every candidate on a strided sample of a device-resident
+ * batch; the best is kept in the context and used by every later call.
+ * Results never depend on the tuning; only speed does.  Synchronous. */
+typedef struct {
+    int32_t persist_block;  /* 32, 64, 128, 256 */
+    int32_t grab;           /* 1, 2, 4 */
+    int32_t bucket_step;    /* 16, 32, 64 */
+    int32_t rescue_lanes;   /* 8, 16, 32 */
+    int32_t rescue_kernel;  /* BWACUDA_RESCUE_AUTO (wavefront where it fits) or BWACUDA_RESCUE_TPJ */
+    int32_t candidates;     /* candidates timed by the last autotune call */
+    double ext_gcups;       /* best extension candidate on its sample (0 if not tuned) */
+    double rescue_gcups;    /* best rescue candidate on its sample (0 if not tuned) */
+} bwacuda_tuning;
+
+int bwacuda_get_tuning(bwacuda_ctx *ctx, bwacuda_tuning *out);
+/* sample = jobs timed per candidate (0: up to 1,048,576 for extension, 262,144 for rescue). */
+int bwacuda_autotune_extend(bwacuda_ctx *ctx, const uint8_t *d_seq, const bwacuda_dev_ext_job *d_jobs,
+                            size_t n, const bwacuda_scoring *sc, int end_bonus, int zdrop, size_t sample,
+                            bwacuda_tuning *out);
+int bwacuda_autotune_rescue(bwacuda_ctx *ctx, const uint8_t *d_seq, const bwacuda_dev_rescue_job *d_jobs,
+                            size_t n, const bwacuda_scoring *sc, int minsc, int max_sc, size_t sample,
+                            bwacuda_tuning *out);
 
 #ifdef __cplusplus
 }

@@ -194,6 +194,45 @@ def test_persistent_block_sizes(ctx, block):
     assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("step,grab", [(16, 1), (16, 4), (32, 2), (64, 1), (64, 4)])
+def test_bucket_width_and_grab(ctx, step, grab):
+    # the launch-shape knobs the autotuner turns: results never change
+    js = B.synth_ext(3, 30000, seed=14)
+    want, _ = oracle.extend_batch(js)
+    ctx.set_option(B.OPT_BUCKET_STEP, step)
+    ctx.set_option(B.OPT_GRAB, grab)
+    try:
+        outs = _device_run(ctx, js, B.PATH_BATCHED, reps=2)  # capture and replay under the new shape
+    finally:
+        ctx.set_option(B.OPT_BUCKET_STEP, 32)
+        ctx.set_option(B.OPT_GRAB, 1)
+    for got in outs:
+        assert np.array_equal(got, want)
+
+
+def test_autotune_extend_keeps_results(ctx):
+    import torch
+
+    js = B.synth_ext(3, 60000, seed=15)
+    want, _ = oracle.extend_batch(js)
+    d_seq = torch.from_numpy(js.seq).cuda()
+    d_jobs = torch.from_numpy(js.dev_ext_jobs().view(np.uint8)).cuda()
+    try:
+        t = ctx.autotune_extend(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), sample=20000)
+        assert t["candidates"] == 36 and t["ext_gcups"] > 0
+        assert t["persist_block"] in (32, 64, 128, 256) and t["grab"] in (1, 2, 4)
+        assert t["bucket_step"] in (16, 32, 64)
+        assert ctx.tuning() == t
+        got = _device_run(ctx, js, B.PATH_BATCHED)[0]
+        assert np.array_equal(got, want)
+        # host-buffer calls run under the tuned shape too
+        _check_jobset(ctx, js.take(np.arange(5000)), path=(B.PATH_BATCHED, B.GATHER_AUTO))
+    finally:
+        ctx.set_option(B.OPT_PERSIST_BLOCK, 128)
+        ctx.set_option(B.OPT_BUCKET_STEP, 32)
+        ctx.set_option(B.OPT_GRAB, 1)
+
+
 @pytest.mark.parametrize("path", PATHS)
 def test_edge_cases(ctx, path):
     mat = oracle.scmat(1, 4)

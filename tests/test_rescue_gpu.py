@@ -9,15 +9,20 @@ import refstreams as R
 
 pytestmark = pytest.mark.gpu
 
-KERNELS = [pytest.param(B.RESCUE_AUTO, id="wavefront"), pytest.param(B.RESCUE_TPJ, id="tpj")]
+# (kernel family, lanes per job of the register wavefront)
+KERNELS = [pytest.param((B.RESCUE_AUTO, 16), id="wavefront16"), pytest.param((B.RESCUE_AUTO, 8), id="wavefront8"),
+           pytest.param((B.RESCUE_AUTO, 32), id="wavefront32"), pytest.param((B.RESCUE_TPJ, 16), id="tpj")]
 
 
 @pytest.fixture(params=KERNELS)
 def rctx(ctx, request):
     """The context with the rescue kernel family under test selected."""
-    ctx.set_option(B.OPT_RESCUE_KERNEL, request.param)
+    kernel, lanes = request.param
+    ctx.set_option(B.OPT_RESCUE_KERNEL, kernel)
+    ctx.set_option(B.OPT_RESCUE_LANES, lanes)
     yield ctx
     ctx.set_option(B.OPT_RESCUE_KERNEL, B.RESCUE_AUTO)
+    ctx.set_option(B.OPT_RESCUE_LANES, 16)
 
 
 def _js(pairs):
@@ -125,3 +130,24 @@ def test_invalid_inputs(ctx):
     with pytest.raises(B.BwaCudaError) as e:
         ctx.ksw_align2_batch(_js([([0], [0])]), max_sc=0)
     assert e.value.code == B.EINVAL
+
+
+def test_autotune_rescue_keeps_results(ctx):
+    import torch
+
+    js = B.synth_rescue(20000, seed=41)
+    want, _ = oracle.align2_batch(js, minsc=20, mode=0)
+    d_seq = torch.from_numpy(js.seq).cuda()
+    d_jobs = torch.from_numpy(js.dev_res_jobs().view(np.uint8)).cuda()
+    d_out = torch.zeros(len(js) * 28, dtype=torch.uint8, device="cuda")
+    try:
+        t = ctx.autotune_rescue(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), minsc=20, max_sc=1, sample=8192)
+        assert t["candidates"] == 4 and t["rescue_gcups"] > 0
+        assert (t["rescue_kernel"], t["rescue_lanes"]) in {(B.RESCUE_AUTO, 8), (B.RESCUE_AUTO, 16),
+                                                           (B.RESCUE_AUTO, 32), (B.RESCUE_TPJ, 16)}
+        ctx.ksw_align2_device(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), d_out.data_ptr(), minsc=20, max_sc=1)
+        ctx.sync()
+        assert np.array_equal(d_out.cpu().numpy().view(B.ALN_RES), want)
+    finally:
+        ctx.set_option(B.OPT_RESCUE_KERNEL, B.RESCUE_AUTO)
+        ctx.set_option(B.OPT_RESCUE_LANES, 16)
