@@ -16,7 +16,8 @@ e2e      : the same metric through bwacuda_extend_batch with HOST buffers, every
            transfers); the headline is device-gather where the device supports it.
 plain    : the plain path (one launch per 256k-job chunk, caller order).
 configs  : the mixed-length extension workload (32M jobs, per-job bands) and
-           mate rescue (2M jobs), device-resident.
+           mate rescue (2M jobs), device-resident; the CIGAR stage
+           (ksw_global2 with traceback, 1M jobs) through host buffers.
 served   : the serving loop replaying Poisson arrivals of mixed extension and
            rescue requests, p50/p99 latency and jobs/s against a FIFO of
            synchronous plain-path calls on the same arrivals.
@@ -63,6 +64,7 @@ def parse():
     ap.add_argument("--no-configs", action="store_true", help="skip the mixed-length and rescue workloads")
     ap.add_argument("--mixed-jobs", type=int, default=32 * 1024 * 1024)
     ap.add_argument("--rescue-jobs", type=int, default=2 * 1024 * 1024)
+    ap.add_argument("--global-jobs", type=int, default=1024 * 1024)
     ap.add_argument("--serve-rates", default="50,500,2000", help="Poisson arrival rates (requests/s)")
     ap.add_argument("--serve-requests", type=int, default=600, help="requests per arrival rate")
     ap.add_argument("--case", choices=["ext-batched", "ext-plain", "rescue"],
@@ -310,6 +312,25 @@ def other_configs(args, B, ctx, st, barrier, max_over_ranks, world, rank):
         "tuning": {k: tuning_res[k] for k in ("rescue_kernel", "rescue_lanes", "rescue_gcups", "candidates")}}
     del d_seq, d_jobs, d_out
     torch.cuda.empty_cache()
+
+    # CIGAR stage: banded global alignment with traceback, through the host-buffer call
+    n = args.global_jobs
+    js = B.synth_global(n, seed=4000 + rank)
+    ctx.ksw_global2_batch(js.head(min(n, 65536)))  # warm-up (buffers)
+    ctx.reset_stats()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        sc, offs, words = ctx.ksw_global2_batch(js)
+    dt = max_over_ranks((time.perf_counter() - t0) / 3)
+    stg = ctx.stats()
+    res["cigar_stage"] = {
+        "workload": f"ksw_global2 with traceback, {n} jobs per GPU: reads of 100/150/250 bp against their aligned "
+                    "reference interval (1% substitutions, 1-3 bp indels), per-job band from bwa-mem's sizing rule; "
+                    "host buffers in and out (CIGAR runs compacted on the device)",
+        "value": round(stg["global_cells"] / 3 * world / dt / 1e9, 2), "unit": "GCUPS",
+        "cells": "sum over target rows of the band width",
+        "ms_per_step": round(dt * 1e3, 2), "jobs_per_s": round(n * world / dt, 1),
+        "cigar_runs_per_job": round(float(offs[-1]) / n, 3)}
     return res
 
 

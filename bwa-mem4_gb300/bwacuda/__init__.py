@@ -17,7 +17,7 @@ _PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(_PKG, "libbwacuda.so")
 SYNTH_PATH = os.path.join(_PKG, "libbwasynth.so")
 
-OK, EINVAL, EBASE, ENOMEM, ECUDA, ETIMEOUT, EUNSUPPORTED, EBUSY, EAGAIN = 0, -1, -2, -3, -4, -5, -6, -7, -8
+OK, EINVAL, EBASE, ENOMEM, ECUDA, ETIMEOUT, EUNSUPPORTED, EBUSY, EAGAIN, ESHORT = 0, -1, -2, -3, -4, -5, -6, -7, -8, -9
 OPT_EXT_PATH, OPT_CHUNK_JOBS, OPT_GRAPHS, OPT_PERSIST_BLOCK, OPT_RESCUE_KERNEL = 1, 2, 3, 4, 5
 RESCUE_AUTO, RESCUE_TPJ = 0, 1
 OPT_HOST_GATHER = 6
@@ -32,6 +32,8 @@ EXT_JOB = np.dtype([("query", "u8"), ("target", "u8"), ("qlen", "i4"), ("tlen", 
 RES_JOB = np.dtype([("query", "u8"), ("target", "u8"), ("qlen", "i4"), ("tlen", "i4")], align=True)
 FWD_JOB = np.dtype([("query", "u8"), ("target", "u8"), ("qlen", "i4"), ("tlen", "i4"), ("minsc", "i4"),
                     ("endsc", "i4")], align=True)
+GLOBAL_JOB = np.dtype([("query", "u8"), ("target", "u8"), ("qlen", "i4"), ("tlen", "i4"), ("w", "i4")],
+                      align=True)
 DEV_EXT_JOB = np.dtype([("q_off", "u8"), ("t_off", "u8"), ("qlen", "i4"), ("tlen", "i4"), ("h0", "i4"),
                         ("w", "i4")], align=True)
 DEV_RES_JOB = np.dtype([("q_off", "u8"), ("t_off", "u8"), ("qlen", "i4"), ("tlen", "i4"), ("minsc", "i4"),
@@ -50,7 +52,7 @@ class Scoring(C.Structure):
 
 STAT_FIELDS = ("ext_jobs", "ext_cells", "ext_bin_u8", "ext_bin_i16", "ext_bin_i32", "rescue_jobs",
                "rescue_cells", "rescue_width_u8", "rescue_width_i16", "rescue_width_i32",
-               "kernel_launches", "h2d_bytes", "d2h_bytes")
+               "kernel_launches", "h2d_bytes", "d2h_bytes", "global_jobs", "global_cells")
 
 
 class ServerConfig(C.Structure):
@@ -78,7 +80,7 @@ EXPORTS = ("bwacuda_ctx_create", "bwacuda_ctx_destroy", "bwacuda_set_option", "b
            "bwacuda_ksw_align2_device_noalloc", "bwacuda_server_start", "bwacuda_server_stop",
            "bwacuda_server_submit_extend", "bwacuda_server_submit_rescue", "bwacuda_server_wait",
            "bwacuda_server_stats", "bwacuda_measure_alu_peak", "bwacuda_get_tuning", "bwacuda_autotune_extend",
-           "bwacuda_autotune_rescue")
+           "bwacuda_autotune_rescue", "bwacuda_ksw_global2_batch")
 
 _lib = None
 _synth = None
@@ -103,6 +105,7 @@ def lib():
     L.bwacuda_ctx_create.argtypes = [I, C.POINTER(vp)]
     L.bwacuda_measure_alu_peak.argtypes = [vp, C.POINTER(C.c_double)]
     L.bwacuda_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
+    L.bwacuda_ksw_global2_batch.argtypes = [vp, vp, sz, I, vp, I, I, I, I, vp, vp, vp, sz]
     L.bwacuda_autotune_extend.argtypes = [vp, vp, vp, sz, C.POINTER(Scoring), I, I, sz, C.POINTER(Tuning)]
     L.bwacuda_autotune_rescue.argtypes = [vp, vp, vp, sz, C.POINTER(Scoring), I, I, sz, C.POINTER(Tuning)]
     L.bwacuda_ctx_destroy.argtypes = [vp]
@@ -145,6 +148,8 @@ def synth_lib():
         S.synth_ext2_fill.argtypes = [u64, i64, I, vp, vp, vp, vp, vp]
         S.synth_res4_sizes.argtypes = [u64, i64, vp, vp]
         S.synth_res4_fill.argtypes = [u64, i64, vp, vp, vp, vp, vp]
+        S.synth_glb5_sizes.argtypes = [u64, i64, vp, vp, vp]
+        S.synth_glb5_fill.argtypes = [u64, i64, vp, vp, vp, vp, vp]
         _synth = S
     return _synth
 
@@ -262,6 +267,18 @@ def synth_rescue(n: int, seed: int = 0) -> JobSet:
     return JobSet(seq, qo, to, ql, tl, np.ones(n, np.int32), np.zeros(n, np.int32))
 
 
+def synth_global(n: int, seed: int = 0) -> JobSet:
+    """CIGAR-stage workload for ksw_global2: reads of 100/150/250 bp against the reference interval
+    they aligned to (1% substitutions, 1-3 bp indels), band per job from bwa-mem's sizing rule."""
+    S = synth_lib()
+    ql, tl, w = np.zeros(n, np.int32), np.zeros(n, np.int32), np.zeros(n, np.int32)
+    S.synth_glb5_sizes(seed, n, _ptr(ql), _ptr(tl), _ptr(w))
+    qo, to, total = _layout(ql, tl)
+    seq = np.zeros(max(total, 1), np.uint8)
+    S.synth_glb5_fill(seed, n, _ptr(qo), _ptr(to), _ptr(ql), _ptr(tl), _ptr(seq))
+    return JobSet(seq, qo, to, ql, tl, np.ones(n, np.int32), w)
+
+
 # ---------------------------------------------------------------- context
 
 class Context:
@@ -339,6 +356,25 @@ class Context:
                                   e_ins, w, end_bonus, zdrop, h0, _ptr(out))
         self._check(rc, "bwacuda_extend")
         return tuple(int(x) for x in out[0])
+
+    def ksw_global2_batch(self, js: JobSet, mat=None, o_del=6, e_del=1, o_ins=6, e_ins=1, m=5):
+        """ksw_global2 per job (band js.w per job): (scores, offsets, cigar words); job k's CIGAR
+        is words[offsets[k]:offsets[k + 1]]."""
+        mat = np.ascontiguousarray(scmat() if mat is None else mat, dtype=np.int8)
+        n = len(js)
+        base = js.seq.ctypes.data
+        jobs = np.zeros(n, dtype=GLOBAL_JOB)
+        jobs["query"] = base + js.q_off.astype(np.uint64)
+        jobs["target"] = base + js.t_off.astype(np.uint64)
+        jobs["qlen"], jobs["tlen"], jobs["w"] = js.qlen, js.tlen, js.w
+        score = np.zeros(max(n, 1), dtype=np.int32)
+        offs = np.zeros(n + 1, dtype=np.uint64)
+        cap = int(js.qlen.astype(np.int64).sum() + js.tlen.astype(np.int64).sum()) + 1
+        words = np.zeros(cap, dtype=np.uint32)
+        rc = lib().bwacuda_ksw_global2_batch(self.h, _ptr(jobs), n, m, _ptr(mat), o_del, e_del, o_ins, e_ins,
+                                             _ptr(score), _ptr(offs), _ptr(words), cap)
+        self._check(rc, "bwacuda_ksw_global2_batch")
+        return score[:n], offs.astype(np.int64), words[:int(offs[-1])]
 
     def ksw_align2_batch(self, js: JobSet, mat=None, o_del=6, e_del=1, o_ins=6, e_ins=1, minsc=19, max_sc=1,
                          m=5) -> np.ndarray:

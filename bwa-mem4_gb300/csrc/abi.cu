@@ -227,6 +227,7 @@ extern "C" void bwacuda_ctx_destroy(bwacuda_ctx *c)
     c->d_dev_aux.release();
     c->d_dev_scratch.release();
     ats_release(c);
+    global_release(c);
     batched_release(c);
     delete c;
 }
@@ -284,6 +285,7 @@ extern "C" const char *bwacuda_strerror(int code)
     case BWACUDA_ENOMEM: return "out of memory";
     case BWACUDA_ECUDA: return "CUDA runtime error";
     case BWACUDA_ETIMEOUT: return "bounded device wait timed out";
+    case BWACUDA_ESHORT: return "output buffer too small (required sizes written)";
     case BWACUDA_EUNSUPPORTED: return "input beyond the kernels' limits";
     case BWACUDA_EBUSY: return "serving queue full";
     case BWACUDA_EAGAIN: return "request not finished";

@@ -1,0 +1,389 @@
+// global.cu -- banded global alignment with traceback (ksw_global2,
+// crates/bwa-extend/src/sw.rs:561-740), batched on the GPU.
+//
+// One thread per alignment.  The DP row pair (H and E of the previous row)
+// lives in shared memory, interleaved across the block (column j of thread t
+// at j * TB + t), with the query codes beside it.  The traceback byte of every
+// band cell (f << 4 | e << 2 | h, the reference's encoding) goes to HBM; the 32
+// jobs of a warp share one block there, interleaved word by word
+// (word (row * ncw + col / 4) * 32 + lane), so the warp's lanes, which sweep the
+// same band-relative column in lockstep, store 128 contiguous bytes per
+// instruction.  The traceback then walks only its path's cells and writes the
+// CIGAR runs (len << 4 | op), merged and reversed as the reference does.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include <cub/device/device_scan.cuh>
+
+#include "kernels.h"
+#include "runtime.h"
+
+namespace bwacuda {
+
+namespace {
+
+constexpr int MINUS_INF = -0x40000000;
+constexpr size_t SMEM_LIMIT = 227u * 1024u;
+
+// One alignment as the kernel sees it (bases addressed from the chunk's base buffer).
+struct GlobalDevJob {
+    uint64_t q_off, t_off;
+    uint64_t z_off;    // word offset of the warp group's traceback block
+    uint64_t cig_off;  // word offset of this job's CIGAR scratch (qlen + tlen + 1 words)
+    int32_t qlen, tlen, w;
+    int32_t ncw;       // traceback words per row of the warp group
+};
+static_assert(sizeof(GlobalDevJob) == 48, "descriptor layout");
+
+__host__ __device__ inline size_t global_smem(int qcap, int tb) { return (size_t)tb * ((size_t)(qcap + 1) * 8 + qcap); }
+
+__device__ __forceinline__ void cigar_push(uint32_t *cig, int &n, uint32_t op, uint32_t len)
+{
+    if (n > 0 && (cig[n - 1] & 0xfu) == op) {
+        cig[n - 1] += len << 4;
+        return;
+    }
+    cig[n++] = (len << 4) | op;
+}
+
+template <int TB>
+__global__ void __launch_bounds__(TB)
+global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restrict__ jobs, uint32_t n,
+                  const __grid_constant__ Scoring sc, int qcap, uint32_t *__restrict__ z, uint32_t *__restrict__ cig,
+                  int32_t *__restrict__ score_out, int32_t *__restrict__ ncig_out, uint32_t *__restrict__ err,
+                  unsigned long long *__restrict__ cells_total)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int tid = threadIdx.x;
+    const uint32_t k = blockIdx.x * TB + tid;
+    unsigned long long ncells = 0;
+    if (k >= n) return;
+    const uint32_t lane = k & 31u;
+    int2 *cell = reinterpret_cast<int2 *>(smem_raw) + tid;  // cell[j * TB]: {H, E}
+    uint8_t *qs = smem_raw + (size_t)(qcap + 1) * 8 * TB + tid;  // qs[j * TB]: query code
+    const GlobalDevJob J = jobs[k];
+    const int qlen = J.qlen, tlen = J.tlen;
+    const int w = J.w < 0 ? 0 : J.w;
+    const int n_col = qlen < 2 * w + 1 ? qlen : 2 * w + 1;
+    const int oe_del = sc.o_del + sc.e_del, oe_ins = sc.o_ins + sc.e_ins;
+    const uint8_t *q = seq + J.q_off;
+    const uint8_t *t = seq + J.t_off;
+    uint32_t *zj = z + J.z_off + lane;
+    bool bad = false;
+    for (int j = 0; j < qlen; ++j) {
+        uint32_t c = q[j];
+        bad |= c >= (uint32_t)sc.m;
+        qs[(size_t)j * TB] = (uint8_t)(c < (uint32_t)sc.m ? c : PAD_CODE);
+    }
+    // row -1: the origin, a leading insertion over columns 1..w, unreachable beyond
+    for (int j = 0; j <= qlen; ++j) {
+        int h = MINUS_INF;
+        if (j == 0) h = 0;
+        else if (j <= w) h = -(sc.o_ins + sc.e_ins * j);
+        cell[(size_t)j * TB] = make_int2(h, MINUS_INF);
+    }
+    for (int i = 0; i < tlen; ++i) {
+        int f = MINUS_INF;
+        const int beg = i > w ? i - w : 0;
+        const int end = i + w + 1 < qlen ? i + w + 1 : qlen;
+        int h1 = beg == 0 ? -(sc.o_del + sc.e_del * (i + 1)) : MINUS_INF;
+        uint32_t tc = t[i];
+        bad |= tc >= (uint32_t)sc.m;
+        tc = tc < (uint32_t)sc.m ? tc : (uint32_t)PAD_CODE;
+        const uint32_t plo = sc.prof[tc & 7u][0], phi = sc.prof[tc & 7u][1];
+        uint32_t *zr = zj + (size_t)i * (size_t)J.ncw * 32u;
+        uint32_t word = 0;
+        for (int j = beg; j < end; ++j) {
+            const int2 he = cell[(size_t)j * TB];
+            int mm = he.x, e = he.y;
+            mm += prof_score(plo, phi, qs[(size_t)j * TB]);
+            uint32_t d = mm < e ? 1u : 0u;
+            int h = mm >= e ? mm : e;
+            if (!(h >= f)) { d = 2u; h = f; }
+            int tt = mm - oe_del;
+            e -= sc.e_del;
+            if (e > tt) d |= 1u << 2;
+            else e = tt;
+            cell[(size_t)j * TB] = make_int2(h1, e);  // H(i, j-1) for the next row's diagonal; E(i+1, j)
+            h1 = h;
+            tt = mm - oe_ins;
+            f -= sc.e_ins;
+            if (f > tt) d |= 2u << 4;
+            else f = tt;
+            const int jj = j - beg;
+            word |= d << ((jj & 3) * 8);
+            if ((jj & 3) == 3 || j == end - 1) {
+                zr[(size_t)(jj >> 2) * 32u] = word;
+                word = 0;
+            }
+        }
+        cell[(size_t)end * TB] = make_int2(h1, MINUS_INF);
+        // band cells this row did not reach read as 0, as in the reference's zeroed matrix
+        for (int wi = end > beg ? (end - beg + 3) >> 2 : 0; wi < (n_col + 3) >> 2; ++wi) zr[(size_t)wi * 32u] = 0u;
+        ncells += (unsigned long long)(end > beg ? end - beg : 0);
+    }
+    score_out[k] = cell[(size_t)qlen * TB].x;
+    // traceback from the band's last cell of the last row
+    uint32_t *cg = cig + J.cig_off;
+    int nc = 0;
+    long i = (long)tlen - 1;
+    long kk = ((long)tlen - 1 + w + 1 < qlen ? (long)tlen - 1 + w + 1 : (long)qlen) - 1;
+    uint32_t which = 0;
+    bool range = false;
+    while (i >= 0 && kk >= 0) {
+        const long beg = i > w ? i - w : 0;
+        // the reference reads the flat row-major matrix: an offset past the row lands in a later row
+        const long flat = i * (long)n_col + (kk - beg);
+        if (kk < beg || flat >= (long)n_col * tlen) { range = true; break; }
+        const long row = flat / n_col, col = flat - row * n_col;
+        const uint32_t wv = zj[((size_t)row * (size_t)J.ncw + (size_t)(col >> 2)) * 32u];
+        const uint32_t d = (wv >> ((col & 3) * 8)) & 0xffu;
+        which = (d >> (which << 1)) & 3u;
+        if (which == 0) { cigar_push(cg, nc, 0, 1); --i; --kk; }
+        else if (which == 1) { cigar_push(cg, nc, 2, 1); --i; }
+        else { cigar_push(cg, nc, 1, 1); --kk; }
+    }
+    if (!range) {
+        if (i >= 0) cigar_push(cg, nc, 2, (uint32_t)(i + 1));
+        if (kk >= 0) cigar_push(cg, nc, 1, (uint32_t)(kk + 1));
+        for (int a = 0, b = nc - 1; a < b; ++a, --b) {
+            const uint32_t x = cg[a];
+            cg[a] = cg[b];
+            cg[b] = x;
+        }
+    } else {
+        nc = 0;
+        atomicOr(err, ERR_RANGE);
+    }
+    ncig_out[k] = nc;
+    if (bad) atomicOr(err, ERR_BASE);
+    atomicAdd(cells_total, ncells);
+}
+
+// dense[doff[k] ..] = cig[cig_off[k] .. + ncig[k]]: one warp per job.
+__global__ void global_compact_kernel(const GlobalDevJob *__restrict__ jobs, uint32_t n,
+                                      const uint32_t *__restrict__ cig, const int32_t *__restrict__ ncig,
+                                      const uint64_t *__restrict__ doff, uint32_t *__restrict__ dense)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < n; k += (gridDim.x * blockDim.x) >> 5) {
+        const uint32_t *src = cig + jobs[k].cig_off;
+        uint32_t *dst = dense + doff[k];
+        for (int x = (int)lane; x < ncig[k]; x += 32) dst[x] = src[x];
+    }
+}
+
+template <int TB>
+cudaError_t launch_global_tb(const uint8_t *seq, const GlobalDevJob *jobs, uint32_t n, const Scoring &sc, int qcap,
+                             uint32_t *z, uint32_t *cig, int32_t *score, int32_t *ncig, uint32_t *err,
+                             unsigned long long *cells, cudaStream_t s)
+{
+    const size_t smem = global_smem(qcap, TB);
+    auto kern = global_tpj_kernel<TB>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<(n + TB - 1) / TB, TB, smem, s>>>(seq, jobs, n, sc, qcap, z, cig, score, ncig, err, cells);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_global(const uint8_t *seq, const GlobalDevJob *jobs, uint32_t n, const Scoring &sc, int qcap,
+                          uint32_t *z, uint32_t *cig, int32_t *score, int32_t *ncig, uint32_t *err,
+                          unsigned long long *cells, cudaStream_t s)
+{
+    if (global_smem(qcap, 128) <= SMEM_LIMIT)
+        return launch_global_tb<128>(seq, jobs, n, sc, qcap, z, cig, score, ncig, err, cells, s);
+    if (global_smem(qcap, 64) <= SMEM_LIMIT)
+        return launch_global_tb<64>(seq, jobs, n, sc, qcap, z, cig, score, ncig, err, cells, s);
+    return launch_global_tb<32>(seq, jobs, n, sc, qcap, z, cig, score, ncig, err, cells, s);
+}
+
+// Longest query a 32-thread block holds.
+int global_max_qlen()
+{
+    int q = (int)(SMEM_LIMIT / (32 * 9));
+    while (q > 0 && global_smem(q + 1, 32) > SMEM_LIMIT) --q;
+    return q;
+}
+
+struct GlobalBufs {
+    HostBuf h_seq, h_jobs, h_res;
+    DevBuf d_seq, d_jobs, d_z, d_cig, d_res, d_doff, d_dense, d_tmp;
+};
+
+}  // namespace
+
+struct GlobalState {
+    GlobalBufs b;
+};
+
+void global_release(bwacuda_ctx *c)
+{
+    if (!c->global) return;
+    GlobalBufs &b = c->global->b;
+    b.h_seq.release(); b.h_jobs.release(); b.h_res.release();
+    b.d_seq.release(); b.d_jobs.release(); b.d_z.release(); b.d_cig.release(); b.d_res.release();
+    b.d_doff.release(); b.d_dense.release(); b.d_tmp.release();
+    delete c->global;
+    c->global = nullptr;
+}
+
+}  // namespace bwacuda
+
+using namespace bwacuda;
+
+extern "C" int bwacuda_ksw_global2_batch(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n, int m,
+                                         const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins,
+                                         int32_t *score, uint64_t *cigar_off, uint32_t *cigar, size_t cigar_cap)
+{
+    if (!c) return BWACUDA_EINVAL;
+    std::lock_guard<std::mutex> g(c->mu);
+    int rc = validate_scoring(m, mat, o_del, e_del, o_ins, e_ins);
+    if (rc) return rc;
+    if (n && (!jobs || !score || !cigar_off)) return BWACUDA_EINVAL;
+    if (cigar_off) cigar_off[0] = 0;
+    if (n == 0) return BWACUDA_OK;
+    const int qlim = global_max_qlen();
+    for (size_t k = 0; k < n; ++k) {
+        const bwacuda_global_job &J = jobs[k];
+        if (J.qlen < 0 || J.tlen < 0 || (J.qlen && !J.query) || (J.tlen && !J.target)) return BWACUDA_EINVAL;
+        if (J.qlen > qlim) return BWACUDA_EUNSUPPORTED;
+    }
+    if (cudaSetDevice(c->device) != cudaSuccess) return BWACUDA_ECUDA;
+    if (!c->global) {
+        c->global = new (std::nothrow) GlobalState();
+        if (!c->global) return BWACUDA_ENOMEM;
+    }
+    GlobalBufs &b = c->global->b;
+    const Scoring sc = make_scoring(m, mat, o_del, e_del, o_ins, e_ins);
+    cudaStream_t s = c->stream;
+    uint32_t *d_err = static_cast<uint32_t *>(c->d_misc.p);
+    // chunks bounded in jobs and in traceback bytes
+    const size_t kMaxJobs = 262144, kMaxZWords = (size_t)1 << 29;  // 2 GiB of traceback per chunk
+    uint64_t out_base = 0;
+    bool short_buf = false;
+    cudaError_t e = cudaSuccess;
+    size_t c0 = 0;
+    while (c0 < n && rc == BWACUDA_OK && e == cudaSuccess) {
+        // grow the chunk 32 jobs (one warp group) at a time
+        size_t cn = 0;
+        uint64_t zwords = 0, cigw = 0, bytes = 0;
+        int qmax = 0;
+        while (c0 + cn < n && cn < kMaxJobs) {
+            const size_t g1 = std::min(n, c0 + cn + 32);
+            int tmax = 0, ncmax = 0;
+            uint64_t gb = 0, gc = 0;
+            for (size_t k = c0 + cn; k < g1; ++k) {
+                const bwacuda_global_job &J = jobs[k];
+                const int w = J.w < 0 ? 0 : J.w;
+                tmax = std::max(tmax, J.tlen);
+                ncmax = std::max(ncmax, std::min(J.qlen, 2 * w + 1));
+                gb += (uint64_t)J.qlen + (uint64_t)J.tlen;
+                gc += (uint64_t)J.qlen + (uint64_t)J.tlen + 1;
+                qmax = std::max(qmax, J.qlen);
+            }
+            const uint64_t gz = (uint64_t)tmax * (uint64_t)((ncmax + 3) / 4) * 32u;
+            if (cn > 0 && zwords + gz > kMaxZWords) break;
+            zwords += gz;
+            cigw += gc;
+            bytes += gb;
+            cn = g1 - c0;
+        }
+        // pack: bases, descriptors (warp groups share their traceback block)
+        if ((e = b.h_seq.ensure(bytes + 16)) != cudaSuccess) break;
+        if ((e = b.h_jobs.ensure(cn * sizeof(GlobalDevJob))) != cudaSuccess) break;
+        if ((e = b.h_res.ensure(cn * 8 + 16)) != cudaSuccess) break;
+        uint8_t *hs = static_cast<uint8_t *>(b.h_seq.p);
+        GlobalDevJob *hj = static_cast<GlobalDevJob *>(b.h_jobs.p);
+        uint64_t so = 0, zo = 0, co = 0;
+        for (size_t g0 = 0; g0 < cn; g0 += 32) {
+            const size_t g1 = std::min(cn, g0 + 32);
+            int tmax = 0, ncmax = 0;
+            for (size_t k = g0; k < g1; ++k) {
+                const bwacuda_global_job &J = jobs[c0 + k];
+                const int w = J.w < 0 ? 0 : J.w;
+                tmax = std::max(tmax, J.tlen);
+                ncmax = std::max(ncmax, std::min(J.qlen, 2 * w + 1));
+            }
+            const int ncw = (ncmax + 3) / 4;
+            for (size_t k = g0; k < g1; ++k) {
+                const bwacuda_global_job &J = jobs[c0 + k];
+                GlobalDevJob D;
+                D.q_off = so;
+                if (J.qlen) memcpy(hs + so, J.query, (size_t)J.qlen);
+                so += (uint64_t)J.qlen;
+                D.t_off = so;
+                if (J.tlen) memcpy(hs + so, J.target, (size_t)J.tlen);
+                so += (uint64_t)J.tlen;
+                D.z_off = zo;
+                D.cig_off = co;
+                co += (uint64_t)J.qlen + (uint64_t)J.tlen + 1;
+                D.qlen = J.qlen;
+                D.tlen = J.tlen;
+                D.w = J.w;
+                D.ncw = ncw;
+                hj[k] = D;
+            }
+            zo += (uint64_t)tmax * (uint64_t)ncw * 32u;
+        }
+        size_t scan_bytes = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, (const int32_t *)nullptr, (uint64_t *)nullptr, (int)cn + 1);
+        if ((e = b.d_seq.ensure(bytes + 16)) != cudaSuccess) break;
+        if ((e = b.d_jobs.ensure(cn * sizeof(GlobalDevJob))) != cudaSuccess) break;
+        if ((e = b.d_z.ensure(zwords * 4 + 16)) != cudaSuccess) break;
+        if ((e = b.d_cig.ensure(cigw * 4 + 16)) != cudaSuccess) break;
+        if ((e = b.d_res.ensure((cn + 1) * 8 + 16)) != cudaSuccess) break;
+        if ((e = b.d_doff.ensure((cn + 1) * 8)) != cudaSuccess) break;
+        if ((e = b.d_tmp.ensure(scan_bytes + 16)) != cudaSuccess) break;
+        int32_t *d_score = static_cast<int32_t *>(b.d_res.p);
+        int32_t *d_ncig = d_score + cn + 1;  // one spare slot: the scan's n+1-th input is zero
+        uint64_t *d_doff = static_cast<uint64_t *>(b.d_doff.p);
+        if (bytes && (e = cudaMemcpyAsync(b.d_seq.p, hs, bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(b.d_jobs.p, hj, cn * sizeof(GlobalDevJob), cudaMemcpyHostToDevice, s)) != cudaSuccess) break;
+        if ((e = cudaMemsetAsync(d_ncig + cn, 0, 4, s)) != cudaSuccess) break;
+        c->stats.h2d_bytes += bytes + cn * sizeof(GlobalDevJob);
+        e = launch_global(static_cast<const uint8_t *>(b.d_seq.p), static_cast<const GlobalDevJob *>(b.d_jobs.p),
+                          (uint32_t)cn, sc, qmax + 1, static_cast<uint32_t *>(b.d_z.p),
+                          static_cast<uint32_t *>(b.d_cig.p), d_score, d_ncig, d_err,
+                          reinterpret_cast<unsigned long long *>((char *)c->d_misc.p + 8), s);
+        if (e != cudaSuccess) break;
+        if ((e = cub::DeviceScan::ExclusiveSum(b.d_tmp.p, scan_bytes, d_ncig, d_doff, (int)cn + 1, s)) != cudaSuccess) break;
+        // scores and run counts back; the host derives the offsets the device scan also made
+        int32_t *hr = static_cast<int32_t *>(b.h_res.p);
+        if ((e = cudaMemcpyAsync(hr, d_score, cn * 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(hr + cn, d_ncig, cn * 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) break;
+        uint64_t tot = 0;
+        for (size_t k = 0; k < cn; ++k) {
+            score[c0 + k] = hr[k];
+            tot += (uint64_t)hr[cn + k];
+            cigar_off[c0 + k + 1] = out_base + tot;
+        }
+        if (cigar && out_base + tot <= cigar_cap && tot) {
+            if ((e = b.d_dense.ensure(tot * 4 + 16)) != cudaSuccess) break;
+            const uint32_t grid = (uint32_t)std::min<size_t>((cn * 32 + 255) / 256, 4096);
+            global_compact_kernel<<<grid, 256, 0, s>>>(static_cast<const GlobalDevJob *>(b.d_jobs.p), (uint32_t)cn,
+                                                       static_cast<const uint32_t *>(b.d_cig.p), d_ncig, d_doff,
+                                                       static_cast<uint32_t *>(b.d_dense.p));
+            if ((e = cudaGetLastError()) != cudaSuccess) break;
+            if ((e = cudaMemcpyAsync(cigar + out_base, b.d_dense.p, tot * 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+            if ((e = cudaStreamSynchronize(s)) != cudaSuccess) break;
+            c->stats.d2h_bytes += tot * 4;
+        } else if (out_base + tot > cigar_cap || !cigar) {
+            short_buf = true;
+        }
+        c->stats.d2h_bytes += cn * 8;
+        c->stats.kernel_launches += 3;
+        out_base += tot;
+        c0 += cn;
+    }
+    if (e != cudaSuccess) return cuda_status(e);
+    uint64_t cells = 0;
+    rc = collect_device_status(c, s, &cells);
+    if (rc) return rc;
+    c->stats.global_jobs += n;
+    c->stats.global_cells += cells;
+    return short_buf ? BWACUDA_ESHORT : BWACUDA_OK;
+}

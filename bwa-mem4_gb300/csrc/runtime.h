@@ -63,6 +63,7 @@ struct Slot {
 struct BatchedState;  // batched path (batched.cu)
 struct ServerState;   // serving loop (server.cu)
 struct AtsState;      // device-side gather of host buffers (ats.cu)
+struct GlobalState;   // ksw_global2 buffers (global.cu)
 
 int cuda_status(cudaError_t e);
 Scoring make_scoring(int m, const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins);
@@ -95,6 +96,7 @@ struct bwacuda_ctx {
     bool pageable_access = false;  // the device reads pageable host memory (host page tables)
     bwacuda::BatchedState *batched = nullptr;
     bwacuda::AtsState *ats = nullptr;
+    bwacuda::GlobalState *global = nullptr;
     bwacuda::ServerState *server = nullptr;
 };
 
@@ -148,6 +150,9 @@ int batched_bucket_count(bwacuda_ctx *c);
 int extend_batch_ats(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int m, const int8_t *mat,
                      const ExtParams &P, int w, bwacuda_ext_result *out);
 void ats_release(bwacuda_ctx *c);
+
+// global.cu
+void global_release(bwacuda_ctx *c);
 
 // server.cu
 void server_shutdown(bwacuda_ctx *c);

@@ -227,3 +227,84 @@ void synth_res4_fill(uint64_t seed, int64_t n, const int64_t *q_off, const int64
         }
     }
 }
+
+/* ------------------------------------------------------------------ glb5 */
+/*
+ * CIGAR stage (ksw_global2 as crates/bwa-mem/src/cigar.rs:400-447 calls it):
+ * a read of 100 / 150 / 250 bp (30 / 50 / 20%) against the reference interval
+ * it aligned to: 1% substitutions and 0.05%-per-base indel events of 1-3 bp,
+ * band w from the caller's rule at bwa's default scoring
+ *   max_gap = max(((l+1)/2 - 6) / 1 + 1, 1), w = min((max_gap + |rlen - l| + 1) / 2, 100),
+ *   w = max(w, |rlen - l| + 3).
+ * The geometry (read length, indel events) comes from stream 1, so the sizes
+ * pass and the fill pass walk the same events; bases come from stream 2.
+ */
+
+static int glb5_read_len(rng_t *g)
+{
+    const uint32_t u = runder(g, 10);
+    return u < 3 ? 100 : (u < 8 ? 150 : 250);
+}
+
+/* One step of the edit walk at query position p: 0 = aligned base,
+ * 1 = deletion of *len target bases, 2 = insertion of *len query bases. */
+static int glb5_event(rng_t *g, int *len)
+{
+    if (!rppm(g, 500)) return 0;
+    *len = 1 + (int)runder(g, 3);
+    return runder(g, 2) ? 1 : 2;
+}
+
+void synth_glb5_sizes(uint64_t seed, int64_t n, int32_t *qlen, int32_t *tlen, int32_t *w)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < n; ++k) {
+        rng_t g = rng_for(seed, (uint64_t)k, 1);
+        const int l = glb5_read_len(&g);
+        int rlen = 0;
+        for (int p = 0; p < l;) {
+            int len = 0;
+            const int ev = glb5_event(&g, &len);
+            if (ev == 1) rlen += len;
+            else if (ev == 2) p += len;
+            else { rlen += 1; p += 1; }
+        }
+        int max_gap = ((l + 1) / 2 - 6) / 1 + 1;
+        if (max_gap < 1) max_gap = 1;
+        const int diff = rlen > l ? rlen - l : l - rlen;
+        int ww = (max_gap + diff + 1) >> 1;
+        if (ww > 100) ww = 100;
+        if (ww < diff + 3) ww = diff + 3;
+        qlen[k] = l;
+        tlen[k] = rlen;
+        w[k] = ww;
+    }
+}
+
+void synth_glb5_fill(uint64_t seed, int64_t n, const int64_t *q_off, const int64_t *t_off,
+                     const int32_t *qlen, const int32_t *tlen, uint8_t *seq)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < n; ++k) {
+        rng_t g = rng_for(seed, (uint64_t)k, 1);
+        rng_t r = rng_for(seed, (uint64_t)k, 2);
+        uint8_t *q = seq + q_off[k], *t = seq + t_off[k];
+        const int l = glb5_read_len(&g);
+        int tp = 0;
+        for (int p = 0; p < l;) {
+            int len = 0;
+            const int ev = glb5_event(&g, &len);
+            if (ev == 1) {
+                for (int x = 0; x < len; ++x) t[tp++] = rbase(&r);
+            } else if (ev == 2) {
+                for (int x = 0; x < len && p < l; ++x) q[p++] = rbase(&r);
+            } else {
+                const uint8_t b = rbase(&r);
+                t[tp++] = b;
+                q[p++] = rppm(&r, 10000) ? (uint8_t)((b + 1 + runder(&r, 3)) & 3) : b;
+            }
+        }
+        (void)qlen;
+        (void)tlen;
+    }
+}

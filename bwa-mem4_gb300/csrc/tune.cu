@@ -118,7 +118,7 @@ extern "C" int bwacuda_autotune_extend(bwacuda_ctx *c, const uint8_t *d_seq, con
         if (rc) return rc;
         if (cudaSetDevice(c->device) != cudaSuccess) return BWACUDA_ECUDA;
         if ((rc = batched_prepare(c)) != BWACUDA_OK) return rc;
-        const size_t count = std::min(n, sample ? sample : (size_t)1 << 20);
+        const size_t count = std::min(n, sample ? sample : (size_t)1 << 22);
         cudaStream_t s = c->stream;
         DevBuf tmp, dout;
         const void *jp = nullptr;

@@ -11,6 +11,7 @@
  *   bwacuda_ksw_align2_batch    bwa_neon::batched_ksw_align2  crates/bwa-neon/src/matesw.rs:299-309
  *   bwacuda_ksw_align2_scalar_batch  bwa_extend::ksw_align2 (per job)  crates/bwa-extend/src/sw.rs:1108-1185
  *   bwacuda_ksw_local_fwd_batch bwa_extend::ksw_local_fwd (per job)  crates/bwa-extend/src/sw.rs:921-1075
+ *   bwacuda_ksw_global2_batch   bwa_extend::ksw_global2 (per job)    crates/bwa-extend/src/sw.rs:561-740
  *
  * Conventions (all entry points):
  *  - Plain pointers and sizes only.  The caller owns every input and output
@@ -45,6 +46,7 @@ extern "C" {
 #define BWACUDA_EUNSUPPORTED (-6) /* input beyond the kernels' limits (e.g. score range) */
 #define BWACUDA_EBUSY (-7)        /* serving queue full / request not admitted */
 #define BWACUDA_EAGAIN (-8)       /* serving request not finished yet */
+#define BWACUDA_ESHORT (-9)       /* output buffer too small; the sizes it needs were written */
 
 /* Largest alphabet the kernels' score profile holds. */
 #define BWACUDA_MAX_M 7
@@ -159,6 +161,29 @@ int bwacuda_ksw_align2_scalar_batch(bwacuda_ctx *ctx, const bwacuda_rescue_job *
                                     int e_ins, int minsc, int max_sc, int lanes,
                                     bwacuda_rescue_result *out);
 
+/* ksw_global2 (crates/bwa-extend/src/sw.rs:561-740), the banded global
+ * alignment with traceback that bwa-mem's CIGAR step calls per alignment
+ * (crates/bwa-mem/src/cigar.rs:446).  w is per job (the caller sizes it per
+ * region).  Outputs: score[k]; job k's CIGAR runs (len << 4 | op, op 0=M 1=I
+ * 2=D, left to right) are cigar[cigar_off[k] .. cigar_off[k+1]) with
+ * cigar_off[0] = 0 (n + 1 entries).  When cigar_cap words are too few (or
+ * cigar is NULL) the call still writes score and cigar_off and returns
+ * BWACUDA_ESHORT; cigar_cap >= sum(qlen + tlen) always suffices.  A traceback
+ * that the reference could not complete (its index leaves the matrix; its
+ * caller's band sizing rules that out) makes the call return
+ * BWACUDA_EUNSUPPORTED. */
+typedef struct {
+    const uint8_t *query;
+    const uint8_t *target;
+    int32_t qlen;
+    int32_t tlen;
+    int32_t w;
+} bwacuda_global_job;
+
+int bwacuda_ksw_global2_batch(bwacuda_ctx *ctx, const bwacuda_global_job *jobs, size_t n, int m,
+                              const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins,
+                              int32_t *score, uint64_t *cigar_off, uint32_t *cigar, size_t cigar_cap);
+
 /* ksw_local_fwd per job with its own minsc / endsc (lanes as above). */
 int bwacuda_ksw_local_fwd_batch(bwacuda_ctx *ctx, const bwacuda_fwd_job *jobs, size_t n, int m,
                                 const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins,
@@ -263,6 +288,7 @@ typedef struct {
     uint64_t rescue_width_u8, rescue_width_i16, rescue_width_i32; /* per call */
     uint64_t kernel_launches;
     uint64_t h2d_bytes, d2h_bytes;
+    uint64_t global_jobs, global_cells; /* ksw_global2: cells = sum over rows of the band width */
 } bwacuda_stats;
 
 int bwacuda_get_stats(bwacuda_ctx *ctx, bwacuda_stats *out);
@@ -295,7 +321,7 @@ typedef struct {
 } bwacuda_tuning;
 
 int bwacuda_get_tuning(bwacuda_ctx *ctx, bwacuda_tuning *out);
-/* sample = jobs timed per candidate (0: up to 1,048,576 for extension, 262,144 for rescue). */
+/* sample = jobs timed per candidate (0: up to 4,194,304 for extension, 262,144 for rescue). */
 int bwacuda_autotune_extend(bwacuda_ctx *ctx, const uint8_t *d_seq, const bwacuda_dev_ext_job *d_jobs,
                             size_t n, const bwacuda_scoring *sc, int end_bonus, int zdrop, size_t sample,
                             bwacuda_tuning *out);

@@ -99,6 +99,12 @@ def lib():
         L.ko_align2_batch.restype = None
         L.ko_align2_batch.argtypes = [u8p, C.c_int64, i64p, i64p, i32p, i32p, I, i8p, I, I, I,
                                       I, I, I, I, I, I, C.c_void_p, C.POINTER(C.c_uint64)]
+        L.ko_global2.restype = I
+        L.ko_global2.argtypes = [u8p, I, u8p, I, I, i8p, I, I, I, I, I, i32p, C.POINTER(C.c_uint32),
+                                 C.POINTER(I)]
+        L.ko_global2_batch.restype = I
+        L.ko_global2_batch.argtypes = [u8p, C.c_int64, i64p, i64p, i32p, i32p, i32p, I, i8p, I, I, I, I, I,
+                                       i32p, i64p, C.POINTER(C.c_uint32), i32p]
         L.ko_local_fwd_batch.restype = None
         L.ko_local_fwd_batch.argtypes = [u8p, C.c_int64, i64p, i64p, i32p, i32p, i32p, i32p, I,
                                          i8p, I, I, I, I, I, I, I, C.c_void_p]
@@ -273,3 +279,49 @@ def local_fwd_batch(js, minsc, endsc, mat=None, o_del=6, e_del=1, o_ins=6, e_ins
                              m, _p(mat, C.c_int8), o_del, e_del, o_ins, e_ins, max_sc, lanes,
                              nthreads, out.ctypes.data_as(C.c_void_p))
     return out
+
+
+def global2(q, t, w, mat=None, o_del=6, e_del=1, o_ins=6, e_ins=1, m=5):
+    """ksw_global2 (crates/bwa-extend/src/sw.rs:561-740): (score, cigar words) or None where the
+    reference's traceback would index out of range."""
+    q, t = _u8(q), _u8(t)
+    mat = _mat(scmat() if mat is None else mat)
+    cig = np.zeros(len(q) + len(t) + 1, dtype=np.uint32)
+    sc, nc = C.c_int32(), C.c_int()
+    rc = lib().ko_global2(_p(q, C.c_uint8), len(q), _p(t, C.c_uint8), len(t), m, _p(mat, C.c_int8), o_del, e_del,
+                          o_ins, e_ins, w, C.byref(sc), _p(cig, C.c_uint32), C.byref(nc))
+    if rc != 0:
+        return None
+    return int(sc.value), [int(x) for x in cig[:nc.value]]
+
+
+def global2_batch(js, mat=None, o_del=6, e_del=1, o_ins=6, e_ins=1, nthreads=0, m=5):
+    """Every job of a JobSet-like object (per-job w).  Returns (scores, offsets, words): job k's
+    CIGAR is words[offsets[k]:offsets[k+1]]; raises if any traceback leaves the matrix."""
+    mat = _mat(scmat() if mat is None else mat)
+    n = len(js.qlen)
+    ql = np.ascontiguousarray(js.qlen, dtype=np.int32)
+    tl = np.ascontiguousarray(js.tlen, dtype=np.int32)
+    w = np.ascontiguousarray(js.w, dtype=np.int32)
+    cap = ql.astype(np.int64) + tl + 1
+    cig_off = np.zeros(n, dtype=np.int64)
+    if n:
+        cig_off[1:] = np.cumsum(cap)[:-1]
+    words = np.zeros(int(cap.sum()) + 1, dtype=np.uint32)
+    score = np.zeros(n, dtype=np.int32)
+    ncig = np.zeros(n, dtype=np.int32)
+    qo = np.ascontiguousarray(js.q_off, dtype=np.int64)
+    to = np.ascontiguousarray(js.t_off, dtype=np.int64)
+    seq = _u8(js.seq) if len(js.seq) else np.zeros(1, np.uint8)
+    rc = lib().ko_global2_batch(_p(seq, C.c_uint8), n, _p(qo, C.c_int64), _p(to, C.c_int64), _p(ql, C.c_int32),
+                                _p(tl, C.c_int32), _p(w, C.c_int32), m, _p(mat, C.c_int8), o_del, e_del, o_ins,
+                                e_ins, nthreads, _p(score, C.c_int32), _p(cig_off, C.c_int64),
+                                _p(words, C.c_uint32), _p(ncig, C.c_int32))
+    if rc != 0:
+        raise ValueError("a traceback left the stored band")
+    offsets = np.zeros(n + 1, dtype=np.int64)
+    offsets[1:] = np.cumsum(ncig)
+    dense = np.zeros(int(offsets[-1]), dtype=np.uint32)
+    for k in range(n):
+        dense[offsets[k]:offsets[k + 1]] = words[cig_off[k]:cig_off[k] + ncig[k]]
+    return score, offsets, dense

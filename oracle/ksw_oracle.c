@@ -606,3 +606,111 @@ void ko_local_fwd_batch(const uint8_t *seq, int64_t n, const int64_t *q_off,
                               e_del, o_ins, e_ins, minsc[k], endsc[k], max_sc, l);
     }
 }
+
+/* ------------------------------------------------------------------------- */
+/* Banded global alignment with traceback                                     */
+/* ------------------------------------------------------------------------- */
+
+#define KO_MINUS_INF (-0x40000000)
+
+static void cigar_push(uint32_t *cig, int *n, uint32_t op, uint32_t len)
+{
+    /* crates/bwa-extend/src/sw.rs:516-524: a repeated op extends the previous run */
+    if (*n > 0 && (cig[*n - 1] & 0xfu) == op) {
+        cig[*n - 1] += len << 4;
+        return;
+    }
+    cig[(*n)++] = (len << 4) | op;
+}
+
+int ko_global2(const uint8_t *q, int qlen, const uint8_t *t, int tlen, int m, const int8_t *mat,
+               int o_del, int e_del, int o_ins, int e_ins, int w, int32_t *score, uint32_t *cigar,
+               int *n_cigar)
+{
+    /* crates/bwa-extend/src/sw.rs:561-740.  cigar must hold qlen + tlen + 1 words.  Returns 0, or
+     * -1 where the reference's traceback index goes out of range (it panics there); its caller,
+     * crates/bwa-mem/src/cigar.rs:420-447, sizes w >= |tlen - qlen| + 3, which keeps the path in
+     * the band. */
+    const int oe_del = o_del + e_del, oe_ins = o_ins + e_ins;
+    if (w < 0) w = 0;
+    const int n_col = qlen < 2 * w + 1 ? qlen : 2 * w + 1;
+    uint8_t *z = malloc((size_t)(n_col > 0 ? n_col : 1) * (size_t)(tlen > 0 ? tlen : 1));
+    int32_t *eh_h = malloc(sizeof(int32_t) * (size_t)(qlen + 1));
+    int32_t *eh_e = malloc(sizeof(int32_t) * (size_t)(qlen + 1));
+    for (int j = 0; j <= qlen; ++j) { eh_h[j] = KO_MINUS_INF; eh_e[j] = KO_MINUS_INF; }
+    eh_h[0] = 0;
+    for (int j = 1; j <= (qlen < w ? qlen : w); ++j) eh_h[j] = -(o_ins + e_ins * j);
+    for (int i = 0; i < tlen; ++i) {
+        int32_t f = KO_MINUS_INF;
+        const int beg = i > w ? i - w : 0;
+        const int end = i + w + 1 < qlen ? i + w + 1 : qlen;
+        int32_t h1 = beg == 0 ? -(o_del + e_del * (i + 1)) : KO_MINUS_INF;
+        const int8_t *row = mat + t[i] * m;
+        uint8_t *zr = z + (size_t)i * (size_t)n_col;
+        for (int j = beg; j < end; ++j) {
+            int32_t mm = eh_h[j], e = eh_e[j];
+            eh_h[j] = h1;
+            mm += row[q[j]];
+            uint8_t d = mm < e ? 1 : 0;
+            int32_t h = mm >= e ? mm : e;
+            if (!(h >= f)) { d = 2; h = f; }
+            h1 = h;
+            int32_t tt = mm - oe_del;
+            e -= e_del;
+            if (e > tt) d |= 1 << 2;
+            else e = tt;
+            eh_e[j] = e;
+            tt = mm - oe_ins;
+            f -= e_ins;
+            if (f > tt) d |= 2 << 4;
+            else f = tt;
+            zr[j - beg] = d;
+        }
+        eh_h[end] = h1;
+        eh_e[end] = KO_MINUS_INF;
+    }
+    *score = eh_h[qlen];
+    /* traceback from the band's last cell of the last row (sw.rs:684-737) */
+    int n = 0, rc = 0;
+    long i = (long)tlen - 1;
+    long k = ((long)tlen - 1 + w + 1 < qlen ? (long)tlen - 1 + w + 1 : qlen) - 1;
+    int which = 0;
+    while (i >= 0 && k >= 0) {
+        const long beg = i > w ? i - w : 0;
+        /* the reference indexes the flat matrix: an offset past the row reads the next row's
+         * byte; below the row's start, or past the matrix, it stops with an index error */
+        const long flat = i * (long)n_col + (k - beg);
+        if (k < beg || flat >= (long)n_col * tlen) { rc = -1; break; }
+        const uint8_t d = z[flat];
+        which = (d >> (which << 1)) & 3;
+        if (which == 0) { cigar_push(cigar, &n, 0, 1); --i; --k; }
+        else if (which == 1) { cigar_push(cigar, &n, 2, 1); --i; }
+        else { cigar_push(cigar, &n, 1, 1); --k; }
+    }
+    if (rc == 0) {
+        if (i >= 0) cigar_push(cigar, &n, 2, (uint32_t)(i + 1));
+        if (k >= 0) cigar_push(cigar, &n, 1, (uint32_t)(k + 1));
+        for (int a = 0, b = n - 1; a < b; ++a, --b) { uint32_t x = cigar[a]; cigar[a] = cigar[b]; cigar[b] = x; }
+    }
+    *n_cigar = rc == 0 ? n : 0;
+    free(z); free(eh_h); free(eh_e);
+    return rc;
+}
+
+int ko_global2_batch(const uint8_t *seq, int64_t n, const int64_t *q_off, const int64_t *t_off,
+                     const int32_t *qlen, const int32_t *tlen, const int32_t *w, int m,
+                     const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins, int nthreads,
+                     int32_t *score, const int64_t *cig_off, uint32_t *cigar, int32_t *n_cigar)
+{
+    /* cigar[cig_off[k] ..] holds job k's runs (room for qlen + tlen + 1 words each). */
+    int nt = pick_threads(nthreads), bad = 0;
+    (void)nt;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nt) reduction(| : bad)
+    for (int64_t k = 0; k < n; ++k) {
+        int nc = 0;
+        bad |= ko_global2(seq + q_off[k], qlen[k], seq + t_off[k], tlen[k], m, mat, o_del, e_del, o_ins,
+                          e_ins, w[k], &score[k], cigar + cig_off[k], &nc) != 0;
+        n_cigar[k] = nc;
+    }
+    return bad ? -1 : 0;
+}

@@ -119,6 +119,17 @@ void ko_local_fwd_batch(const uint8_t *seq, int64_t n, const int64_t *q_off,
                         const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins,
                         int max_sc, int lanes, int nthreads, ko_fwd_result *out);
 
+/* ksw_global2, crates/bwa-extend/src/sw.rs:561-740: banded global alignment with traceback.
+ * cigar (room for qlen + tlen + 1 words) receives the runs (len << 4 | op, op 0=M 1=I 2=D).
+ * Returns 0, or -1 where the reference's traceback index would go out of range. */
+int ko_global2(const uint8_t *q, int qlen, const uint8_t *t, int tlen, int m, const int8_t *mat,
+               int o_del, int e_del, int o_ins, int e_ins, int w, int32_t *score, uint32_t *cigar,
+               int *n_cigar);
+int ko_global2_batch(const uint8_t *seq, int64_t n, const int64_t *q_off, const int64_t *t_off,
+                     const int32_t *qlen, const int32_t *tlen, const int32_t *w, int m,
+                     const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins, int nthreads,
+                     int32_t *score, const int64_t *cig_off, uint32_t *cigar, int32_t *n_cigar);
+
 /* bwa_fill_scmat, crates/bwa-core/src/opt.rs:419-460 (match a, mismatch -b, N -1). */
 void ko_fill_scmat(int a, int b, int8_t mat[25]);
 

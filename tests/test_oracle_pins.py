@@ -150,3 +150,100 @@ def test_band_clamp_truncates_toward_zero():
     assert oracle.clamp_band(100, 0, 1, 0, 6, 1, 6, 1) == 1
     assert oracle.clamp_band(100, 10, 1, 0, 6, 4, 6, 1) == 2   # (10-6)/4+1 = 2
     assert oracle.clamp_band(100, 3, 1, 0, 6, 4, 6, 1) == 1    # (3-6)/4+1 = 0.25 -> 0 -> 1
+
+
+# ---------------------------------------------------------------- ksw_global2
+
+def test_global2_kat_exact_match_is_all_m():
+    # crates/bwa-extend/src/sw.rs:1358-1365
+    s = [0, 1, 2, 3, 0, 1, 2, 3, 0, 1]
+    assert oracle.global2(s, s, 100) == (len(s), [len(s) << 4])
+
+
+def test_global2_kat_single_deletion():
+    # crates/bwa-extend/src/sw.rs:1367-1380
+    q = [0, 1, 2, 3, 0, 1, 2, 3]
+    t = q[:4] + [2] + q[4:]
+    _, cig = oracle.global2(q, t, 100)
+    assert sum(c >> 4 for c in cig if c & 0xf == 2) == 1
+    assert sum(c >> 4 for c in cig if c & 0xf == 0) == len(q)
+
+
+def _gotoh_global(q, t, mat, o_del, e_del, o_ins, e_ins, m=5):
+    """Textbook unbanded global affine-gap score (independent of the reference's code), with gaps
+    opened from the match state as ksw does; small inputs only."""
+    NEG = -(1 << 40)
+    Q, T = len(q), len(t)
+    M = [[NEG] * (Q + 1) for _ in range(T + 1)]
+    E = [[NEG] * (Q + 1) for _ in range(T + 1)]  # deletion: consumes target
+    F = [[NEG] * (Q + 1) for _ in range(T + 1)]  # insertion: consumes query
+    M[0][0] = 0
+    for j in range(1, Q + 1):
+        F[0][j] = -(o_ins + e_ins * j)
+    for i in range(1, T + 1):
+        E[i][0] = -(o_del + e_del * i)
+    for i in range(1, T + 1):
+        for j in range(1, Q + 1):
+            best_prev = max(M[i - 1][j - 1], E[i - 1][j - 1], F[i - 1][j - 1])
+            M[i][j] = best_prev + mat[t[i - 1] * m + q[j - 1]]
+            E[i][j] = max(M[i - 1][j] - o_del - e_del, E[i - 1][j] - e_del)
+            F[i][j] = max(M[i][j - 1] - o_ins - e_ins, F[i][j - 1] - e_ins)
+    return max(M[T][Q], E[T][Q], F[T][Q])
+
+
+def _cigar_score(q, t, cig, mat, o_del, e_del, o_ins, e_ins, m=5):
+    i = j = 0
+    s = 0
+    for c in cig:
+        op, ln = c & 0xf, c >> 4
+        if op == 0:
+            for _ in range(ln):
+                s += int(mat[t[i] * m + q[j]])
+                i += 1
+                j += 1
+        elif op == 1:
+            s -= o_ins + e_ins * ln
+            j += ln
+        else:
+            s -= o_del + e_del * ln
+            i += ln
+    assert (i, j) == (len(t), len(q))
+    return s
+
+
+def test_global2_against_textbook_and_own_cigar():
+    # wide band: the score equals an independent unbanded global DP; in any band where the path
+    # stays inside, re-scoring the returned CIGAR gives the returned score
+    rng = np.random.default_rng(3)
+    mat = oracle.scmat(1, 4)
+    for k in range(120):
+        t = rng.integers(0, 5 if k % 7 == 0 else 4, int(rng.integers(0, 40))).tolist()
+        q = list(t)
+        for _ in range(int(rng.integers(0, 4))):  # substitutions and short indels
+            if not q:
+                break
+            p = int(rng.integers(0, len(q)))
+            r = rng.random()
+            if r < 0.5:
+                q[p] = int(rng.integers(0, 4))
+            elif r < 0.75:
+                del q[p:p + int(rng.integers(1, 3))]
+            else:
+                q[p:p] = rng.integers(0, 4, int(rng.integers(1, 3))).tolist()
+        wide = max(len(q), len(t)) + 1
+        score, cig = oracle.global2(q, t, wide, mat)
+        assert score == _gotoh_global(q, t, mat, 6, 1, 6, 1), (q, t)
+        assert _cigar_score(q, t, cig, mat, 6, 1, 6, 1) == score
+        w = abs(len(t) - len(q)) + 3  # the caller's narrowest band, crates/bwa-mem/src/cigar.rs:438-445
+        r = oracle.global2(q, t, w, mat)
+        assert r is not None
+        if len(q) and len(t):
+            assert _cigar_score(q, t, r[1], mat, 6, 1, 6, 1) == r[0]
+
+
+def test_global2_edge_conventions():
+    # empty query: the whole target is one leading deletion; empty target: the traceback's
+    # leftover column count min(w, qlen) becomes the insertion (sw.rs:726-733)
+    assert oracle.global2([], [1, 2, 3], 5) == (-9, [3 << 4 | 2])
+    assert oracle.global2([1, 2, 3], [], 2) == (-0x40000000, [2 << 4 | 1])
+    assert oracle.global2([], [], 3) == (0, [])
