@@ -43,19 +43,13 @@ __device__ __forceinline__ bool job_ok(const bwacuda_ext_job &J)
            (J.tlen == 0 || J.target != nullptr);
 }
 
-// Slices are copied as whole aligned 16-byte words: a slice of len bytes at
-// host address src covers words [src >> 4, (src + len - 1) >> 4], and lands at
-// a 16-byte aligned HBM base plus (src & 15), so every word maps to one aligned
-// word of HBM.  The bytes of a covering word outside the slice lie in the same
-// page as bytes of the slice (a 16-byte word never straddles a page), so the
-// widened reads touch only mapped memory; in HBM they land in the slice's own
-// reserve.
-__device__ __forceinline__ uint32_t slice_words(const uint8_t *src, int len)
-{
-    const uint64_t a = reinterpret_cast<uint64_t>(src);
-    return len > 0 ? (uint32_t)(((a + (uint64_t)len - 1) >> 4) - (a >> 4) + 1) : 0u;
-}
-
+// Slices are copied as whole aligned 16-byte words (slice_words, common.cuh):
+// a slice of len bytes at host address src covers words [src >> 4,
+// (src + len - 1) >> 4] and lands at a 16-byte aligned HBM base plus
+// (src & 15), so every word maps to one aligned word of HBM.  The bytes of a
+// covering word outside the slice lie in the same page as bytes of the slice,
+// so the widened reads touch only mapped memory; in HBM they land in the
+// slice's own reserve.
 __global__ void ats_lengths_kernel(const bwacuda_ext_job *__restrict__ hjobs, uint32_t n, BinRule br,
                                    uint64_t *__restrict__ sizes, uint32_t *__restrict__ flags)
 {

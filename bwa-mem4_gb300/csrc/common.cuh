@@ -72,6 +72,16 @@ __host__ __device__ inline int clamp_band(int w, int qlen, int max_sc, int end_b
     return w;
 }
 
+// Aligned 16-byte words covering a slice of len bytes at address src.  A
+// device gather copies slices as whole words and places each one at a 16-byte
+// aligned base plus (src & 15); the widened reads stay in the slice's own pages
+// (a 16-byte word never straddles a page).
+__host__ __device__ inline uint32_t slice_words(const uint8_t *src, int len)
+{
+    const uint64_t a = reinterpret_cast<uint64_t>(src);
+    return len > 0 ? (uint32_t)(((a + (uint64_t)len - 1) >> 4) - (a >> 4) + 1) : 0u;
+}
+
 // bwa-mem's 8/16-bit bin label of an extension job, the rule of
 // crates/bwa-neon/src/batched.rs:817-865 split in two: bin_rule() summarises
 // the matrix once per call, bin_label() classifies one job (statistics only).

@@ -176,6 +176,124 @@ __global__ void global_compact_kernel(const GlobalDevJob *__restrict__ jobs, uin
     }
 }
 
+// ---- device-side planning and gather for host-buffer calls (pageable host memory)
+
+__device__ __forceinline__ bool gjob_ok(const bwacuda_global_job &J)
+{
+    return J.qlen >= 0 && J.tlen >= 0 && (J.qlen == 0 || J.query != nullptr) && (J.tlen == 0 || J.target != nullptr);
+}
+
+// One warp per group of 32 jobs: per-job base reserve and CIGAR capacity, per-group
+// traceback words, the chunk's longest query.  flags[0]: input error bits; flags[1]: max qlen.
+__global__ void glb_plan_kernel(const bwacuda_global_job *__restrict__ hj, uint32_t n, int qlim,
+                                uint64_t *__restrict__ seq_sz, uint64_t *__restrict__ cig_sz,
+                                uint64_t *__restrict__ z_sz, uint32_t *__restrict__ flags)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t ngroups = (n + 31) / 32;
+    for (uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ngroups; g += (gridDim.x * blockDim.x) >> 5) {
+        const uint32_t k = g * 32 + lane;
+        int tl = 0, nc = 0, ql = 0;
+        bool bad = false;
+        if (k < n) {
+            const bwacuda_global_job J = hj[k];
+            const bool ok = gjob_ok(J);
+            bad = !ok || J.qlen > qlim;
+            ql = ok ? J.qlen : 0;
+            tl = ok ? J.tlen : 0;
+            const int w = J.w < 0 ? 0 : J.w;
+            nc = ql < 2 * w + 1 ? ql : 2 * w + 1;
+            seq_sz[k] = ok ? 16ull * (slice_words(J.query, ql) + slice_words(J.target, tl)) : 0u;
+            cig_sz[k] = (uint64_t)ql + (uint64_t)tl + 1u;
+        }
+        const int tmax = __reduce_max_sync(0xffffffffu, (unsigned)tl);
+        const int ncmax = __reduce_max_sync(0xffffffffu, (unsigned)nc);
+        const int qmax = __reduce_max_sync(0xffffffffu, (unsigned)ql);
+        const unsigned anybad = __reduce_or_sync(0xffffffffu, bad ? 1u : 0u);
+        if (lane == 0) {
+            z_sz[g] = (uint64_t)tmax * (uint64_t)((ncmax + 3) / 4) * 32u;
+            if (anybad) atomicOr(flags, 1u);
+            atomicMax(flags + 1, (unsigned)qmax);
+        }
+    }
+}
+
+// One warp per group: lane l writes job g*32+l's descriptor, then the warp copies the
+// group's slices as aligned 16-byte words (one job at a time, lanes over its words).
+__global__ void __launch_bounds__(256) glb_gather_kernel(const bwacuda_global_job *__restrict__ hj, uint32_t n,
+                                                         const uint64_t *__restrict__ seq_off,
+                                                         const uint64_t *__restrict__ cig_off,
+                                                         const uint64_t *__restrict__ z_off,
+                                                         uint8_t *__restrict__ seq, GlobalDevJob *__restrict__ dj)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t ngroups = (n + 31) / 32;
+    for (uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ngroups; g += (gridDim.x * blockDim.x) >> 5) {
+        const uint32_t k = g * 32 + lane;
+        uint64_t qa = 0, ta = 0, base = 0;
+        uint32_t qw = 0, tw = 0;
+        int nc = 0;
+        GlobalDevJob D{};
+        if (k < n) {
+            const bwacuda_global_job J = hj[k];
+            const bool ok = gjob_ok(J);
+            const int ql = ok ? J.qlen : 0, tl = ok ? J.tlen : 0;
+            const int w = J.w < 0 ? 0 : J.w;
+            nc = ql < 2 * w + 1 ? ql : 2 * w + 1;
+            base = seq_off[k];
+            qa = reinterpret_cast<uint64_t>(J.query);
+            ta = reinterpret_cast<uint64_t>(J.target);
+            qw = slice_words(J.query, ql);
+            tw = slice_words(J.target, tl);
+            D.q_off = base + (qa & 15);
+            D.t_off = base + 16ull * qw + (ta & 15);
+            D.z_off = z_off[g];
+            D.cig_off = cig_off[k];
+            D.qlen = ql;
+            D.tlen = tl;
+            D.w = J.w;
+        }
+        D.ncw = (int)((__reduce_max_sync(0xffffffffu, (unsigned)nc) + 3) / 4);
+        if (k < n) dj[k] = D;
+        const uint32_t cnt = min(32u, n - g * 32);
+        for (uint32_t j = 0; j < cnt; ++j) {
+            const uint64_t jqa = __shfl_sync(0xffffffffu, qa, j) & ~15ull;
+            const uint64_t jta = __shfl_sync(0xffffffffu, ta, j) & ~15ull;
+            const uint64_t jb = __shfl_sync(0xffffffffu, base, j);
+            const uint32_t jqw = __shfl_sync(0xffffffffu, qw, j);
+            const uint32_t jtw = __shfl_sync(0xffffffffu, tw, j);
+            uint4 *dst = reinterpret_cast<uint4 *>(seq + jb);
+            for (uint32_t x = lane; x < jqw + jtw; x += 32) {
+                const uint4 *src = x < jqw ? reinterpret_cast<const uint4 *>(jqa) + x
+                                           : reinterpret_cast<const uint4 *>(jta) + (x - jqw);
+                dst[x] = *src;
+            }
+        }
+    }
+}
+
+// Results straight into the caller's arrays: score[k], cigar_off[k + 1] = base + doff[k + 1],
+// and (when the chunk's runs fit the caller's capacity) the runs themselves, one warp per job.
+__global__ void glb_store_kernel(const GlobalDevJob *__restrict__ dj, uint32_t n, const int32_t *__restrict__ dscore,
+                                 const uint32_t *__restrict__ cig, const int32_t *__restrict__ ncig,
+                                 const uint64_t *__restrict__ doff, uint64_t out_base, size_t cap,
+                                 int32_t *__restrict__ hscore, uint64_t *__restrict__ hoff, uint32_t *__restrict__ hcig)
+{
+    const bool fits = hcig != nullptr && out_base + doff[n] <= cap;
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < n; k += (gridDim.x * blockDim.x) >> 5) {
+        if (lane == 0) {
+            hscore[k] = dscore[k];
+            hoff[k + 1] = out_base + doff[k + 1];
+        }
+        if (fits) {
+            const uint32_t *src = cig + dj[k].cig_off;
+            uint32_t *dst = hcig + out_base + doff[k];
+            for (int x = (int)lane; x < ncig[k]; x += 32) dst[x] = src[x];
+        }
+    }
+}
+
 template <int TB>
 cudaError_t launch_global_tb(const uint8_t *seq, const GlobalDevJob *jobs, uint32_t n, const Scoring &sc, int qcap,
                              uint32_t *z, uint32_t *cig, int32_t *score, int32_t *ncig, uint32_t *err,
@@ -211,6 +329,9 @@ int global_max_qlen()
 struct GlobalBufs {
     HostBuf h_seq, h_jobs, h_res;
     DevBuf d_seq, d_jobs, d_z, d_cig, d_res, d_doff, d_dense, d_tmp;
+    // device-gather route
+    DevBuf d_sz, d_flags;
+    HostBuf h_tot;
 };
 
 }  // namespace
@@ -226,6 +347,7 @@ void global_release(bwacuda_ctx *c)
     b.h_seq.release(); b.h_jobs.release(); b.h_res.release();
     b.d_seq.release(); b.d_jobs.release(); b.d_z.release(); b.d_cig.release(); b.d_res.release();
     b.d_doff.release(); b.d_dense.release(); b.d_tmp.release();
+    b.d_sz.release(); b.d_flags.release(); b.h_tot.release();
     delete c->global;
     c->global = nullptr;
 }
@@ -233,6 +355,110 @@ void global_release(bwacuda_ctx *c)
 }  // namespace bwacuda
 
 using namespace bwacuda;
+
+namespace {
+
+// The device-gather route: planning, gather, DP, compaction and the result stores
+// run as kernels that read and write the caller's host arrays through the host
+// page tables; the host launches and reads back four words per chunk.
+int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n, const Scoring &sc, int32_t *score,
+                        uint64_t *cigar_off, uint32_t *cigar, size_t cigar_cap)
+{
+    GlobalBufs &b = c->global->b;
+    cudaStream_t s = c->stream;
+    uint32_t *d_err = static_cast<uint32_t *>(c->d_misc.p);
+    unsigned long long *d_cells = reinterpret_cast<unsigned long long *>((char *)c->d_misc.p + 8);
+    const size_t kChunk = 262144;
+    const int qlim = global_max_qlen();
+    int nsm = 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || nsm < 1) nsm = 1;
+    uint64_t out_base = 0;
+    bool short_buf = false;
+    int rc = BWACUDA_OK;
+    cudaError_t e = cudaSuccess;
+    if ((e = b.d_flags.ensure(64)) != cudaSuccess) return cuda_status(e);
+    if ((e = b.h_tot.ensure(64)) != cudaSuccess) return cuda_status(e);
+    uint64_t *ht = static_cast<uint64_t *>(b.h_tot.p);
+    for (size_t c0 = 0; c0 < n && rc == BWACUDA_OK; c0 += kChunk) {
+        const size_t cn = std::min(kChunk, n - c0);
+        const size_t ng = (cn + 31) / 32;
+        const bwacuda_global_job *hj = jobs + c0;
+        // planning arrays: seq sizes/offsets, cig sizes/offsets (cn + 1 each), z sizes/offsets (ng + 1 each)
+        if ((e = b.d_sz.ensure(((cn + 1) * 4 + (ng + 1) * 2) * 8 + 64)) != cudaSuccess) break;
+        uint64_t *seq_sz = static_cast<uint64_t *>(b.d_sz.p), *seq_off = seq_sz + cn + 1;
+        uint64_t *cig_sz = seq_off + cn + 1, *cig_off = cig_sz + cn + 1;
+        uint64_t *z_sz = cig_off + cn + 1, *z_off = z_sz + ng + 1;
+        uint32_t *flags = static_cast<uint32_t *>(b.d_flags.p);
+        size_t t1 = 0, t2 = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, t1, (const uint64_t *)nullptr, (uint64_t *)nullptr, (int)cn + 1);
+        cub::DeviceScan::ExclusiveSum(nullptr, t2, (const int32_t *)nullptr, (uint64_t *)nullptr, (int)cn + 1);
+        if ((e = b.d_tmp.ensure(std::max(t1, t2) + 64)) != cudaSuccess) break;
+        if ((e = cudaMemsetAsync(flags, 0, 16, s)) != cudaSuccess) break;
+        if ((e = cudaMemsetAsync(seq_sz + cn, 0, 8, s)) != cudaSuccess) break;
+        if ((e = cudaMemsetAsync(cig_sz + cn, 0, 8, s)) != cudaSuccess) break;
+        if ((e = cudaMemsetAsync(z_sz + ng, 0, 8, s)) != cudaSuccess) break;
+        uint32_t grid = (uint32_t)std::min<size_t>((ng * 32 + 255) / 256, (size_t)nsm * 8);
+        glb_plan_kernel<<<grid, 256, 0, s>>>(hj, (uint32_t)cn, qlim, seq_sz, cig_sz, z_sz, flags);
+        if ((e = cudaGetLastError()) != cudaSuccess) break;
+        if ((e = cub::DeviceScan::ExclusiveSum(b.d_tmp.p, t1, seq_sz, seq_off, (int)cn + 1, s)) != cudaSuccess) break;
+        if ((e = cub::DeviceScan::ExclusiveSum(b.d_tmp.p, t1, cig_sz, cig_off, (int)cn + 1, s)) != cudaSuccess) break;
+        if ((e = cub::DeviceScan::ExclusiveSum(b.d_tmp.p, t1, z_sz, z_off, (int)ng + 1, s)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(ht + 0, seq_off + cn, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(ht + 1, cig_off + cn, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(ht + 2, z_off + ng, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(ht + 3, flags, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) break;
+        const uint32_t fl = (uint32_t)ht[3], qmax = (uint32_t)(ht[3] >> 32);
+        if (fl & 1u) {
+            // an invalid job, or a query longer than the kernel takes: find which on the host
+            rc = BWACUDA_EINVAL;
+            for (size_t k = 0; k < cn; ++k)
+                if (hj[k].qlen > qlim && hj[k].qlen >= 0 && hj[k].tlen >= 0) rc = BWACUDA_EUNSUPPORTED;
+            break;
+        }
+        if ((e = b.d_seq.ensure(ht[0] + 16)) != cudaSuccess) break;
+        if ((e = b.d_cig.ensure(ht[1] * 4 + 16)) != cudaSuccess) break;
+        if ((e = b.d_z.ensure(ht[2] * 4 + 16)) != cudaSuccess) break;
+        if ((e = b.d_jobs.ensure(cn * sizeof(GlobalDevJob))) != cudaSuccess) break;
+        if ((e = b.d_res.ensure((cn + 1) * 8 + 16)) != cudaSuccess) break;
+        if ((e = b.d_doff.ensure((cn + 1) * 8)) != cudaSuccess) break;
+        GlobalDevJob *dj = static_cast<GlobalDevJob *>(b.d_jobs.p);
+        glb_gather_kernel<<<grid, 256, 0, s>>>(hj, (uint32_t)cn, seq_off, cig_off, z_off,
+                                              static_cast<uint8_t *>(b.d_seq.p), dj);
+        if ((e = cudaGetLastError()) != cudaSuccess) break;
+        int32_t *d_score = static_cast<int32_t *>(b.d_res.p);
+        int32_t *d_ncig = d_score + cn + 1;
+        uint64_t *d_doff = static_cast<uint64_t *>(b.d_doff.p);
+        if ((e = cudaMemsetAsync(d_ncig + cn, 0, 4, s)) != cudaSuccess) break;
+        e = launch_global(static_cast<const uint8_t *>(b.d_seq.p), dj, (uint32_t)cn, sc, (int)qmax + 1,
+                          static_cast<uint32_t *>(b.d_z.p), static_cast<uint32_t *>(b.d_cig.p), d_score, d_ncig, d_err,
+                          d_cells, s);
+        if (e != cudaSuccess) break;
+        if ((e = cub::DeviceScan::ExclusiveSum(b.d_tmp.p, t2, d_ncig, d_doff, (int)cn + 1, s)) != cudaSuccess) break;
+        grid = (uint32_t)std::min<size_t>((cn * 32 + 255) / 256, (size_t)nsm * 8);
+        glb_store_kernel<<<grid, 256, 0, s>>>(dj, (uint32_t)cn, d_score, static_cast<const uint32_t *>(b.d_cig.p), d_ncig,
+                                             d_doff, out_base, cigar ? cigar_cap : 0, score + c0, cigar_off + c0, cigar);
+        if ((e = cudaGetLastError()) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(ht + 4, d_doff + cn, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) break;
+        if (!cigar || out_base + ht[4] > cigar_cap) short_buf = true;
+        out_base += ht[4];
+        c->stats.kernel_launches += 9;
+    }
+    if (e != cudaSuccess) return cuda_status(e);
+    if (rc) {
+        uint64_t dummy;
+        collect_device_status(c, s, &dummy);
+        return rc;
+    }
+    uint64_t cells = 0;
+    if ((rc = collect_device_status(c, s, &cells)) != BWACUDA_OK) return rc;
+    c->stats.global_jobs += n;
+    c->stats.global_cells += cells;
+    return short_buf ? BWACUDA_ESHORT : BWACUDA_OK;
+}
+
+}  // namespace
 
 extern "C" int bwacuda_ksw_global2_batch(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n, int m,
                                          const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins,
@@ -245,6 +471,18 @@ extern "C" int bwacuda_ksw_global2_batch(bwacuda_ctx *c, const bwacuda_global_jo
     if (n && (!jobs || !score || !cigar_off)) return BWACUDA_EINVAL;
     if (cigar_off) cigar_off[0] = 0;
     if (n == 0) return BWACUDA_OK;
+    if (cudaSetDevice(c->device) != cudaSuccess) return BWACUDA_ECUDA;
+    if (!c->global) {
+        c->global = new (std::nothrow) GlobalState();
+        if (!c->global) return BWACUDA_ENOMEM;
+    }
+    const bool device_gather = c->host_gather == BWACUDA_GATHER_DEVICE ||
+                               (c->host_gather == BWACUDA_GATHER_AUTO && c->pageable_access);
+    if (device_gather) {
+        if (!c->pageable_access) return BWACUDA_EUNSUPPORTED;
+        return global_batch_device(c, jobs, n, make_scoring(m, mat, o_del, e_del, o_ins, e_ins), score, cigar_off,
+                                   cigar, cigar_cap);
+    }
     const int qlim = global_max_qlen();
     for (size_t k = 0; k < n; ++k) {
         const bwacuda_global_job &J = jobs[k];

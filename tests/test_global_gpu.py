@@ -9,6 +9,21 @@ import oracle
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(params=[pytest.param(B.GATHER_DEVICE, id="devgather"), pytest.param(B.GATHER_HOST, id="hostpack")])
+def gctx(ctx, request):
+    """The context with the host-buffer route under test (device gather needs pageable access)."""
+    ctx.set_option(B.OPT_HOST_GATHER, request.param)
+    if request.param == B.GATHER_DEVICE:
+        try:
+            ctx.ksw_global2_batch(B.JobSet.from_lists([[0, 1]], [[0, 1]], w=[3]))
+        except B.BwaCudaError as e:
+            ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_AUTO)
+            assert e.code == B.EUNSUPPORTED
+            pytest.skip("device cannot read pageable host memory")
+    yield ctx
+    ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_AUTO)
+
+
 def _cigars(offs, words):
     return [[int(x) for x in words[offs[k]:offs[k + 1]]] for k in range(len(offs) - 1)]
 
@@ -24,25 +39,25 @@ def _check(ctx, js, mat=None, o_del=6, e_del=1, o_ins=6, e_ins=1):
     return sc, offs, words
 
 
-def test_known_answers(ctx):
+def test_known_answers(gctx):
     # crates/bwa-extend/src/sw.rs:1358-1380
     s = [0, 1, 2, 3, 0, 1, 2, 3, 0, 1]
     q = [0, 1, 2, 3, 0, 1, 2, 3]
     t = q[:4] + [2] + q[4:]
     js = B.JobSet.from_lists([s, q], [s, t], w=[100, 100])
-    sc, offs, words = ctx.ksw_global2_batch(js)
+    sc, offs, words = gctx.ksw_global2_batch(js)
     cig = _cigars(offs, words)
     assert sc[0] == len(s) and cig[0] == [len(s) << 4]
     assert sum(c >> 4 for c in cig[1] if c & 0xf == 2) == 1
     assert sum(c >> 4 for c in cig[1] if c & 0xf == 0) == len(q)
 
 
-def test_cigar_stage_workload(ctx):
+def test_cigar_stage_workload(gctx):
     js = B.synth_global(200000, seed=3)
-    _check(ctx, js)
+    _check(gctx, js)
 
 
-def test_random_lengths_bands_and_scoring(ctx):
+def test_random_lengths_bands_and_scoring(gctx):
     rng = np.random.default_rng(11)
     qs, ts, ws = [], [], []
     for k in range(3000):
@@ -64,15 +79,15 @@ def test_random_lengths_bands_and_scoring(ctx):
         qs.append(q)
         ts.append(t)
     js = B.JobSet.from_lists(qs, ts, w=ws)
-    _check(ctx, js)
+    _check(gctx, js)
     # other scoring: larger match / gap values and a non-uniform matrix
-    _check(ctx, js, oracle.scmat(2, 5), 5, 2, 4, 3)
+    _check(gctx, js, oracle.scmat(2, 5), 5, 2, 4, 3)
     mat = rng.integers(-6, 4, 25).astype(np.int8)
     mat[0] = 3
-    _check(ctx, js, mat, 7, 1, 5, 2)
+    _check(gctx, js, mat, 7, 1, 5, 2)
 
 
-def test_edge_conventions(ctx):
+def test_edge_conventions(gctx):
     # empty query, empty target, both empty, narrow bands that cannot reach the corner
     qs = [[], [1, 2, 3], [], [0, 1, 2, 3] * 10, [0] * 30, [1, 2]]
     ts = [[1, 2, 3], [], [], [0, 1, 2, 3] * 12, [0] * 5, [1, 2, 3, 0, 0, 0, 0, 0]]
@@ -81,18 +96,18 @@ def test_edge_conventions(ctx):
     want = [oracle.global2(q, t, w) for q, t, w in zip(qs, ts, ws)]
     keep = [k for k, r in enumerate(want) if r is not None]
     sub = js.take(np.array(keep))
-    sc, offs, words = ctx.ksw_global2_batch(sub)
+    sc, offs, words = gctx.ksw_global2_batch(sub)
     cig = _cigars(offs, words)
     for i, k in enumerate(keep):
         assert (int(sc[i]), cig[i]) == want[k], k
     # where the reference's traceback index leaves the matrix, the call fails loudly
     for k in [k for k, r in enumerate(want) if r is None]:
         with pytest.raises(B.BwaCudaError) as e:
-            ctx.ksw_global2_batch(js.take(np.array([k])))
+            gctx.ksw_global2_batch(js.take(np.array([k])))
         assert e.value.code == B.EUNSUPPORTED
 
 
-def test_short_buffer_reports_sizes(ctx):
+def test_short_buffer_reports_sizes(gctx):
     js = B.synth_global(5000, seed=4)
     wsc, woffs, wwords = oracle.global2_batch(js)
     import ctypes as C
@@ -106,29 +121,29 @@ def test_short_buffer_reports_sizes(ctx):
     score = np.zeros(len(js), np.int32)
     offs = np.zeros(len(js) + 1, np.uint64)
     small = np.zeros(10, np.uint32)
-    rc = B.lib().bwacuda_ksw_global2_batch(ctx.h, C.c_void_p(jobs.ctypes.data), len(js), 5,
+    rc = B.lib().bwacuda_ksw_global2_batch(gctx.h, C.c_void_p(jobs.ctypes.data), len(js), 5,
                                            C.c_void_p(mat.ctypes.data), 6, 1, 6, 1,
                                            C.c_void_p(score.ctypes.data), C.c_void_p(offs.ctypes.data),
                                            C.c_void_p(small.ctypes.data), len(small))
     assert rc == B.ESHORT
     assert np.array_equal(score, wsc) and np.array_equal(offs.astype(np.int64), woffs)
     # sizes only: a NULL buffer
-    rc = B.lib().bwacuda_ksw_global2_batch(ctx.h, C.c_void_p(jobs.ctypes.data), len(js), 5,
+    rc = B.lib().bwacuda_ksw_global2_batch(gctx.h, C.c_void_p(jobs.ctypes.data), len(js), 5,
                                            C.c_void_p(mat.ctypes.data), 6, 1, 6, 1,
                                            C.c_void_p(score.ctypes.data), C.c_void_p(offs.ctypes.data), None, 0)
     assert rc == B.ESHORT and int(offs[-1]) == len(wwords)
 
 
-def test_invalid_inputs(ctx):
+def test_invalid_inputs(gctx):
     js = B.JobSet.from_lists([[0, 1, 7]], [[0, 1, 2]], w=[5])
     with pytest.raises(B.BwaCudaError) as e:
-        ctx.ksw_global2_batch(js)
+        gctx.ksw_global2_batch(js)
     assert e.value.code == B.EBASE
     js = B.JobSet.from_lists([[0, 1]], [[0, 1, 2]], w=[5])
     js.qlen[0] = -1
     with pytest.raises(B.BwaCudaError) as e:
-        ctx.ksw_global2_batch(js)
+        gctx.ksw_global2_batch(js)
     assert e.value.code == B.EINVAL
     # the context stays usable
     js = B.synth_global(100, seed=5)
-    _check(ctx, js)
+    _check(gctx, js)
