@@ -2,8 +2,11 @@
 // crates/bwa-extend/src/sw.rs:561-740), batched on the GPU.
 //
 // One thread per alignment.  The DP row pair (H and E of the previous row)
-// lives in shared memory, interleaved across the block (column j of thread t
-// at j * TB + t), with the query codes beside it.  The traceback byte of every
+// lives in shared memory, interleaved across the block (slot x of thread t at
+// x * TB + t), with the query codes beside it.  Only the band is kept: row i
+// reads and writes columns [i - w, i + w + 1] and every column it reads was
+// written by the previous row (or by the row -1 initialisation), so the row is
+// a circular buffer of B = min(2w + 2, qlen + 1) slots, column j in slot j % B.  The traceback byte of every
 // band cell (f << 4 | e << 2 | h, the reference's encoding) goes to HBM; the 32
 // jobs of a warp share one block there, interleaved word by word
 // (word (row * ncw + col / 4) * 32 + lane), so the warp's lanes, which sweep the
@@ -38,7 +41,19 @@ struct GlobalDevJob {
 };
 static_assert(sizeof(GlobalDevJob) == 48, "descriptor layout");
 
-__host__ __device__ inline size_t global_smem(int qcap, int tb) { return (size_t)tb * ((size_t)(qcap + 1) * 8 + qcap); }
+// Shared memory of a block: bcap band slots of {H, E} and qcap query codes per thread.
+__host__ __device__ inline size_t global_smem(int bcap, int qcap, int tb)
+{
+    return (size_t)tb * ((size_t)bcap * 8 + (size_t)qcap);
+}
+
+// Band slots a job needs.
+__host__ __device__ inline int global_band_slots(int qlen, int w)
+{
+    if (w < 0) w = 0;
+    const long long b = 2LL * w + 2;
+    return (int)(b < (long long)qlen + 1 ? b : (long long)qlen + 1);
+}
 
 __device__ __forceinline__ void cigar_push(uint32_t *cig, int &n, uint32_t op, uint32_t len)
 {
@@ -52,9 +67,9 @@ __device__ __forceinline__ void cigar_push(uint32_t *cig, int &n, uint32_t op, u
 template <int TB>
 __global__ void __launch_bounds__(TB)
 global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restrict__ jobs, uint32_t n,
-                  const __grid_constant__ Scoring sc, int qcap, uint32_t *__restrict__ z, uint32_t *__restrict__ cig,
-                  int32_t *__restrict__ score_out, int32_t *__restrict__ ncig_out, uint32_t *__restrict__ err,
-                  unsigned long long *__restrict__ cells_total)
+                  const __grid_constant__ Scoring sc, int bcap, int qcap, uint32_t *__restrict__ z,
+                  uint32_t *__restrict__ cig, int32_t *__restrict__ score_out, int32_t *__restrict__ ncig_out,
+                  uint32_t *__restrict__ err, unsigned long long *__restrict__ cells_total)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int tid = threadIdx.x;
@@ -62,24 +77,31 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
     unsigned long long ncells = 0;
     if (k >= n) return;
     const uint32_t lane = k & 31u;
-    int2 *cell = reinterpret_cast<int2 *>(smem_raw) + tid;  // cell[j * TB]: {H, E}
-    uint8_t *qs = smem_raw + (size_t)(qcap + 1) * 8 * TB + tid;  // qs[j * TB]: query code
+    int2 *cell = reinterpret_cast<int2 *>(smem_raw) + tid;        // cell[x * TB]: {H, E} of band slot x
+    uint8_t *qs = smem_raw + (size_t)bcap * 8 * TB + tid;          // qs[j * TB]: query code
     const GlobalDevJob J = jobs[k];
     const int qlen = J.qlen, tlen = J.tlen;
     const int w = J.w < 0 ? 0 : J.w;
     const int n_col = qlen < 2 * w + 1 ? qlen : 2 * w + 1;
+    const int B = global_band_slots(qlen, w);
     const int oe_del = sc.o_del + sc.e_del, oe_ins = sc.o_ins + sc.e_ins;
     const uint8_t *q = seq + J.q_off;
     const uint8_t *t = seq + J.t_off;
     uint32_t *zj = z + J.z_off + lane;
     bool bad = false;
+    if (B > bcap || qlen > qcap) {  // the host sizes bcap / qcap from the launch's jobs
+        atomicOr(err, ERR_RANGE);
+        ncig_out[k] = 0;
+        return;
+    }
     for (int j = 0; j < qlen; ++j) {
         uint32_t c = q[j];
         bad |= c >= (uint32_t)sc.m;
         qs[(size_t)j * TB] = (uint8_t)(c < (uint32_t)sc.m ? c : PAD_CODE);
     }
     // row -1: the origin, a leading insertion over columns 1..w, unreachable beyond
-    for (int j = 0; j <= qlen; ++j) {
+    // (slots 0..B-1 hold columns 0..B-1, which covers every column row 0 reads)
+    for (int j = 0; j < B; ++j) {
         int h = MINUS_INF;
         if (j == 0) h = 0;
         else if (j <= w) h = -(sc.o_ins + sc.e_ins * j);
@@ -96,8 +118,10 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
         const uint32_t plo = sc.prof[tc & 7u][0], phi = sc.prof[tc & 7u][1];
         uint32_t *zr = zj + (size_t)i * (size_t)J.ncw * 32u;
         uint32_t word = 0;
+        int x = beg % (B > 0 ? B : 1);  // slot of column j
         for (int j = beg; j < end; ++j) {
-            const int2 he = cell[(size_t)j * TB];
+            int2 *cp = cell + (size_t)x * TB;
+            const int2 he = *cp;
             int mm = he.x, e = he.y;
             mm += prof_score(plo, phi, qs[(size_t)j * TB]);
             uint32_t d = mm < e ? 1u : 0u;
@@ -107,7 +131,7 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
             e -= sc.e_del;
             if (e > tt) d |= 1u << 2;
             else e = tt;
-            cell[(size_t)j * TB] = make_int2(h1, e);  // H(i, j-1) for the next row's diagonal; E(i+1, j)
+            *cp = make_int2(h1, e);  // H(i, j-1) for the next row's diagonal; E(i+1, j)
             h1 = h;
             tt = mm - oe_ins;
             f -= sc.e_ins;
@@ -119,13 +143,20 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
                 zr[(size_t)(jj >> 2) * 32u] = word;
                 word = 0;
             }
+            if (++x == B) x = 0;
         }
-        cell[(size_t)end * TB] = make_int2(h1, MINUS_INF);
+        if (B > 0) cell[(size_t)(end % B) * TB] = make_int2(h1, MINUS_INF);
         // band cells this row did not reach read as 0, as in the reference's zeroed matrix
         for (int wi = end > beg ? (end - beg + 3) >> 2 : 0; wi < (n_col + 3) >> 2; ++wi) zr[(size_t)wi * 32u] = 0u;
         ncells += (unsigned long long)(end > beg ? end - beg : 0);
     }
-    score_out[k] = cell[(size_t)qlen * TB].x;
+    // eh_h[qlen] after the last row: written by that row's epilogue when its band reaches the last
+    // column, else still its row -1 value (the bands' ends never decrease)
+    const int end_last = tlen > 0 ? (tlen + w < qlen ? tlen + w : qlen) : -1;
+    int score;
+    if (end_last == qlen) score = cell[(size_t)(qlen % B) * TB].x;
+    else score = qlen == 0 ? 0 : (qlen <= w ? -(sc.o_ins + sc.e_ins * qlen) : MINUS_INF);
+    score_out[k] = score;
     // traceback from the band's last cell of the last row
     uint32_t *cg = cig + J.cig_off;
     int nc = 0;
@@ -184,7 +215,8 @@ __device__ __forceinline__ bool gjob_ok(const bwacuda_global_job &J)
 }
 
 // One warp per group of 32 jobs: per-job base reserve and CIGAR capacity, per-group
-// traceback words, the chunk's longest query.  flags[0]: input error bits; flags[1]: max qlen.
+// traceback words, the chunk's longest query.  flags[0]: input error bits; flags[1]: max qlen;
+// flags[2]: max band slots.
 __global__ void glb_plan_kernel(const bwacuda_global_job *__restrict__ hj, uint32_t n, int qlim,
                                 uint64_t *__restrict__ seq_sz, uint64_t *__restrict__ cig_sz,
                                 uint64_t *__restrict__ z_sz, uint32_t *__restrict__ flags)
@@ -193,7 +225,7 @@ __global__ void glb_plan_kernel(const bwacuda_global_job *__restrict__ hj, uint3
     const uint32_t ngroups = (n + 31) / 32;
     for (uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ngroups; g += (gridDim.x * blockDim.x) >> 5) {
         const uint32_t k = g * 32 + lane;
-        int tl = 0, nc = 0, ql = 0;
+        int tl = 0, nc = 0, ql = 0, bs = 0;
         bool bad = false;
         if (k < n) {
             const bwacuda_global_job J = hj[k];
@@ -204,16 +236,19 @@ __global__ void glb_plan_kernel(const bwacuda_global_job *__restrict__ hj, uint3
             const int w = J.w < 0 ? 0 : J.w;
             nc = ql < 2 * w + 1 ? ql : 2 * w + 1;
             seq_sz[k] = ok ? 16ull * (slice_words(J.query, ql) + slice_words(J.target, tl)) : 0u;
+            bs = global_band_slots(ql, J.w);
             cig_sz[k] = (uint64_t)ql + (uint64_t)tl + 1u;
         }
         const int tmax = __reduce_max_sync(0xffffffffu, (unsigned)tl);
         const int ncmax = __reduce_max_sync(0xffffffffu, (unsigned)nc);
         const int qmax = __reduce_max_sync(0xffffffffu, (unsigned)ql);
+        const int bmax = __reduce_max_sync(0xffffffffu, (unsigned)bs);
         const unsigned anybad = __reduce_or_sync(0xffffffffu, bad ? 1u : 0u);
         if (lane == 0) {
             z_sz[g] = (uint64_t)tmax * (uint64_t)((ncmax + 3) / 4) * 32u;
             if (anybad) atomicOr(flags, 1u);
             atomicMax(flags + 1, (unsigned)qmax);
+            atomicMax(flags + 2, (unsigned)bmax);
         }
     }
 }
@@ -295,34 +330,33 @@ __global__ void glb_store_kernel(const GlobalDevJob *__restrict__ dj, uint32_t n
 }
 
 template <int TB>
-cudaError_t launch_global_tb(const uint8_t *seq, const GlobalDevJob *jobs, uint32_t n, const Scoring &sc, int qcap,
-                             uint32_t *z, uint32_t *cig, int32_t *score, int32_t *ncig, uint32_t *err,
+cudaError_t launch_global_tb(const uint8_t *seq, const GlobalDevJob *jobs, uint32_t n, const Scoring &sc, int bcap,
+                             int qcap, uint32_t *z, uint32_t *cig, int32_t *score, int32_t *ncig, uint32_t *err,
                              unsigned long long *cells, cudaStream_t s)
 {
-    const size_t smem = global_smem(qcap, TB);
+    const size_t smem = global_smem(bcap, qcap, TB);
     auto kern = global_tpj_kernel<TB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<(n + TB - 1) / TB, TB, smem, s>>>(seq, jobs, n, sc, qcap, z, cig, score, ncig, err, cells);
+    kern<<<(n + TB - 1) / TB, TB, smem, s>>>(seq, jobs, n, sc, bcap, qcap, z, cig, score, ncig, err, cells);
     return cudaGetLastError();
 }
 
-cudaError_t launch_global(const uint8_t *seq, const GlobalDevJob *jobs, uint32_t n, const Scoring &sc, int qcap,
-                          uint32_t *z, uint32_t *cig, int32_t *score, int32_t *ncig, uint32_t *err,
+// bcap / qcap: the launch's largest band-slot count and query length.
+cudaError_t launch_global(const uint8_t *seq, const GlobalDevJob *jobs, uint32_t n, const Scoring &sc, int bcap,
+                          int qcap, uint32_t *z, uint32_t *cig, int32_t *score, int32_t *ncig, uint32_t *err,
                           unsigned long long *cells, cudaStream_t s)
 {
-    if (global_smem(qcap, 128) <= SMEM_LIMIT)
-        return launch_global_tb<128>(seq, jobs, n, sc, qcap, z, cig, score, ncig, err, cells, s);
-    if (global_smem(qcap, 64) <= SMEM_LIMIT)
-        return launch_global_tb<64>(seq, jobs, n, sc, qcap, z, cig, score, ncig, err, cells, s);
-    return launch_global_tb<32>(seq, jobs, n, sc, qcap, z, cig, score, ncig, err, cells, s);
+    if (global_smem(bcap, qcap, 64) <= SMEM_LIMIT)
+        return launch_global_tb<64>(seq, jobs, n, sc, bcap, qcap, z, cig, score, ncig, err, cells, s);
+    return launch_global_tb<32>(seq, jobs, n, sc, bcap, qcap, z, cig, score, ncig, err, cells, s);
 }
 
-// Longest query a 32-thread block holds.
+// Longest query a 32-thread block holds (its band slots are at most qlen + 1).
 int global_max_qlen()
 {
     int q = (int)(SMEM_LIMIT / (32 * 9));
-    while (q > 0 && global_smem(q + 1, 32) > SMEM_LIMIT) --q;
+    while (q > 0 && global_smem(q + 1, q, 32) > SMEM_LIMIT) --q;
     return q;
 }
 
@@ -406,9 +440,9 @@ int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n
         if ((e = cudaMemcpyAsync(ht + 0, seq_off + cn, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(ht + 1, cig_off + cn, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(ht + 2, z_off + ng, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
-        if ((e = cudaMemcpyAsync(ht + 3, flags, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(ht + 3, flags, 16, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) break;
-        const uint32_t fl = (uint32_t)ht[3], qmax = (uint32_t)(ht[3] >> 32);
+        const uint32_t fl = (uint32_t)ht[3], qmax = (uint32_t)(ht[3] >> 32), bmax = (uint32_t)ht[4];
         if (fl & 1u) {
             // an invalid job, or a query longer than the kernel takes: find which on the host
             rc = BWACUDA_EINVAL;
@@ -430,7 +464,7 @@ int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n
         int32_t *d_ncig = d_score + cn + 1;
         uint64_t *d_doff = static_cast<uint64_t *>(b.d_doff.p);
         if ((e = cudaMemsetAsync(d_ncig + cn, 0, 4, s)) != cudaSuccess) break;
-        e = launch_global(static_cast<const uint8_t *>(b.d_seq.p), dj, (uint32_t)cn, sc, (int)qmax + 1,
+        e = launch_global(static_cast<const uint8_t *>(b.d_seq.p), dj, (uint32_t)cn, sc, (int)bmax, (int)qmax,
                           static_cast<uint32_t *>(b.d_z.p), static_cast<uint32_t *>(b.d_cig.p), d_score, d_ncig, d_err,
                           d_cells, s);
         if (e != cudaSuccess) break;
@@ -439,10 +473,10 @@ int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n
         glb_store_kernel<<<grid, 256, 0, s>>>(dj, (uint32_t)cn, d_score, static_cast<const uint32_t *>(b.d_cig.p), d_ncig,
                                              d_doff, out_base, cigar ? cigar_cap : 0, score + c0, cigar_off + c0, cigar);
         if ((e = cudaGetLastError()) != cudaSuccess) break;
-        if ((e = cudaMemcpyAsync(ht + 4, d_doff + cn, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(ht + 5, d_doff + cn, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) break;
-        if (!cigar || out_base + ht[4] > cigar_cap) short_buf = true;
-        out_base += ht[4];
+        if (!cigar || out_base + ht[5] > cigar_cap) short_buf = true;
+        out_base += ht[5];
         c->stats.kernel_launches += 9;
     }
     if (e != cudaSuccess) return cuda_status(e);
@@ -508,7 +542,7 @@ extern "C" int bwacuda_ksw_global2_batch(bwacuda_ctx *c, const bwacuda_global_jo
         // grow the chunk 32 jobs (one warp group) at a time
         size_t cn = 0;
         uint64_t zwords = 0, cigw = 0, bytes = 0;
-        int qmax = 0;
+        int qmax = 0, bmax = 1;
         while (c0 + cn < n && cn < kMaxJobs) {
             const size_t g1 = std::min(n, c0 + cn + 32);
             int tmax = 0, ncmax = 0;
@@ -521,6 +555,7 @@ extern "C" int bwacuda_ksw_global2_batch(bwacuda_ctx *c, const bwacuda_global_jo
                 gb += (uint64_t)J.qlen + (uint64_t)J.tlen;
                 gc += (uint64_t)J.qlen + (uint64_t)J.tlen + 1;
                 qmax = std::max(qmax, J.qlen);
+                bmax = std::max(bmax, global_band_slots(J.qlen, J.w));
             }
             const uint64_t gz = (uint64_t)tmax * (uint64_t)((ncmax + 3) / 4) * 32u;
             if (cn > 0 && zwords + gz > kMaxZWords) break;
@@ -583,7 +618,7 @@ extern "C" int bwacuda_ksw_global2_batch(bwacuda_ctx *c, const bwacuda_global_jo
         if ((e = cudaMemsetAsync(d_ncig + cn, 0, 4, s)) != cudaSuccess) break;
         c->stats.h2d_bytes += bytes + cn * sizeof(GlobalDevJob);
         e = launch_global(static_cast<const uint8_t *>(b.d_seq.p), static_cast<const GlobalDevJob *>(b.d_jobs.p),
-                          (uint32_t)cn, sc, qmax + 1, static_cast<uint32_t *>(b.d_z.p),
+                          (uint32_t)cn, sc, bmax, qmax, static_cast<uint32_t *>(b.d_z.p),
                           static_cast<uint32_t *>(b.d_cig.p), d_score, d_ncig, d_err,
                           reinterpret_cast<unsigned long long *>((char *)c->d_misc.p + 8), s);
         if (e != cudaSuccess) break;
