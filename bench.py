@@ -67,8 +67,9 @@ def parse():
     ap.add_argument("--global-jobs", type=int, default=1024 * 1024)
     ap.add_argument("--serve-rates", default="50,500,2000", help="Poisson arrival rates (requests/s)")
     ap.add_argument("--serve-requests", type=int, default=600, help="requests per arrival rate")
-    ap.add_argument("--case", choices=["ext-batched", "ext-plain", "rescue"],
+    ap.add_argument("--case", choices=["ext-batched", "ext-plain", "ext-mixed", "ext-gather", "rescue", "global"],
                     help="profiling case: run the small workload twice through one path, no timing")
+    ap.add_argument("--lanes", type=int, default=8, help="rescue case: wavefront lanes per job")
     return ap.parse_args()
 
 
@@ -459,17 +460,30 @@ def run_case(args):
 
     ctx = B.Context(0)
     ctx.set_option(B.OPT_GRAPHS, 0)  # plain stream launches (no graph nodes) under the profiler
-    if args.case.startswith("ext"):
-        js = B.synth_ext(2, args.jobs, seed=0)
+    if args.case in ("ext-batched", "ext-plain", "ext-mixed"):
+        js = B.synth_ext(3 if args.case == "ext-mixed" else 2, args.jobs, seed=0)
         d_seq = torch.from_numpy(js.seq).cuda()
         d_jobs = torch.from_numpy(js.dev_ext_jobs().view(np.uint8)).cuda()
         d_out = torch.zeros(len(js) * 24, dtype=torch.uint8, device="cuda")
-        path = B.PATH_BATCHED if args.case == "ext-batched" else B.PATH_PLAIN
+        path = B.PATH_PLAIN if args.case == "ext-plain" else B.PATH_BATCHED
         for _ in range(2):
             ctx.extend_device(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), d_out.data_ptr(), path=path)
             ctx.sync()
+    elif args.case == "ext-gather":
+        # host buffers, batched path fed by the device gather (one chunk per call)
+        js = B.synth_ext(2, args.jobs, seed=0)
+        ctx.set_option(B.OPT_EXT_PATH, B.PATH_BATCHED)
+        ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_DEVICE)
+        ctx.set_option(B.OPT_CHUNK_JOBS, args.jobs)
+        for _ in range(2):
+            ctx.extend_batch(js)
+    elif args.case == "global":
+        js = B.synth_global(args.jobs, seed=0)
+        for _ in range(2):
+            ctx.ksw_global2_batch(js)
     else:
         js = B.synth_rescue(args.jobs, seed=0)
+        ctx.set_option(B.OPT_RESCUE_LANES, args.lanes)
         d_seq = torch.from_numpy(js.seq).cuda()
         d_jobs = torch.from_numpy(js.dev_res_jobs().view(np.uint8)).cuda()
         d_out = torch.zeros(len(js) * 28, dtype=torch.uint8, device="cuda")

@@ -78,9 +78,8 @@ __global__ void ats_lengths_kernel(const bwacuda_ext_job *__restrict__ hjobs, ui
 
 // A warp takes 32 consecutive jobs: lane i loads job i's descriptor (one
 // coalesced read of the caller's array) and writes its device descriptor; then
-// the warp copies the 32 jobs one after the other, lane l moving words l,
-// l + 32, ... of the job's query words followed by its target words.  An invalid
-// job becomes an empty one (qlen = tlen = 0, h0 = 1); the call then fails.
+// the warp copies all 32 jobs' words as one flat list (warp_gather_slices).  An
+// invalid job becomes an empty one (qlen = tlen = 0, h0 = 1); the call then fails.
 __global__ void __launch_bounds__(256) ats_gather_kernel(const bwacuda_ext_job *__restrict__ hjobs, uint32_t n,
                                                          const uint64_t *__restrict__ offs, int w,
                                                          uint8_t *__restrict__ seq,
@@ -110,20 +109,7 @@ __global__ void __launch_bounds__(256) ats_gather_kernel(const bwacuda_ext_job *
             D.w = w;
             djobs[k] = D;
         }
-        const uint32_t cnt = min(32u, n - k0);
-        for (uint32_t j = 0; j < cnt; ++j) {
-            const uint64_t jqa = __shfl_sync(0xffffffffu, qa, j) & ~15ull;
-            const uint64_t jta = __shfl_sync(0xffffffffu, ta, j) & ~15ull;
-            const uint64_t jb = __shfl_sync(0xffffffffu, base, j);
-            const uint32_t jqw = __shfl_sync(0xffffffffu, qw, j);
-            const uint32_t jtw = __shfl_sync(0xffffffffu, tw, j);
-            uint4 *dst = reinterpret_cast<uint4 *>(seq + jb);
-            for (uint32_t x = lane; x < jqw + jtw; x += 32) {
-                const uint4 *src = x < jqw ? reinterpret_cast<const uint4 *>(jqa) + x
-                                           : reinterpret_cast<const uint4 *>(jta) + (x - jqw);
-                dst[x] = *src;
-            }
-        }
+        warp_gather_slices(qa & ~15ull, ta & ~15ull, base, qw, tw, seq);
     }
 }
 

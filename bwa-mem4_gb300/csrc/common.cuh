@@ -82,6 +82,56 @@ __host__ __device__ inline uint32_t slice_words(const uint8_t *src, int len)
     return len > 0 ? (uint32_t)(((a + (uint64_t)len - 1) >> 4) - (a >> 4) + 1) : 0u;
 }
 
+#ifdef __CUDACC__
+// Copy the slices of the warp's 32 jobs (lane l's job: qw words at qa, then tw
+// words at ta, both 16-byte aligned addresses) to seq + base_l, as one flat list
+// of words over the whole warp: word x belongs to the lane whose exclusive
+// prefix of word counts is the largest one <= x (a 5-step shuffle search), and
+// every lane keeps four independent 16-byte loads in flight before storing.
+// All 32 lanes must call it.
+__device__ __forceinline__ void warp_gather_slices(uint64_t qa, uint64_t ta, uint64_t base, uint32_t qw, uint32_t tw,
+                                                   uint8_t *seq)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t wc = qw + tw;
+    uint32_t pre = wc;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, pre, o);
+        if (lane >= (uint32_t)o) pre += v;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, pre, 31);
+    pre -= wc;
+    for (uint32_t x0 = 0; x0 < total; x0 += 128) {
+        uint4 v[4];
+        uint4 *dst[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t x = x0 + (uint32_t)u * 32u + lane;
+            int j = 0;
+#pragma unroll
+            for (int st = 16; st > 0; st >>= 1) {
+                const uint32_t pj = __shfl_sync(0xffffffffu, pre, j + st);
+                if (x >= pj) j += st;
+            }
+            const uint32_t pre_j = __shfl_sync(0xffffffffu, pre, j);
+            const uint32_t qw_j = __shfl_sync(0xffffffffu, qw, j);
+            const uint64_t qa_j = __shfl_sync(0xffffffffu, qa, j);
+            const uint64_t ta_j = __shfl_sync(0xffffffffu, ta, j);
+            const uint64_t b_j = __shfl_sync(0xffffffffu, base, j);
+            const uint32_t wi = x - pre_j;
+            dst[u] = reinterpret_cast<uint4 *>(seq + b_j) + wi;
+            if (x < total)
+                v[u] = wi < qw_j ? reinterpret_cast<const uint4 *>(qa_j)[wi]
+                                 : reinterpret_cast<const uint4 *>(ta_j)[wi - qw_j];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (x0 + (uint32_t)u * 32u + lane < total) *dst[u] = v[u];
+    }
+}
+#endif
+
 // bwa-mem's 8/16-bit bin label of an extension job, the rule of
 // crates/bwa-neon/src/batched.rs:817-865 split in two: bin_rule() summarises
 // the matrix once per call, bin_label() classifies one job (statistics only).

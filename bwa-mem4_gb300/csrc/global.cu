@@ -254,7 +254,7 @@ __global__ void glb_plan_kernel(const bwacuda_global_job *__restrict__ hj, uint3
 }
 
 // One warp per group: lane l writes job g*32+l's descriptor, then the warp copies the
-// group's slices as aligned 16-byte words (one job at a time, lanes over its words).
+// group's slices as aligned 16-byte words (warp_gather_slices).
 __global__ void __launch_bounds__(256) glb_gather_kernel(const bwacuda_global_job *__restrict__ hj, uint32_t n,
                                                          const uint64_t *__restrict__ seq_off,
                                                          const uint64_t *__restrict__ cig_off,
@@ -290,20 +290,7 @@ __global__ void __launch_bounds__(256) glb_gather_kernel(const bwacuda_global_jo
         }
         D.ncw = (int)((__reduce_max_sync(0xffffffffu, (unsigned)nc) + 3) / 4);
         if (k < n) dj[k] = D;
-        const uint32_t cnt = min(32u, n - g * 32);
-        for (uint32_t j = 0; j < cnt; ++j) {
-            const uint64_t jqa = __shfl_sync(0xffffffffu, qa, j) & ~15ull;
-            const uint64_t jta = __shfl_sync(0xffffffffu, ta, j) & ~15ull;
-            const uint64_t jb = __shfl_sync(0xffffffffu, base, j);
-            const uint32_t jqw = __shfl_sync(0xffffffffu, qw, j);
-            const uint32_t jtw = __shfl_sync(0xffffffffu, tw, j);
-            uint4 *dst = reinterpret_cast<uint4 *>(seq + jb);
-            for (uint32_t x = lane; x < jqw + jtw; x += 32) {
-                const uint4 *src = x < jqw ? reinterpret_cast<const uint4 *>(jqa) + x
-                                           : reinterpret_cast<const uint4 *>(jta) + (x - jqw);
-                dst[x] = *src;
-            }
-        }
+        warp_gather_slices(qa & ~15ull, ta & ~15ull, base, qw, tw, seq);
     }
 }
 
