@@ -1,0 +1,170 @@
+// ext_persist.cuh -- the persistent bucket kernels of the batched extension
+// path (ext_persist.cu has the sort, the buckets and the overview).  Warps pull
+// 32 * GRAB consecutive sorted jobs per grab from the bucket's work counter;
+// GRAB (1, 2 or 4, picked by the autotuner) is a template parameter so each
+// value compiles to its own straight-line loop; ext_persist_g{1,2,4}.cu
+// instantiate one value each (separate translation units build in parallel).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "ext_job.cuh"
+#include "kernels.h"
+#include "persist.h"
+
+namespace bwacuda {
+namespace persist {
+
+template <class F, int TB, int GRAB>
+__global__ void __launch_bounds__(TB)
+ext_persist_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *__restrict__ jobs,
+                   const uint32_t *__restrict__ order, uint32_t *__restrict__ table,
+                   const __grid_constant__ ExtParams P, int qcap, bwacuda_ext_result *__restrict__ out,
+                   uint32_t *__restrict__ err, unsigned long long *__restrict__ cells_total)
+{
+    using CellT = typename F::T;
+    constexpr bool WIDE = sizeof(CellT) == 8;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int tid = threadIdx.x, lane = tid & 31;
+    CellT *cell = reinterpret_cast<CellT *>(smem_raw) + tid;
+    uint32_t *qw = reinterpret_cast<uint32_t *>(reinterpret_cast<CellT *>(smem_raw) + (size_t)qcap * TB) + tid;
+    const uint32_t start = table[0], stop = table[1];
+    uint32_t *counter = table + 2;
+    unsigned long long ncells = 0;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(counter, 32u * (uint32_t)GRAB);
+        base = __shfl_sync(0xffffffffu, base, 0) + start;
+        if (base >= stop) break;
+#pragma unroll
+        for (int g = 0; g < GRAB; ++g) {
+        const uint32_t k = base + 32u * (uint32_t)g + lane;
+        if (k < stop) {
+            const uint32_t jid = order[k];
+            const bwacuda_dev_ext_job J = jobs[jid];
+            const bool fits = WIDE || ext_fits_i16(J.qlen, J.tlen, J.h0, P.sc.max_sc);
+            if (J.qlen < 0 || J.qlen + 1 > qcap || !fits) {
+                atomicOr(err, ERR_RANGE);
+            } else {
+                bool bad = false;
+                const bwacuda_ext_result r = ext_run_job<F, TB>(cell, qw, seq, J, P, bad, ncells);
+                if (bad) atomicOr(err, ERR_BASE);
+                out[jid] = r;
+            }
+        }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ncells += __shfl_xor_sync(0xffffffffu, ncells, o);
+    if (lane == 0 && ncells) atomicAdd(cells_total, ncells);
+}
+
+// The same persistent loop over 8-bit pair cells.
+template <int TB, int GRAB>
+__global__ void __launch_bounds__(TB)
+ext_persist_u8p_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *__restrict__ jobs,
+                       const uint32_t *__restrict__ order, uint32_t *__restrict__ table,
+                       const __grid_constant__ ExtParams P, int qcap, bwacuda_ext_result *__restrict__ out,
+                       uint32_t *__restrict__ err, unsigned long long *__restrict__ cells_total)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int tid = threadIdx.x, lane = tid & 31;
+    uint32_t *cellw = reinterpret_cast<uint32_t *>(smem_raw) + tid;
+    uint32_t *qw = reinterpret_cast<uint32_t *>(smem_raw) + ((size_t)qcap / 2 + 2) * TB + tid;
+    const uint32_t start = table[0], stop = table[1];
+    uint32_t *counter = table + 2;
+    unsigned long long ncells = 0;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(counter, 32u * (uint32_t)GRAB);
+        base = __shfl_sync(0xffffffffu, base, 0) + start;
+        if (base >= stop) break;
+#pragma unroll
+        for (int g = 0; g < GRAB; ++g) {
+        const uint32_t k = base + 32u * (uint32_t)g + lane;
+        if (k < stop) {
+            const uint32_t jid = order[k];
+            const bwacuda_dev_ext_job J = jobs[jid];
+            if (J.qlen < 0 || J.qlen + 1 > qcap || !ext_fits_u8(J.qlen, J.tlen, J.h0, P.sc.max_sc)) {
+                atomicOr(err, ERR_RANGE);
+            } else {
+                bool bad = false;
+                const bwacuda_ext_result r = ext_run_job_u8p<TB>(cellw, qw, seq, J, P, bad, ncells);
+                if (bad) atomicOr(err, ERR_BASE);
+                out[jid] = r;
+            }
+        }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ncells += __shfl_xor_sync(0xffffffffu, ncells, o);
+    if (lane == 0 && ncells) atomicAdd(cells_total, ncells);
+}
+
+constexpr size_t SMEM_MAX = 227u * 1024u;
+
+template <class F, int TB, int GRAB>
+cudaError_t launch_persist_tb(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm)
+{
+    const size_t smem = ext_block_smem(d.qcap, TB, sizeof(typename F::T));
+    if (smem > SMEM_MAX) return cudaErrorInvalidValue;
+    auto kern = ext_persist_kernel<F, TB, GRAB>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TB, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidValue;
+    const int grid = per_sm * nsm;
+    kern<<<grid, TB, smem, L.stream>>>(L.seq, L.jobs, L.order, table, L.P, d.qcap, L.out, L.err, L.cells);
+    return cudaGetLastError();
+}
+
+template <int TB, int GRAB>
+cudaError_t launch_persist_u8p_tb(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm)
+{
+    const size_t smem = ext_block_smem_u8p(d.qcap, TB);
+    if (smem > SMEM_MAX) return cudaErrorInvalidValue;
+    auto kern = ext_persist_u8p_kernel<TB, GRAB>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TB, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidValue;
+    kern<<<per_sm * nsm, TB, smem, L.stream>>>(L.seq, L.jobs, L.order, table, L.P, d.qcap, L.out, L.err, L.cells);
+    return cudaGetLastError();
+}
+
+template <int GRAB>
+cudaError_t launch_persist_u8p(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm, int tb)
+{
+    if (tb >= 256 && ext_block_smem_u8p(d.qcap, 256) <= SMEM_MAX) return launch_persist_u8p_tb<256, GRAB>(L, d, table, nsm);
+    if (tb >= 128 && ext_block_smem_u8p(d.qcap, 128) <= SMEM_MAX) return launch_persist_u8p_tb<128, GRAB>(L, d, table, nsm);
+    if (tb >= 64 && ext_block_smem_u8p(d.qcap, 64) <= SMEM_MAX) return launch_persist_u8p_tb<64, GRAB>(L, d, table, nsm);
+    return launch_persist_u8p_tb<32, GRAB>(L, d, table, nsm);
+}
+
+template <class F, int GRAB>
+cudaError_t launch_persist(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm, int tb)
+{
+    const int cb = sizeof(typename F::T);
+    // requested block size if it fits, else the largest that does
+    if (tb >= 256 && ext_block_smem(d.qcap, 256, cb) <= SMEM_MAX) return launch_persist_tb<F, 256, GRAB>(L, d, table, nsm);
+    if (tb >= 128 && ext_block_smem(d.qcap, 128, cb) <= SMEM_MAX) return launch_persist_tb<F, 128, GRAB>(L, d, table, nsm);
+    if (tb >= 64 && ext_block_smem(d.qcap, 64, cb) <= SMEM_MAX) return launch_persist_tb<F, 64, GRAB>(L, d, table, nsm);
+    return launch_persist_tb<F, 32, GRAB>(L, d, table, nsm);
+}
+
+// One bucket's persistent launch with GRAB 32-job rounds per work grab.
+template <int GRAB>
+cudaError_t ext_persist_launch_grab(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm, int tb)
+{
+    if (d.cls == 0) return launch_persist_u8p<GRAB>(L, d, table, nsm, tb);
+    return d.cls == 2 ? launch_persist<FmtI32, GRAB>(L, d, table, nsm, tb)
+                      : launch_persist<FmtI16, GRAB>(L, d, table, nsm, tb);
+}
+
+
+}  // namespace persist
+}  // namespace bwacuda

@@ -39,6 +39,10 @@ cudaError_t ext_sort_and_bucket(const bwacuda_dev_ext_job *jobs, size_t n, int m
                                 uint16_t *keys_out, uint32_t *idx_in, uint32_t *idx_out, void *tmp,
                                 size_t tmp_bytes, const ExtBucketDef *d_defs, int nb, uint32_t *d_table,
                                 cudaStream_t s);
+// per-grab instantiations (ext_persist_g1.cu, _g2.cu, _g4.cu)
+cudaError_t ext_persist_launch_g1(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm, int tb);
+cudaError_t ext_persist_launch_g2(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm, int tb);
+cudaError_t ext_persist_launch_g4(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm, int tb);
 cudaError_t ext_persist_launch(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *d_bucket_table, int nsm,
                                int tb);
 
