@@ -159,6 +159,24 @@ int validate_scoring(int m, const int8_t *mat, int o_del, int e_del, int o_ins, 
     return BWACUDA_OK;
 }
 
+// The ungapped fast path's gate and threshold, crates/bwa-neon/src/batched.rs:721-765:
+// uniform matrix only (and bwa's 5-letter alphabet, where code 4 = N declines the
+// fast path and codes >= 5 reach the DP, which reports them);
+// x = (o_min + e_min - 1) / (a + b), the most mismatches a diagonal may carry
+// while every gapped alternative scores strictly less.
+UngappedRule ungapped_rule(const bwacuda_ctx *c, int m, const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins)
+{
+    UngappedRule u{0, 0, 0, -1};
+    if (!c->ungapped || m != 5 || !bin_rule(m, mat).uniform) return u;
+    u.enabled = 1;
+    u.a = mat[0];
+    u.b = -(int)mat[1];
+    const int o_min = std::min(o_del, o_ins), e_min = std::min(e_del, e_ins);
+    const int denom = u.a + u.b;
+    u.x = denom > 0 ? (o_min + e_min - 1) / denom : -1;
+    return u;
+}
+
 // bwa-mem's 8/16-bit bin label, crates/bwa-neon/src/batched.rs:817-865 (statistics only).
 int ext_bin_label(int qlen, int tlen, int h0, int m, const int8_t *mat)
 {
@@ -267,6 +285,10 @@ extern "C" int bwacuda_set_option(bwacuda_ctx *c, int option, int64_t value)
         if (value != 16 && value != 32 && value != 64) return BWACUDA_EINVAL;
         if (cudaSetDevice(c->device) != cudaSuccess) return BWACUDA_ECUDA;
         return batched_set_bucket_step(c, (int)value);
+    case BWACUDA_OPT_UNGAPPED:
+        if (value != 0 && value != 1) return BWACUDA_EINVAL;
+        c->ungapped = value != 0;
+        return BWACUDA_OK;
     case BWACUDA_OPT_RESCUE_LANES:
         if (value != 8 && value != 16 && value != 32) return BWACUDA_EINVAL;
         c->rescue_lanes = (int)value;
@@ -548,6 +570,7 @@ int extend_batch_host(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int
     P.sc = make_scoring(m, mat, o_del, e_del, o_ins, e_ins);
     P.end_bonus = end_bonus;
     P.zdrop = zdrop;
+    P.ug = ungapped_rule(c, m, mat, o_del, e_del, o_ins, e_ins);
     if (c->ext_path == BWACUDA_PATH_BATCHED) {
         const bool device_gather = c->host_gather == BWACUDA_GATHER_DEVICE ||
                                    (c->host_gather == BWACUDA_GATHER_AUTO && c->pageable_access);
@@ -912,6 +935,7 @@ extern "C" int bwacuda_extend_device(bwacuda_ctx *c, const uint8_t *d_seq, const
     P.sc = make_scoring(scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
     P.end_bonus = end_bonus;
     P.zdrop = zdrop;
+    P.ug = ungapped_rule(c, scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
     if (path == BWACUDA_PATH_BATCHED) return extend_device_batched(c, d_seq, d_jobs, n, P, d_out, s);
     int qmax = 0;
     if ((rc = device_qmax(c, d_jobs, n, s, &qmax)) != BWACUDA_OK) return rc;

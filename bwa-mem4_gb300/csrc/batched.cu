@@ -151,7 +151,8 @@ static cudaError_t enqueue_batched(bwacuda_ctx *c, BatchBufs &bb, const uint8_t 
                                    unsigned long long *cells = nullptr)
 {
     BatchedState *B = c->batched;
-    cudaError_t e = ext_sort_and_bucket(d_jobs, n, P.sc.max_sc, static_cast<uint16_t *>(bb.keys_in.p),
+    cudaError_t e = ext_sort_and_bucket(d_jobs, n, P.sc.max_sc, d_seq, P.ug, P.zdrop, d_out,
+                                        static_cast<uint16_t *>(bb.keys_in.p),
                                         static_cast<uint16_t *>(bb.keys_out.p), static_cast<uint32_t *>(bb.idx_in.p),
                                         static_cast<uint32_t *>(bb.idx_out.p), bb.tmp.p, bb.tmp.cap,
                                         static_cast<const ExtBucketDef *>(B->d_defs.p), B->nb,

@@ -22,9 +22,18 @@ struct Scoring {
     uint32_t prof[8][2]; // profile rows, see above; rows >= m unused
 };
 
+// The ungapped-diagonal fast path of the reference's batched extension
+// (crates/bwa-neon/src/batched.rs:602-697, gated at :721-775): enabled only for a
+// uniform matrix; a = match score, b = mismatch penalty magnitude, x = the most
+// mismatches a diagonal may carry and still be provably optimal.
+struct UngappedRule {
+    int32_t enabled, a, b, x;
+};
+
 struct ExtParams {
     Scoring sc;
     int32_t end_bonus, zdrop;
+    UngappedRule ug;
 };
 
 // Device error flags (OR-ed into ctx->d_err).

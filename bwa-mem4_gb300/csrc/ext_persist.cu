@@ -38,11 +38,64 @@ __device__ __forceinline__ uint16_t ext_sort_key(const bwacuda_dev_ext_job &J, i
     return (uint16_t)((cls << 14) | ((1023u - ql) << 4) | (15u - tb));
 }
 
+// ungapped_hit (crates/bwa-neon/src/batched.rs:602-697): the result of a job whose
+// diagonal carries at most x mismatches, no N and no z-drop, or false ("run the DP").
+__device__ bool ungapped_hit(const uint8_t *q, int qlen, const uint8_t *t, int tlen, int h0, const UngappedRule &u,
+                             int zdrop, bwacuda_ext_result &r)
+{
+    if (qlen == 0 || h0 <= 0 || tlen < qlen || u.x < 0) return false;
+    // mismatch columns; only the first 128 are representable (the reference's u128 bitmap)
+    uint32_t mis[4] = {0u, 0u, 0u, 0u};
+    int nmis = 0;
+    for (int c = 0; c < qlen; ++c) {
+        const uint32_t qb = q[c], tb = t[c];
+        if (qb >= 4u || tb >= 4u) return false;
+        if (qb != tb) {
+            if (++nmis > u.x) return false;
+            if (c >= 128) return false;
+            mis[c >> 5] |= 1u << (c & 31);
+        }
+    }
+    if (nmis == 0) {
+        const int s = h0 + qlen * u.a;
+        r.score = s; r.qle = qlen; r.tle = qlen; r.gtle = qlen; r.gscore = s; r.max_off = 0;
+        return true;
+    }
+    if (qlen > 128) return false;
+    int run = h0, best = h0, best_end = 0;
+    for (int c = 0; c < qlen; ++c) {
+        if (run == 0) continue;
+        if (((mis[c >> 5] >> (c & 31)) & 1u) == 0u) run += u.a;
+        else {
+            run -= u.b;
+            if (run < 0) run = 0;
+        }
+        if (run > best) { best = run; best_end = c + 1; }
+        else if (zdrop > 0 && best - run > zdrop) return false;
+    }
+    if (run == 0) return false;
+    r.score = best; r.qle = best_end; r.tle = best_end; r.gtle = qlen; r.gscore = run; r.max_off = 0;
+    return true;
+}
+
+// Sort keys; with the ungapped rule on, jobs it settles get their result here
+// and key class 3, which no bucket covers.
 __global__ void ext_keys_kernel(const bwacuda_dev_ext_job *__restrict__ jobs, uint32_t n, int max_sc,
-                                uint16_t *__restrict__ keys, uint32_t *__restrict__ idx)
+                                const uint8_t *__restrict__ seq, const UngappedRule ug, int zdrop,
+                                bwacuda_ext_result *__restrict__ out, uint16_t *__restrict__ keys,
+                                uint32_t *__restrict__ idx)
 {
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        keys[k] = ext_sort_key(jobs[k], max_sc);
+        const bwacuda_dev_ext_job J = jobs[k];
+        uint16_t key = ext_sort_key(J, max_sc);
+        if (ug.enabled) {
+            bwacuda_ext_result r;
+            if (ungapped_hit(seq + J.q_off, J.qlen, seq + J.t_off, J.tlen, J.h0, ug, zdrop, r)) {
+                out[k] = r;
+                key = (uint16_t)(3u << 14);
+            }
+        }
+        keys[k] = key;
         idx[k] = k;
     }
 }
@@ -130,7 +183,8 @@ size_t ext_sort_temp_bytes(size_t n)
     return bytes;
 }
 
-cudaError_t ext_sort_and_bucket(const bwacuda_dev_ext_job *jobs, size_t n, int max_sc, uint16_t *keys_in,
+cudaError_t ext_sort_and_bucket(const bwacuda_dev_ext_job *jobs, size_t n, int max_sc, const uint8_t *seq,
+                                const UngappedRule &ug, int zdrop, bwacuda_ext_result *out, uint16_t *keys_in,
                                 uint16_t *keys_out, uint32_t *idx_in, uint32_t *idx_out, void *tmp,
                                 size_t tmp_bytes, const ExtBucketDef *d_defs, int nb, uint32_t *d_table,
                                 cudaStream_t s)
@@ -138,7 +192,7 @@ cudaError_t ext_sort_and_bucket(const bwacuda_dev_ext_job *jobs, size_t n, int m
     if (n == 0) return cudaSuccess;
     uint32_t grid = (uint32_t)((n + 255) / 256);
     if (grid > 8192) grid = 8192;
-    ext_keys_kernel<<<grid, 256, 0, s>>>(jobs, (uint32_t)n, max_sc, keys_in, idx_in);
+    ext_keys_kernel<<<grid, 256, 0, s>>>(jobs, (uint32_t)n, max_sc, seq, ug, zdrop, out, keys_in, idx_in);
     cudaError_t e = cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys_in, keys_out, idx_in, idx_out, (int)n, 0,
                                                     16, s);
     if (e != cudaSuccess) return e;

@@ -69,6 +69,7 @@ int cuda_status(cudaError_t e);
 Scoring make_scoring(int m, const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins);
 int validate_scoring(int m, const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins);
 int ext_bin_label(int qlen, int tlen, int h0, int m, const int8_t *mat);
+UngappedRule ungapped_rule(const bwacuda_ctx *c, int m, const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins);
 
 }  // namespace bwacuda
 
@@ -88,6 +89,7 @@ struct bwacuda_ctx {
     bool use_graphs = true;
     int rescue_kernel = BWACUDA_RESCUE_AUTO;
     int rescue_lanes = 16;  // lanes per job of the register wavefront (8, 16, 32)
+    bool ungapped = false;  // ungapped-diagonal fast path on the batched extension path
     int tune_candidates = 0;        // last autotune call
     double tuned_ext_gcups = 0.0;   // best candidates' rates on their samples
     double tuned_rescue_gcups = 0.0;

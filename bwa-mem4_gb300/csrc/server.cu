@@ -587,6 +587,7 @@ extern "C" int bwacuda_server_submit_extend(bwacuda_ctx *c, const bwacuda_ext_jo
     r->P.sc = make_scoring(sc->m, sc->mat, sc->o_del, sc->e_del, sc->o_ins, sc->e_ins);
     r->P.end_bonus = end_bonus;
     r->P.zdrop = zdrop;
+    r->P.ug = ungapped_rule(c, sc->m, sc->mat, sc->o_del, sc->e_del, sc->o_ins, sc->e_ins);
     rc = submit(c, r);
     if (rc == BWACUDA_OK) *req_id = r->id;
     return rc;

@@ -131,6 +131,7 @@ extern "C" int bwacuda_autotune_extend(bwacuda_ctx *c, const uint8_t *d_seq, con
         P.sc = make_scoring(scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
         P.end_bonus = end_bonus;
         P.zdrop = zdrop;
+        P.ug = ungapped_rule(c, scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
         const bwacuda_stats saved = c->stats;
         const bool graphs = c->use_graphs;
         c->use_graphs = false;

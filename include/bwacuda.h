@@ -127,6 +127,12 @@ typedef struct bwacuda_ctx bwacuda_ctx;
 #define BWACUDA_OPT_BUCKET_STEP 8
 /* Rescue register wavefront: lanes per job (8, 16 or 32). */
 #define BWACUDA_OPT_RESCUE_LANES 9
+/* Batched extension: settle jobs whose seed diagonal carries at most
+ * (o_min + e_min - 1) / (a + b) mismatches in closed form before the DP (the
+ * reference's ungapped_hit fast path, crates/bwa-neon/src/batched.rs:602-697;
+ * uniform 5x5 matrices only).  Results are identical with it on or off; 0 = off
+ * (default), 1 = on. */
+#define BWACUDA_OPT_UNGAPPED 10
 
 int bwacuda_ctx_create(int device, bwacuda_ctx **out);
 void bwacuda_ctx_destroy(bwacuda_ctx *ctx);

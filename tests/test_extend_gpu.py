@@ -360,3 +360,43 @@ def test_cell_counter_matches_oracle(ctx):
     assert st["ext_cells"] == cells
     assert st["ext_jobs"] == len(js)
     assert st["ext_bin_u8"] + st["ext_bin_i16"] + st["ext_bin_i32"] == len(js)
+
+
+@pytest.fixture
+def ugctx(ctx):
+    """The context with the ungapped-diagonal fast path on (batched path)."""
+    ctx.set_option(B.OPT_UNGAPPED, 1)
+    yield ctx
+    ctx.set_option(B.OPT_UNGAPPED, 0)
+
+
+def test_ungapped_prefilter_on_reference_streams(ugctx):
+    # the reference's own ungapped stream (random z-drop, N bases, 1..3 mismatches) and the
+    # swept-scoring gate stream: the closed form must agree with the DP wherever it fires
+    for k, c in enumerate(R.ungapped()):
+        _check_batch(ugctx, c["qs"], c["ts"], c["h0s"], c["a"], c["b"], c["o_del"], c["e_del"], c["o_ins"],
+                     c["e_ins"], c["w"], c["end_bonus"], c["zdrop"], path=(B.PATH_BATCHED, B.GATHER_AUTO),
+                     what=f"ungapped round {k}")
+    groups = {}
+    for c in R.backend_matches_scalar():
+        key = (c["a"], c["b"], c["o_del"], c["e_del"], c["o_ins"], c["e_ins"], c["w"], c["end_bonus"], c["zdrop"])
+        groups.setdefault(key, []).append(c)
+    for key, cs in groups.items():
+        a, b, od, ed, oi, ei, w, eb, zd = key
+        _check_batch(ugctx, [c["q"] for c in cs], [c["t"] for c in cs], [c["h0"] for c in cs], a, b, od, ed, oi,
+                     ei, w, eb, zd, path=(B.PATH_BATCHED, B.GATHER_AUTO), what=f"gate {key}")
+
+
+@pytest.mark.parametrize("cfg,n", [(1, 20000), (2, 200000), (3, 60000)])
+def test_ungapped_prefilter_on_workloads(ugctx, cfg, n):
+    js = B.synth_ext(cfg, n, seed=30 + cfg)
+    want, cells = oracle.extend_batch(js)
+    got = _device_run(ugctx, js, B.PATH_BATCHED, reps=2)
+    for g in got:
+        assert np.array_equal(g, want)
+    _check_jobset(ugctx, js, path=(B.PATH_BATCHED, B.GATHER_AUTO))
+    if cfg == 2:
+        # the fast path settled most clean read-pair jobs: far fewer DP cells were run
+        ugctx.reset_stats()
+        ugctx.extend_batch(js, w=100) if len(np.unique(js.w)) == 1 else None
+        assert ugctx.stats()["ext_cells"] < cells // 4
