@@ -657,6 +657,22 @@ def main():
         e2e["route"] = best
         e2e["routes"] = {k: {"value": v["value"], "ms_per_step": v["ms_per_step"]} for k, v in routes.items()}
 
+    # the reference's ungapped-diagonal fast path (opt-in): same results, most clean read-pair
+    # jobs settled in closed form before the DP
+    ug = None
+    if not args.no_e2e:
+        ctx.set_option(B.OPT_UNGAPPED, 1)
+        ms_u, st_u = timed_device(B.PATH_BATCHED, max(1, min(args.steps, 5)), 2)
+        ms_u = max_over_ranks(ms_u) / max(1, min(args.steps, 5))
+        ug_same = bool(np.array_equal(batched_out, d_out.cpu().numpy().view(B.EXT_RES)))
+        ctx.set_option(B.OPT_UNGAPPED, 0)
+        ug = {"ms_per_step": round(ms_u, 3), "jobs_per_s": round(n * world / (ms_u / 1e3), 1),
+              "equivalent_gcups": round(cells_step * world / (ms_u / 1e3) / 1e9, 2),
+              "dp_cells_per_step": int(st_u["ext_cells"] / max(1, min(args.steps, 5))),
+              "identical_to_full_dp": ug_same,
+              "note": "BWACUDA_OPT_UNGAPPED: equivalent_gcups = the full DP's cells / this time (the "
+                      "reference's production path applies the same fast path)"}
+
     # roofline: integer-ALU bound (no tensor cores, about 0.03 B of HBM per cell)
     pk, kind = peaks()
     nsm = torch.cuda.get_device_properties(local).multi_processor_count
@@ -693,6 +709,8 @@ def main():
     }
     if e2e:
         line["e2e"] = e2e
+    if ug:
+        line["ungapped_prefilter"] = ug
     if not args.no_configs:
         line["configs"] = other_configs(args, B, ctx, st, barrier, max_over_ranks, world, rank)
     if not args.no_serve and world == 1:
