@@ -52,7 +52,7 @@ class Scoring(C.Structure):
 
 STAT_FIELDS = ("ext_jobs", "ext_cells", "ext_bin_u8", "ext_bin_i16", "ext_bin_i32", "rescue_jobs",
                "rescue_cells", "rescue_width_u8", "rescue_width_i16", "rescue_width_i32",
-               "kernel_launches", "h2d_bytes", "d2h_bytes", "global_jobs", "global_cells")
+               "kernel_launches", "h2d_bytes", "d2h_bytes", "global_jobs", "global_cells", "ext_retry_jobs")
 
 
 class ServerConfig(C.Structure):
@@ -80,7 +80,8 @@ EXPORTS = ("bwacuda_ctx_create", "bwacuda_ctx_destroy", "bwacuda_set_option", "b
            "bwacuda_ksw_align2_device_noalloc", "bwacuda_server_start", "bwacuda_server_stop",
            "bwacuda_server_submit_extend", "bwacuda_server_submit_rescue", "bwacuda_server_wait",
            "bwacuda_server_stats", "bwacuda_measure_alu_peak", "bwacuda_get_tuning", "bwacuda_autotune_extend",
-           "bwacuda_autotune_rescue", "bwacuda_ksw_global2_batch")
+           "bwacuda_autotune_rescue", "bwacuda_ksw_global2_batch", "bwacuda_extend_batch_retry",
+           "bwacuda_extend_retry_device")
 
 _lib = None
 _synth = None
@@ -106,6 +107,8 @@ def lib():
     L.bwacuda_measure_alu_peak.argtypes = [vp, C.POINTER(C.c_double)]
     L.bwacuda_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.bwacuda_ksw_global2_batch.argtypes = [vp, vp, sz, I, vp, I, I, I, I, vp, vp, vp, sz]
+    L.bwacuda_extend_batch_retry.argtypes = [vp, vp, sz, I, vp, I, I, I, I, I, I, I, I, vp, vp, vp]
+    L.bwacuda_extend_retry_device.argtypes = [vp, vp, vp, sz, C.POINTER(Scoring), I, I, I, vp, vp, vp, vp]
     L.bwacuda_autotune_extend.argtypes = [vp, vp, vp, sz, C.POINTER(Scoring), I, I, sz, C.POINTER(Tuning)]
     L.bwacuda_autotune_rescue.argtypes = [vp, vp, vp, sz, C.POINTER(Scoring), I, I, sz, C.POINTER(Tuning)]
     L.bwacuda_ctx_destroy.argtypes = [vp]
@@ -356,6 +359,29 @@ class Context:
                                   e_ins, w, end_bonus, zdrop, h0, _ptr(out))
         self._check(rc, "bwacuda_extend")
         return tuple(int(x) for x in out[0])
+
+    def extend_batch_retry(self, js: JobSet, prev=None, max_tries=2, mat=None, o_del=6, e_del=1, o_ins=6, e_ins=1,
+                           w=100, end_bonus=5, zdrop=100, m=5):
+        """run_side's band-doubling loop: (results, band each job was accepted at)."""
+        mat = np.ascontiguousarray(scmat() if mat is None else mat, dtype=np.int8)
+        jobs = self._host_jobs(js, EXT_JOB)
+        out = np.zeros(len(js), dtype=EXT_RES)
+        wu = np.zeros(len(js), dtype=np.int32)
+        pv = None if prev is None else np.ascontiguousarray(prev, dtype=np.int32)
+        rc = lib().bwacuda_extend_batch_retry(self.h, _ptr(jobs), len(js), m, _ptr(mat), o_del, e_del, o_ins, e_ins,
+                                              w, end_bonus, zdrop, max_tries, None if pv is None else _ptr(pv),
+                                              _ptr(out), _ptr(wu))
+        self._check(rc, "bwacuda_extend_batch_retry")
+        return out, wu
+
+    def extend_retry_device(self, d_seq, d_jobs, n, d_out, d_w_used=0, d_prev=0, max_tries=2, sc: Scoring = None,
+                            end_bonus=5, zdrop=100, stream=None):
+        sc = sc or self.scoring()
+        rc = lib().bwacuda_extend_retry_device(self.h, C.c_void_p(d_seq), C.c_void_p(d_jobs), n, C.byref(sc),
+                                               end_bonus, zdrop, max_tries, C.c_void_p(d_prev) if d_prev else None,
+                                               C.c_void_p(d_out), C.c_void_p(d_w_used) if d_w_used else None,
+                                               C.c_void_p(stream) if stream else None)
+        self._check(rc, "bwacuda_extend_retry_device")
 
     def ksw_global2_batch(self, js: JobSet, mat=None, o_del=6, e_del=1, o_ins=6, e_ins=1, m=5):
         """ksw_global2 per job (band js.w per job): (scores, offsets, cigar words); job k's CIGAR

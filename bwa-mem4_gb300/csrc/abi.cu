@@ -246,6 +246,7 @@ extern "C" void bwacuda_ctx_destroy(bwacuda_ctx *c)
     c->d_dev_scratch.release();
     ats_release(c);
     global_release(c);
+    retry_release(c);
     batched_release(c);
     delete c;
 }

@@ -217,6 +217,49 @@ cudaError_t ats_enqueue_chunk(bwacuda_ctx *c, int si, const bwacuda_ext_job *hj,
 
 }  // namespace
 
+// Gather n host jobs (caller's array, caller's slices) into seq / djobs on stream s,
+// every job with band w; synchronous up to the gather launch.  EINVAL if a job is
+// invalid (nothing of it is read).
+int ats_gather_ext(bwacuda_ctx *c, const bwacuda_ext_job *hj, size_t n, int w, DevBuf &seq, DevBuf &djobs,
+                   DevBuf &tmp, HostBuf &htmp, cudaStream_t s)
+{
+    if (!c->pageable_access) return BWACUDA_EUNSUPPORTED;
+    if (n > ATS_MAX_CHUNK * 16) return BWACUDA_EUNSUPPORTED;
+    int rc = batched_prepare(c);
+    if (rc) return rc;
+    size_t scan_bytes = 0;
+    cudaError_t e = cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, (const uint64_t *)nullptr, (uint64_t *)nullptr,
+                                                  (int)n + 1);
+    const size_t flag_at = ((n + 1) * 16 + 255) & ~(size_t)255, scan_at = flag_at + 256;
+    if (e == cudaSuccess) e = tmp.ensure(scan_at + scan_bytes + 16);
+    if (e == cudaSuccess) e = htmp.ensure(64);
+    if (e == cudaSuccess) e = djobs.ensure(n * sizeof(bwacuda_dev_ext_job));
+    if (e != cudaSuccess) return cuda_status(e);
+    uint64_t *sizes = static_cast<uint64_t *>(tmp.p), *offs = sizes + n + 1;
+    uint32_t *flags = reinterpret_cast<uint32_t *>(static_cast<char *>(tmp.p) + flag_at);
+    void *scan_tmp = static_cast<char *>(tmp.p) + scan_at;
+    if ((e = cudaMemsetAsync(flags, 0, ATS_FLAG_BYTES, s)) != cudaSuccess) return cuda_status(e);
+    if ((e = cudaMemsetAsync(sizes + n, 0, 8, s)) != cudaSuccess) return cuda_status(e);
+    const int nsm = batched_nsm(c);
+    const uint32_t grid = (uint32_t)std::min<size_t>((n + 255) / 256, (size_t)nsm * 8);
+    BinRule br{0, 0, 0};
+    ats_lengths_kernel<<<grid, 256, 0, s>>>(hj, (uint32_t)n, br, sizes, flags);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
+    if ((e = cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, sizes, offs, (int)n + 1, s)) != cudaSuccess)
+        return cuda_status(e);
+    uint64_t *h = static_cast<uint64_t *>(htmp.p);
+    if ((e = cudaMemcpyAsync(h, offs + n, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_status(e);
+    if ((e = cudaMemcpyAsync(h + 1, flags, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_status(e);
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_status(e);
+    if (static_cast<uint32_t>(h[1]) & ERR_INPUT) return BWACUDA_EINVAL;
+    if ((e = seq.ensure(h[0] + 16)) != cudaSuccess) return cuda_status(e);
+    ats_gather_kernel<<<grid, 256, 0, s>>>(hj, (uint32_t)n, offs, w, static_cast<uint8_t *>(seq.p),
+                                          static_cast<bwacuda_dev_ext_job *>(djobs.p));
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
+    c->stats.kernel_launches += 4;
+    return BWACUDA_OK;
+}
+
 // extend_batch with the device doing the gather; validated arguments, n > 0.
 int extend_batch_ats(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int m, const int8_t *mat,
                      const ExtParams &P, int w, bwacuda_ext_result *out)

@@ -64,6 +64,7 @@ struct BatchedState;  // batched path (batched.cu)
 struct ServerState;   // serving loop (server.cu)
 struct AtsState;      // device-side gather of host buffers (ats.cu)
 struct GlobalState;   // ksw_global2 buffers (global.cu)
+struct RetryState;    // band-doubling retry buffers (retry.cu)
 
 int cuda_status(cudaError_t e);
 Scoring make_scoring(int m, const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins);
@@ -99,6 +100,7 @@ struct bwacuda_ctx {
     bwacuda::BatchedState *batched = nullptr;
     bwacuda::AtsState *ats = nullptr;
     bwacuda::GlobalState *global = nullptr;
+    bwacuda::RetryState *retry = nullptr;
     bwacuda::ServerState *server = nullptr;
 };
 
@@ -152,6 +154,12 @@ int batched_bucket_count(bwacuda_ctx *c);
 int extend_batch_ats(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int m, const int8_t *mat,
                      const ExtParams &P, int w, bwacuda_ext_result *out);
 void ats_release(bwacuda_ctx *c);
+int ats_gather_ext(bwacuda_ctx *c, const bwacuda_ext_job *hj, size_t n, int w, DevBuf &seq, DevBuf &djobs,
+                   DevBuf &tmp, HostBuf &htmp, cudaStream_t s);
+
+// retry.cu
+struct RetryState;
+void retry_release(bwacuda_ctx *c);
 
 // global.cu
 void global_release(bwacuda_ctx *c);

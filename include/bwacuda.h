@@ -153,6 +153,21 @@ int bwacuda_extend_batch(bwacuda_ctx *ctx, const bwacuda_ext_job *jobs, size_t n
                          const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins, int w,
                          int end_bonus, int zdrop, bwacuda_ext_result *out);
 
+/* The extension loop of bwa-mem's run_side (crates/bwa-mem/src/across.rs:1357-1500)
+ * with its band-doubling retry on the device: round r runs the still-active jobs
+ * at band w << r; a job is accepted when score == prev, or max_off < (w >> 1) +
+ * (w >> 2), or r + 1 == max_tries (bwa's MAX_BAND_TRY is 2); a rejected job's prev
+ * becomes this round's score.  prev[k] is the job's value before round 0 (bwa-mem:
+ * -1 for a left extension, h0 for a right one; NULL means -1 for every job).
+ * out[k] is the accepted round's result, w_used[k] (may be NULL) its band.  The
+ * jobs stay on the GPU across rounds (one count readback per round).  No
+ * single-call counterpart in the reference, which loops on the host around
+ * SwBackend::extend_batch. */
+int bwacuda_extend_batch_retry(bwacuda_ctx *ctx, const bwacuda_ext_job *jobs, size_t n, int m,
+                               const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins, int w,
+                               int end_bonus, int zdrop, int max_tries, const int32_t *prev,
+                               bwacuda_ext_result *out, int32_t *w_used);
+
 /* batched_ksw_align2: forward pass with bwa's padding rule, then the reverse
  * start-recovery pass over the truncated reversed prefixes. */
 int bwacuda_ksw_align2_batch(bwacuda_ctx *ctx, const bwacuda_rescue_job *jobs, size_t n, int m,
@@ -226,6 +241,13 @@ typedef struct {
 int bwacuda_extend_device(bwacuda_ctx *ctx, const uint8_t *d_seq, const bwacuda_dev_ext_job *d_jobs,
                           size_t n, const bwacuda_scoring *sc, int end_bonus, int zdrop,
                           int path, bwacuda_ext_result *d_out, void *stream);
+/* bwacuda_extend_batch_retry on device-resident jobs: round 0 uses each job's own
+ * w (doubled per round); d_prev as prev above (NULL: -1); returns after the last
+ * round is enqueued on stream (bwacuda_ctx_sync waits and reports errors). */
+int bwacuda_extend_retry_device(bwacuda_ctx *ctx, const uint8_t *d_seq, const bwacuda_dev_ext_job *d_jobs,
+                                size_t n, const bwacuda_scoring *sc, int end_bonus, int zdrop, int max_tries,
+                                const int32_t *d_prev, bwacuda_ext_result *d_out, int32_t *d_w_used,
+                                void *stream);
 
 /* mode 0 = batched_ksw_align2 semantics, 1 = scalar ksw_align2 (lanes as above). */
 int bwacuda_ksw_align2_device(bwacuda_ctx *ctx, const uint8_t *d_seq,
@@ -295,6 +317,7 @@ typedef struct {
     uint64_t kernel_launches;
     uint64_t h2d_bytes, d2h_bytes;
     uint64_t global_jobs, global_cells; /* ksw_global2: cells = sum over rows of the band width */
+    uint64_t ext_retry_jobs;            /* band-doubling retry: jobs run again at a wider band */
 } bwacuda_stats;
 
 int bwacuda_get_stats(bwacuda_ctx *ctx, bwacuda_stats *out);
