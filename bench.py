@@ -673,6 +673,36 @@ def main():
               "note": "BWACUDA_OPT_UNGAPPED: equivalent_gcups = the full DP's cells / this time (the "
                       "reference's production path applies the same fast path)"}
 
+    # run_side's band-doubling loop on the device (bwa's MAX_BAND_TRY = 2), left/right prev
+    retry = None
+    if not args.no_e2e:
+        prev = torch.from_numpy(np.where(np.arange(n) % 2 == 0, -1, js.h0).astype(np.int32)).cuda()
+        d_w = torch.zeros(n, dtype=torch.int32, device="cuda")
+
+        def retry_step():
+            ctx.extend_retry_device(d_seq.data_ptr(), d_jobs.data_ptr(), n, d_out.data_ptr(), d_w.data_ptr(),
+                                    prev.data_ptr(), max_tries=2, stream=stream)
+
+        rsteps = max(1, min(args.steps, 3))
+        retry_step()
+        ctx.sync()
+        ctx.reset_stats()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(rsteps):
+            retry_step()
+        ctx.sync()
+        barrier()
+        rt = max_over_ranks((time.perf_counter() - t0) / rsteps)
+        str_ = ctx.stats()
+        retry = {"ms_per_step": round(rt * 1e3, 2), "jobs_per_s": round(n * world / rt, 1),
+                 "gcups": round(str_["ext_cells"] / rsteps * world / rt / 1e9, 2),
+                 "retried_jobs_per_step": int(str_["ext_retry_jobs"] / rsteps),
+                 "note": "bwacuda_extend_retry_device: round 0 at w = 100, rejected jobs again at 200, "
+                         "acceptance as run_side (across.rs:1357-1500); host clock around the call "
+                         "(one count readback per round)"}
+        del prev, d_w
+
     # roofline: integer-ALU bound (no tensor cores, about 0.03 B of HBM per cell)
     pk, kind = peaks()
     nsm = torch.cuda.get_device_properties(local).multi_processor_count
@@ -711,6 +741,8 @@ def main():
         line["e2e"] = e2e
     if ug:
         line["ungapped_prefilter"] = ug
+    if retry:
+        line["band_retry"] = retry
     if not args.no_configs:
         line["configs"] = other_configs(args, B, ctx, st, barrier, max_over_ranks, world, rank)
     if not args.no_serve and world == 1:
