@@ -32,6 +32,10 @@ EXT_JOB = np.dtype([("query", "u8"), ("target", "u8"), ("qlen", "i4"), ("tlen", 
 RES_JOB = np.dtype([("query", "u8"), ("target", "u8"), ("qlen", "i4"), ("tlen", "i4")], align=True)
 FWD_JOB = np.dtype([("query", "u8"), ("target", "u8"), ("qlen", "i4"), ("tlen", "i4"), ("minsc", "i4"),
                     ("endsc", "i4")], align=True)
+WINDOW_REQ = np.dtype([("mate", "u8"), ("l_ms", "i4"), ("orient", "i4"), ("anchor_rb", "i8"), ("anchor_rid", "i4"),
+                       ("low", "i4"), ("high", "i4")], align=True)
+WINDOW_RES = np.dtype([("rb", "i8"), ("re", "i8"), ("rid", "i4"), ("valid", "i4")] +
+                      [(n, "i4") for n in ("score", "qb", "qe", "tb", "te", "score2", "te2")], align=True)
 GLOBAL_JOB = np.dtype([("query", "u8"), ("target", "u8"), ("qlen", "i4"), ("tlen", "i4"), ("w", "i4")],
                       align=True)
 DEV_EXT_JOB = np.dtype([("q_off", "u8"), ("t_off", "u8"), ("qlen", "i4"), ("tlen", "i4"), ("h0", "i4"),
@@ -81,7 +85,7 @@ EXPORTS = ("bwacuda_ctx_create", "bwacuda_ctx_destroy", "bwacuda_set_option", "b
            "bwacuda_server_submit_extend", "bwacuda_server_submit_rescue", "bwacuda_server_wait",
            "bwacuda_server_stats", "bwacuda_measure_alu_peak", "bwacuda_get_tuning", "bwacuda_autotune_extend",
            "bwacuda_autotune_rescue", "bwacuda_ksw_global2_batch", "bwacuda_extend_batch_retry",
-           "bwacuda_extend_retry_device")
+           "bwacuda_extend_retry_device", "bwacuda_ref_set", "bwacuda_mate_rescue_windows")
 
 _lib = None
 _synth = None
@@ -107,6 +111,8 @@ def lib():
     L.bwacuda_measure_alu_peak.argtypes = [vp, C.POINTER(C.c_double)]
     L.bwacuda_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.bwacuda_ksw_global2_batch.argtypes = [vp, vp, sz, I, vp, I, I, I, I, vp, vp, vp, sz]
+    L.bwacuda_ref_set.argtypes = [vp, vp, C.c_int64, vp, vp, C.c_int32]
+    L.bwacuda_mate_rescue_windows.argtypes = [vp, vp, sz, I, vp, I, I, I, I, I, I, I, vp]
     L.bwacuda_extend_batch_retry.argtypes = [vp, vp, sz, I, vp, I, I, I, I, I, I, I, I, vp, vp, vp]
     L.bwacuda_extend_retry_device.argtypes = [vp, vp, vp, sz, C.POINTER(Scoring), I, I, I, vp, vp, vp, vp]
     L.bwacuda_autotune_extend.argtypes = [vp, vp, vp, sz, C.POINTER(Scoring), I, I, sz, C.POINTER(Tuning)]
@@ -282,6 +288,66 @@ def synth_global(n: int, seed: int = 0) -> JobSet:
     return JobSet(seq, qo, to, ql, tl, np.ones(n, np.int32), w)
 
 
+class RescueWindows:
+    """A synthetic genome in bwa's 2-bit .pac layout with its contig table, and mate-rescue
+    requests against it: anchors on both strands and all four orientations, insert window
+    [low, high], 150 bp mates drawn from inside their window (reverse-complemented where the
+    orientation expects it) with 0.5% substitutions, 10% unrelated mates."""
+
+    def __init__(self, n, seed=0, contig_lens=(3_000_000, 1_000_000, 500_000, 2_000_000), low=100, high=700,
+                 l_ms=150):
+        rng = np.random.default_rng(seed)
+        self.contig_lens = np.array(contig_lens, dtype=np.int32)
+        self.contig_off = np.zeros(len(contig_lens), dtype=np.int64)
+        self.contig_off[1:] = np.cumsum(self.contig_lens.astype(np.int64))[:-1]
+        self.l_pac = int(self.contig_lens.sum())
+        self.bases = rng.integers(0, 4, self.l_pac).astype(np.uint8)
+        pad = (-self.l_pac) % 4
+        b = np.concatenate([self.bases, np.zeros(pad, np.uint8)]).reshape(-1, 4)
+        self.pac = np.ascontiguousarray((b[:, 0] << 6) | (b[:, 1] << 4) | (b[:, 2] << 2) | b[:, 3], dtype=np.uint8)
+        L2 = 2 * self.l_pac
+        two = np.concatenate([self.bases, 3 - self.bases[::-1]])  # the 2L text
+        # anchors: a contig, a position inside it, a strand
+        c = rng.integers(0, len(contig_lens), n)
+        pos = self.contig_off[c] + (rng.random(n) * self.contig_lens[c]).astype(np.int64)
+        rev = rng.random(n) < 0.5
+        self.anchor_rb = np.where(rev, L2 - 1 - pos, pos).astype(np.int64)
+        self.anchor_rid = c.astype(np.int32)
+        self.orient = rng.integers(0, 4, n).astype(np.int32)
+        self.low, self.high = low, high
+        # the expected window (before the contig clamp) and a mate from inside it
+        is_rev = (self.orient >> 1) != (self.orient & 1)
+        larger = (self.orient >> 1) == 0
+        a = self.anchor_rb
+        rb = np.where(~is_rev, np.where(larger, a + low, a - high), np.where(larger, a + low, a - high) - l_ms)
+        re = np.where(~is_rev, np.where(larger, a + high, a - low) + l_ms, np.where(larger, a + high, a - low))
+        rb = np.clip(rb, 0, L2)
+        re = np.clip(re, 0, L2)
+        span = np.maximum(re - rb - l_ms, 0)
+        start = rb + (rng.random(n) * (span + 1)).astype(np.int64)
+        start = np.clip(start, 0, L2 - l_ms)
+        idx = start[:, None] + np.arange(l_ms)[None, :]
+        seg = two[idx]
+        mates = np.where(is_rev[:, None], 3 - seg[:, ::-1], seg)
+        mut = rng.random((n, l_ms)) < 0.005
+        mates = np.where(mut, (mates + 1 + rng.integers(0, 3, (n, l_ms))) & 3, mates)
+        unrelated = rng.random(n) < 0.10
+        mates[unrelated] = rng.integers(0, 4, (int(unrelated.sum()), l_ms))
+        self.mates = np.ascontiguousarray(mates.astype(np.uint8))
+        self.l_ms = l_ms
+        self.n = n
+
+    def requests(self):
+        r = np.zeros(self.n, dtype=WINDOW_REQ)
+        r["mate"] = self.mates.ctypes.data + np.arange(self.n, dtype=np.uint64) * self.l_ms
+        r["l_ms"] = self.l_ms
+        r["orient"] = self.orient
+        r["anchor_rb"] = self.anchor_rb
+        r["anchor_rid"] = self.anchor_rid
+        r["low"], r["high"] = self.low, self.high
+        return r
+
+
 # ---------------------------------------------------------------- context
 
 class Context:
@@ -382,6 +448,20 @@ class Context:
                                                C.c_void_p(d_out), C.c_void_p(d_w_used) if d_w_used else None,
                                                C.c_void_p(stream) if stream else None)
         self._check(rc, "bwacuda_extend_retry_device")
+
+    def ref_set(self, rw: "RescueWindows"):
+        rc = lib().bwacuda_ref_set(self.h, _ptr(rw.pac), rw.l_pac, _ptr(rw.contig_off), _ptr(rw.contig_lens),
+                                   len(rw.contig_lens))
+        self._check(rc, "bwacuda_ref_set")
+
+    def mate_rescue_windows(self, reqs: np.ndarray, mat=None, o_del=6, e_del=1, o_ins=6, e_ins=1, minsc=20,
+                            max_sc=1, min_seed_len=19, m=5) -> np.ndarray:
+        mat = np.ascontiguousarray(scmat() if mat is None else mat, dtype=np.int8)
+        out = np.zeros(len(reqs), dtype=WINDOW_RES)
+        rc = lib().bwacuda_mate_rescue_windows(self.h, _ptr(reqs), len(reqs), m, _ptr(mat), o_del, e_del, o_ins,
+                                               e_ins, minsc, max_sc, min_seed_len, _ptr(out))
+        self._check(rc, "bwacuda_mate_rescue_windows")
+        return out
 
     def ksw_global2_batch(self, js: JobSet, mat=None, o_del=6, e_del=1, o_ins=6, e_ins=1, m=5):
         """ksw_global2 per job (band js.w per job): (scores, offsets, cigar words); job k's CIGAR

@@ -247,6 +247,7 @@ extern "C" void bwacuda_ctx_destroy(bwacuda_ctx *c)
     ats_release(c);
     global_release(c);
     retry_release(c);
+    ref_release(c);
     batched_release(c);
     delete c;
 }

@@ -65,6 +65,7 @@ struct ServerState;   // serving loop (server.cu)
 struct AtsState;      // device-side gather of host buffers (ats.cu)
 struct GlobalState;   // ksw_global2 buffers (global.cu)
 struct RetryState;    // band-doubling retry buffers (retry.cu)
+struct RefState;      // reference in HBM for rescue windows (window.cu)
 
 int cuda_status(cudaError_t e);
 Scoring make_scoring(int m, const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins);
@@ -101,6 +102,7 @@ struct bwacuda_ctx {
     bwacuda::AtsState *ats = nullptr;
     bwacuda::GlobalState *global = nullptr;
     bwacuda::RetryState *retry = nullptr;
+    bwacuda::RefState *ref = nullptr;
     bwacuda::ServerState *server = nullptr;
 };
 
@@ -158,8 +160,10 @@ int ats_gather_ext(bwacuda_ctx *c, const bwacuda_ext_job *hj, size_t n, int w, D
                    DevBuf &tmp, HostBuf &htmp, cudaStream_t s);
 
 // retry.cu
-struct RetryState;
 void retry_release(bwacuda_ctx *c);
+
+// window.cu
+void ref_release(bwacuda_ctx *c);
 
 // global.cu
 void global_release(bwacuda_ctx *c);

@@ -205,6 +205,41 @@ int bwacuda_ksw_global2_batch(bwacuda_ctx *ctx, const bwacuda_global_job *jobs, 
                               const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins,
                               int32_t *score, uint64_t *cigar_off, uint32_t *cigar, size_t cigar_cap);
 
+/* ------------------------------------------------------------------------
+ * Mate rescue with the windows fetched on the device (matesw_collect +
+ * bns_fetch_seq, crates/bwa-mem/src/pe.rs:232-270 and :596-679).  The reference
+ * stays in HBM as bwa's 2-bit forward-strand .pac (4 bases per byte, first base
+ * in the top two bits; position p >= l_pac reads the complement of forward base
+ * 2*l_pac - 1 - p) with its contig table (offsets ascending from 0).  For each
+ * request the device computes the orientation's window from the anchor, clamps it
+ * to [0, 2*l_pac) and to the contig holding its midpoint, accepts it when that
+ * contig is the anchor's and the window holds >= min_seed_len bases, unpacks it,
+ * reverse-complements the mate where the orientation asks, and runs
+ * batched_ksw_align2 on every accepted window.  Which orientations to request
+ * (the pes / existing-region skip test) stays with the caller. */
+int bwacuda_ref_set(bwacuda_ctx *ctx, const uint8_t *pac, int64_t l_pac, const int64_t *contig_offset,
+                    const int32_t *contig_len, int32_t n_contigs);
+
+typedef struct {
+    const uint8_t *mate;  /* the mate read, codes 0..4, sequencing orientation */
+    int32_t l_ms;         /* its length */
+    int32_t orient;       /* pes index r: 0 FF, 1 FR, 2 RF, 3 RR */
+    int64_t anchor_rb;    /* the anchor region's rb (2*l_pac space) */
+    int32_t anchor_rid;   /* the anchor region's contig */
+    int32_t low, high;    /* pes[r].low, pes[r].high */
+} bwacuda_window_req;
+
+typedef struct {
+    int64_t rb, re;       /* the clamped window (2*l_pac space) */
+    int32_t rid;          /* contig of the window's midpoint, -1 if none */
+    int32_t valid;        /* 1: rid == anchor_rid and re - rb >= min_seed_len, aln holds the result */
+    bwacuda_rescue_result aln;
+} bwacuda_window_result;
+
+int bwacuda_mate_rescue_windows(bwacuda_ctx *ctx, const bwacuda_window_req *reqs, size_t n, int m,
+                                const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins, int minsc,
+                                int max_sc, int min_seed_len, bwacuda_window_result *out);
+
 /* ksw_local_fwd per job with its own minsc / endsc (lanes as above). */
 int bwacuda_ksw_local_fwd_batch(bwacuda_ctx *ctx, const bwacuda_fwd_job *jobs, size_t n, int m,
                                 const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins,

@@ -105,6 +105,11 @@ def lib():
         L.ko_global2_batch.restype = I
         L.ko_global2_batch.argtypes = [u8p, C.c_int64, i64p, i64p, i32p, i32p, i32p, I, i8p, I, I, I, I, I,
                                        i32p, i64p, C.POINTER(C.c_uint32), i32p]
+        L.ko_ref_base.restype = C.c_uint8
+        L.ko_ref_base.argtypes = [u8p, C.c_int64, C.c_int64]
+        L.ko_rescue_window.restype = I
+        L.ko_rescue_window.argtypes = [u8p, C.c_int64, i64p, i32p, C.c_int32, C.c_int64, C.c_int32, I, I, I, I, I,
+                                       i64p, i64p, i32p]
         L.ko_local_fwd_batch.restype = None
         L.ko_local_fwd_batch.argtypes = [u8p, C.c_int64, i64p, i64p, i32p, i32p, i32p, i32p, I,
                                          i8p, I, I, I, I, I, I, I, C.c_void_p]
@@ -325,3 +330,41 @@ def global2_batch(js, mat=None, o_del=6, e_del=1, o_ins=6, e_ins=1, nthreads=0, 
     for k in range(n):
         dense[offsets[k]:offsets[k + 1]] = words[cig_off[k]:cig_off[k] + ncig[k]]
     return score, offsets, dense
+
+
+class Reference:
+    """A 2-bit packed reference (bwa's .pac layout) with its contig table."""
+
+    def __init__(self, bases, contig_lens):
+        bases = np.ascontiguousarray(bases, dtype=np.uint8)
+        self.l_pac = len(bases)
+        pad = (-len(bases)) % 4
+        b = np.concatenate([bases, np.zeros(pad, np.uint8)]).reshape(-1, 4)
+        self.pac = np.ascontiguousarray((b[:, 0] << 6) | (b[:, 1] << 4) | (b[:, 2] << 2) | b[:, 3], dtype=np.uint8)
+        self.len = np.ascontiguousarray(contig_lens, dtype=np.int32)
+        self.off = np.zeros(len(self.len), dtype=np.int64)
+        self.off[1:] = np.cumsum(self.len.astype(np.int64))[:-1]
+        assert int(self.off[-1]) + int(self.len[-1]) == self.l_pac
+
+    def bases(self, rb, re):
+        """Bases of [rb, re) in 2*l_pac space (reverse half = reverse complement)."""
+        return np.array([lib().ko_ref_base(_p(self.pac, C.c_uint8), self.l_pac, p) for p in range(rb, re)],
+                        dtype=np.uint8)
+
+
+def rescue_window(ref, anchor_rb, anchor_rid, orient, low, high, l_ms, min_seed_len):
+    """(valid, rb, re, rid) of one orientation's window (matesw_collect + bns_fetch_seq)."""
+    rb, re, rid = C.c_int64(), C.c_int64(), C.c_int32()
+    ok = lib().ko_rescue_window(_p(ref.pac, C.c_uint8), ref.l_pac, _p(ref.off, C.c_int64), _p(ref.len, C.c_int32),
+                                len(ref.len), anchor_rb, anchor_rid, orient, low, high, l_ms, min_seed_len,
+                                C.byref(rb), C.byref(re), C.byref(rid))
+    return bool(ok), rb.value, re.value, rid.value
+
+
+def mate_for_orientation(mate, orient):
+    """The query matesw_collect aligns: the mate, reverse-complemented when the orientation is
+    reverse (pe.rs:641-648; N stays N)."""
+    mate = np.asarray(mate, dtype=np.uint8)
+    if (orient >> 1) != (orient & 1):
+        return np.where(mate[::-1] < 4, 3 - mate[::-1], 4).astype(np.uint8)
+    return mate.copy()

@@ -714,3 +714,81 @@ int ko_global2_batch(const uint8_t *seq, int64_t n, const int64_t *q_off, const 
     }
     return bad ? -1 : 0;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Mate-rescue windows                                                        */
+/* ------------------------------------------------------------------------- */
+
+uint8_t ko_ref_base(const uint8_t *pac, int64_t l_pac, int64_t pos)
+{
+    /* crates/bwa-index/src/fmindex.rs:173-185: forward unpack, most significant pair first;
+     * the reverse half is the complement of the mirrored forward base */
+    int rc = pos >= l_pac;
+    int64_t f = rc ? 2 * l_pac - 1 - pos : pos;
+    uint8_t b = (uint8_t)((pac[f >> 2] >> ((3 - (int)(f & 3)) << 1)) & 3);
+    return rc ? (uint8_t)(3 - b) : b;
+}
+
+static int32_t ko_pos2rid(const int64_t *off, int32_t n, int64_t l_pac, int64_t pos_f)
+{
+    /* crates/bwa-index/src/bntseq.rs:337-365, including its "last probe" return */
+    if (pos_f >= l_pac) return -1;
+    int32_t left = 0, mid = 0, right = n;
+    while (left < right) {
+        mid = (left + right) >> 1;
+        if (pos_f >= off[mid]) {
+            if (mid == n - 1) break;
+            if (pos_f < off[mid + 1]) break;
+            left = mid + 1;
+        } else {
+            right = mid;
+        }
+    }
+    return mid;
+}
+
+int ko_rescue_window(const uint8_t *pac, int64_t l_pac, const int64_t *off, const int32_t *len, int32_t n,
+                     int64_t anchor_rb, int32_t anchor_rid, int orient, int low, int high, int l_ms,
+                     int min_seed_len, int64_t *rb_out, int64_t *re_out, int32_t *rid_out)
+{
+    /* matesw_collect's window for one orientation (crates/bwa-mem/src/pe.rs:631-674) and
+     * bns_fetch_seq's contig clamp (pe.rs:232-270).  Returns 1 when the window is accepted.
+     * (pac is unused: the window depends only on the contig table.) */
+    (void)pac;
+    int is_rev = (orient >> 1) != (orient & 1);
+    int is_larger = (orient >> 1) == 0;
+    int64_t lo = low, hi = high, rb, re;
+    if (!is_rev) {
+        rb = is_larger ? anchor_rb + lo : anchor_rb - hi;
+        re = (is_larger ? anchor_rb + hi : anchor_rb - lo) + l_ms;
+    } else {
+        rb = (is_larger ? anchor_rb + lo : anchor_rb - hi) - l_ms;
+        re = is_larger ? anchor_rb + hi : anchor_rb - lo;
+    }
+    if (rb < 0) rb = 0;
+    if (re > (l_pac << 1)) re = l_pac << 1;
+    *rb_out = rb;
+    *re_out = re;
+    *rid_out = -1;
+    if (!(rb < re)) return 0;
+    int64_t mid = (rb + re) >> 1;
+    int mrev = mid >= l_pac;
+    int64_t mid_f = mrev ? (l_pac << 1) - 1 - mid : mid;
+    int32_t rid = ko_pos2rid(off, n, l_pac, mid_f);
+    int64_t fb = 0, fe = l_pac << 1;
+    if (rid >= 0) {
+        fb = off[rid];
+        fe = off[rid] + (int64_t)len[rid];
+        if (mrev) {
+            int64_t t = fb;
+            fb = (l_pac << 1) - fe;
+            fe = (l_pac << 1) - t;
+        }
+    }
+    if (rb < fb) rb = fb;
+    if (re > fe) re = fe;
+    *rb_out = rb;
+    *re_out = re;
+    *rid_out = rid;
+    return rid == anchor_rid && re - rb >= min_seed_len;
+}

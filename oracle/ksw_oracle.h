@@ -130,6 +130,13 @@ int ko_global2_batch(const uint8_t *seq, int64_t n, const int64_t *q_off, const 
                      const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins, int nthreads,
                      int32_t *score, const int64_t *cig_off, uint32_t *cigar, int32_t *n_cigar);
 
+/* Mate-rescue windows: the 2-bit reference base at 2L-space position pos, and one
+ * orientation's window (matesw_collect + bns_fetch_seq); returns 1 when accepted. */
+uint8_t ko_ref_base(const uint8_t *pac, int64_t l_pac, int64_t pos);
+int ko_rescue_window(const uint8_t *pac, int64_t l_pac, const int64_t *off, const int32_t *len, int32_t n,
+                     int64_t anchor_rb, int32_t anchor_rid, int orient, int low, int high, int l_ms,
+                     int min_seed_len, int64_t *rb_out, int64_t *re_out, int32_t *rid_out);
+
 /* bwa_fill_scmat, crates/bwa-core/src/opt.rs:419-460 (match a, mismatch -b, N -1). */
 void ko_fill_scmat(int a, int b, int8_t mat[25]);
 

@@ -247,3 +247,40 @@ def test_global2_edge_conventions():
     assert oracle.global2([], [1, 2, 3], 5) == (-9, [3 << 4 | 2])
     assert oracle.global2([1, 2, 3], [], 2) == (-0x40000000, [2 << 4 | 1])
     assert oracle.global2([], [], 3) == (0, [])
+
+
+# ---------------------------------------------------------------- rescue windows
+
+def test_pac_unpack_definition():
+    # crates/bwa-index/src/fmindex.rs:1170-1190 builds this 64-base .pac (bytes i*37+11) and checks
+    # the range unpack against the per-base definition; the oracle is that definition
+    pac = np.array([(i * 37 + 11) & 0xff for i in range(17)], dtype=np.uint8)
+    l_pac = 64
+    fwd = [(int(pac[p >> 2]) >> ((3 - (p & 3)) * 2)) & 3 for p in range(l_pac)]
+    want = fwd + [3 - fwd[2 * l_pac - 1 - p] for p in range(l_pac, 2 * l_pac)]
+    got = [oracle.lib().ko_ref_base(pac.ctypes.data_as(oracle.C.POINTER(oracle.C.c_uint8)), l_pac, p)
+           for p in range(2 * l_pac)]
+    assert got == want
+
+
+def test_rescue_window_rules():
+    ref = oracle.Reference(np.zeros(1000, np.uint8), [600, 400])  # contigs [0, 600), [600, 1000)
+    L2 = 2000
+    # FR (r = 1): reverse, larger: [a + lo - l_ms, a + hi)
+    assert oracle.rescue_window(ref, 100, 0, 1, 100, 400, 150, 19) == (True, 50, 500, 0)
+    # FF (r = 0): forward, larger: [a + lo, a + hi + l_ms) = [400, 850); its midpoint 625 lies in
+    # contig 1, so the window clamps to contig 1 and the anchor's contig 0 does not match
+    assert oracle.rescue_window(ref, 300, 0, 0, 100, 400, 150, 19) == (False, 600, 850, 1)
+    assert oracle.rescue_window(ref, 300, 1, 0, 100, 400, 150, 19) == (True, 600, 850, 1)
+    # RR (r = 3): forward orientation, smaller: [a - hi, a - lo + l_ms), clamped at 0
+    assert oracle.rescue_window(ref, 150, 0, 3, 100, 400, 150, 19) == (True, 0, 200, 0)
+    # reverse half: [1600, 2050) clipped to 2 * l_pac; midpoint 1800 mirrors to forward 199
+    # (contig 0), whose span mirrors to [2000 - 600, 2000) = [1400, 2000)
+    assert oracle.rescue_window(ref, 1500, 0, 0, 100, 400, 150, 19) == (True, 1600, 2000, 0)
+    # midpoint 1425 mirrors to 574 (contig 0): [1400, 2000) clamps [1200, 1650) to [1400, 1650)
+    assert oracle.rescue_window(ref, 1100, 1, 0, 100, 400, 150, 19) == (False, 1400, 1650, 0)
+    # too short after the clamp
+    assert oracle.rescue_window(ref, 590, 0, 2, 5, 8, 10, 19)[0] is False
+    # window entirely outside [0, 2 * l_pac)
+    ok, rb, re, rid = oracle.rescue_window(ref, L2 + 500, 1, 0, 100, 400, 150, 19)
+    assert not ok and rid == -1
