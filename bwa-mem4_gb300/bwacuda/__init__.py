@@ -326,8 +326,7 @@ class RescueWindows:
         span = np.maximum(re - rb - l_ms, 0)
         start = rb + (rng.random(n) * (span + 1)).astype(np.int64)
         start = np.clip(start, 0, L2 - l_ms)
-        idx = start[:, None] + np.arange(l_ms)[None, :]
-        seg = two[idx]
+        seg = np.lib.stride_tricks.sliding_window_view(two, l_ms)[start]
         mates = np.where(is_rev[:, None], 3 - seg[:, ::-1], seg)
         mut = rng.random((n, l_ms)) < 0.005
         mates = np.where(mut, (mates + 1 + rng.integers(0, 3, (n, l_ms))) & 3, mates)
