@@ -194,7 +194,14 @@ static int ctx_init(bwacuda_ctx *c)
     cudaError_t e = cudaSetDevice(c->device);
     if (e != cudaSuccess) return cuda_status(e);
     for (int s = 0; s < 2; ++s) {
-        if ((e = cudaStreamCreateWithFlags(&c->slot[s].stream, cudaStreamNonBlocking)) != cudaSuccess) return cuda_status(e);
+        // The pipeline slots carry the short gather / sort / scatter kernels and run at the
+        // device's highest stream priority: their blocks then take the SM room that the
+        // persistent bucket kernels (default priority, shared-memory bound) leave free
+        // instead of queueing behind bucket launches that cannot be placed yet.
+        int lo_prio = 0, hi_prio = 0;
+        if ((e = cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio)) != cudaSuccess) return cuda_status(e);
+        if ((e = cudaStreamCreateWithPriority(&c->slot[s].stream, cudaStreamNonBlocking, hi_prio)) != cudaSuccess)
+            return cuda_status(e);
         if ((e = cudaEventCreateWithFlags(&c->slot[s].done, cudaEventDisableTiming)) != cudaSuccess) return cuda_status(e);
     }
     c->stream = c->slot[0].stream;

@@ -36,6 +36,11 @@ namespace {
 constexpr uint32_t ERR_INPUT = 8u;
 constexpr size_t ATS_MAX_CHUNK = size_t(1) << 24;  // 32-bit word indexing in the scatter
 constexpr int ATS_FLAG_BYTES = 32;                 // u32 input flag, pad, u64 bins[3]
+// Blocks per SM of the pipeline's length / gather / scatter launches.  They run
+// beside the previous chunk's persistent DP kernels; a full-occupancy grid would
+// crowd those off the SMs, while two blocks per SM with eight 16-byte loads in
+// flight per lane already keep several MB of host reads outstanding.
+constexpr int ATS_BLOCKS_PER_SM = 2;
 
 __device__ __forceinline__ bool job_ok(const bwacuda_ext_job &J)
 {
@@ -123,6 +128,7 @@ __global__ void ats_scatter_kernel(const uint32_t *__restrict__ src, uint32_t wo
 struct AtsSlot {
     DevBuf sizes, offs, scan_tmp, seq, djobs, dout, flags;
     HostBuf h_total, h_flags;
+    cudaEvent_t gathered = nullptr;  // this slot's last gather finished
     bool busy = false;
 };
 
@@ -139,6 +145,7 @@ void ats_release(bwacuda_ctx *c)
         s.sizes.release(); s.offs.release(); s.scan_tmp.release(); s.seq.release();
         s.djobs.release(); s.dout.release(); s.flags.release();
         s.h_total.release(); s.h_flags.release();
+        if (s.gathered) cudaEventDestroy(s.gathered);
     }
     delete c->ats;
     c->ats = nullptr;
@@ -183,10 +190,15 @@ cudaError_t ats_enqueue_chunk(bwacuda_ctx *c, int si, const bwacuda_ext_job *hj,
     if ((e = S.h_flags.ensure(ATS_FLAG_BYTES)) != cudaSuccess) return e;
     uint64_t *sizes = static_cast<uint64_t *>(S.sizes.p), *offs = static_cast<uint64_t *>(S.offs.p);
     uint32_t *flags = static_cast<uint32_t *>(S.flags.p);
+    if (!S.gathered && (e = cudaEventCreateWithFlags(&S.gathered, cudaEventDisableTiming)) != cudaSuccess) return e;
+    // One chunk reads host memory at a time: the host-memory link is the shared resource,
+    // and the chunk whose DP runs next gets all of it.
+    AtsSlot &O = c->ats->slot[si ^ 1];
+    if (O.busy && O.gathered && (e = cudaStreamWaitEvent(s, O.gathered, 0)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(flags, 0, ATS_FLAG_BYTES, s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(sizes + cn, 0, 8, s)) != cudaSuccess) return e;
     const int nsm = batched_nsm(c);
-    uint32_t grid = (uint32_t)std::min<size_t>((cn + 255) / 256, (size_t)nsm * 8);
+    uint32_t grid = (uint32_t)std::min<size_t>((cn + 255) / 256, (size_t)nsm * ATS_BLOCKS_PER_SM);
     ats_lengths_kernel<<<grid, 256, 0, s>>>(hj, (uint32_t)cn, br, sizes, flags);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = cub::DeviceScan::ExclusiveSum(S.scan_tmp.p, scan_bytes, sizes, offs, (int)cn + 1, s)) != cudaSuccess)
@@ -196,16 +208,17 @@ cudaError_t ats_enqueue_chunk(bwacuda_ctx *c, int si, const bwacuda_ext_job *hj,
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
     const uint64_t total = *static_cast<const uint64_t *>(S.h_total.p);
     if ((e = S.seq.ensure(total + 16)) != cudaSuccess) return e;
-    grid = (uint32_t)std::min<size_t>((cn + 255) / 256, (size_t)nsm * 8);
+    grid = (uint32_t)std::min<size_t>((cn + 255) / 256, (size_t)nsm * ATS_BLOCKS_PER_SM);
     ats_gather_kernel<<<grid, 256, 0, s>>>(hj, (uint32_t)cn, offs, w, static_cast<uint8_t *>(S.seq.p),
                                           static_cast<bwacuda_dev_ext_job *>(S.djobs.p));
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(S.gathered, s)) != cudaSuccess) return e;
     e = batched_enqueue(c, batched_slot_bufs(c, si), static_cast<const uint8_t *>(S.seq.p),
                         static_cast<const bwacuda_dev_ext_job *>(S.djobs.p), cn, P,
                         static_cast<bwacuda_ext_result *>(S.dout.p), s, nullptr, nullptr);
     if (e != cudaSuccess) return e;
     const uint32_t words = (uint32_t)(cn * (sizeof(bwacuda_ext_result) / 4));
-    grid = (uint32_t)std::min<size_t>((words + 255) / 256, (size_t)nsm * 8);
+    grid = (uint32_t)std::min<size_t>((words + 255) / 256, (size_t)nsm * ATS_BLOCKS_PER_SM);
     ats_scatter_kernel<<<grid, 256, 0, s>>>(static_cast<const uint32_t *>(S.dout.p), words,
                                            reinterpret_cast<uint32_t *>(hout));
     if ((e = cudaGetLastError()) != cudaSuccess) return e;

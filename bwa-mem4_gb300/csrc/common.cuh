@@ -96,8 +96,9 @@ __host__ __device__ inline uint32_t slice_words(const uint8_t *src, int len)
 // words at ta, both 16-byte aligned addresses) to seq + base_l, as one flat list
 // of words over the whole warp: word x belongs to the lane whose exclusive
 // prefix of word counts is the largest one <= x (a 5-step shuffle search), and
-// every lane keeps four independent 16-byte loads in flight before storing.
-// All 32 lanes must call it.
+// every lane keeps eight independent 16-byte loads in flight before storing
+// (the kernel is bound by host-memory latency, and beside the persistent DP
+// kernels it gets few warps per SM).  All 32 lanes must call it.
 __device__ __forceinline__ void warp_gather_slices(uint64_t qa, uint64_t ta, uint64_t base, uint32_t qw, uint32_t tw,
                                                    uint8_t *seq)
 {
@@ -111,11 +112,12 @@ __device__ __forceinline__ void warp_gather_slices(uint64_t qa, uint64_t ta, uin
     }
     const uint32_t total = __shfl_sync(0xffffffffu, pre, 31);
     pre -= wc;
-    for (uint32_t x0 = 0; x0 < total; x0 += 128) {
-        uint4 v[4];
-        uint4 *dst[4];
+    constexpr int U = 8;
+    for (uint32_t x0 = 0; x0 < total; x0 += 32u * U) {
+        uint4 v[U];
+        uint4 *dst[U];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < U; ++u) {
             const uint32_t x = x0 + (uint32_t)u * 32u + lane;
             int j = 0;
 #pragma unroll
@@ -135,7 +137,7 @@ __device__ __forceinline__ void warp_gather_slices(uint64_t qa, uint64_t ta, uin
                                  : reinterpret_cast<const uint4 *>(ta_j)[wi - qw_j];
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < U; ++u)
             if (x0 + (uint32_t)u * 32u + lane < total) *dst[u] = v[u];
     }
 }
