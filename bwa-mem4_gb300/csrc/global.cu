@@ -6,19 +6,24 @@
 // x * TB + t), with the query codes beside it.  Only the band is kept: row i
 // reads and writes columns [i - w, i + w + 1] and every column it reads was
 // written by the previous row (or by the row -1 initialisation), so the row is
-// a circular buffer of B = min(2w + 2, qlen + 1) slots, column j in slot j % B.  The traceback byte of every
-// band cell (f << 4 | e << 2 | h, the reference's encoding) goes to HBM; the 32
-// jobs of a warp share one block there, interleaved word by word
-// (word (row * ncw + col / 4) * 32 + lane), so the warp's lanes, which sweep the
-// same band-relative column in lockstep, store 128 contiguous bytes per
-// instruction.  The traceback then walks only its path's cells and writes the
-// CIGAR runs (len << 4 | op), merged and reversed as the reference does.
+// a circular buffer of B = min(2w + 2, qlen + 1) slots, column j in slot j % B.
+// The traceback byte of every band cell (f << 4 | e << 2 | h, the reference's
+// encoding) goes to HBM, each alignment's matrix contiguous with rows padded to
+// 16 bytes and written 16 cells per store.  The traceback then walks only its
+// path's cells and writes the CIGAR runs (len << 4 | op), merged and reversed
+// as the reference does.
+//
+// On the device route the alignments are radix-sorted by (query-length bucket,
+// query length, target length) and each bucket is launched with the shared
+// memory its own longest query and widest band need, so warps hold alignments
+// of one read length and short reads are not held to the long reads' footprint.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstring>
 #include <vector>
 
+#include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
 #include "kernels.h"
@@ -34,10 +39,10 @@ constexpr size_t SMEM_LIMIT = 227u * 1024u;
 // One alignment as the kernel sees it (bases addressed from the chunk's base buffer).
 struct GlobalDevJob {
     uint64_t q_off, t_off;
-    uint64_t z_off;    // word offset of the warp group's traceback block
+    uint64_t z_off;    // byte offset of this job's traceback matrix (tlen rows of zrow bytes)
     uint64_t cig_off;  // word offset of this job's CIGAR scratch (qlen + tlen + 1 words)
     int32_t qlen, tlen, w;
-    int32_t ncw;       // traceback words per row of the warp group
+    int32_t zrow;      // traceback bytes per row: the band width rounded up to 16
 };
 static_assert(sizeof(GlobalDevJob) == 48, "descriptor layout");
 
@@ -45,6 +50,22 @@ static_assert(sizeof(GlobalDevJob) == 48, "descriptor layout");
 __host__ __device__ inline size_t global_smem(int bcap, int qcap, int tb)
 {
     return (size_t)tb * ((size_t)bcap * 8 + (size_t)qcap);
+}
+
+// Traceback bytes per row.
+__host__ __device__ inline int global_zrow(int qlen, int w)
+{
+    if (w < 0) w = 0;
+    const long long nc = qlen < 2LL * w + 1 ? qlen : 2LL * w + 1;
+    return (int)((nc + 15) & ~15LL);
+}
+
+// Query-length buckets of the device route (upper bounds, inclusive).
+constexpr int GLB_NBUCKETS = 8;
+__host__ __device__ inline int global_bucket(int qlen)
+{
+    return qlen <= 64 ? 0 : qlen <= 128 ? 1 : qlen <= 192 ? 2 : qlen <= 256 ? 3 : qlen <= 320 ? 4 : qlen <= 448 ? 5
+           : qlen <= 640 ? 6 : 7;
 }
 
 // Band slots a job needs.
@@ -66,17 +87,18 @@ __device__ __forceinline__ void cigar_push(uint32_t *cig, int &n, uint32_t op, u
 
 template <int TB>
 __global__ void __launch_bounds__(TB)
-global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restrict__ jobs, uint32_t n,
-                  const __grid_constant__ Scoring sc, int bcap, int qcap, uint32_t *__restrict__ z,
+global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restrict__ jobs,
+                  const uint32_t *__restrict__ order, uint32_t base, uint32_t count,
+                  const __grid_constant__ Scoring sc, int bcap, int qcap, uint8_t *__restrict__ z,
                   uint32_t *__restrict__ cig, int32_t *__restrict__ score_out, int32_t *__restrict__ ncig_out,
                   uint32_t *__restrict__ err, unsigned long long *__restrict__ cells_total)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int tid = threadIdx.x;
-    const uint32_t k = blockIdx.x * TB + tid;
+    const uint32_t t = blockIdx.x * TB + tid;
     unsigned long long ncells = 0;
-    if (k >= n) return;
-    const uint32_t lane = k & 31u;
+    if (t >= count) return;
+    const uint32_t k = order ? order[base + t] : base + t;
     int2 *cell = reinterpret_cast<int2 *>(smem_raw) + tid;        // cell[x * TB]: {H, E} of band slot x
     uint8_t *qs = smem_raw + (size_t)bcap * 8 * TB + tid;          // qs[j * TB]: query code
     const GlobalDevJob J = jobs[k];
@@ -86,8 +108,9 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
     const int B = global_band_slots(qlen, w);
     const int oe_del = sc.o_del + sc.e_del, oe_ins = sc.o_ins + sc.e_ins;
     const uint8_t *q = seq + J.q_off;
-    const uint8_t *t = seq + J.t_off;
-    uint32_t *zj = z + J.z_off + lane;
+    const uint8_t *tg = seq + J.t_off;
+    uint8_t *zj = z + J.z_off;
+    const size_t zrow = (size_t)J.zrow;
     bool bad = false;
     if (B > bcap || qlen > qcap) {  // the host sizes bcap / qcap from the launch's jobs
         atomicOr(err, ERR_RANGE);
@@ -112,12 +135,12 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
         const int beg = i > w ? i - w : 0;
         const int end = i + w + 1 < qlen ? i + w + 1 : qlen;
         int h1 = beg == 0 ? -(sc.o_del + sc.e_del * (i + 1)) : MINUS_INF;
-        uint32_t tc = t[i];
+        uint32_t tc = tg[i];
         bad |= tc >= (uint32_t)sc.m;
         tc = tc < (uint32_t)sc.m ? tc : (uint32_t)PAD_CODE;
         const uint32_t plo = sc.prof[tc & 7u][0], phi = sc.prof[tc & 7u][1];
-        uint32_t *zr = zj + (size_t)i * (size_t)J.ncw * 32u;
-        uint32_t word = 0;
+        uint4 *zr = reinterpret_cast<uint4 *>(zj + (size_t)i * zrow);
+        uint32_t word[4] = {0u, 0u, 0u, 0u};
         int x = beg % (B > 0 ? B : 1);  // slot of column j
         for (int j = beg; j < end; ++j) {
             int2 *cp = cell + (size_t)x * TB;
@@ -138,16 +161,17 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
             if (f > tt) d |= 2u << 4;
             else f = tt;
             const int jj = j - beg;
-            word |= d << ((jj & 3) * 8);
-            if ((jj & 3) == 3 || j == end - 1) {
-                zr[(size_t)(jj >> 2) * 32u] = word;
-                word = 0;
+            word[(jj >> 2) & 3] |= d << ((jj & 3) * 8);
+            if ((jj & 15) == 15 || j == end - 1) {
+                zr[jj >> 4] = make_uint4(word[0], word[1], word[2], word[3]);
+                word[0] = word[1] = word[2] = word[3] = 0u;
             }
             if (++x == B) x = 0;
         }
         if (B > 0) cell[(size_t)(end % B) * TB] = make_int2(h1, MINUS_INF);
         // band cells this row did not reach read as 0, as in the reference's zeroed matrix
-        for (int wi = end > beg ? (end - beg + 3) >> 2 : 0; wi < (n_col + 3) >> 2; ++wi) zr[(size_t)wi * 32u] = 0u;
+        for (int ci = end > beg ? (end - beg + 15) >> 4 : 0; ci < (n_col + 15) >> 4; ++ci)
+            zr[ci] = make_uint4(0u, 0u, 0u, 0u);
         ncells += (unsigned long long)(end > beg ? end - beg : 0);
     }
     // eh_h[qlen] after the last row: written by that row's epilogue when its band reaches the last
@@ -170,8 +194,7 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
         const long flat = i * (long)n_col + (kk - beg);
         if (kk < beg || flat >= (long)n_col * tlen) { range = true; break; }
         const long row = flat / n_col, col = flat - row * n_col;
-        const uint32_t wv = zj[((size_t)row * (size_t)J.ncw + (size_t)(col >> 2)) * 32u];
-        const uint32_t d = (wv >> ((col & 3) * 8)) & 0xffu;
+        const uint32_t d = zj[(size_t)row * zrow + (size_t)col];
         which = (d >> (which << 1)) & 3u;
         if (which == 0) { cigar_push(cg, nc, 0, 1); --i; --kk; }
         else if (which == 1) { cigar_push(cg, nc, 2, 1); --i; }
@@ -214,18 +237,20 @@ __device__ __forceinline__ bool gjob_ok(const bwacuda_global_job &J)
     return J.qlen >= 0 && J.tlen >= 0 && (J.qlen == 0 || J.query != nullptr) && (J.tlen == 0 || J.target != nullptr);
 }
 
-// One warp per group of 32 jobs: per-job base reserve and CIGAR capacity, per-group
-// traceback words, the chunk's longest query.  flags[0]: input error bits; flags[1]: max qlen;
-// flags[2]: max band slots.
+// Per job: base reserve, CIGAR capacity, traceback bytes and the sort key
+// (bucket, query length descending, target length descending); per bucket the
+// widest band (slots) and longest query, reduced over the lanes that share a
+// bucket.  flags[0]: input error bits.  bstat[2b], bstat[2b+1]: bucket b's max
+// band slots and max query length.
 __global__ void glb_plan_kernel(const bwacuda_global_job *__restrict__ hj, uint32_t n, int qlim,
                                 uint64_t *__restrict__ seq_sz, uint64_t *__restrict__ cig_sz,
-                                uint64_t *__restrict__ z_sz, uint32_t *__restrict__ flags)
+                                uint64_t *__restrict__ z_sz, uint32_t *__restrict__ keys, uint32_t *__restrict__ idx,
+                                uint32_t *__restrict__ flags, uint32_t *__restrict__ bstat)
 {
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t ngroups = (n + 31) / 32;
-    for (uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ngroups; g += (gridDim.x * blockDim.x) >> 5) {
-        const uint32_t k = g * 32 + lane;
-        int tl = 0, nc = 0, ql = 0, bs = 0;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t k0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); k0 < n; k0 += stride) {
+        const uint32_t k = k0 + (threadIdx.x & 31u);
+        int ql = 0, tl = 0, bs = 0, bucket = 0;
         bool bad = false;
         if (k < n) {
             const bwacuda_global_job J = hj[k];
@@ -233,28 +258,50 @@ __global__ void glb_plan_kernel(const bwacuda_global_job *__restrict__ hj, uint3
             bad = !ok || J.qlen > qlim;
             ql = ok ? J.qlen : 0;
             tl = ok ? J.tlen : 0;
-            const int w = J.w < 0 ? 0 : J.w;
-            nc = ql < 2 * w + 1 ? ql : 2 * w + 1;
             seq_sz[k] = ok ? 16ull * (slice_words(J.query, ql) + slice_words(J.target, tl)) : 0u;
-            bs = global_band_slots(ql, J.w);
             cig_sz[k] = (uint64_t)ql + (uint64_t)tl + 1u;
+            z_sz[k] = (uint64_t)tl * (uint64_t)global_zrow(ql, J.w);
+            bs = global_band_slots(ql, J.w);
+            bucket = global_bucket(ql);
+            const uint32_t qk = ql > 1023 ? 0u : 1023u - (uint32_t)ql;
+            const uint32_t tk = tl > 4095 ? 0u : 4095u - (uint32_t)tl;
+            keys[k] = ((uint32_t)bucket << 22) | (qk << 12) | tk;
+            idx[k] = k;
         }
-        const int tmax = __reduce_max_sync(0xffffffffu, (unsigned)tl);
-        const int ncmax = __reduce_max_sync(0xffffffffu, (unsigned)nc);
-        const int qmax = __reduce_max_sync(0xffffffffu, (unsigned)ql);
-        const int bmax = __reduce_max_sync(0xffffffffu, (unsigned)bs);
-        const unsigned anybad = __reduce_or_sync(0xffffffffu, bad ? 1u : 0u);
-        if (lane == 0) {
-            z_sz[g] = (uint64_t)tmax * (uint64_t)((ncmax + 3) / 4) * 32u;
-            if (anybad) atomicOr(flags, 1u);
-            atomicMax(flags + 1, (unsigned)qmax);
-            atomicMax(flags + 2, (unsigned)bmax);
+        const unsigned live = __ballot_sync(0xffffffffu, k < n);
+        if (__reduce_or_sync(0xffffffffu, bad ? 1u : 0u) && (threadIdx.x & 31u) == 0) atomicOr(flags, 1u);
+        // lanes of one bucket reduce together; their lowest lane updates the bucket's maxima
+        const unsigned grp = __match_any_sync(0xffffffffu, bucket) & live;
+        if (k < n) {
+            const unsigned bmax = __reduce_max_sync(grp, (unsigned)bs);
+            const unsigned qmax = __reduce_max_sync(grp, (unsigned)ql);
+            if ((int)(threadIdx.x & 31u) == __ffs(grp) - 1) {
+                atomicMax(bstat + 2 * bucket, bmax);
+                atomicMax(bstat + 2 * bucket + 1, qmax);
+            }
         }
     }
 }
 
-// One warp per group: lane l writes job g*32+l's descriptor, then the warp copies the
-// group's slices as aligned 16-byte words (warp_gather_slices).
+// [start, end) of each bucket in the sorted keys.
+__global__ void glb_bucket_bounds_kernel(const uint32_t *__restrict__ keys, uint32_t n, uint32_t *__restrict__ bounds)
+{
+    const int b = threadIdx.x;
+    if (b >= GLB_NBUCKETS) return;
+    for (int side = 0; side < 2; ++side) {
+        const uint32_t v = (uint32_t)(b + side) << 22;
+        uint32_t lo = 0, hi = n;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (keys[mid] < v) lo = mid + 1;
+            else hi = mid;
+        }
+        bounds[2 * b + side] = lo;
+    }
+}
+
+// One warp per 32 jobs: lane l writes its job's descriptor, then the warp copies the
+// 32 jobs' slices as aligned 16-byte words (warp_gather_slices).
 __global__ void __launch_bounds__(256) glb_gather_kernel(const bwacuda_global_job *__restrict__ hj, uint32_t n,
                                                          const uint64_t *__restrict__ seq_off,
                                                          const uint64_t *__restrict__ cig_off,
@@ -267,29 +314,26 @@ __global__ void __launch_bounds__(256) glb_gather_kernel(const bwacuda_global_jo
         const uint32_t k = g * 32 + lane;
         uint64_t qa = 0, ta = 0, base = 0;
         uint32_t qw = 0, tw = 0;
-        int nc = 0;
-        GlobalDevJob D{};
         if (k < n) {
             const bwacuda_global_job J = hj[k];
             const bool ok = gjob_ok(J);
             const int ql = ok ? J.qlen : 0, tl = ok ? J.tlen : 0;
-            const int w = J.w < 0 ? 0 : J.w;
-            nc = ql < 2 * w + 1 ? ql : 2 * w + 1;
             base = seq_off[k];
             qa = reinterpret_cast<uint64_t>(J.query);
             ta = reinterpret_cast<uint64_t>(J.target);
             qw = slice_words(J.query, ql);
             tw = slice_words(J.target, tl);
+            GlobalDevJob D;
             D.q_off = base + (qa & 15);
             D.t_off = base + 16ull * qw + (ta & 15);
-            D.z_off = z_off[g];
+            D.z_off = z_off[k];
             D.cig_off = cig_off[k];
             D.qlen = ql;
             D.tlen = tl;
             D.w = J.w;
+            D.zrow = global_zrow(ql, J.w);
+            dj[k] = D;
         }
-        D.ncw = (int)((__reduce_max_sync(0xffffffffu, (unsigned)nc) + 3) / 4);
-        if (k < n) dj[k] = D;
         warp_gather_slices(qa & ~15ull, ta & ~15ull, base, qw, tw, seq);
     }
 }
@@ -317,26 +361,32 @@ __global__ void glb_store_kernel(const GlobalDevJob *__restrict__ dj, uint32_t n
 }
 
 template <int TB>
-cudaError_t launch_global_tb(const uint8_t *seq, const GlobalDevJob *jobs, uint32_t n, const Scoring &sc, int bcap,
-                             int qcap, uint32_t *z, uint32_t *cig, int32_t *score, int32_t *ncig, uint32_t *err,
-                             unsigned long long *cells, cudaStream_t s)
+cudaError_t launch_global_tb(const uint8_t *seq, const GlobalDevJob *jobs, const uint32_t *order, uint32_t base,
+                             uint32_t count, const Scoring &sc, int bcap, int qcap, uint8_t *z, uint32_t *cig,
+                             int32_t *score, int32_t *ncig, uint32_t *err, unsigned long long *cells, cudaStream_t s)
 {
     const size_t smem = global_smem(bcap, qcap, TB);
     auto kern = global_tpj_kernel<TB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<(n + TB - 1) / TB, TB, smem, s>>>(seq, jobs, n, sc, bcap, qcap, z, cig, score, ncig, err, cells);
+    kern<<<(count + TB - 1) / TB, TB, smem, s>>>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig,
+                                                 err, cells);
     return cudaGetLastError();
 }
 
-// bcap / qcap: the launch's largest band-slot count and query length.
-cudaError_t launch_global(const uint8_t *seq, const GlobalDevJob *jobs, uint32_t n, const Scoring &sc, int bcap,
-                          int qcap, uint32_t *z, uint32_t *cig, int32_t *score, int32_t *ncig, uint32_t *err,
-                          unsigned long long *cells, cudaStream_t s)
+// Jobs order[base .. base + count) (or base .. base + count without an order); bcap / qcap:
+// their largest band-slot count and query length.
+cudaError_t launch_global(const uint8_t *seq, const GlobalDevJob *jobs, const uint32_t *order, uint32_t base,
+                          uint32_t count, const Scoring &sc, int bcap, int qcap, uint8_t *z, uint32_t *cig,
+                          int32_t *score, int32_t *ncig, uint32_t *err, unsigned long long *cells, cudaStream_t s)
 {
+    if (count == 0) return cudaSuccess;
+    if (bcap < 1) bcap = 1;
+    if (global_smem(bcap, qcap, 128) <= SMEM_LIMIT / 2)
+        return launch_global_tb<128>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig, err, cells, s);
     if (global_smem(bcap, qcap, 64) <= SMEM_LIMIT)
-        return launch_global_tb<64>(seq, jobs, n, sc, bcap, qcap, z, cig, score, ncig, err, cells, s);
-    return launch_global_tb<32>(seq, jobs, n, sc, bcap, qcap, z, cig, score, ncig, err, cells, s);
+        return launch_global_tb<64>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig, err, cells, s);
+    return launch_global_tb<32>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig, err, cells, s);
 }
 
 // Longest query a 32-thread block holds (its band slots are at most qlen + 1).
@@ -397,40 +447,50 @@ int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n
     bool short_buf = false;
     int rc = BWACUDA_OK;
     cudaError_t e = cudaSuccess;
-    if ((e = b.d_flags.ensure(64)) != cudaSuccess) return cuda_status(e);
-    if ((e = b.h_tot.ensure(64)) != cudaSuccess) return cuda_status(e);
+    if ((e = b.d_flags.ensure(256)) != cudaSuccess) return cuda_status(e);
+    if ((e = b.h_tot.ensure(512)) != cudaSuccess) return cuda_status(e);
     uint64_t *ht = static_cast<uint64_t *>(b.h_tot.p);
     for (size_t c0 = 0; c0 < n && rc == BWACUDA_OK; c0 += kChunk) {
         const size_t cn = std::min(kChunk, n - c0);
-        const size_t ng = (cn + 31) / 32;
         const bwacuda_global_job *hj = jobs + c0;
-        // planning arrays: seq sizes/offsets, cig sizes/offsets (cn + 1 each), z sizes/offsets (ng + 1 each)
-        if ((e = b.d_sz.ensure(((cn + 1) * 4 + (ng + 1) * 2) * 8 + 64)) != cudaSuccess) break;
-        uint64_t *seq_sz = static_cast<uint64_t *>(b.d_sz.p), *seq_off = seq_sz + cn + 1;
-        uint64_t *cig_sz = seq_off + cn + 1, *cig_off = cig_sz + cn + 1;
-        uint64_t *z_sz = cig_off + cn + 1, *z_off = z_sz + ng + 1;
-        uint32_t *flags = static_cast<uint32_t *>(b.d_flags.p);
-        size_t t1 = 0, t2 = 0;
+        // planning arrays: seq / cig / z sizes and offsets (cn + 1 each), keys and indices (two
+        // copies each for the sort)
+        const size_t n1 = cn + 1;
+        if ((e = b.d_sz.ensure(n1 * 6 * 8 + n1 * 4 * 4 + 256)) != cudaSuccess) break;
+        uint64_t *seq_sz = static_cast<uint64_t *>(b.d_sz.p), *seq_off = seq_sz + n1;
+        uint64_t *cig_sz = seq_off + n1, *cig_off = cig_sz + n1;
+        uint64_t *z_sz = cig_off + n1, *z_off = z_sz + n1;
+        uint32_t *keys = reinterpret_cast<uint32_t *>(z_off + n1), *keys2 = keys + n1;
+        uint32_t *idx = keys2 + n1, *order = idx + n1;
+        uint32_t *flags = static_cast<uint32_t *>(b.d_flags.p);  // [0] errors, [16..31] bucket stats, [32..47] bounds
+        uint32_t *bstat = flags + 16, *bounds = flags + 32;
+        size_t t1 = 0, t2 = 0, t3 = 0;
         cub::DeviceScan::ExclusiveSum(nullptr, t1, (const uint64_t *)nullptr, (uint64_t *)nullptr, (int)cn + 1);
         cub::DeviceScan::ExclusiveSum(nullptr, t2, (const int32_t *)nullptr, (uint64_t *)nullptr, (int)cn + 1);
-        if ((e = b.d_tmp.ensure(std::max(t1, t2) + 64)) != cudaSuccess) break;
-        if ((e = cudaMemsetAsync(flags, 0, 16, s)) != cudaSuccess) break;
+        cub::DeviceRadixSort::SortPairs(nullptr, t3, (const uint32_t *)nullptr, (uint32_t *)nullptr,
+                                        (const uint32_t *)nullptr, (uint32_t *)nullptr, (int)cn, 0, 25);
+        if ((e = b.d_tmp.ensure(std::max(std::max(t1, t2), t3) + 64)) != cudaSuccess) break;
+        if ((e = cudaMemsetAsync(flags, 0, 256, s)) != cudaSuccess) break;
         if ((e = cudaMemsetAsync(seq_sz + cn, 0, 8, s)) != cudaSuccess) break;
         if ((e = cudaMemsetAsync(cig_sz + cn, 0, 8, s)) != cudaSuccess) break;
-        if ((e = cudaMemsetAsync(z_sz + ng, 0, 8, s)) != cudaSuccess) break;
-        uint32_t grid = (uint32_t)std::min<size_t>((ng * 32 + 255) / 256, (size_t)nsm * 8);
-        glb_plan_kernel<<<grid, 256, 0, s>>>(hj, (uint32_t)cn, qlim, seq_sz, cig_sz, z_sz, flags);
+        if ((e = cudaMemsetAsync(z_sz + cn, 0, 8, s)) != cudaSuccess) break;
+        uint32_t grid = (uint32_t)std::min<size_t>((cn + 255) / 256, (size_t)nsm * 8);
+        glb_plan_kernel<<<grid, 256, 0, s>>>(hj, (uint32_t)cn, qlim, seq_sz, cig_sz, z_sz, keys, idx, flags, bstat);
         if ((e = cudaGetLastError()) != cudaSuccess) break;
         if ((e = cub::DeviceScan::ExclusiveSum(b.d_tmp.p, t1, seq_sz, seq_off, (int)cn + 1, s)) != cudaSuccess) break;
         if ((e = cub::DeviceScan::ExclusiveSum(b.d_tmp.p, t1, cig_sz, cig_off, (int)cn + 1, s)) != cudaSuccess) break;
-        if ((e = cub::DeviceScan::ExclusiveSum(b.d_tmp.p, t1, z_sz, z_off, (int)ng + 1, s)) != cudaSuccess) break;
+        if ((e = cub::DeviceScan::ExclusiveSum(b.d_tmp.p, t1, z_sz, z_off, (int)cn + 1, s)) != cudaSuccess) break;
+        if ((e = cub::DeviceRadixSort::SortPairs(b.d_tmp.p, t3, keys, keys2, idx, order, (int)cn, 0, 25, s)) != cudaSuccess)
+            break;
+        glb_bucket_bounds_kernel<<<1, 32, 0, s>>>(keys2, (uint32_t)cn, bounds);
+        if ((e = cudaGetLastError()) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(ht + 0, seq_off + cn, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(ht + 1, cig_off + cn, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
-        if ((e = cudaMemcpyAsync(ht + 2, z_off + ng, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
-        if ((e = cudaMemcpyAsync(ht + 3, flags, 16, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(ht + 2, z_off + cn, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(ht + 3, flags, 256, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) break;
-        const uint32_t fl = (uint32_t)ht[3], qmax = (uint32_t)(ht[3] >> 32), bmax = (uint32_t)ht[4];
-        if (fl & 1u) {
+        const uint32_t *hf = reinterpret_cast<const uint32_t *>(ht + 3);
+        if (hf[0] & 1u) {
             // an invalid job, or a query longer than the kernel takes: find which on the host
             rc = BWACUDA_EINVAL;
             for (size_t k = 0; k < cn; ++k)
@@ -439,7 +499,7 @@ int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n
         }
         if ((e = b.d_seq.ensure(ht[0] + 16)) != cudaSuccess) break;
         if ((e = b.d_cig.ensure(ht[1] * 4 + 16)) != cudaSuccess) break;
-        if ((e = b.d_z.ensure(ht[2] * 4 + 16)) != cudaSuccess) break;
+        if ((e = b.d_z.ensure(ht[2] + 16)) != cudaSuccess) break;
         if ((e = b.d_jobs.ensure(cn * sizeof(GlobalDevJob))) != cudaSuccess) break;
         if ((e = b.d_res.ensure((cn + 1) * 8 + 16)) != cudaSuccess) break;
         if ((e = b.d_doff.ensure((cn + 1) * 8)) != cudaSuccess) break;
@@ -451,20 +511,27 @@ int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n
         int32_t *d_ncig = d_score + cn + 1;
         uint64_t *d_doff = static_cast<uint64_t *>(b.d_doff.p);
         if ((e = cudaMemsetAsync(d_ncig + cn, 0, 4, s)) != cudaSuccess) break;
-        e = launch_global(static_cast<const uint8_t *>(b.d_seq.p), dj, (uint32_t)cn, sc, (int)bmax, (int)qmax,
-                          static_cast<uint32_t *>(b.d_z.p), static_cast<uint32_t *>(b.d_cig.p), d_score, d_ncig, d_err,
-                          d_cells, s);
+        // one launch per non-empty length bucket, sized by the bucket's own maxima
+        const uint32_t *hb = hf + 16, *hbd = hf + 32;
+        for (int bk = 0; bk < GLB_NBUCKETS && e == cudaSuccess; ++bk) {
+            const uint32_t b0 = hbd[2 * bk], b1 = hbd[2 * bk + 1];
+            if (b1 <= b0) continue;
+            e = launch_global(static_cast<const uint8_t *>(b.d_seq.p), dj, order, b0, b1 - b0, sc, (int)hb[2 * bk],
+                              (int)hb[2 * bk + 1], static_cast<uint8_t *>(b.d_z.p), static_cast<uint32_t *>(b.d_cig.p),
+                              d_score, d_ncig, d_err, d_cells, s);
+            c->stats.kernel_launches += 1;
+        }
         if (e != cudaSuccess) break;
         if ((e = cub::DeviceScan::ExclusiveSum(b.d_tmp.p, t2, d_ncig, d_doff, (int)cn + 1, s)) != cudaSuccess) break;
         grid = (uint32_t)std::min<size_t>((cn * 32 + 255) / 256, (size_t)nsm * 8);
         glb_store_kernel<<<grid, 256, 0, s>>>(dj, (uint32_t)cn, d_score, static_cast<const uint32_t *>(b.d_cig.p), d_ncig,
                                              d_doff, out_base, cigar ? cigar_cap : 0, score + c0, cigar_off + c0, cigar);
         if ((e = cudaGetLastError()) != cudaSuccess) break;
-        if ((e = cudaMemcpyAsync(ht + 5, d_doff + cn, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(ht + 40, d_doff + cn, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) break;
-        if (!cigar || out_base + ht[5] > cigar_cap) short_buf = true;
-        out_base += ht[5];
-        c->stats.kernel_launches += 9;
+        if (!cigar || out_base + ht[40] > cigar_cap) short_buf = true;
+        out_base += ht[40];
+        c->stats.kernel_launches += 10;
     }
     if (e != cudaSuccess) return cuda_status(e);
     if (rc) {
@@ -520,79 +587,57 @@ extern "C" int bwacuda_ksw_global2_batch(bwacuda_ctx *c, const bwacuda_global_jo
     cudaStream_t s = c->stream;
     uint32_t *d_err = static_cast<uint32_t *>(c->d_misc.p);
     // chunks bounded in jobs and in traceback bytes
-    const size_t kMaxJobs = 262144, kMaxZWords = (size_t)1 << 29;  // 2 GiB of traceback per chunk
+    const size_t kMaxJobs = 262144, kMaxZBytes = (size_t)1 << 31;  // 2 GiB of traceback per chunk
     uint64_t out_base = 0;
     bool short_buf = false;
     cudaError_t e = cudaSuccess;
     size_t c0 = 0;
     while (c0 < n && rc == BWACUDA_OK && e == cudaSuccess) {
-        // grow the chunk 32 jobs (one warp group) at a time
         size_t cn = 0;
-        uint64_t zwords = 0, cigw = 0, bytes = 0;
+        uint64_t zbytes = 0, cigw = 0, bytes = 0;
         int qmax = 0, bmax = 1;
         while (c0 + cn < n && cn < kMaxJobs) {
-            const size_t g1 = std::min(n, c0 + cn + 32);
-            int tmax = 0, ncmax = 0;
-            uint64_t gb = 0, gc = 0;
-            for (size_t k = c0 + cn; k < g1; ++k) {
-                const bwacuda_global_job &J = jobs[k];
-                const int w = J.w < 0 ? 0 : J.w;
-                tmax = std::max(tmax, J.tlen);
-                ncmax = std::max(ncmax, std::min(J.qlen, 2 * w + 1));
-                gb += (uint64_t)J.qlen + (uint64_t)J.tlen;
-                gc += (uint64_t)J.qlen + (uint64_t)J.tlen + 1;
-                qmax = std::max(qmax, J.qlen);
-                bmax = std::max(bmax, global_band_slots(J.qlen, J.w));
-            }
-            const uint64_t gz = (uint64_t)tmax * (uint64_t)((ncmax + 3) / 4) * 32u;
-            if (cn > 0 && zwords + gz > kMaxZWords) break;
-            zwords += gz;
-            cigw += gc;
-            bytes += gb;
-            cn = g1 - c0;
+            const bwacuda_global_job &J = jobs[c0 + cn];
+            const uint64_t jz = (uint64_t)J.tlen * (uint64_t)global_zrow(J.qlen, J.w);
+            if (cn > 0 && zbytes + jz > kMaxZBytes) break;
+            zbytes += jz;
+            bytes += (uint64_t)J.qlen + (uint64_t)J.tlen;
+            cigw += (uint64_t)J.qlen + (uint64_t)J.tlen + 1;
+            qmax = std::max(qmax, J.qlen);
+            bmax = std::max(bmax, global_band_slots(J.qlen, J.w));
+            ++cn;
         }
-        // pack: bases, descriptors (warp groups share their traceback block)
+        // pack: bases and descriptors (each job's traceback matrix contiguous)
         if ((e = b.h_seq.ensure(bytes + 16)) != cudaSuccess) break;
         if ((e = b.h_jobs.ensure(cn * sizeof(GlobalDevJob))) != cudaSuccess) break;
         if ((e = b.h_res.ensure(cn * 8 + 16)) != cudaSuccess) break;
         uint8_t *hs = static_cast<uint8_t *>(b.h_seq.p);
         GlobalDevJob *hj = static_cast<GlobalDevJob *>(b.h_jobs.p);
         uint64_t so = 0, zo = 0, co = 0;
-        for (size_t g0 = 0; g0 < cn; g0 += 32) {
-            const size_t g1 = std::min(cn, g0 + 32);
-            int tmax = 0, ncmax = 0;
-            for (size_t k = g0; k < g1; ++k) {
-                const bwacuda_global_job &J = jobs[c0 + k];
-                const int w = J.w < 0 ? 0 : J.w;
-                tmax = std::max(tmax, J.tlen);
-                ncmax = std::max(ncmax, std::min(J.qlen, 2 * w + 1));
-            }
-            const int ncw = (ncmax + 3) / 4;
-            for (size_t k = g0; k < g1; ++k) {
-                const bwacuda_global_job &J = jobs[c0 + k];
-                GlobalDevJob D;
-                D.q_off = so;
-                if (J.qlen) memcpy(hs + so, J.query, (size_t)J.qlen);
-                so += (uint64_t)J.qlen;
-                D.t_off = so;
-                if (J.tlen) memcpy(hs + so, J.target, (size_t)J.tlen);
-                so += (uint64_t)J.tlen;
-                D.z_off = zo;
-                D.cig_off = co;
-                co += (uint64_t)J.qlen + (uint64_t)J.tlen + 1;
-                D.qlen = J.qlen;
-                D.tlen = J.tlen;
-                D.w = J.w;
-                D.ncw = ncw;
-                hj[k] = D;
-            }
-            zo += (uint64_t)tmax * (uint64_t)ncw * 32u;
+        for (size_t k = 0; k < cn; ++k) {
+            const bwacuda_global_job &J = jobs[c0 + k];
+            GlobalDevJob D;
+            D.q_off = so;
+            if (J.qlen) memcpy(hs + so, J.query, (size_t)J.qlen);
+            so += (uint64_t)J.qlen;
+            D.t_off = so;
+            if (J.tlen) memcpy(hs + so, J.target, (size_t)J.tlen);
+            so += (uint64_t)J.tlen;
+            D.z_off = zo;
+            D.zrow = global_zrow(J.qlen, J.w);
+            zo += (uint64_t)J.tlen * (uint64_t)D.zrow;
+            D.cig_off = co;
+            co += (uint64_t)J.qlen + (uint64_t)J.tlen + 1;
+            D.qlen = J.qlen;
+            D.tlen = J.tlen;
+            D.w = J.w;
+            hj[k] = D;
         }
         size_t scan_bytes = 0;
         cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, (const int32_t *)nullptr, (uint64_t *)nullptr, (int)cn + 1);
         if ((e = b.d_seq.ensure(bytes + 16)) != cudaSuccess) break;
         if ((e = b.d_jobs.ensure(cn * sizeof(GlobalDevJob))) != cudaSuccess) break;
-        if ((e = b.d_z.ensure(zwords * 4 + 16)) != cudaSuccess) break;
+        if ((e = b.d_z.ensure(zbytes + 16)) != cudaSuccess) break;
         if ((e = b.d_cig.ensure(cigw * 4 + 16)) != cudaSuccess) break;
         if ((e = b.d_res.ensure((cn + 1) * 8 + 16)) != cudaSuccess) break;
         if ((e = b.d_doff.ensure((cn + 1) * 8)) != cudaSuccess) break;
@@ -605,7 +650,7 @@ extern "C" int bwacuda_ksw_global2_batch(bwacuda_ctx *c, const bwacuda_global_jo
         if ((e = cudaMemsetAsync(d_ncig + cn, 0, 4, s)) != cudaSuccess) break;
         c->stats.h2d_bytes += bytes + cn * sizeof(GlobalDevJob);
         e = launch_global(static_cast<const uint8_t *>(b.d_seq.p), static_cast<const GlobalDevJob *>(b.d_jobs.p),
-                          (uint32_t)cn, sc, bmax, qmax, static_cast<uint32_t *>(b.d_z.p),
+                          nullptr, 0, (uint32_t)cn, sc, bmax, qmax, static_cast<uint8_t *>(b.d_z.p),
                           static_cast<uint32_t *>(b.d_cig.p), d_score, d_ncig, d_err,
                           reinterpret_cast<unsigned long long *>((char *)c->d_misc.p + 8), s);
         if (e != cudaSuccess) break;
