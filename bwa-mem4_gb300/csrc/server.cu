@@ -6,15 +6,18 @@
 // Inputs, queues of descriptors and results stay on the GPU; a client's
 // bwacuda_server_wait copies its results out and releases its memory.
 //
-// Memory: one device arena of `hbm_budget_bytes` and a pinned host arena of the
-// same size mirror each other offset for offset; a request occupies one
-// contiguous range of both: [descriptors | (rescue) tracker offsets | results |
+// Memory: one device arena of `hbm_budget_bytes`; a request occupies one
+// contiguous range of it: [descriptors | (rescue) tracker offsets | results |
 // bases | (rescue) tracker entries].  Descriptor offsets address the arena base,
 // so a wave's jobs from many requests run in one launch.
 //
-// Scheduling is a host thread that admits (packs + validates + copies in),
-// launches waves, and retires waves by polling their completion events; every
-// wait is bounded by the caller's timeout.
+// Admission: where the device reads pageable host memory (Grace-Blackwell), a
+// gather kernel on a high-priority copy stream reads the caller's job array and
+// slices straight into the request's range and checks the base codes; otherwise
+// worker threads pack into a pinned mirror of the arena and the copy engines
+// move it.  Scheduling is a host thread that admits, settles gathered requests
+// (a bad base fails its request alone), launches waves, and retires waves by
+// polling their completion events; every wait is bounded by the caller's timeout.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -98,6 +101,12 @@ struct Request {
     int rc = BWACUDA_OK;
     Clock::time_point t_submit, t_done;
     cudaEvent_t h2d = nullptr;
+    // device-gather admission: per-job base and tracker offsets inside the request's
+    // range, and the status word the gather kernel sets when a base code is >= m
+    bool dev = false;
+    bool ready = true;  // device-gather admissions: false until settled
+    std::vector<uint64_t> goff, gsoff;
+    volatile uint32_t status = 0;
 };
 
 struct WaveSlot {
@@ -131,11 +140,77 @@ struct ServerState {
     cudaStream_t copy_stream = nullptr, read_stream = nullptr;
     WorkerPool *pool = nullptr;
     uint64_t served_jobs = 0, served_cells = 0, waves = 0;
+    bool dev = false;  // admission by device gather (the device reads pageable host memory)
 };
 
 namespace {
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Device-gather admission of one request: one warp per 32 jobs writes their
+// descriptors (absolute arena offsets) and, for rescue, their tracker offsets,
+// copies the slices from the caller's host memory into the arena as aligned
+// 16-byte words, then scans the copied bases and sets *status if any code is
+// >= m (the request then fails alone instead of failing its wave).  Both job
+// structs begin with query, target, qlen, tlen.
+template <int KIND>
+__global__ void __launch_bounds__(256) srv_gather_kernel(const void *__restrict__ hjobs, uint32_t n,
+                                                         const uint64_t *__restrict__ goff,
+                                                         const uint64_t *__restrict__ gsoff, uint8_t *__restrict__ arena,
+                                                         uint64_t desc_abs, uint64_t soff_abs, uint64_t seq_abs,
+                                                         uint64_t scr_base, int w, int m, volatile uint32_t *status)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t ngroups = (n + 31) / 32;
+    for (uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ngroups; g += (gridDim.x * blockDim.x) >> 5) {
+        const uint32_t k = g * 32 + lane;
+        uint64_t qa = 0, ta = 0, base = 0, qo = 0, to = 0;
+        uint32_t qw = 0, tw = 0;
+        int ql = 0, tl = 0;
+        if (k < n) {
+            const uint8_t *q, *t;
+            if (KIND == 0) {
+                const bwacuda_ext_job J = static_cast<const bwacuda_ext_job *>(hjobs)[k];
+                q = J.query; t = J.target; ql = J.qlen; tl = J.tlen;
+                base = seq_abs + goff[k];
+                qa = reinterpret_cast<uint64_t>(q);
+                ta = reinterpret_cast<uint64_t>(t);
+                qw = slice_words(q, ql);
+                tw = slice_words(t, tl);
+                bwacuda_dev_ext_job D;
+                D.q_off = qo = base + (qa & 15);
+                D.t_off = to = base + 16ull * qw + (ta & 15);
+                D.qlen = ql; D.tlen = tl; D.h0 = J.h0; D.w = w;
+                reinterpret_cast<bwacuda_dev_ext_job *>(arena + desc_abs)[k] = D;
+            } else {
+                const bwacuda_rescue_job J = static_cast<const bwacuda_rescue_job *>(hjobs)[k];
+                q = J.query; t = J.target; ql = J.qlen; tl = J.tlen;
+                base = seq_abs + goff[k];
+                qa = reinterpret_cast<uint64_t>(q);
+                ta = reinterpret_cast<uint64_t>(t);
+                qw = slice_words(q, ql);
+                tw = slice_words(t, tl);
+                bwacuda_dev_rescue_job D;
+                D.q_off = qo = base + (qa & 15);
+                D.t_off = to = base + 16ull * qw + (ta & 15);
+                D.qlen = ql; D.tlen = tl; D.minsc = 0; D.endsc = 0;
+                reinterpret_cast<bwacuda_dev_rescue_job *>(arena + desc_abs)[k] = D;
+                reinterpret_cast<uint64_t *>(arena + soff_abs)[k] = scr_base + gsoff[k];
+            }
+        }
+        warp_gather_slices(qa & ~15ull, ta & ~15ull, base, qw, tw, arena);
+        __syncwarp();
+        bool bad = false;
+        const uint32_t cnt = min(32u, n - g * 32);
+        for (uint32_t j = 0; j < cnt; ++j) {
+            const uint64_t jq = __shfl_sync(0xffffffffu, qo, j), jt = __shfl_sync(0xffffffffu, to, j);
+            const int jql = __shfl_sync(0xffffffffu, ql, j), jtl = __shfl_sync(0xffffffffu, tl, j);
+            for (int x = (int)lane; x < jql; x += 32) bad |= arena[jq + x] >= (uint32_t)m;
+            for (int x = (int)lane; x < jtl; x += 32) bad |= arena[jt + x] >= (uint32_t)m;
+        }
+        if (__any_sync(0xffffffffu, bad) && lane == 0) *status = 1u;
+    }
+}
 
 // Lays out a request's range and checks its inputs on the host.
 int plan_request(Request *r, int m)
@@ -143,6 +218,10 @@ int plan_request(Request *r, int m)
     uint64_t seq = 0, scr = 0;
     int qmax = 0;
     bool wide = false;
+    if (r->dev) {
+        r->goff.resize(r->n);
+        if (r->kind == 1) r->gsoff.resize(r->n);
+    }
     for (size_t k = 0; k < r->n; ++k) {
         const int32_t ql = r->kind == 0 ? r->ejobs[k].qlen : r->rjobs[k].qlen;
         const int32_t tl = r->kind == 0 ? r->ejobs[k].tlen : r->rjobs[k].tlen;
@@ -150,9 +229,16 @@ int plan_request(Request *r, int m)
         const uint8_t *t = r->kind == 0 ? r->ejobs[k].target : r->rjobs[k].target;
         if (ql < 0 || tl < 0 || (ql && !q) || (tl && !t)) return BWACUDA_EINVAL;
         if (r->kind == 0 && r->ejobs[k].h0 <= 0) return BWACUDA_EINVAL;
-        seq += (uint64_t)ql + (uint64_t)tl;
+        if (r->dev) {
+            // slices travel as the aligned 16-byte words that cover them
+            r->goff[k] = seq;
+            seq += 16ull * (slice_words(q, ql) + slice_words(t, tl));
+        } else {
+            seq += (uint64_t)ql + (uint64_t)tl;
+        }
         qmax = std::max(qmax, ql);
         if (r->kind == 1) {
+            if (r->dev) r->gsoff[k] = scr;
             scr += rescue_scratch_entries(tl);
             if ((long long)std::min(ql, tl) * std::max(r->max_sc, 0) >= 32768) wide = true;
         }
@@ -278,8 +364,6 @@ void finish(ServerState *S, Request *r, int rc)
 // Admit pending requests in arrival order while their range fits the arena.
 void admit(ServerState *S)
 {
-    const int m = 0;
-    (void)m;
     while (!S->pending.empty()) {
         Request *r = S->pending.front();
         size_t off;
@@ -287,20 +371,40 @@ void admit(ServerState *S)
         S->pending.pop_front();
         r->off = off;
         const int mm = r->kind == 0 ? r->P.sc.m : r->sc.m;
-        int rc = pack_request(S, r, mm);
-        if (rc != BWACUDA_OK) {
-            S->alloc->release(r->off, r->bytes);
-            r->bytes = 0;
-            finish(S, r, rc);
-            continue;
+        cudaError_t e = cudaSuccess;
+        if (r->dev) {
+            r->ready = false;
+            // the device reads the caller's jobs and slices; the request is usable
+            // once its event fires and its status word is still 0
+            int nsm = 0;
+            if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, S->c->device) != cudaSuccess || nsm < 1) nsm = 1;
+            const uint32_t grid = (uint32_t)std::min<size_t>((r->n * 32 + 255) / 256, (size_t)nsm * 2);
+            const uint64_t scr_base = (r->off + r->scr_at) / 8;  // uint2 index from the arena base
+            if (r->kind == 0)
+                srv_gather_kernel<0><<<grid, 256, 0, S->copy_stream>>>(r->ejobs, (uint32_t)r->n, r->goff.data(), nullptr,
+                                                                      S->d_arena, r->off + r->desc_at, 0,
+                                                                      r->off + r->seq_at, 0, r->w, mm, &r->status);
+            else
+                srv_gather_kernel<1><<<grid, 256, 0, S->copy_stream>>>(r->rjobs, (uint32_t)r->n, r->goff.data(),
+                                                                      r->gsoff.data(), S->d_arena, r->off + r->desc_at,
+                                                                      r->off + r->soff_at, r->off + r->seq_at, scr_base,
+                                                                      0, mm, &r->status);
+            e = cudaGetLastError();
+        } else {
+            int rc = pack_request(S, r, mm);
+            if (rc != BWACUDA_OK) {
+                S->alloc->release(r->off, r->bytes);
+                r->bytes = 0;
+                finish(S, r, rc);
+                continue;
+            }
+            // copy in: descriptors (+ tracker offsets) and bases
+            const size_t head = r->kind == 1 ? r->res_at : r->n * 32;
+            e = cudaMemcpyAsync(S->d_arena + r->off, S->h_arena + r->off, head, cudaMemcpyHostToDevice, S->copy_stream);
+            if (e == cudaSuccess && r->seq_bytes)
+                e = cudaMemcpyAsync(S->d_arena + r->off + r->seq_at, S->h_arena + r->off + r->seq_at, r->seq_bytes,
+                                    cudaMemcpyHostToDevice, S->copy_stream);
         }
-        // copy in: descriptors (+ tracker offsets) and bases
-        const size_t head = r->kind == 1 ? r->res_at : r->n * 32;
-        cudaError_t e = cudaMemcpyAsync(S->d_arena + r->off, S->h_arena + r->off, head, cudaMemcpyHostToDevice,
-                                        S->copy_stream);
-        if (e == cudaSuccess && r->seq_bytes)
-            e = cudaMemcpyAsync(S->d_arena + r->off + r->seq_at, S->h_arena + r->off + r->seq_at, r->seq_bytes,
-                                cudaMemcpyHostToDevice, S->copy_stream);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->h2d, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventRecord(r->h2d, S->copy_stream);
         if (e != cudaSuccess) {
@@ -312,6 +416,33 @@ void admit(ServerState *S)
     }
 }
 
+// Device-gather admissions whose copy has landed: a request with a bad base code
+// fails alone; the rest may join a wave.  Returns true when anything changed.
+bool settle_admitted(ServerState *S)
+{
+    bool any = false;
+    std::vector<Request *> keep;
+    keep.reserve(S->admitted.size());
+    for (Request *r : S->admitted) {
+        if (!r->dev) { keep.push_back(r); continue; }
+        const cudaError_t q = cudaEventQuery(r->h2d);
+        if (q == cudaErrorNotReady) { keep.push_back(r); continue; }
+        if (q != cudaSuccess || r->status != 0u) {
+            S->alloc->release(r->off, r->bytes);
+            r->bytes = 0;
+            finish(S, r, q != cudaSuccess ? cuda_status(q) : BWACUDA_EBASE);
+            any = true;
+            continue;
+        }
+        r->dev = false;  // settled: behaves like a copied request from here on
+        r->ready = true;
+        keep.push_back(r);
+        any = true;
+    }
+    S->admitted.swap(keep);
+    return any;
+}
+
 // Launch one wave on a free slot from the admitted requests of one group.
 bool launch_wave(ServerState *S)
 {
@@ -320,10 +451,13 @@ bool launch_wave(ServerState *S)
     for (auto &w : S->slots)
         if (!w.busy) { slot = &w; break; }
     if (!slot) return false;
-    Request *lead = S->admitted.front();
+    Request *lead = nullptr;
+    for (Request *r : S->admitted)
+        if (r->ready) { lead = r; break; }
+    if (!lead) return false;
     std::vector<Request *> group, rest;
     size_t n = 0;
-    for (Request *r : S->admitted) (same_group(lead, r) ? group : rest).push_back(r);
+    for (Request *r : S->admitted) (r->ready && same_group(lead, r) ? group : rest).push_back(r);
     for (Request *r : group) n += r->n;
     S->admitted.swap(rest);
     cudaStream_t s = slot->stream;
@@ -435,11 +569,13 @@ void scheduler(ServerState *S)
         bool progress = retire(S);
         if (progress) S->cv_done.notify_all();
         admit(S);
+        progress |= settle_admitted(S);
         while (launch_wave(S)) progress = true;
         // notify waiters of requests that failed at admission
         S->cv_done.notify_all();
         bool busy = false;
         for (auto &w : S->slots) busy |= w.busy;
+        for (Request *r : S->admitted) busy |= !r->ready;  // gathers in flight are polled too
         if (S->stop && !busy) {
             for (Request *r : S->pending) finish(S, r, BWACUDA_EBUSY);
             for (Request *r : S->admitted) finish(S, r, BWACUDA_EBUSY);
@@ -518,9 +654,16 @@ extern "C" int bwacuda_server_start(bwacuda_ctx *c, const bwacuda_server_config 
     S->budget = cfg && cfg->hbm_budget_bytes ? (size_t)cfg->hbm_budget_bytes : ((size_t)4 << 30);
     const int nw = cfg && cfg->max_waves > 0 ? cfg->max_waves : 3;
     if (cfg && cfg->max_requests > 0) S->max_requests = (size_t)cfg->max_requests;
+    // admission by device gather where the device reads pageable host memory (no
+    // pinned mirror of the arena then), else host packing through a pinned mirror
+    S->dev = c->pageable_access && c->host_gather != BWACUDA_GATHER_HOST;
     cudaError_t e = cudaMalloc(&S->d_arena, S->budget);
-    if (e == cudaSuccess) e = cudaHostAlloc(reinterpret_cast<void **>(&S->h_arena), S->budget, cudaHostAllocDefault);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->copy_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess && !S->dev)
+        e = cudaHostAlloc(reinterpret_cast<void **>(&S->h_arena), S->budget, cudaHostAllocDefault);
+    int lo_prio = 0, hi_prio = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+    // admission copies run beside the waves' persistent kernels: highest priority
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&S->copy_stream, cudaStreamNonBlocking, hi_prio);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->read_stream, cudaStreamNonBlocking);
     S->slots.resize(nw);
     for (auto &w : S->slots) {
@@ -557,6 +700,7 @@ static int submit(bwacuda_ctx *c, Request *r)
 {
     ServerState *S = c->server;
     if (!S) { delete r; return BWACUDA_EINVAL; }
+    r->dev = S->dev;
     int rc = plan_request(r, r->kind == 0 ? r->P.sc.m : r->sc.m);
     if (rc == BWACUDA_OK && r->bytes > S->budget) rc = BWACUDA_ENOMEM;  // could never be admitted
     if (rc != BWACUDA_OK) { delete r; return rc; }

@@ -12,11 +12,16 @@ import oracle
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture
-def server(ctx):
+@pytest.fixture(params=[pytest.param(B.GATHER_AUTO, id="admit-auto"),
+                        pytest.param(B.GATHER_HOST, id="admit-hostpack")])
+def server(ctx, request):
+    """A serving loop admitting by device gather (where the device reads host memory) or by host
+    packing through a pinned mirror of the arena."""
+    ctx.set_option(B.OPT_HOST_GATHER, request.param)
     ctx.server_start(hbm_budget_bytes=256 << 20, max_waves=3)
     yield ctx
     ctx.server_stop()
+    ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_AUTO)
 
 
 def _mixed_requests(seed, count, lo=200, hi=6000):
