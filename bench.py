@@ -555,12 +555,10 @@ def main():
         if world > 1:
             torch.distributed.barrier()
 
+    from bwacuda import shard
+
     def max_over_ranks(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+        return shard.max_over_ranks(x, device="cuda")
 
     def timed_device(path, steps, warmup):
         for _ in range(warmup):
