@@ -8,13 +8,18 @@
 //   bwa_cuda::KswAlignResult            <->  KswAlignResult (crates/bwa-extend/src/sw.rs:750-774)
 //   bwa_cuda::batched_ksw_align2        <->  bwa_neon::batched_ksw_align2 (crates/bwa-neon/src/matesw.rs:299-309)
 //   bwa_cuda::ksw_align2                <->  bwa_extend::ksw_align2 (crates/bwa-extend/src/sw.rs:1108-1185)
+//   bwa_cuda::ksw_global2               <->  bwa_extend::ksw_global2 (crates/bwa-extend/src/sw.rs:561-740)
+//   bwa_cuda::ksw_global2_batch            (the same over many alignments, per-job band)
+//   bwa_cuda::run_side_extend           <->  the band-doubling loop of run_side (crates/bwa-mem/src/across.rs:1357-1500)
 //
 // Same argument names, meanings and result order.  The reference's calls are
 // infallible (they panic on bugs); these throw bwa_cuda::Error with the C ABI's
 // code instead, and never fall back to a CPU implementation.
 #pragma once
+#include <cstddef>
 #include <cstdint>
 #include <memory>
+#include <utility>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -159,6 +164,63 @@ inline KswAlignResult ksw_align2(Context &ctx, Bytes query, Bytes target, size_t
                                           lanes, &r),
           "bwacuda_ksw_align2_scalar_batch");
     return r;
+}
+
+// bwa_extend::ksw_global2 over many alignments: (score, CIGAR runs) per job,
+// the CIGAR as the reference's packed words (len << 4 | op, op 0=M 1=I 2=D).
+struct GlobalJob {
+    Bytes query, target;
+    int32_t w;
+};
+
+inline std::vector<std::pair<int32_t, std::vector<uint32_t>>> ksw_global2_batch(
+    Context &ctx, const std::vector<GlobalJob> &jobs, size_t m, const int8_t *mat, int o_del, int e_del, int o_ins,
+    int e_ins)
+{
+    std::vector<bwacuda_global_job> cj(jobs.size());
+    size_t cap = 0;
+    for (size_t k = 0; k < jobs.size(); ++k) {
+        cj[k] = bwacuda_global_job{jobs[k].query.ptr, jobs[k].target.ptr, (int32_t)jobs[k].query.len,
+                                   (int32_t)jobs[k].target.len, jobs[k].w};
+        cap += jobs[k].query.len + jobs[k].target.len;  // always enough words
+    }
+    std::vector<int32_t> score(jobs.size());
+    std::vector<uint64_t> off(jobs.size() + 1);
+    std::vector<uint32_t> words(cap + 1);
+    check(bwacuda_ksw_global2_batch(ctx.get(), cj.data(), cj.size(), (int)m, mat, o_del, e_del, o_ins, e_ins,
+                                    score.data(), off.data(), words.data(), words.size()),
+          "bwacuda_ksw_global2_batch");
+    std::vector<std::pair<int32_t, std::vector<uint32_t>>> out(jobs.size());
+    for (size_t k = 0; k < jobs.size(); ++k)
+        out[k] = {score[k], std::vector<uint32_t>(words.begin() + (ptrdiff_t)off[k], words.begin() + (ptrdiff_t)off[k + 1])};
+    return out;
+}
+
+// bwa_extend::ksw_global2: one alignment.
+inline std::pair<int32_t, std::vector<uint32_t>> ksw_global2(Context &ctx, Bytes query, Bytes target, size_t m,
+                                                            const int8_t *mat, int o_del, int e_del, int o_ins,
+                                                            int e_ins, int w)
+{
+    return ksw_global2_batch(ctx, {GlobalJob{query, target, w}}, m, mat, o_del, e_del, o_ins, e_ins)[0];
+}
+
+// run_side's band-doubling loop over one side's jobs: results and the band each
+// job was accepted at; prev as run_side starts it (-1 left, h0 right).
+inline std::pair<std::vector<ExtendResult>, std::vector<int32_t>> run_side_extend(
+    Context &ctx, const std::vector<ExtendJob> &jobs, const std::vector<int32_t> &prev, size_t m, const int8_t *mat,
+    int o_del, int e_del, int o_ins, int e_ins, int w, int pen_clip, int zdrop, int max_band_try)
+{
+    std::vector<bwacuda_ext_job> cj(jobs.size());
+    for (size_t k = 0; k < jobs.size(); ++k)
+        cj[k] = bwacuda_ext_job{jobs[k].query.ptr, jobs[k].target.ptr, (int32_t)jobs[k].query.len,
+                                (int32_t)jobs[k].target.len, jobs[k].h0};
+    std::vector<ExtendResult> out(jobs.size());
+    std::vector<int32_t> w_used(jobs.size());
+    check(bwacuda_extend_batch_retry(ctx.get(), cj.data(), cj.size(), (int)m, mat, o_del, e_del, o_ins, e_ins, w,
+                                     pen_clip, zdrop, max_band_try, prev.empty() ? nullptr : prev.data(), out.data(),
+                                     w_used.data()),
+          "bwacuda_extend_batch_retry");
+    return {out, w_used};
 }
 
 }  // namespace bwa_cuda

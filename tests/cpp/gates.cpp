@@ -5,6 +5,7 @@
 //   matesw_equals_scalar (first 500 jobs) crates/bwa-neon/src/matesw.rs:5045-5139
 // The expected values come from the CPU oracle (oracle/ksw_oracle.c), the checker.
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -109,6 +110,59 @@ int gate_rescue(bwa_cuda::Context &ctx)
     return 0;
 }
 
+// crates/bwa-extend/src/sw.rs:1358-1380 through the C++ mirror, and a batch of
+// random alignments against the oracle's restatement.
+int gate_global(bwa_cuda::Context &ctx)
+{
+    int8_t mat[25];
+    ko_fill_scmat(1, 4, mat);
+    const std::vector<uint8_t> s = {0, 1, 2, 3, 0, 1, 2, 3, 0, 1};
+    auto r = bwa_cuda::ksw_global2(ctx, s, s, 5, mat, 6, 1, 6, 1, 100);
+    if (r.first != (int)s.size() || r.second != std::vector<uint32_t>{(uint32_t)s.size() << 4}) {
+        std::printf("global exact match diverged\n");
+        return 1;
+    }
+    std::vector<uint8_t> q = {0, 1, 2, 3, 0, 1, 2, 3}, t = q;
+    t.insert(t.begin() + 4, 2);
+    r = bwa_cuda::ksw_global2(ctx, q, t, 5, mat, 6, 1, 6, 1, 100);
+    uint32_t dsum = 0, msum = 0;
+    for (uint32_t c : r.second) {
+        if ((c & 0xf) == 2) dsum += c >> 4;
+        if ((c & 0xf) == 0) msum += c >> 4;
+    }
+    if (dsum != 1 || msum != q.size()) {
+        std::printf("global single deletion diverged\n");
+        return 1;
+    }
+    uint64_t x = 88172645463325252ull;
+    auto rnd = [&x]() { x ^= x << 13; x ^= x >> 7; x ^= x << 17; return x; };
+    std::vector<std::vector<uint8_t>> qs(400), ts(400);
+    std::vector<bwa_cuda::GlobalJob> jobs;
+    for (int k = 0; k < 400; ++k) {
+        const int len = 20 + (int)(rnd() % 200);
+        for (int i = 0; i < len; ++i) ts[k].push_back((uint8_t)(rnd() % 4));
+        qs[k] = ts[k];
+        for (int e = 0; e < 3; ++e) qs[k][rnd() % qs[k].size()] = (uint8_t)(rnd() % 4);
+        if (rnd() % 3 == 0) qs[k].erase(qs[k].begin() + (ptrdiff_t)(rnd() % qs[k].size()));
+        const int diff = std::abs((int)qs[k].size() - (int)ts[k].size());
+        jobs.push_back(bwa_cuda::GlobalJob{qs[k], ts[k], diff + 3 + (int)(rnd() % 40)});
+    }
+    auto got = bwa_cuda::ksw_global2_batch(ctx, jobs, 5, mat, 6, 1, 6, 1);
+    std::vector<uint32_t> cig(1024);
+    for (size_t k = 0; k < jobs.size(); ++k) {
+        int32_t sc = 0;
+        int nc = 0;
+        if (ko_global2(qs[k].data(), (int)qs[k].size(), ts[k].data(), (int)ts[k].size(), 5, mat, 6, 1, 6, 1,
+                       jobs[k].w, &sc, cig.data(), &nc) != 0)
+            continue;
+        if (got[k].first != sc || got[k].second != std::vector<uint32_t>(cig.begin(), cig.begin() + nc)) {
+            std::printf("global job %zu diverged\n", k);
+            return 1;
+        }
+    }
+    return 0;
+}
+
 }  // namespace
 
 int main()
@@ -119,7 +173,7 @@ int main()
         if (std::strcmp(be.name(), "cuda") != 0) return 2;
         int rc = gate_single(be) | gate_batch(be);
         ctx.set_option(BWACUDA_OPT_EXT_PATH, BWACUDA_PATH_BATCHED);
-        rc |= gate_batch(be) | gate_rescue(ctx);
+        rc |= gate_batch(be) | gate_rescue(ctx) | gate_global(ctx);
         std::printf(rc ? "FAIL\n" : "gates ok\n");
         return rc;
     } catch (const bwa_cuda::Error &e) {
