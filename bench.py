@@ -47,7 +47,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "bit-exact SW extension GCUPS: batched/served vs plain on 1 GB300; p50/p99 latency"
 N_JOBS = 8 * 1024 * 1024
-OPS_PER_CELL = 9  # minimal fused integer op count of one extension cell (see the design doc roofline)
+OPS_PER_CELL = 9  # minimal fused integer op count of one extension cell
+# DRAM bytes per read-pair job of the batched step, from an ncu capture of every persistent bucket
+# kernel of a 2,000,000-job call (dram__bytes_read.sum + dram__bytes_write.sum = 862.4 MB + 68.9 MB)
+DRAM_BYTES_PER_JOB = 931294208 / 2000000
 
 
 def parse():
@@ -749,7 +752,8 @@ def main():
         "clocks": clocks,
         "roofline": {"bound": "alu", "achieved": round(achieved, 1), "peak": round(peak_g, 1), "unit": "Gop/s",
                      "frac": round(achieved / peak_g, 4),
-                     "traffic": None,
+                     "traffic": int(DRAM_BYTES_PER_JOB * n),
+                     "traffic_unit": "bytes per step (ncu capture of all bucket kernels, scaled by jobs)",
                      "peak_nominal": round(peak_nominal, 1),
                      "note": f"integer ops = GCUPS x {OPS_PER_CELL} ops/cell (minimal fused count) over the whole step "
                              "(the persistent extension kernels hold ~95% of its device time); peak = "
