@@ -74,11 +74,40 @@ __device__ __forceinline__ uint8_t ref_base(const RefView &R, int64_t p)
     return (uint8_t)(rc ? 3u - b : b);
 }
 
-__global__ void win_plan_kernel(const WinReqDev *__restrict__ reqs, uint32_t n, const RefView R, int min_seed_len,
+// A request as the kernels see it: staged (WinReqDev, mates in a staging buffer)
+// or the caller's own bwacuda_window_req read in place (mates at their pointers).
+struct ReqView {
+    const WinReqDev *staged;
+    const bwacuda_window_req *direct;
+    const uint8_t *mates;  // staged mates
+    __device__ __forceinline__ WinReqDev get(uint32_t k, const uint8_t **mate) const
+    {
+        if (staged) {
+            const WinReqDev q = staged[k];
+            *mate = mates + q.mate_off;
+            return q;
+        }
+        const bwacuda_window_req r = direct[k];
+        WinReqDev q;
+        q.mate_off = 0;
+        q.anchor_rb = r.anchor_rb;
+        q.l_ms = r.l_ms;
+        q.orient = r.orient;
+        q.anchor_rid = r.anchor_rid;
+        q.low = r.low;
+        q.high = r.high;
+        q.pad = 0;
+        *mate = r.mate;
+        return q;
+    }
+};
+
+__global__ void win_plan_kernel(const ReqView V, uint32_t n, const RefView R, int min_seed_len,
                                 WinInfo *__restrict__ info, uint64_t *__restrict__ sizes)
 {
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const WinReqDev q = reqs[k];
+        const uint8_t *unused;
+        const WinReqDev q = V.get(k, &unused);
         const int r = q.orient;
         const bool is_rev = (r >> 1) != (r & 1);
         const bool is_larger = (r >> 1) == 0;
@@ -122,18 +151,18 @@ __global__ void win_plan_kernel(const WinReqDev *__restrict__ reqs, uint32_t n, 
 
 // One warp per request: the mate (reverse-complemented for the reverse orientations)
 // and the window bases, then the rescue descriptor.
-__global__ void win_fill_kernel(const WinReqDev *__restrict__ reqs, uint32_t n, const uint8_t *__restrict__ mates,
-                                const RefView R, const WinInfo *__restrict__ info, const uint64_t *__restrict__ offs,
-                                uint8_t *__restrict__ seq, bwacuda_dev_rescue_job *__restrict__ jobs)
+__global__ void win_fill_kernel(const ReqView V, uint32_t n, const RefView R, const WinInfo *__restrict__ info,
+                                const uint64_t *__restrict__ offs, uint8_t *__restrict__ seq,
+                                bwacuda_dev_rescue_job *__restrict__ jobs)
 {
     const uint32_t lane = threadIdx.x & 31u;
     for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < n; k += (gridDim.x * blockDim.x) >> 5) {
-        const WinReqDev q = reqs[k];
+        const uint8_t *ms;
+        const WinReqDev q = V.get(k, &ms);
         const WinInfo w = info[k];
         const int r = q.orient;
         const bool is_rev = (r >> 1) != (r & 1);
         uint8_t *dq = seq + offs[k];
-        const uint8_t *ms = mates + q.mate_off;
         const int lq = w.valid ? q.l_ms : 0;
         for (int x = (int)lane; x < lq; x += 32) {
             uint8_t b;
@@ -158,6 +187,22 @@ __global__ void win_fill_kernel(const WinReqDev *__restrict__ reqs, uint32_t n, 
             J.endsc = 0;
             jobs[k] = J;
         }
+    }
+}
+
+// The caller's result records, written in place (window and alignment per request).
+__global__ void win_store_kernel(const WinInfo *__restrict__ info, const bwacuda_rescue_result *__restrict__ aln,
+                                 uint32_t n, bwacuda_window_result *__restrict__ out)
+{
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const WinInfo w = info[k];
+        bwacuda_window_result o;
+        o.rb = w.rb;
+        o.re = w.re;
+        o.rid = w.rid;
+        o.valid = w.valid;
+        o.aln = aln[k];
+        out[k] = o;
     }
 }
 
@@ -241,30 +286,34 @@ extern "C" int bwacuda_mate_rescue_windows(bwacuda_ctx *c, const bwacuda_window_
     RefState &S = *c->ref;
     cudaStream_t s = c->stream;
     cudaError_t e;
-    // stage the requests and the mates
+    // where the device reads pageable host memory the kernels read the caller's requests and
+    // mates in place; otherwise they are staged through pinned memory
+    const bool direct = c->pageable_access && c->host_gather != BWACUDA_GATHER_HOST;
     const size_t rq_bytes = n * sizeof(WinReqDev);
-    if ((e = S.h_reqs.ensure(rq_bytes + mate_bytes + 16)) != cudaSuccess) return cuda_status(e);
-    WinReqDev *hr = static_cast<WinReqDev *>(S.h_reqs.p);
-    uint8_t *hm = reinterpret_cast<uint8_t *>(hr + n);
-    uint64_t mo = 0;
-    for (size_t k = 0; k < n; ++k) {
-        const bwacuda_window_req &q = reqs[k];
-        WinReqDev d;
-        d.mate_off = mo;
-        d.anchor_rb = q.anchor_rb;
-        d.l_ms = q.l_ms;
-        d.orient = q.orient;
-        d.anchor_rid = q.anchor_rid;
-        d.low = q.low;
-        d.high = q.high;
-        d.pad = 0;
-        hr[k] = d;
-        if (q.l_ms) memcpy(hm + mo, q.mate, (size_t)q.l_ms);
-        mo += (uint64_t)q.l_ms;
+    if (!direct) {
+        if ((e = S.h_reqs.ensure(rq_bytes + mate_bytes + 16)) != cudaSuccess) return cuda_status(e);
+        WinReqDev *hr = static_cast<WinReqDev *>(S.h_reqs.p);
+        uint8_t *hm = reinterpret_cast<uint8_t *>(hr + n);
+        uint64_t mo = 0;
+        for (size_t k = 0; k < n; ++k) {
+            const bwacuda_window_req &q = reqs[k];
+            WinReqDev d;
+            d.mate_off = mo;
+            d.anchor_rb = q.anchor_rb;
+            d.l_ms = q.l_ms;
+            d.orient = q.orient;
+            d.anchor_rid = q.anchor_rid;
+            d.low = q.low;
+            d.high = q.high;
+            d.pad = 0;
+            hr[k] = d;
+            if (q.l_ms) memcpy(hm + mo, q.mate, (size_t)q.l_ms);
+            mo += (uint64_t)q.l_ms;
+        }
     }
     size_t scan_bytes = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, (const uint64_t *)nullptr, (uint64_t *)nullptr, (int)n + 1);
-    if ((e = S.reqs.ensure(rq_bytes + mate_bytes + 16)) != cudaSuccess) return cuda_status(e);
+    if (!direct && (e = S.reqs.ensure(rq_bytes + mate_bytes + 16)) != cudaSuccess) return cuda_status(e);
     if ((e = S.info.ensure(n * sizeof(WinInfo))) != cudaSuccess) return cuda_status(e);
     if ((e = S.sizes.ensure((n + 1) * 8)) != cudaSuccess) return cuda_status(e);
     if ((e = S.offs.ensure((n + 1) * 8)) != cudaSuccess) return cuda_status(e);
@@ -272,11 +321,16 @@ extern "C" int bwacuda_mate_rescue_windows(bwacuda_ctx *c, const bwacuda_window_
     if ((e = S.h_tot.ensure(64)) != cudaSuccess) return cuda_status(e);
     if ((e = S.jobs.ensure(n * sizeof(bwacuda_dev_rescue_job))) != cudaSuccess) return cuda_status(e);
     if ((e = S.res.ensure(n * sizeof(bwacuda_rescue_result))) != cudaSuccess) return cuda_status(e);
-    if ((e = cudaMemcpyAsync(S.reqs.p, hr, rq_bytes + mate_bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
-        return cuda_status(e);
-    c->stats.h2d_bytes += rq_bytes + mate_bytes;
-    const WinReqDev *dreq = static_cast<const WinReqDev *>(S.reqs.p);
-    const uint8_t *dmates = reinterpret_cast<const uint8_t *>(dreq + n);
+    ReqView V{nullptr, nullptr, nullptr};
+    if (direct) {
+        V.direct = reqs;
+    } else {
+        if ((e = cudaMemcpyAsync(S.reqs.p, S.h_reqs.p, rq_bytes + mate_bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return cuda_status(e);
+        c->stats.h2d_bytes += rq_bytes + mate_bytes;
+        V.staged = static_cast<const WinReqDev *>(S.reqs.p);
+        V.mates = reinterpret_cast<const uint8_t *>(V.staged + n);
+    }
     WinInfo *info = static_cast<WinInfo *>(S.info.p);
     uint64_t *sizes = static_cast<uint64_t *>(S.sizes.p), *offs = static_cast<uint64_t *>(S.offs.p);
     RefView R{static_cast<const uint8_t *>(S.pac.p), static_cast<const int64_t *>(S.off.p),
@@ -285,7 +339,7 @@ extern "C" int bwacuda_mate_rescue_windows(bwacuda_ctx *c, const bwacuda_window_
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || nsm < 1) nsm = 1;
     if ((e = cudaMemsetAsync(sizes + n, 0, 8, s)) != cudaSuccess) return cuda_status(e);
     uint32_t grid = (uint32_t)std::min<size_t>((n + 255) / 256, (size_t)nsm * 8);
-    win_plan_kernel<<<grid, 256, 0, s>>>(dreq, (uint32_t)n, R, min_seed_len, info, sizes);
+    win_plan_kernel<<<grid, 256, 0, s>>>(V, (uint32_t)n, R, min_seed_len, info, sizes);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
     if ((e = cub::DeviceScan::ExclusiveSum(S.tmp.p, scan_bytes, sizes, offs, (int)n + 1, s)) != cudaSuccess)
         return cuda_status(e);
@@ -294,7 +348,7 @@ extern "C" int bwacuda_mate_rescue_windows(bwacuda_ctx *c, const bwacuda_window_
     const uint64_t total = *static_cast<const uint64_t *>(S.h_tot.p);
     if ((e = S.seq.ensure(total + 16)) != cudaSuccess) return cuda_status(e);
     grid = (uint32_t)std::min<size_t>((n * 32 + 255) / 256, (size_t)nsm * 16);
-    win_fill_kernel<<<grid, 256, 0, s>>>(dreq, (uint32_t)n, dmates, R, info, offs, static_cast<uint8_t *>(S.seq.p),
+    win_fill_kernel<<<grid, 256, 0, s>>>(V, (uint32_t)n, R, info, offs, static_cast<uint8_t *>(S.seq.p),
                                          static_cast<bwacuda_dev_rescue_job *>(S.jobs.p));
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
     c->stats.kernel_launches += 4;
@@ -307,25 +361,39 @@ extern "C" int bwacuda_mate_rescue_windows(bwacuda_ctx *c, const bwacuda_window_
                                   static_cast<const bwacuda_dev_rescue_job *>(S.jobs.p), n, &sc, minsc, max_sc, 0, 0,
                                   static_cast<bwacuda_rescue_result *>(S.res.p), s);
     if (rc) return rc;
-    // windows and alignments back (through the staging buffer), then into the caller's records
-    if ((e = S.h_reqs.ensure(n * (sizeof(WinInfo) + sizeof(bwacuda_rescue_result)) + 16)) != cudaSuccess)
-        return cuda_status(e);
-    WinInfo *hi = static_cast<WinInfo *>(S.h_reqs.p);
-    bwacuda_rescue_result *ha = reinterpret_cast<bwacuda_rescue_result *>(hi + n);
-    if ((e = cudaMemcpyAsync(hi, info, n * sizeof(WinInfo), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_status(e);
-    if ((e = cudaMemcpyAsync(ha, S.res.p, n * sizeof(bwacuda_rescue_result), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
-        return cuda_status(e);
-    uint64_t dummy = 0;
-    if ((rc = collect_device_status(c, s, &dummy)) != BWACUDA_OK) return rc;  // synchronises
     uint64_t cells = 0;
-    for (size_t k = 0; k < n; ++k) {
-        bwacuda_window_result &o = out[k];
-        o.rb = hi[k].rb;
-        o.re = hi[k].re;
-        o.rid = hi[k].rid;
-        o.valid = hi[k].valid;
-        o.aln = ha[k];
-        if (hi[k].valid) cells += (uint64_t)reqs[k].l_ms * (uint64_t)(hi[k].re - hi[k].rb);
+    if (direct) {
+        // the records go straight into the caller's array; the cell count is summed on the host
+        grid = (uint32_t)std::min<size_t>((n + 255) / 256, (size_t)nsm * 8);
+        win_store_kernel<<<grid, 256, 0, s>>>(info, static_cast<const bwacuda_rescue_result *>(S.res.p), (uint32_t)n,
+                                              out);
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
+        uint64_t dummy = 0;
+        if ((rc = collect_device_status(c, s, &dummy)) != BWACUDA_OK) return rc;  // synchronises
+        for (size_t k = 0; k < n; ++k)
+            if (out[k].valid) cells += (uint64_t)reqs[k].l_ms * (uint64_t)(out[k].re - out[k].rb);
+    } else {
+        // windows and alignments back through the staging buffer, then into the caller's records
+        if ((e = S.h_reqs.ensure(n * (sizeof(WinInfo) + sizeof(bwacuda_rescue_result)) + 16)) != cudaSuccess)
+            return cuda_status(e);
+        WinInfo *hi = static_cast<WinInfo *>(S.h_reqs.p);
+        bwacuda_rescue_result *ha = reinterpret_cast<bwacuda_rescue_result *>(hi + n);
+        if ((e = cudaMemcpyAsync(hi, info, n * sizeof(WinInfo), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+            return cuda_status(e);
+        if ((e = cudaMemcpyAsync(ha, S.res.p, n * sizeof(bwacuda_rescue_result), cudaMemcpyDeviceToHost, s)) !=
+            cudaSuccess)
+            return cuda_status(e);
+        uint64_t dummy = 0;
+        if ((rc = collect_device_status(c, s, &dummy)) != BWACUDA_OK) return rc;  // synchronises
+        for (size_t k = 0; k < n; ++k) {
+            bwacuda_window_result &o = out[k];
+            o.rb = hi[k].rb;
+            o.re = hi[k].re;
+            o.rid = hi[k].rid;
+            o.valid = hi[k].valid;
+            o.aln = ha[k];
+            if (hi[k].valid) cells += (uint64_t)reqs[k].l_ms * (uint64_t)(hi[k].re - hi[k].rb);
+        }
     }
     c->stats.d2h_bytes += n * (sizeof(WinInfo) + sizeof(bwacuda_rescue_result));
     c->stats.rescue_cells += cells;

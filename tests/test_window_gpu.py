@@ -43,11 +43,17 @@ def _check(got, win, aln):
         assert np.array_equal(valid[f], aln[f]), f
 
 
-def test_windows_and_alignments(ctx):
+@pytest.mark.parametrize("route", [pytest.param(B.GATHER_AUTO, id="in-place"),
+                                   pytest.param(B.GATHER_HOST, id="staged")])
+def test_windows_and_alignments(ctx, route):
     rw = B.RescueWindows(20000, seed=3, contig_lens=(300_000, 100_000, 50_000, 200_000))
     ctx.ref_set(rw)
     reqs = rw.requests()
-    got = ctx.mate_rescue_windows(reqs, minsc=20)
+    ctx.set_option(B.OPT_HOST_GATHER, route)
+    try:
+        got = ctx.mate_rescue_windows(reqs, minsc=20)
+    finally:
+        ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_AUTO)
     win, aln = _expected(rw, reqs)
     _check(got, win, aln)
     assert got["valid"].mean() > 0.9 and (got["score"][got["valid"] == 1] >= 20).mean() > 0.5
