@@ -288,8 +288,9 @@ int extend_batch_ats(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int 
     const size_t CH = std::min(c->chunk_jobs, ATS_MAX_CHUNK);
     uint32_t input_flags = 0;
     int si = 0;
-    for (size_t c0 = 0; c0 < n && rc == BWACUDA_OK; c0 += CH) {
-        const size_t cn = std::min(CH, n - c0);
+    for (size_t c0 = 0, cn = 0; c0 < n && rc == BWACUDA_OK; c0 += cn) {
+        // a short first chunk: the DP starts after a short gather, later gathers hide behind it
+        cn = std::min(c0 == 0 ? std::max(CH / 8, std::min(CH, (size_t)65536)) : CH, n - c0);
         if ((rc = ats_drain(c, si, &input_flags)) != BWACUDA_OK) break;
         cudaError_t e = ats_enqueue_chunk(c, si, jobs + c0, cn, br, P, w, out + c0);
         if (e != cudaSuccess) rc = cuda_status(e);

@@ -321,11 +321,10 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
                 ++j;
             }
             uint32_t wn = cellw[(j >> 1) * TB];  // j <= end <= qlen: allocated
-            for (; j + 1 < end; j += 2) {
-                // columns j, j+1 of one word as 16x2 lanes; only F runs column by column
+            // columns j, j+1 of one word as 16x2 lanes; only F runs column by column
+            auto pair = [&](int jj, uint32_t sel) {
                 const uint32_t wv = wn;
-                wn = cellw[((j >> 1) + 1) * TB];  // spare word keeps this in bounds
-                const uint32_t sel = qw[(j >> 2) * TB] >> ((j & 2) * 8);
+                wn = cellw[((jj >> 1) + 1) * TB];  // spare word keeps this in bounds
                 const uint32_t s2 = prmt(plo, phi, sel);   // (s_j, s_j+1)
                 const uint32_t hd2 = prmt(wv, 0u, 0x4240u);  // (H(i-1,j-1), H(i-1,j))
                 const uint32_t e2 = prmt(wv, 0u, 0x4341u);   // (E(i,j), E(i,j+1))
@@ -343,11 +342,30 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
                 const uint32_t h2 = __vimax3_s16x2(M2, e2, f2);  // (H(i,j), H(i,j+1))
                 // stored bytes: H(i,j-1), E(i+1,j), H(i,j), E(i+1,j+1)
                 const uint32_t lo = prmt((uint32_t)h1, h2, 0x4040u);
-                cellw[(j >> 1) * TB] = prmt(lo, en2, 0x6140u);
+                cellw[(jj >> 1) * TB] = prmt(lo, en2, 0x6140u);
                 h1 = (int)(h2 >> 16);
-                const int32_t ka = (int32_t)(h2 << 16) | j;              // ties -> later column
-                const int32_t kb = (int32_t)(h2 & 0xffff0000u) | (j + 1);
+                const int32_t ka = (int32_t)(h2 << 16) | jj;              // ties -> later column
+                const int32_t kb = (int32_t)(h2 & 0xffff0000u) | (jj + 1);
                 rowkey = __vimax3_s32(rowkey, ka, kb);
+            };
+            // one pair to reach a query-word boundary, then whole words (four columns) with
+            // the next word loaded one step ahead, then a last pair
+            if ((j & 2) && j + 1 < end) {
+                pair(j, qw[(j >> 2) * TB] >> 16);
+                j += 2;
+            }
+            if (j + 3 < end) {
+                uint32_t qn = qw[(j >> 2) * TB];
+                for (; j + 3 < end; j += 4) {
+                    const uint32_t qv = qn;
+                    qn = qw[((j >> 2) + 1) * TB];  // j + 4 <= qlen < qcap: inside the query words
+                    pair(j, qv);
+                    pair(j + 2, qv >> 16);
+                }
+            }
+            if (j + 1 < end) {
+                pair(j, qw[(j >> 2) * TB] >> ((j & 2) * 8));
+                j += 2;
             }
             if (j < end) {  // even last column: the low half of its word
                 const uint32_t wv = wn;
