@@ -239,6 +239,28 @@ __device__ __forceinline__ void ext_cell(int hd, int e, uint32_t qc, uint32_t pl
     f = f > oi ? f : oi;
 }
 
+// F through one column pair in 16x2 lanes.  In: fv's high half = F(i, j), ti2 =
+// (max(M_j - oe_ins, 0), max(M_j+1 - oe_ins, 0)); fsel2 = (-32768, -e_ins) and
+// ne_ins2 = (-e_ins, -e_ins).  Returns (F(i, j), F(i, j+1)) and leaves F(i, j+2) in
+// fv's high half.  The low lane of the first step is max(fv.lo - 32768, F(i, j)) =
+// F(i, j) because fv's low half always lies in [0, 32768).
+__device__ __forceinline__ uint32_t f_pair(uint32_t &fv, uint32_t ti2, uint32_t fsel2, uint32_t ne_ins2)
+{
+    const uint32_t d2 = prmt(fv, ti2, 0x5432u);           // (F(i,j), ti_j)
+    const uint32_t f2 = __viaddmax_s16x2(fv, fsel2, d2);  // (F(i,j), max(F(i,j) - e_ins, ti_j))
+    fv = __viaddmax_s16x2(f2, ne_ins2, ti2);              // high: max(F(i,j+1) - e_ins, ti_j+1)
+    return f2;
+}
+
+// Row-maximum key over a column pair (H(i,jj), H(i,jj+1)) in h2: max of
+// (H << 16) | column, so ties go to the later column.  H < 32768 keeps keys positive.
+__device__ __forceinline__ int32_t pair_rowkey(int32_t rowkey, uint32_t h2, int jj)
+{
+    const int32_t ka = (int32_t)prmt((uint32_t)jj, h2, 0x5410u);  // (H_jj << 16) | jj
+    const int32_t kb = (int32_t)((h2 & 0xffff0000u) | (uint32_t)(jj + 1));
+    return __vimax3_s32(rowkey, ka, kb);
+}
+
 template <int TB>
 __device__ __forceinline__ bool u8p_dead(const uint32_t *cellw, int x)
 {
@@ -290,6 +312,8 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
     const uint32_t noe_ins2 = (uint32_t)(-oe_ins & 0xffff) * 0x10001u;
     const uint32_t noe_del2 = (uint32_t)(-oe_del & 0xffff) * 0x10001u;
     const uint32_t ne_del2 = (uint32_t)(-e_del & 0xffff) * 0x10001u;
+    const uint32_t ne_ins2 = (uint32_t)(-e_ins & 0xffff) * 0x10001u;
+    const uint32_t fsel2 = 0x8000u | ((uint32_t)(-e_ins & 0xffff) << 16);
     for (int i = 0; i < tlen; ++i) {
         uint32_t tc = tnext;
         if (i + 1 < tlen) tnext = t[i + 1];
@@ -321,7 +345,9 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
                 ++j;
             }
             uint32_t wn = cellw[(j >> 1) * TB];  // j <= end <= qlen: allocated
-            // columns j, j+1 of one word as 16x2 lanes; only F runs column by column
+            // columns j, j+1 of one word as 16x2 lanes.  F runs through the lanes too:
+            // fv holds F(i, j) in its high half, h1v holds H(i, j-1) in its high half.
+            uint32_t fv = (uint32_t)f << 16, h1v = (uint32_t)h1 << 16;
             auto pair = [&](int jj, uint32_t sel) {
                 const uint32_t wv = wn;
                 wn = cellw[((jj >> 1) + 1) * TB];  // spare word keeps this in bounds
@@ -335,18 +361,12 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
                 const uint32_t ti2 = __viaddmax_s16x2_relu(M2, noe_ins2, 0u);  // max(M - oe_ins, 0)
                 const uint32_t td2 = __viaddmax_s16x2_relu(M2, noe_del2, 0u);  // max(M - oe_del, 0)
                 const uint32_t en2 = __viaddmax_s16x2(e2, ne_del2, td2);       // E(i+1, .)
-                const int f0 = f;
-                const int f1 = __viaddmax_s32(f0, -e_ins, (int)(ti2 & 0xffffu));
-                f = __viaddmax_s32(f1, -e_ins, (int)(ti2 >> 16));
-                const uint32_t f2 = prmt((uint32_t)f0, (uint32_t)f1, 0x5410u);
+                const uint32_t f2 = f_pair(fv, ti2, fsel2, ne_ins2);            // (F(i,j), F(i,j+1))
                 const uint32_t h2 = __vimax3_s16x2(M2, e2, f2);  // (H(i,j), H(i,j+1))
                 // stored bytes: H(i,j-1), E(i+1,j), H(i,j), E(i+1,j+1)
-                const uint32_t lo = prmt((uint32_t)h1, h2, 0x4040u);
-                cellw[(jj >> 1) * TB] = prmt(lo, en2, 0x6140u);
-                h1 = (int)(h2 >> 16);
-                const int32_t ka = (int32_t)(h2 << 16) | jj;              // ties -> later column
-                const int32_t kb = (int32_t)(h2 & 0xffff0000u) | (jj + 1);
-                rowkey = __vimax3_s32(rowkey, ka, kb);
+                cellw[(jj >> 1) * TB] = prmt(prmt(h1v, h2, 0x0042u), en2, 0x6140u);
+                h1v = h2;
+                rowkey = pair_rowkey(rowkey, h2, jj);
             };
             // one pair to reach a query-word boundary, then whole words (four columns) with
             // the next word loaded one step ahead, then a last pair
@@ -367,6 +387,8 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
                 pair(j, qw[(j >> 2) * TB] >> ((j & 2) * 8));
                 j += 2;
             }
+            f = (int)(fv >> 16);
+            h1 = (int)(h1v >> 16);
             if (j < end) {  // even last column: the low half of its word
                 const uint32_t wv = wn;
                 const uint32_t qc = (qw[(j >> 2) * TB] >> ((j & 3) * 8)) & 7u;
@@ -411,6 +433,201 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
         beg = lo;
         int hi = end;
         while (hi >= beg && u8p_dead<TB>(cellw, hi)) --hi;
+        end = hi + 2 < qlen ? hi + 2 : qlen;
+    }
+    bwacuda_ext_result r;
+    r.score = best;
+    r.qle = best_j + 1;
+    r.tle = best_i + 1;
+    r.gtle = best_ie + 1;
+    r.gscore = gscore;
+    r.max_off = max_off;
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// 16-bit pair cells: pair word k of a thread (8 bytes) holds columns 2k and
+// 2k+1 as .x = (H_2k, H_2k+1) and .y = (E_2k, E_2k+1), 16 bits each.  Exact
+// whenever every DP value < 32768 (the reference's 16-bit bin).  The same
+// footprint per column as FmtI16, but every lane operation serves two columns
+// and H and E arrive already split into lanes.
+// ---------------------------------------------------------------------------
+
+// Shared-memory bytes of a block for 16-bit pair cells (one spare pair word for
+// the look-ahead, one for the sentinel) plus the query words.
+__host__ __device__ inline size_t ext_block_smem_i16p(int qcap, int tb)
+{
+    size_t cpairs = (size_t)qcap / 2 + 2;
+    size_t qwords = (size_t)qcap / 4 + 1;
+    return (cpairs * 8 + qwords * 4) * tb;
+}
+
+template <int TB>
+__device__ __forceinline__ bool i16p_dead(const uint2 *cell2, int x)
+{
+    const uint2 c = cell2[(x >> 1) * TB];
+    return (((c.x | c.y) >> ((x & 1) * 16)) & 0xffffu) == 0u;
+}
+
+template <int TB>
+__device__ __forceinline__ bwacuda_ext_result ext_run_job_i16p(uint2 *__restrict__ cell2, uint32_t *__restrict__ qw,
+                                                               const uint8_t *__restrict__ seq,
+                                                               const bwacuda_dev_ext_job &J, const ExtParams &P,
+                                                               bool &bad, unsigned long long &ncells)
+{
+    const int qlen = J.qlen, tlen = J.tlen, h0 = J.h0, m = P.sc.m;
+    const uint8_t *q = seq + J.q_off;
+    const uint8_t *t = seq + J.t_off;
+    const int o_del = P.sc.o_del, e_del = P.sc.e_del, o_ins = P.sc.o_ins, e_ins = P.sc.e_ins;
+    const int oe_del = o_del + e_del, oe_ins = o_ins + e_ins;
+
+    // Query codes as prmt selector bytes, as in the 8-bit pair form.
+    for (int jw = 0; jw * 4 <= qlen; ++jw) {
+        uint32_t v = 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int j = jw * 4 + u;
+            uint32_t c = j < qlen ? (uint32_t)q[j] : 0u;
+            bad |= c >= (uint32_t)m;
+            v |= (0x80u | (c & 7u) * 0x11u) << (8 * u);
+        }
+        qw[jw * TB] = v;
+    }
+    // Row -1 (sw.rs:269-279), E = 0.
+    {
+        int hv = h0;
+        for (int k = 0; 2 * k <= qlen; ++k) {
+            const int a = hv;  // column 2k
+            if (2 * k == 0) hv = h0 > oe_ins ? h0 - oe_ins : 0;
+            else hv = hv > e_ins ? hv - e_ins : 0;
+            const int b = 2 * k + 1 <= qlen ? hv : 0;  // column 2k+1
+            if (2 * k + 1 <= qlen) hv = hv > e_ins ? hv - e_ins : 0;
+            cell2[k * TB] = make_uint2((uint32_t)a | ((uint32_t)b << 16), 0u);
+        }
+    }
+    const int w = clamp_band(J.w < 0 ? 0 : J.w, qlen, P.sc.max_sc, P.end_bonus, o_ins, e_ins, o_del, e_del);
+    int best = h0, best_i = -1, best_j = -1, best_ie = -1, gscore = -1, max_off = 0;
+    int beg = 0, end = qlen;
+    uint32_t tnext = tlen > 0 ? t[0] : 0u;
+    const uint32_t noe_ins2 = (uint32_t)(-oe_ins & 0xffff) * 0x10001u;
+    const uint32_t noe_del2 = (uint32_t)(-oe_del & 0xffff) * 0x10001u;
+    const uint32_t ne_del2 = (uint32_t)(-e_del & 0xffff) * 0x10001u;
+    const uint32_t ne_ins2 = (uint32_t)(-e_ins & 0xffff) * 0x10001u;
+    const uint32_t fsel2 = 0x8000u | ((uint32_t)(-e_ins & 0xffff) << 16);
+    for (int i = 0; i < tlen; ++i) {
+        uint32_t tc = tnext;
+        if (i + 1 < tlen) tnext = t[i + 1];
+        bad |= tc >= (uint32_t)m;
+        tc &= 7u;
+        const uint32_t plo = P.sc.prof[tc][0], phi = P.sc.prof[tc][1];
+        if (beg < i - w) beg = i - w;
+        if (end > i + w + 1) end = i + w + 1;
+        if (end > qlen) end = qlen;
+        int h1 = 0;
+        if (beg == 0) {
+            h1 = h0 - (o_del + e_del * (i + 1));
+            h1 = h1 > 0 ? h1 : 0;
+        }
+        int f = 0;
+        int32_t rowkey = 0;
+        if (beg < end) {
+            int j = beg;
+            if (j & 1) {  // odd first column: the high lanes of its pair
+                const uint2 wv = cell2[(j >> 1) * TB];
+                const uint32_t qc = (qw[(j >> 2) * TB] >> ((j & 3) * 8)) & 7u;
+                int h, en;
+                ext_cell((int)(wv.x >> 16), (int)(wv.y >> 16), qc, plo, phi, oe_del, e_del, oe_ins, e_ins, f, h, en);
+                cell2[(j >> 1) * TB] =
+                    make_uint2((wv.x & 0xffffu) | ((uint32_t)h1 << 16), (wv.y & 0xffffu) | ((uint32_t)en << 16));
+                h1 = h;
+                const int32_t kk = (h << 16) | j;
+                rowkey = rowkey > kk ? rowkey : kk;
+                ++j;
+            }
+            uint2 wn = cell2[(j >> 1) * TB];  // j <= end <= qlen: allocated
+            uint32_t fv = (uint32_t)f << 16, h1v = (uint32_t)h1 << 16;
+            auto pair = [&](int jj, uint32_t sel) {
+                const uint2 wv = wn;
+                wn = cell2[((jj >> 1) + 1) * TB];  // spare pair keeps this in bounds
+                const uint32_t s2 = prmt(plo, phi, sel);  // (s_j, s_j+1)
+                const uint32_t hd2 = wv.x, e2 = wv.y;
+                // M = hd ? hd + s : 0, as min(hd + s, 32767 * min(hd, 1)): every path score
+                // is < 32768 here, and a non-positive M acts as 0 below (E, F >= 0)
+                const uint32_t g2 = __viaddmin_u16x2(hd2, 0u, 0x00010001u) * 0x7fffu;
+                const uint32_t M2 = __viaddmin_s16x2(hd2, s2, g2);
+                const uint32_t ti2 = __viaddmax_s16x2_relu(M2, noe_ins2, 0u);
+                const uint32_t td2 = __viaddmax_s16x2_relu(M2, noe_del2, 0u);
+                const uint32_t en2 = __viaddmax_s16x2(e2, ne_del2, td2);
+                const uint32_t f2 = f_pair(fv, ti2, fsel2, ne_ins2);
+                const uint32_t h2 = __vimax3_s16x2(M2, e2, f2);
+                // stored: H(i,j-1), H(i,j) and E(i+1,j), E(i+1,j+1)
+                cell2[(jj >> 1) * TB] = make_uint2(prmt(h1v, h2, 0x5432u), en2);
+                h1v = h2;
+                rowkey = pair_rowkey(rowkey, h2, jj);
+            };
+            if ((j & 2) && j + 1 < end) {
+                pair(j, qw[(j >> 2) * TB] >> 16);
+                j += 2;
+            }
+            if (j + 3 < end) {
+                uint32_t qn = qw[(j >> 2) * TB];
+                for (; j + 3 < end; j += 4) {
+                    const uint32_t qv = qn;
+                    qn = qw[((j >> 2) + 1) * TB];  // j + 4 <= qlen < qcap: inside the query words
+                    pair(j, qv);
+                    pair(j + 2, qv >> 16);
+                }
+            }
+            if (j + 1 < end) {
+                pair(j, qw[(j >> 2) * TB] >> ((j & 2) * 8));
+                j += 2;
+            }
+            f = (int)(fv >> 16);
+            h1 = (int)(h1v >> 16);
+            if (j < end) {  // even last column: the low lanes of its pair
+                const uint2 wv = wn;
+                const uint32_t qc = (qw[(j >> 2) * TB] >> ((j & 3) * 8)) & 7u;
+                int h, en;
+                ext_cell((int)(wv.x & 0xffffu), (int)(wv.y & 0xffffu), qc, plo, phi, oe_del, e_del, oe_ins, e_ins, f,
+                         h, en);
+                cell2[(j >> 1) * TB] = make_uint2((wv.x & 0xffff0000u) | (uint32_t)h1, (wv.y & 0xffff0000u) | (uint32_t)en);
+                h1 = h;
+                const int32_t kk = (h << 16) | j;
+                rowkey = rowkey > kk ? rowkey : kk;
+            }
+            ncells += (unsigned long long)(end - beg);
+        }
+        {   // sentinel column end (sw.rs:418-419): H = h1, E = 0
+            const uint2 wv = cell2[(end >> 1) * TB];
+            cell2[(end >> 1) * TB] = (end & 1) ? make_uint2((wv.x & 0xffffu) | ((uint32_t)h1 << 16), wv.y & 0xffffu)
+                                               : make_uint2((wv.x & 0xffff0000u) | (uint32_t)h1, wv.y & 0xffff0000u);
+        }
+        const int jf = end > beg ? end : beg;
+        if (jf == qlen && gscore <= h1) {
+            best_ie = i;
+            gscore = h1;
+        }
+        const int rmax = rowkey >> 16;
+        const int mj = rowkey & 0xffff;
+        if (rmax == 0) break;
+        if (rmax > best) {
+            best = rmax;
+            best_i = i;
+            best_j = mj;
+            const int off = mj > i ? mj - i : i - mj;
+            if (off > max_off) max_off = off;
+        } else if (P.zdrop > 0) {
+            if (i - best_i > mj - best_j) {
+                if (best - rmax - ((i - best_i) - (mj - best_j)) * e_del > P.zdrop) break;
+            } else if (best - rmax - ((mj - best_j) - (i - best_i)) * e_ins > P.zdrop) {
+                break;
+            }
+        }
+        int lo = beg;
+        while (lo < end && i16p_dead<TB>(cell2, lo)) ++lo;
+        beg = lo;
+        int hi = end;
+        while (hi >= beg && i16p_dead<TB>(cell2, hi)) --hi;
         end = hi + 2 < qlen ? hi + 2 : qlen;
     }
     bwacuda_ext_result r;

@@ -59,18 +59,21 @@ ext_persist_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *_
     if (lane == 0 && ncells) atomicAdd(cells_total, ncells);
 }
 
-// The same persistent loop over 8-bit pair cells.
-template <int TB, int GRAB>
+// The same persistent loop over pair cells: 8-bit (W16 false, jobs of the 8-bit
+// class) or 16-bit (W16 true, jobs of the 16-bit class).
+template <int TB, int GRAB, bool W16>
 __global__ void __launch_bounds__(TB)
-ext_persist_u8p_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *__restrict__ jobs,
-                       const uint32_t *__restrict__ order, uint32_t *__restrict__ table,
-                       const __grid_constant__ ExtParams P, int qcap, bwacuda_ext_result *__restrict__ out,
-                       uint32_t *__restrict__ err, unsigned long long *__restrict__ cells_total)
+ext_persist_pair_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *__restrict__ jobs,
+                        const uint32_t *__restrict__ order, uint32_t *__restrict__ table,
+                        const __grid_constant__ ExtParams P, int qcap, bwacuda_ext_result *__restrict__ out,
+                        uint32_t *__restrict__ err, unsigned long long *__restrict__ cells_total)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int tid = threadIdx.x, lane = tid & 31;
+    const size_t cpairs = (size_t)qcap / 2 + 2;
     uint32_t *cellw = reinterpret_cast<uint32_t *>(smem_raw) + tid;
-    uint32_t *qw = reinterpret_cast<uint32_t *>(smem_raw) + ((size_t)qcap / 2 + 2) * TB + tid;
+    uint2 *cell2 = reinterpret_cast<uint2 *>(smem_raw) + tid;
+    uint32_t *qw = reinterpret_cast<uint32_t *>(smem_raw) + cpairs * (W16 ? 2 : 1) * TB + tid;
     const uint32_t start = table[0], stop = table[1];
     uint32_t *counter = table + 2;
     unsigned long long ncells = 0;
@@ -85,11 +88,14 @@ ext_persist_u8p_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_jo
         if (k < stop) {
             const uint32_t jid = order[k];
             const bwacuda_dev_ext_job J = jobs[jid];
-            if (J.qlen < 0 || J.qlen + 1 > qcap || !ext_fits_u8(J.qlen, J.tlen, J.h0, P.sc.max_sc)) {
+            const bool fits = W16 ? ext_fits_i16(J.qlen, J.tlen, J.h0, P.sc.max_sc)
+                                  : ext_fits_u8(J.qlen, J.tlen, J.h0, P.sc.max_sc);
+            if (J.qlen < 0 || J.qlen + 1 > qcap || !fits) {
                 atomicOr(err, ERR_RANGE);
             } else {
                 bool bad = false;
-                const bwacuda_ext_result r = ext_run_job_u8p<TB>(cellw, qw, seq, J, P, bad, ncells);
+                const bwacuda_ext_result r = W16 ? ext_run_job_i16p<TB>(cell2, qw, seq, J, P, bad, ncells)
+                                                 : ext_run_job_u8p<TB>(cellw, qw, seq, J, P, bad, ncells);
                 if (bad) atomicOr(err, ERR_BASE);
                 out[jid] = r;
             }
@@ -120,12 +126,17 @@ cudaError_t launch_persist_tb(const PersistLaunch &L, const ExtBucketDef &d, uin
     return cudaGetLastError();
 }
 
-template <int TB, int GRAB>
-cudaError_t launch_persist_u8p_tb(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm)
+__host__ __device__ inline size_t pair_block_smem(int qcap, int tb, bool w16)
 {
-    const size_t smem = ext_block_smem_u8p(d.qcap, TB);
+    return w16 ? ext_block_smem_i16p(qcap, tb) : ext_block_smem_u8p(qcap, tb);
+}
+
+template <int TB, int GRAB, bool W16>
+cudaError_t launch_persist_pair_tb(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm)
+{
+    const size_t smem = pair_block_smem(d.qcap, TB, W16);
     if (smem > SMEM_MAX) return cudaErrorInvalidValue;
-    auto kern = ext_persist_u8p_kernel<TB, GRAB>;
+    auto kern = ext_persist_pair_kernel<TB, GRAB, W16>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -136,13 +147,16 @@ cudaError_t launch_persist_u8p_tb(const PersistLaunch &L, const ExtBucketDef &d,
     return cudaGetLastError();
 }
 
-template <int GRAB>
-cudaError_t launch_persist_u8p(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm, int tb)
+template <int GRAB, bool W16>
+cudaError_t launch_persist_pair(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm, int tb)
 {
-    if (tb >= 256 && ext_block_smem_u8p(d.qcap, 256) <= SMEM_MAX) return launch_persist_u8p_tb<256, GRAB>(L, d, table, nsm);
-    if (tb >= 128 && ext_block_smem_u8p(d.qcap, 128) <= SMEM_MAX) return launch_persist_u8p_tb<128, GRAB>(L, d, table, nsm);
-    if (tb >= 64 && ext_block_smem_u8p(d.qcap, 64) <= SMEM_MAX) return launch_persist_u8p_tb<64, GRAB>(L, d, table, nsm);
-    return launch_persist_u8p_tb<32, GRAB>(L, d, table, nsm);
+    if (tb >= 256 && pair_block_smem(d.qcap, 256, W16) <= SMEM_MAX)
+        return launch_persist_pair_tb<256, GRAB, W16>(L, d, table, nsm);
+    if (tb >= 128 && pair_block_smem(d.qcap, 128, W16) <= SMEM_MAX)
+        return launch_persist_pair_tb<128, GRAB, W16>(L, d, table, nsm);
+    if (tb >= 64 && pair_block_smem(d.qcap, 64, W16) <= SMEM_MAX)
+        return launch_persist_pair_tb<64, GRAB, W16>(L, d, table, nsm);
+    return launch_persist_pair_tb<32, GRAB, W16>(L, d, table, nsm);
 }
 
 template <class F, int GRAB>
@@ -160,9 +174,11 @@ cudaError_t launch_persist(const PersistLaunch &L, const ExtBucketDef &d, uint32
 template <int GRAB>
 cudaError_t ext_persist_launch_grab(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm, int tb)
 {
-    if (d.cls == 0) return launch_persist_u8p<GRAB>(L, d, table, nsm, tb);
-    return d.cls == 2 ? launch_persist<FmtI32, GRAB>(L, d, table, nsm, tb)
-                      : launch_persist<FmtI16, GRAB>(L, d, table, nsm, tb);
+    if (d.cls == 0) return launch_persist_pair<GRAB, false>(L, d, table, nsm, tb);
+    if (d.cls == 2) return launch_persist<FmtI32, GRAB>(L, d, table, nsm, tb);
+    // 16-bit pair cells where one warp's rows fit, else one column per cell
+    if (pair_block_smem(d.qcap, 32, true) <= SMEM_MAX) return launch_persist_pair<GRAB, true>(L, d, table, nsm, tb);
+    return launch_persist<FmtI16, GRAB>(L, d, table, nsm, tb);
 }
 
 

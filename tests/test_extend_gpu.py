@@ -69,7 +69,9 @@ def test_known_answers(ctx):
     assert r[0] == 11 and r[2] == 10
 
 
-def test_gate_stream_scoring_swept(ctx):
+@pytest.mark.parametrize("path", [pytest.param(B.PATH_PLAIN, id="plain"),
+                                  pytest.param((B.PATH_BATCHED, B.GATHER_HOST), id="batched")])
+def test_gate_stream_scoring_swept(ctx, path):
     # crates/bwa-extend/src/lib.rs:283-354: 2000 cases, scoring swept; batched per scoring.
     groups = {}
     for c in R.backend_matches_scalar():
@@ -78,16 +80,18 @@ def test_gate_stream_scoring_swept(ctx):
     for key, cs in groups.items():
         a, b, od, ed, oi, ei, w, eb, zd = key
         _check_batch(ctx, [c["q"] for c in cs], [c["t"] for c in cs], [c["h0"] for c in cs], a, b, od, ed, oi,
-                     ei, w, eb, zd, what=f"gate {key}")
+                     ei, w, eb, zd, path=path, what=f"gate {key}")
 
 
+@pytest.mark.parametrize("path", [pytest.param(B.PATH_PLAIN, id="plain"),
+                                  pytest.param((B.PATH_BATCHED, B.GATHER_HOST), id="batched")])
 @pytest.mark.parametrize("stream", ["batch", "read_sized", "ungapped", "simd_verify"])
-def test_reference_batch_streams(ctx, stream):
+def test_reference_batch_streams(ctx, stream, path):
     gen = {"batch": R.backend_batch_matches_scalar, "read_sized": R.read_sized, "ungapped": R.ungapped,
            "simd_verify": R.simd_verify}[stream]
     for k, c in enumerate(gen()):
         _check_batch(ctx, c["qs"], c["ts"], c["h0s"], c["a"], c["b"], c["o_del"], c["e_del"], c["o_ins"],
-                     c["e_ins"], c["w"], c["end_bonus"], c["zdrop"], what=f"{stream} round {k}")
+                     c["e_ins"], c["w"], c["end_bonus"], c["zdrop"], path=path, what=f"{stream} round {k}")
 
 
 def _check_jobset(ctx, js, w=100, path=B.PATH_PLAIN, **kw):
@@ -246,6 +250,49 @@ def test_edge_cases(ctx, path):
     assert ctx.extend([], [1, 2, 3], 10) == (10, 0, 0, 1, 3, 0)
     empty = B.JobSet.from_lists([], [])
     assert len(ctx.extend_batch(empty)) == 0
+
+
+def _mutated_pairs(rng, n, qmax, h0_choices):
+    """Query/target pairs that share most bases (long, high-scoring alignments with
+    indels), lengths 0..qmax, h0 drawn from h0_choices ranges."""
+    qs, ts, h0s = [], [], []
+    for _ in range(n):
+        ql = int(rng.integers(0, qmax + 1)) if rng.random() < 0.5 else int(rng.integers(0, 150))
+        q = rng.integers(0, 4, ql)
+        t = q.copy()
+        for _ in range(int(rng.integers(0, 6))):  # point edits, N bases, short indels
+            if len(t) == 0:
+                break
+            p = int(rng.integers(0, len(t)))
+            op = int(rng.integers(0, 4))
+            if op == 0:
+                t[p] = (t[p] + 1) % 4
+            elif op == 1:
+                t[p] = 4
+            elif op == 2:
+                t = np.delete(t, slice(p, p + int(rng.integers(1, 4))))
+            else:
+                t = np.insert(t, p, rng.integers(0, 4, int(rng.integers(1, 4))))
+        tail = rng.integers(0, 4, int(rng.integers(0, 40)))
+        t = np.concatenate([t, tail]) if rng.random() < 0.7 else t
+        lo, hi = h0_choices[int(rng.integers(0, len(h0_choices)))]
+        qs.append(q.tolist())
+        ts.append(t.tolist())
+        h0s.append(int(rng.integers(lo, hi)))
+    return qs, ts, h0s
+
+
+@pytest.mark.parametrize("scoring", [(1, 4, 6, 1, 6, 1, 5, 100), (2, 3, 5, 2, 4, 3, 0, 40), (1, 1, 0, 1, 0, 1, 9, 0),
+                                     (3, 5, 11, 1, 7, 2, 1, 200), (1, 4, 6, 1, 6, 1, 5, 1)])
+def test_pair_cell_classes_swept(ctx, scoring):
+    # jobs of the 8-bit and 16-bit classes (two columns per lane operation) with odd and
+    # even band edges, swept scoring and bands, through the batched route
+    a, b, od, ed, oi, ei, eb, zd = scoring
+    rng = np.random.default_rng(sum(scoring))
+    qs, ts, h0s = _mutated_pairs(rng, 1500, 700, [(1, 60), (100, 250), (300, 3000), (8000, 20000)])
+    for w in (1, 4, 33, 100):
+        _check_batch(ctx, qs, ts, h0s, a, b, od, ed, oi, ei, w, eb, zd, path=(B.PATH_BATCHED, B.GATHER_HOST),
+                     what=f"classes {scoring} w={w}")
 
 
 @pytest.mark.parametrize("path", PATHS)
