@@ -7,6 +7,7 @@
 #include <cstring>
 #include <vector>
 
+#include "ext_job.cuh"
 #include "kernels.h"
 #include "persist.h"
 #include "runtime.h"
@@ -151,7 +152,8 @@ static cudaError_t enqueue_batched(bwacuda_ctx *c, BatchBufs &bb, const uint8_t 
                                    unsigned long long *cells = nullptr)
 {
     BatchedState *B = c->batched;
-    cudaError_t e = ext_sort_and_bucket(d_jobs, n, P.sc.max_sc, d_seq, P.ug, P.zdrop, d_out,
+    const bool lanes = ext_pair_lanes_ok(P.sc.o_del, P.sc.e_del, P.sc.o_ins, P.sc.e_ins);
+    cudaError_t e = ext_sort_and_bucket(d_jobs, n, P.sc.max_sc, lanes, d_seq, P.ug, P.zdrop, d_out,
                                         static_cast<uint16_t *>(bb.keys_in.p),
                                         static_cast<uint16_t *>(bb.keys_out.p), static_cast<uint32_t *>(bb.idx_in.p),
                                         static_cast<uint32_t *>(bb.idx_out.p), bb.tmp.p, bb.tmp.cap,

@@ -58,6 +58,14 @@ __host__ __device__ inline bool ext_fits_i16(int qlen, int tlen, int h0, int max
     return ext_value_bound(qlen, tlen, h0, max_sc) < 32768 && qlen < 65535;
 }
 
+// The pair kernels (8- and 16-bit pair cells) subtract gap costs in signed 16-bit
+// lanes; costs up to 16384 keep every lane difference inside the lane.  Larger
+// costs send every narrow job to the one-column-per-cell 16-bit kernel.
+__host__ __device__ inline bool ext_pair_lanes_ok(int o_del, int e_del, int o_ins, int e_ins)
+{
+    return (long long)o_del + e_del <= 16384 && (long long)o_ins + e_ins <= 16384;
+}
+
 // Runs job J; returns the ExtendResult, adds the inner-loop iterations to ncells.
 template <class F, int TB>
 __device__ __forceinline__ bwacuda_ext_result ext_run_job(typename F::T *__restrict__ cell,
@@ -267,7 +275,60 @@ __device__ __forceinline__ bool u8p_dead(const uint32_t *cellw, int x)
     return ((cellw[(x >> 1) * TB] >> ((x & 1) * 16)) & 0xffffu) == 0u;
 }
 
-template <int TB>
+// Row-maximum keys of the 8-bit pair kernel.  K16 (rows of at most 512 columns):
+// two 16-bit lanes, lane 0 over even columns 2k and lane 1 over odd columns 2k+1,
+// each the max of (H << 8) | k (H < 256, k < 256), so a lane keeps its latest
+// column among equal H; the lanes are merged once per row.  Otherwise the 32-bit
+// key (H << 16) | column.
+template <bool K16>
+struct U8Keys {
+    uint32_t v = 0;
+    __device__ __forceinline__ void one(int h, int j)
+    {
+        if (K16) {
+            const uint32_t k = (((uint32_t)h << 8) | (uint32_t)(j >> 1)) << ((j & 1) * 16);
+            v = __vimax3_u16x2(v, k, k);
+        } else {
+            const int32_t kk = (h << 16) | j;
+            v = (uint32_t)((int32_t)v > kk ? (int32_t)v : kk);
+        }
+    }
+    __device__ __forceinline__ void pair(uint32_t h2, int jj)
+    {
+        if (K16) {
+            const uint32_t k = prmt((uint32_t)(jj >> 1), h2, 0x6040u);  // ((H_jj << 8) | k, (H_jj+1 << 8) | k)
+            v = __vimax3_u16x2(v, k, k);
+        } else {
+            v = (uint32_t)pair_rowkey((int32_t)v, h2, jj);
+        }
+    }
+    // two consecutive pairs at columns jj..jj+3 (jj even)
+    __device__ __forceinline__ void quad(uint32_t h2a, uint32_t h2b, int jj)
+    {
+        if (K16) {
+            const uint32_t kk = (uint32_t)(jj >> 1) * 0x0101u + 0x0100u;  // bytes k, k + 1
+            v = __vimax3_u16x2(v, prmt(kk, h2a, 0x6040u), prmt(kk, h2b, 0x6141u));
+        } else {
+            v = (uint32_t)pair_rowkey((int32_t)v, h2a, jj);
+            v = (uint32_t)pair_rowkey((int32_t)v, h2b, jj + 2);
+        }
+    }
+    __device__ __forceinline__ void decode(int &rmax, int &mj) const
+    {
+        if (K16) {
+            const int hlo = (int)((v >> 8) & 0xffu), hhi = (int)(v >> 24);
+            const int jlo = 2 * (int)(v & 0xffu), jhi = 2 * (int)((v >> 16) & 0xffu) + 1;
+            const bool hi = hhi > hlo || (hhi == hlo && jhi > jlo);  // ties -> later column
+            rmax = hi ? hhi : hlo;
+            mj = hi ? jhi : jlo;
+        } else {
+            rmax = (int)v >> 16;
+            mj = (int)(v & 0xffffu);
+        }
+    }
+};
+
+template <int TB, bool K16>
 __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restrict__ cellw, uint32_t *__restrict__ qw,
                                                               const uint8_t *__restrict__ seq,
                                                               const bwacuda_dev_ext_job &J, const ExtParams &P,
@@ -329,7 +390,7 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
             h1 = h1 > 0 ? h1 : 0;
         }
         int f = 0;
-        int32_t rowkey = 0;
+        U8Keys<K16> rowkey;
         if (beg < end) {
             int j = beg;
             if (j & 1) {  // odd first column: the high half of its word
@@ -340,8 +401,7 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
                          en);
                 cellw[(j >> 1) * TB] = (wv & 0xffffu) | ((uint32_t)h1 << 16) | ((uint32_t)en << 24);
                 h1 = h;
-                const int32_t kk = (h << 16) | j;
-                rowkey = rowkey > kk ? rowkey : kk;
+                rowkey.one(h, j);
                 ++j;
             }
             uint32_t wn = cellw[(j >> 1) * TB];  // j <= end <= qlen: allocated
@@ -366,12 +426,12 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
                 // stored bytes: H(i,j-1), E(i+1,j), H(i,j), E(i+1,j+1)
                 cellw[(jj >> 1) * TB] = prmt(prmt(h1v, h2, 0x0042u), en2, 0x6140u);
                 h1v = h2;
-                rowkey = pair_rowkey(rowkey, h2, jj);
+                return h2;
             };
             // one pair to reach a query-word boundary, then whole words (four columns) with
             // the next word loaded one step ahead, then a last pair
             if ((j & 2) && j + 1 < end) {
-                pair(j, qw[(j >> 2) * TB] >> 16);
+                rowkey.pair(pair(j, qw[(j >> 2) * TB] >> 16), j);
                 j += 2;
             }
             if (j + 3 < end) {
@@ -379,12 +439,13 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
                 for (; j + 3 < end; j += 4) {
                     const uint32_t qv = qn;
                     qn = qw[((j >> 2) + 1) * TB];  // j + 4 <= qlen < qcap: inside the query words
-                    pair(j, qv);
-                    pair(j + 2, qv >> 16);
+                    const uint32_t h2a = pair(j, qv);
+                    const uint32_t h2b = pair(j + 2, qv >> 16);
+                    rowkey.quad(h2a, h2b, j);
                 }
             }
             if (j + 1 < end) {
-                pair(j, qw[(j >> 2) * TB] >> ((j & 2) * 8));
+                rowkey.pair(pair(j, qw[(j >> 2) * TB] >> ((j & 2) * 8)), j);
                 j += 2;
             }
             f = (int)(fv >> 16);
@@ -397,8 +458,7 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
                          h, en);
                 cellw[(j >> 1) * TB] = (wv & 0xffff0000u) | (uint32_t)h1 | ((uint32_t)en << 8);
                 h1 = h;
-                const int32_t kk = (h << 16) | j;
-                rowkey = rowkey > kk ? rowkey : kk;
+                rowkey.one(h, j);
             }
             ncells += (unsigned long long)(end - beg);
         }
@@ -412,8 +472,8 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
             best_ie = i;
             gscore = h1;
         }
-        const int rmax = rowkey >> 16;
-        const int mj = rowkey & 0xffff;
+        int rmax, mj;
+        rowkey.decode(rmax, mj);
         if (rmax == 0) break;
         if (rmax > best) {
             best = rmax;

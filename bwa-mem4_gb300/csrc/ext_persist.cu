@@ -28,11 +28,12 @@ __device__ __forceinline__ uint32_t ext_cell_class(const bwacuda_dev_ext_job &J,
     return ext_fits_i16(J.qlen, J.tlen, J.h0, max_sc) ? 1u : 2u;
 }
 
-// 16-bit sort key: cell class, query length descending (clamped at 1023),
-// target length descending in 32-row steps.
-__device__ __forceinline__ uint16_t ext_sort_key(const bwacuda_dev_ext_job &J, int max_sc)
+// 16-bit sort key: cell class (at least min_cls), query length descending
+// (clamped at 1023), target length descending in 32-row steps.
+__device__ __forceinline__ uint16_t ext_sort_key(const bwacuda_dev_ext_job &J, int max_sc, uint32_t min_cls)
 {
-    const uint32_t cls = ext_cell_class(J, max_sc);
+    uint32_t cls = ext_cell_class(J, max_sc);
+    cls = cls > min_cls ? cls : min_cls;
     const uint32_t ql = J.qlen < 0 ? 0u : (J.qlen > 1023 ? 1023u : (uint32_t)J.qlen);
     const uint32_t tb = J.tlen < 0 ? 0u : ((uint32_t)J.tlen >> 5 > 15u ? 15u : (uint32_t)J.tlen >> 5);
     return (uint16_t)((cls << 14) | ((1023u - ql) << 4) | (15u - tb));
@@ -81,13 +82,13 @@ __device__ bool ungapped_hit(const uint8_t *q, int qlen, const uint8_t *t, int t
 // Sort keys; with the ungapped rule on, jobs it settles get their result here
 // and key class 3, which no bucket covers.
 __global__ void ext_keys_kernel(const bwacuda_dev_ext_job *__restrict__ jobs, uint32_t n, int max_sc,
-                                const uint8_t *__restrict__ seq, const UngappedRule ug, int zdrop,
+                                uint32_t min_cls, const uint8_t *__restrict__ seq, const UngappedRule ug, int zdrop,
                                 bwacuda_ext_result *__restrict__ out, uint16_t *__restrict__ keys,
                                 uint32_t *__restrict__ idx)
 {
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const bwacuda_dev_ext_job J = jobs[k];
-        uint16_t key = ext_sort_key(J, max_sc);
+        uint16_t key = ext_sort_key(J, max_sc, min_cls);
         if (ug.enabled) {
             bwacuda_ext_result r;
             if (ungapped_hit(seq + J.q_off, J.qlen, seq + J.t_off, J.tlen, J.h0, ug, zdrop, r)) {
@@ -183,8 +184,8 @@ size_t ext_sort_temp_bytes(size_t n)
     return bytes;
 }
 
-cudaError_t ext_sort_and_bucket(const bwacuda_dev_ext_job *jobs, size_t n, int max_sc, const uint8_t *seq,
-                                const UngappedRule &ug, int zdrop, bwacuda_ext_result *out, uint16_t *keys_in,
+cudaError_t ext_sort_and_bucket(const bwacuda_dev_ext_job *jobs, size_t n, int max_sc, bool pair_lanes,
+                                const uint8_t *seq, const UngappedRule &ug, int zdrop, bwacuda_ext_result *out, uint16_t *keys_in,
                                 uint16_t *keys_out, uint32_t *idx_in, uint32_t *idx_out, void *tmp,
                                 size_t tmp_bytes, const ExtBucketDef *d_defs, int nb, uint32_t *d_table,
                                 cudaStream_t s)
@@ -192,7 +193,8 @@ cudaError_t ext_sort_and_bucket(const bwacuda_dev_ext_job *jobs, size_t n, int m
     if (n == 0) return cudaSuccess;
     uint32_t grid = (uint32_t)((n + 255) / 256);
     if (grid > 8192) grid = 8192;
-    ext_keys_kernel<<<grid, 256, 0, s>>>(jobs, (uint32_t)n, max_sc, seq, ug, zdrop, out, keys_in, idx_in);
+    ext_keys_kernel<<<grid, 256, 0, s>>>(jobs, (uint32_t)n, max_sc, pair_lanes ? 0u : 1u, seq, ug, zdrop, out,
+                                         keys_in, idx_in);
     cudaError_t e = cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys_in, keys_out, idx_in, idx_out, (int)n, 0,
                                                     16, s);
     if (e != cudaSuccess) return e;

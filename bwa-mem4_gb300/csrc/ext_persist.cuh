@@ -94,8 +94,11 @@ ext_persist_pair_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_j
                 atomicOr(err, ERR_RANGE);
             } else {
                 bool bad = false;
-                const bwacuda_ext_result r = W16 ? ext_run_job_i16p<TB>(cell2, qw, seq, J, P, bad, ncells)
-                                                 : ext_run_job_u8p<TB>(cellw, qw, seq, J, P, bad, ncells);
+                // 8-bit rows of at most 512 columns keep their row maxima in 16-bit lanes
+                const bwacuda_ext_result r =
+                    W16 ? ext_run_job_i16p<TB>(cell2, qw, seq, J, P, bad, ncells)
+                        : (qcap <= 513 ? ext_run_job_u8p<TB, true>(cellw, qw, seq, J, P, bad, ncells)
+                                       : ext_run_job_u8p<TB, false>(cellw, qw, seq, J, P, bad, ncells));
                 if (bad) atomicOr(err, ERR_BASE);
                 out[jid] = r;
             }
@@ -174,10 +177,13 @@ cudaError_t launch_persist(const PersistLaunch &L, const ExtBucketDef &d, uint32
 template <int GRAB>
 cudaError_t ext_persist_launch_grab(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm, int tb)
 {
+    // the sort keeps the 8-bit class empty when the gap costs do not fit 16-bit lanes
+    const bool lanes = ext_pair_lanes_ok(L.P.sc.o_del, L.P.sc.e_del, L.P.sc.o_ins, L.P.sc.e_ins);
     if (d.cls == 0) return launch_persist_pair<GRAB, false>(L, d, table, nsm, tb);
     if (d.cls == 2) return launch_persist<FmtI32, GRAB>(L, d, table, nsm, tb);
     // 16-bit pair cells where one warp's rows fit, else one column per cell
-    if (pair_block_smem(d.qcap, 32, true) <= SMEM_MAX) return launch_persist_pair<GRAB, true>(L, d, table, nsm, tb);
+    if (lanes && pair_block_smem(d.qcap, 32, true) <= SMEM_MAX)
+        return launch_persist_pair<GRAB, true>(L, d, table, nsm, tb);
     return launch_persist<FmtI16, GRAB>(L, d, table, nsm, tb);
 }
 

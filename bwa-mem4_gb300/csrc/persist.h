@@ -36,7 +36,10 @@ size_t ext_sort_temp_bytes(size_t n);
 // keys + radix sort + bucket bounds; d_table holds 4 words per bucket
 // (start, end, work counter, spare).
 // With P.ug enabled the key kernel also settles ungapped hits (results written to out).
-cudaError_t ext_sort_and_bucket(const bwacuda_dev_ext_job *jobs, size_t n, int max_sc, const uint8_t *seq,
+// pair_lanes false (gap costs too large for 16-bit lanes) keeps every job out of
+// the 8-bit class.
+cudaError_t ext_sort_and_bucket(const bwacuda_dev_ext_job *jobs, size_t n, int max_sc, bool pair_lanes,
+                                const uint8_t *seq,
                                 const UngappedRule &ug, int zdrop, bwacuda_ext_result *out, uint16_t *keys_in,
                                 uint16_t *keys_out, uint32_t *idx_in, uint32_t *idx_out, void *tmp,
                                 size_t tmp_bytes, const ExtBucketDef *d_defs, int nb, uint32_t *d_table,

@@ -283,10 +283,12 @@ def _mutated_pairs(rng, n, qmax, h0_choices):
 
 
 @pytest.mark.parametrize("scoring", [(1, 4, 6, 1, 6, 1, 5, 100), (2, 3, 5, 2, 4, 3, 0, 40), (1, 1, 0, 1, 0, 1, 9, 0),
-                                     (3, 5, 11, 1, 7, 2, 1, 200), (1, 4, 6, 1, 6, 1, 5, 1)])
+                                     (3, 5, 11, 1, 7, 2, 1, 200), (1, 4, 6, 1, 6, 1, 5, 1),
+                                     (1, 4, 16383, 1, 16000, 384, 5, 100), (2, 4, 30000, 3000, 17000, 5, 5, 100)])
 def test_pair_cell_classes_swept(ctx, scoring):
     # jobs of the 8-bit and 16-bit classes (two columns per lane operation) with odd and
-    # even band edges, swept scoring and bands, through the batched route
+    # even band edges, swept scoring and bands, through the batched route; the last two
+    # scorings sit at and beyond the largest gap costs the 16-bit lanes take
     a, b, od, ed, oi, ei, eb, zd = scoring
     rng = np.random.default_rng(sum(scoring))
     qs, ts, h0s = _mutated_pairs(rng, 1500, 700, [(1, 60), (100, 250), (300, 3000), (8000, 20000)])
