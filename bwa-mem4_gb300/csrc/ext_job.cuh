@@ -328,7 +328,9 @@ struct U8Keys {
     }
 };
 
-template <int TB, bool K16>
+// SYM: o_del + e_del == o_ins + e_ins, so the deletion-open lane equals the
+// insertion-open lane and is not computed twice.
+template <int TB, bool K16, bool SYM>
 __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restrict__ cellw, uint32_t *__restrict__ qw,
                                                               const uint8_t *__restrict__ seq,
                                                               const bwacuda_dev_ext_job &J, const ExtParams &P,
@@ -419,7 +421,7 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
                 // non-positive M acts as 0 below (E, F >= 0)
                 const uint32_t M2 = __viaddmin_s16x2(hd2, s2, hd2 << 7);
                 const uint32_t ti2 = __viaddmax_s16x2_relu(M2, noe_ins2, 0u);  // max(M - oe_ins, 0)
-                const uint32_t td2 = __viaddmax_s16x2_relu(M2, noe_del2, 0u);  // max(M - oe_del, 0)
+                const uint32_t td2 = SYM ? ti2 : __viaddmax_s16x2_relu(M2, noe_del2, 0u);  // max(M - oe_del, 0)
                 const uint32_t en2 = __viaddmax_s16x2(e2, ne_del2, td2);       // E(i+1, .)
                 const uint32_t f2 = f_pair(fv, ti2, fsel2, ne_ins2);            // (F(i,j), F(i,j+1))
                 const uint32_t h2 = __vimax3_s16x2(M2, e2, f2);  // (H(i,j), H(i,j+1))
@@ -529,7 +531,7 @@ __device__ __forceinline__ bool i16p_dead(const uint2 *cell2, int x)
     return (((c.x | c.y) >> ((x & 1) * 16)) & 0xffffu) == 0u;
 }
 
-template <int TB>
+template <int TB, bool SYM>
 __device__ __forceinline__ bwacuda_ext_result ext_run_job_i16p(uint2 *__restrict__ cell2, uint32_t *__restrict__ qw,
                                                                const uint8_t *__restrict__ seq,
                                                                const bwacuda_dev_ext_job &J, const ExtParams &P,
@@ -616,7 +618,7 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_i16p(uint2 *__restrict
                 const uint32_t g2 = __viaddmin_u16x2(hd2, 0u, 0x00010001u) * 0x7fffu;
                 const uint32_t M2 = __viaddmin_s16x2(hd2, s2, g2);
                 const uint32_t ti2 = __viaddmax_s16x2_relu(M2, noe_ins2, 0u);
-                const uint32_t td2 = __viaddmax_s16x2_relu(M2, noe_del2, 0u);
+                const uint32_t td2 = SYM ? ti2 : __viaddmax_s16x2_relu(M2, noe_del2, 0u);
                 const uint32_t en2 = __viaddmax_s16x2(e2, ne_del2, td2);
                 const uint32_t f2 = f_pair(fv, ti2, fsel2, ne_ins2);
                 const uint32_t h2 = __vimax3_s16x2(M2, e2, f2);

@@ -76,6 +76,7 @@ ext_persist_pair_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_j
     uint32_t *qw = reinterpret_cast<uint32_t *>(smem_raw) + cpairs * (W16 ? 2 : 1) * TB + tid;
     const uint32_t start = table[0], stop = table[1];
     uint32_t *counter = table + 2;
+    const bool sym = P.sc.o_del + P.sc.e_del == P.sc.o_ins + P.sc.e_ins;
     unsigned long long ncells = 0;
     for (;;) {
         uint32_t base = 0;
@@ -94,11 +95,18 @@ ext_persist_pair_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_j
                 atomicOr(err, ERR_RANGE);
             } else {
                 bool bad = false;
-                // 8-bit rows of at most 512 columns keep their row maxima in 16-bit lanes
-                const bwacuda_ext_result r =
-                    W16 ? ext_run_job_i16p<TB>(cell2, qw, seq, J, P, bad, ncells)
-                        : (qcap <= 513 ? ext_run_job_u8p<TB, true>(cellw, qw, seq, J, P, bad, ncells)
-                                       : ext_run_job_u8p<TB, false>(cellw, qw, seq, J, P, bad, ncells));
+                // 8-bit rows of at most 512 columns keep their row maxima in 16-bit lanes;
+                // equal open+extend costs share one gap-open lane
+                bwacuda_ext_result r;
+                if (W16)
+                    r = sym ? ext_run_job_i16p<TB, true>(cell2, qw, seq, J, P, bad, ncells)
+                            : ext_run_job_i16p<TB, false>(cell2, qw, seq, J, P, bad, ncells);
+                else if (qcap <= 513)
+                    r = sym ? ext_run_job_u8p<TB, true, true>(cellw, qw, seq, J, P, bad, ncells)
+                            : ext_run_job_u8p<TB, true, false>(cellw, qw, seq, J, P, bad, ncells);
+                else
+                    r = sym ? ext_run_job_u8p<TB, false, true>(cellw, qw, seq, J, P, bad, ncells)
+                            : ext_run_job_u8p<TB, false, false>(cellw, qw, seq, J, P, bad, ncells);
                 if (bad) atomicOr(err, ERR_BASE);
                 out[jid] = r;
             }
