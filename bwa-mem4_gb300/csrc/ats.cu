@@ -10,9 +10,15 @@
 //      into one HBM buffer and writes the device descriptors;
 //   4. the batched extension runs (sort, buckets, persistent kernels);
 //   5. a scatter kernel stores the results straight into the caller's out[].
-// The host only launches.  Chunks alternate between two streams, so the gather
-// of chunk k+1 overlaps the extension of chunk k; one 8-byte readback per chunk
-// (the byte total) sizes the sequence buffer.
+// The host only launches.  Steps 1-3 of every chunk run back to back on one
+// high-priority gather stream (one chunk reads host memory at a time: the link is
+// the shared resource); steps 4-5 run on two alternating extension streams, each
+// chunk's extension waiting only for its own gather.  A ring of ATS_RING chunk
+// buffers lets the gathers run ahead of the extensions; one 8-byte readback per
+// chunk (its byte total) sizes the chunk's sequence buffer.  While a chunk is in
+// flight the persistent bucket kernels leave one small block's worth of registers
+// and threads free on every SM, so the next chunk's length and gather blocks
+// start at once instead of waiting for a bucket to drain.
 //
 // A job is validated before any of its slices is read: a negative length,
 // h0 <= 0, or a null pointer with a non-zero length makes the call return
@@ -36,11 +42,18 @@ namespace {
 constexpr uint32_t ERR_INPUT = 8u;
 constexpr size_t ATS_MAX_CHUNK = size_t(1) << 24;  // 32-bit word indexing in the scatter
 constexpr int ATS_FLAG_BYTES = 32;                 // u32 input flag, pad, u64 bins[3]
-// Blocks per SM of the pipeline's length / gather / scatter launches.  They run
-// beside the previous chunk's persistent DP kernels; a full-occupancy grid would
-// crowd those off the SMs, while two blocks per SM with eight 16-byte loads in
-// flight per lane already keep several MB of host reads outstanding.
-constexpr int ATS_BLOCKS_PER_SM = 2;
+// Blocks per SM (of ATS_THREADS threads) of the pipeline's length / gather /
+// scatter launches.  They run beside the persistent DP kernels, in the room
+// those leave free (ATS_RESERVE_*): one block per SM with eight 16-byte loads in
+// flight per lane keeps about 2.4 MB of host reads outstanding, and a second one
+// would take room from the extension.
+constexpr int ATS_BLOCKS_PER_SM = 1;
+constexpr int ATS_THREADS = 128;
+// What the persistent kernels leave free per SM while the pipeline runs: one
+// ATS_THREADS block at the gather kernel's register bound (64 per thread).
+constexpr int ATS_RESERVE_REGS = ATS_THREADS * 64;
+constexpr int ATS_RESERVE_THREADS = ATS_THREADS;
+constexpr int ATS_RING = 4;  // chunk buffers in flight
 
 __device__ __forceinline__ bool job_ok(const bwacuda_ext_job &J)
 {
@@ -55,7 +68,8 @@ __device__ __forceinline__ bool job_ok(const bwacuda_ext_job &J)
 // covering word outside the slice lie in the same page as bytes of the slice,
 // so the widened reads touch only mapped memory; in HBM they land in the
 // slice's own reserve.
-__global__ void ats_lengths_kernel(const bwacuda_ext_job *__restrict__ hjobs, uint32_t n, BinRule br,
+__global__ void __launch_bounds__(ATS_THREADS) ats_lengths_kernel(const bwacuda_ext_job *__restrict__ hjobs,
+                                                                  uint32_t n, BinRule br,
                                    uint64_t *__restrict__ sizes, uint32_t *__restrict__ flags)
 {
     uint32_t bad = 0, bins[3] = {0, 0, 0};
@@ -85,10 +99,10 @@ __global__ void ats_lengths_kernel(const bwacuda_ext_job *__restrict__ hjobs, ui
 // coalesced read of the caller's array) and writes its device descriptor; then
 // the warp copies all 32 jobs' words as one flat list (warp_gather_slices).  An
 // invalid job becomes an empty one (qlen = tlen = 0, h0 = 1); the call then fails.
-__global__ void __launch_bounds__(256) ats_gather_kernel(const bwacuda_ext_job *__restrict__ hjobs, uint32_t n,
-                                                         const uint64_t *__restrict__ offs, int w,
-                                                         uint8_t *__restrict__ seq,
-                                                         bwacuda_dev_ext_job *__restrict__ djobs)
+__global__ void __launch_bounds__(ATS_THREADS, 8) ats_gather_kernel(const bwacuda_ext_job *__restrict__ hjobs,
+                                                                    uint32_t n, const uint64_t *__restrict__ offs,
+                                                                    int w, uint8_t *__restrict__ seq,
+                                                                    bwacuda_dev_ext_job *__restrict__ djobs)
 {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -120,48 +134,74 @@ __global__ void __launch_bounds__(256) ats_gather_kernel(const bwacuda_ext_job *
 
 // Results to the caller's array, word by word so consecutive threads write
 // consecutive host addresses.
-__global__ void ats_scatter_kernel(const uint32_t *__restrict__ src, uint32_t words, uint32_t *__restrict__ dst)
+__global__ void __launch_bounds__(ATS_THREADS) ats_scatter_kernel(const uint32_t *__restrict__ src, uint32_t words,
+                                                                  uint32_t *__restrict__ dst)
 {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < words; i += gridDim.x * blockDim.x) dst[i] = src[i];
 }
 
-struct AtsSlot {
+struct AtsChunk {
     DevBuf sizes, offs, scan_tmp, seq, djobs, dout, flags;
     HostBuf h_total, h_flags;
-    cudaEvent_t gathered = nullptr;  // this slot's last gather finished
+    cudaEvent_t gathered = nullptr;  // sequence buffer and descriptors are in HBM
+    cudaEvent_t done = nullptr;      // results stored, flags read back
     bool busy = false;
 };
 
 }  // namespace
 
 struct AtsState {
-    AtsSlot slot[2];
+    AtsChunk ring[ATS_RING];
+    cudaStream_t gstream = nullptr;  // lengths, scans, gathers (highest priority)
 };
 
 void ats_release(bwacuda_ctx *c)
 {
     if (!c->ats) return;
-    for (auto &s : c->ats->slot) {
-        s.sizes.release(); s.offs.release(); s.scan_tmp.release(); s.seq.release();
-        s.djobs.release(); s.dout.release(); s.flags.release();
-        s.h_total.release(); s.h_flags.release();
-        if (s.gathered) cudaEventDestroy(s.gathered);
+    if (c->ats->gstream) cudaStreamSynchronize(c->ats->gstream);
+    for (auto &r : c->ats->ring) {
+        if (r.done) cudaEventSynchronize(r.done);
+        r.sizes.release(); r.offs.release(); r.scan_tmp.release(); r.seq.release();
+        r.djobs.release(); r.dout.release(); r.flags.release();
+        r.h_total.release(); r.h_flags.release();
+        if (r.gathered) cudaEventDestroy(r.gathered);
+        if (r.done) cudaEventDestroy(r.done);
     }
+    if (c->ats->gstream) cudaStreamDestroy(c->ats->gstream);
     delete c->ats;
     c->ats = nullptr;
 }
 
 namespace {
 
-// Wait for a slot's chunk and fold its input flag and bin counts in.
-int ats_drain(bwacuda_ctx *c, int si, uint32_t *input_flags)
+int ats_init(bwacuda_ctx *c)
 {
-    AtsSlot &S = c->ats->slot[si];
-    if (!S.busy) return BWACUDA_OK;
-    S.busy = false;
-    cudaError_t e = cudaStreamSynchronize(c->slot[si].stream);
+    if (c->ats) return BWACUDA_OK;
+    AtsState *A = new (std::nothrow) AtsState();
+    if (!A) return BWACUDA_ENOMEM;
+    int lo_prio = 0, hi_prio = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&A->gstream, cudaStreamNonBlocking, hi_prio);
+    for (auto &r : A->ring) {
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r.gathered, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r.done, cudaEventDisableTiming);
+    }
+    c->ats = A;
+    if (e != cudaSuccess) {
+        ats_release(c);
+        return cuda_status(e);
+    }
+    return BWACUDA_OK;
+}
+
+// Wait for a ring entry's chunk and fold its input flag and bin counts in.
+int ats_retire(bwacuda_ctx *c, AtsChunk &R, uint32_t *input_flags)
+{
+    if (!R.busy) return BWACUDA_OK;
+    R.busy = false;
+    cudaError_t e = cudaEventSynchronize(R.done);
     if (e != cudaSuccess) return cuda_status(e);
-    const uint32_t *f = static_cast<const uint32_t *>(S.h_flags.p);
+    const uint32_t *f = static_cast<const uint32_t *>(R.h_flags.p);
     const uint64_t *bins = reinterpret_cast<const uint64_t *>(f + 2);
     *input_flags |= f[0];
     c->stats.ext_bin_u8 += bins[0];
@@ -170,62 +210,69 @@ int ats_drain(bwacuda_ctx *c, int si, uint32_t *input_flags)
     return BWACUDA_OK;
 }
 
-cudaError_t ats_enqueue_chunk(bwacuda_ctx *c, int si, const bwacuda_ext_job *hj, size_t cn, const BinRule &br,
-                              const ExtParams &P, int w, bwacuda_ext_result *hout)
+// Steps 1-3 of a chunk on the gather stream: lengths and validation, the offset
+// scan, the byte total read back (the host waits for it: it sizes the sequence
+// buffer, and the gather stream holds nothing else), then the gather.
+cudaError_t ats_gather_chunk(bwacuda_ctx *c, AtsChunk &R, const bwacuda_ext_job *hj, size_t cn, const BinRule &br,
+                             int w)
 {
-    AtsSlot &S = c->ats->slot[si];
-    cudaStream_t s = c->slot[si].stream;
+    cudaStream_t g = c->ats->gstream;
     cudaError_t e;
     size_t scan_bytes = 0;
     if ((e = cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, (const uint64_t *)nullptr, (uint64_t *)nullptr,
                                            (int)cn + 1)) != cudaSuccess)
         return e;
-    if ((e = S.sizes.ensure((cn + 1) * 8)) != cudaSuccess) return e;
-    if ((e = S.offs.ensure((cn + 1) * 8)) != cudaSuccess) return e;
-    if ((e = S.scan_tmp.ensure(scan_bytes + 16)) != cudaSuccess) return e;
-    if ((e = S.djobs.ensure(cn * sizeof(bwacuda_dev_ext_job))) != cudaSuccess) return e;
-    if ((e = S.dout.ensure(cn * sizeof(bwacuda_ext_result))) != cudaSuccess) return e;
-    if ((e = S.flags.ensure(ATS_FLAG_BYTES)) != cudaSuccess) return e;
-    if ((e = S.h_total.ensure(16)) != cudaSuccess) return e;
-    if ((e = S.h_flags.ensure(ATS_FLAG_BYTES)) != cudaSuccess) return e;
-    uint64_t *sizes = static_cast<uint64_t *>(S.sizes.p), *offs = static_cast<uint64_t *>(S.offs.p);
-    uint32_t *flags = static_cast<uint32_t *>(S.flags.p);
-    if (!S.gathered && (e = cudaEventCreateWithFlags(&S.gathered, cudaEventDisableTiming)) != cudaSuccess) return e;
-    // One chunk reads host memory at a time: the host-memory link is the shared resource,
-    // and the chunk whose DP runs next gets all of it.
-    AtsSlot &O = c->ats->slot[si ^ 1];
-    if (O.busy && O.gathered && (e = cudaStreamWaitEvent(s, O.gathered, 0)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(flags, 0, ATS_FLAG_BYTES, s)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(sizes + cn, 0, 8, s)) != cudaSuccess) return e;
-    const int nsm = batched_nsm(c);
-    uint32_t grid = (uint32_t)std::min<size_t>((cn + 255) / 256, (size_t)nsm * ATS_BLOCKS_PER_SM);
-    ats_lengths_kernel<<<grid, 256, 0, s>>>(hj, (uint32_t)cn, br, sizes, flags);
+    if ((e = R.sizes.ensure((cn + 1) * 8)) != cudaSuccess) return e;
+    if ((e = R.offs.ensure((cn + 1) * 8)) != cudaSuccess) return e;
+    if ((e = R.scan_tmp.ensure(scan_bytes + 16)) != cudaSuccess) return e;
+    if ((e = R.djobs.ensure(cn * sizeof(bwacuda_dev_ext_job))) != cudaSuccess) return e;
+    if ((e = R.dout.ensure(cn * sizeof(bwacuda_ext_result))) != cudaSuccess) return e;
+    if ((e = R.flags.ensure(ATS_FLAG_BYTES)) != cudaSuccess) return e;
+    if ((e = R.h_total.ensure(16)) != cudaSuccess) return e;
+    if ((e = R.h_flags.ensure(ATS_FLAG_BYTES)) != cudaSuccess) return e;
+    uint64_t *sizes = static_cast<uint64_t *>(R.sizes.p), *offs = static_cast<uint64_t *>(R.offs.p);
+    uint32_t *flags = static_cast<uint32_t *>(R.flags.p);
+    if ((e = cudaMemsetAsync(flags, 0, ATS_FLAG_BYTES, g)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(sizes + cn, 0, 8, g)) != cudaSuccess) return e;
+    const uint32_t grid = (uint32_t)std::min<size_t>((cn + ATS_THREADS - 1) / ATS_THREADS,
+                                                     (size_t)batched_nsm(c) * ATS_BLOCKS_PER_SM);
+    ats_lengths_kernel<<<grid, ATS_THREADS, 0, g>>>(hj, (uint32_t)cn, br, sizes, flags);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    if ((e = cub::DeviceScan::ExclusiveSum(S.scan_tmp.p, scan_bytes, sizes, offs, (int)cn + 1, s)) != cudaSuccess)
+    if ((e = cub::DeviceScan::ExclusiveSum(R.scan_tmp.p, scan_bytes, sizes, offs, (int)cn + 1, g)) != cudaSuccess)
         return e;
-    // the chunk's byte total sizes the sequence buffer
-    if ((e = cudaMemcpyAsync(S.h_total.p, offs + cn, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
-    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
-    const uint64_t total = *static_cast<const uint64_t *>(S.h_total.p);
-    if ((e = S.seq.ensure(total + 16)) != cudaSuccess) return e;
-    grid = (uint32_t)std::min<size_t>((cn + 255) / 256, (size_t)nsm * ATS_BLOCKS_PER_SM);
-    ats_gather_kernel<<<grid, 256, 0, s>>>(hj, (uint32_t)cn, offs, w, static_cast<uint8_t *>(S.seq.p),
-                                          static_cast<bwacuda_dev_ext_job *>(S.djobs.p));
+    if ((e = cudaMemcpyAsync(R.h_total.p, offs + cn, 8, cudaMemcpyDeviceToHost, g)) != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(g)) != cudaSuccess) return e;
+    const uint64_t total = *static_cast<const uint64_t *>(R.h_total.p);
+    if ((e = R.seq.ensure(total + 16)) != cudaSuccess) return e;
+    ats_gather_kernel<<<grid, ATS_THREADS, 0, g>>>(hj, (uint32_t)cn, offs, w, static_cast<uint8_t *>(R.seq.p),
+                                                   static_cast<bwacuda_dev_ext_job *>(R.djobs.p));
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    if ((e = cudaEventRecord(S.gathered, s)) != cudaSuccess) return e;
-    e = batched_enqueue(c, batched_slot_bufs(c, si), static_cast<const uint8_t *>(S.seq.p),
-                        static_cast<const bwacuda_dev_ext_job *>(S.djobs.p), cn, P,
-                        static_cast<bwacuda_ext_result *>(S.dout.p), s, nullptr, nullptr);
+    return cudaEventRecord(R.gathered, g);
+}
+
+// Steps 4-5 on extension stream s: the batched extension once the gather is in,
+// then the results into the caller's out[] and the flags back to the host.
+cudaError_t ats_extend_chunk(bwacuda_ctx *c, AtsChunk &R, int si, size_t cn, const ExtParams &P,
+                             bwacuda_ext_result *hout)
+{
+    cudaStream_t s = c->slot[si].stream;
+    cudaError_t e;
+    if ((e = cudaStreamWaitEvent(s, R.gathered, 0)) != cudaSuccess) return e;
+    BatchBufs *bb = batched_slot_bufs(c, si);
+    batched_set_reserve(bb, ATS_RESERVE_REGS, ATS_RESERVE_THREADS);
+    e = batched_enqueue(c, bb, static_cast<const uint8_t *>(R.seq.p), static_cast<const bwacuda_dev_ext_job *>(R.djobs.p),
+                        cn, P, static_cast<bwacuda_ext_result *>(R.dout.p), s, nullptr, nullptr);
+    batched_set_reserve(bb, 0, 0);
     if (e != cudaSuccess) return e;
     const uint32_t words = (uint32_t)(cn * (sizeof(bwacuda_ext_result) / 4));
-    grid = (uint32_t)std::min<size_t>((words + 255) / 256, (size_t)nsm * ATS_BLOCKS_PER_SM);
-    ats_scatter_kernel<<<grid, 256, 0, s>>>(static_cast<const uint32_t *>(S.dout.p), words,
-                                           reinterpret_cast<uint32_t *>(hout));
+    const uint32_t grid = (uint32_t)std::min<size_t>((words + ATS_THREADS - 1) / ATS_THREADS,
+                                                     (size_t)batched_nsm(c) * ATS_BLOCKS_PER_SM);
+    ats_scatter_kernel<<<grid, ATS_THREADS, 0, s>>>(static_cast<const uint32_t *>(R.dout.p), words,
+                                                    reinterpret_cast<uint32_t *>(hout));
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    if ((e = cudaMemcpyAsync(S.h_flags.p, flags, ATS_FLAG_BYTES, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
-    S.busy = true;
-    c->stats.kernel_launches += 4 + 3 + (uint64_t)batched_bucket_count(c);
-    return cudaSuccess;
+    if ((e = cudaMemcpyAsync(R.h_flags.p, R.flags.p, ATS_FLAG_BYTES, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return e;
+    return cudaEventRecord(R.done, s);
 }
 
 }  // namespace
@@ -254,9 +301,9 @@ int ats_gather_ext(bwacuda_ctx *c, const bwacuda_ext_job *hj, size_t n, int w, D
     if ((e = cudaMemsetAsync(flags, 0, ATS_FLAG_BYTES, s)) != cudaSuccess) return cuda_status(e);
     if ((e = cudaMemsetAsync(sizes + n, 0, 8, s)) != cudaSuccess) return cuda_status(e);
     const int nsm = batched_nsm(c);
-    const uint32_t grid = (uint32_t)std::min<size_t>((n + 255) / 256, (size_t)nsm * 8);
+    const uint32_t grid = (uint32_t)std::min<size_t>((n + ATS_THREADS - 1) / ATS_THREADS, (size_t)nsm * 16);
     BinRule br{0, 0, 0};
-    ats_lengths_kernel<<<grid, 256, 0, s>>>(hj, (uint32_t)n, br, sizes, flags);
+    ats_lengths_kernel<<<grid, ATS_THREADS, 0, s>>>(hj, (uint32_t)n, br, sizes, flags);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
     if ((e = cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, sizes, offs, (int)n + 1, s)) != cudaSuccess)
         return cuda_status(e);
@@ -266,8 +313,8 @@ int ats_gather_ext(bwacuda_ctx *c, const bwacuda_ext_job *hj, size_t n, int w, D
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_status(e);
     if (static_cast<uint32_t>(h[1]) & ERR_INPUT) return BWACUDA_EINVAL;
     if ((e = seq.ensure(h[0] + 16)) != cudaSuccess) return cuda_status(e);
-    ats_gather_kernel<<<grid, 256, 0, s>>>(hj, (uint32_t)n, offs, w, static_cast<uint8_t *>(seq.p),
-                                          static_cast<bwacuda_dev_ext_job *>(djobs.p));
+    ats_gather_kernel<<<grid, ATS_THREADS, 0, s>>>(hj, (uint32_t)n, offs, w, static_cast<uint8_t *>(seq.p),
+                                                   static_cast<bwacuda_dev_ext_job *>(djobs.p));
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
     c->stats.kernel_launches += 4;
     return BWACUDA_OK;
@@ -280,25 +327,34 @@ int extend_batch_ats(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int 
     if (!c->pageable_access) return BWACUDA_EUNSUPPORTED;
     int rc = batched_prepare(c);
     if (rc) return rc;
-    if (!c->ats) {
-        c->ats = new (std::nothrow) AtsState();
-        if (!c->ats) return BWACUDA_ENOMEM;
-    }
+    if ((rc = ats_init(c)) != BWACUDA_OK) return rc;
     const BinRule br = bin_rule(m, mat);
     const size_t CH = std::min(c->chunk_jobs, ATS_MAX_CHUNK);
     uint32_t input_flags = 0;
-    int si = 0;
-    for (size_t c0 = 0, cn = 0; c0 < n && rc == BWACUDA_OK; c0 += cn) {
-        // a short first chunk: the DP starts after a short gather, later gathers hide behind it
-        cn = std::min(c0 == 0 ? std::max(CH / 8, std::min(CH, (size_t)65536)) : CH, n - c0);
-        if ((rc = ats_drain(c, si, &input_flags)) != BWACUDA_OK) break;
-        cudaError_t e = ats_enqueue_chunk(c, si, jobs + c0, cn, br, P, w, out + c0);
-        if (e != cudaSuccess) rc = cuda_status(e);
-        si ^= 1;
+    size_t k = 0;
+    for (size_t c0 = 0, cn = 0; c0 < n && rc == BWACUDA_OK; c0 += cn, ++k) {
+        // a short first chunk: the extension starts after a short gather, later gathers hide behind it
+        cn = std::min(k == 0 ? std::max(CH / 8, std::min(CH, (size_t)65536)) : CH, n - c0);
+        AtsChunk &R = c->ats->ring[k % ATS_RING];
+        if ((rc = ats_retire(c, R, &input_flags)) != BWACUDA_OK) break;
+        cudaError_t e = ats_gather_chunk(c, R, jobs + c0, cn, br, w);
+        if (e == cudaSuccess) e = ats_extend_chunk(c, R, (int)(k & 1), cn, P, out + c0);
+        if (e != cudaSuccess) {
+            rc = cuda_status(e);
+            break;
+        }
+        R.busy = true;
+        c->stats.kernel_launches += 3 + 3 + (uint64_t)batched_bucket_count(c);
     }
-    const int rc0 = ats_drain(c, 0, &input_flags);
-    const int rc1 = ats_drain(c, 1, &input_flags);
-    if (!rc) rc = rc0 ? rc0 : rc1;
+    for (auto &R : c->ats->ring) {
+        const int r2 = ats_retire(c, R, &input_flags);
+        if (!rc) rc = r2;
+    }
+    if (rc != BWACUDA_OK) {  // a failed enqueue may leave work behind on the streams
+        cudaStreamSynchronize(c->ats->gstream);
+        cudaStreamSynchronize(c->slot[0].stream);
+        cudaStreamSynchronize(c->slot[1].stream);
+    }
     uint64_t cells = 0;
     const int st = collect_device_status(c, c->slot[0].stream, &cells);
     if (!rc && (input_flags & ERR_INPUT)) rc = BWACUDA_EINVAL;

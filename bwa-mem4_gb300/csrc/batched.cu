@@ -29,10 +29,13 @@ struct BatchBufs {
     size_t g_n = 0;
     cudaStream_t g_stream = nullptr;
     ExtParams g_P{};
+    // per-SM room the bucket kernels leave for kernels running beside them
+    int reserve_regs = 0, reserve_threads = 0;
 };
 
 struct BatchedState {
     int nsm = 0;
+    int sm_regs = 65536, sm_threads = 2048;
     int nb = 0;
     // tuning (set by bwacuda_autotune_extend or the options); gen changes with every setting
     int tb = 128;    // threads per block of the persistent kernels
@@ -50,6 +53,9 @@ static int batched_init(bwacuda_ctx *c)
     BatchedState *B = new (std::nothrow) BatchedState();
     if (!B) return BWACUDA_ENOMEM;
     cudaError_t e = cudaDeviceGetAttribute(&B->nsm, cudaDevAttrMultiProcessorCount, c->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&B->sm_regs, cudaDevAttrMaxRegistersPerMultiprocessor, c->device);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&B->sm_threads, cudaDevAttrMaxThreadsPerMultiProcessor, c->device);
     if (e != cudaSuccess) { delete B; return cuda_status(e); }
     B->nb = ext_bucket_defs(B->defs, EXT_MAX_BUCKETS, B->step);
     if ((e = B->d_defs.ensure(sizeof(B->defs))) != cudaSuccess) { delete B; return cuda_status(e); }
@@ -172,6 +178,10 @@ static cudaError_t enqueue_batched(bwacuda_ctx *c, BatchBufs &bb, const uint8_t 
     L.err = err ? err : reinterpret_cast<uint32_t *>(c->d_misc.p);
     L.cells = cells ? cells : reinterpret_cast<unsigned long long *>((char *)c->d_misc.p + 8);
     L.grab = B->grab;
+    L.reserve_regs = bb.reserve_regs;
+    L.reserve_threads = bb.reserve_threads;
+    L.sm_regs = B->sm_regs;
+    L.sm_threads = B->sm_threads;
     // largest buckets first: they hold the long jobs
     for (int b = B->nb - 1, k = 0; b >= 0; --b, ++k) {
         L.stream = bb.fan[k % FAN];
@@ -229,6 +239,11 @@ int extend_device_batched(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_de
 }
 
 int batched_prepare(bwacuda_ctx *c) { return batched_init(c); }
+void batched_set_reserve(BatchBufs *bb, int regs, int threads)
+{
+    bb->reserve_regs = regs;
+    bb->reserve_threads = threads;
+}
 BatchBufs *batched_slot_bufs(bwacuda_ctx *c, int slot) { return &c->batched->bufs[slot & 1]; }
 int batched_nsm(bwacuda_ctx *c) { return c->batched->nsm; }
 int batched_bucket_count(bwacuda_ctx *c) { return c->batched->nb; }

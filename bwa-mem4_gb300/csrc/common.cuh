@@ -93,12 +93,16 @@ __host__ __device__ inline uint32_t slice_words(const uint8_t *src, int len)
 
 #ifdef __CUDACC__
 // Copy the slices of the warp's 32 jobs (lane l's job: qw words at qa, then tw
-// words at ta, both 16-byte aligned addresses) to seq + base_l, as one flat list
-// of words over the whole warp: word x belongs to the lane whose exclusive
-// prefix of word counts is the largest one <= x (a 5-step shuffle search), and
-// every lane keeps eight independent 16-byte loads in flight before storing
-// (the kernel is bound by host-memory latency, and beside the persistent DP
-// kernels it gets few warps per SM).  All 32 lanes must call it.
+// words at ta, both 16-byte aligned addresses) as one flat list of words over
+// the whole warp: word x belongs to the lane whose exclusive prefix of word
+// counts is the largest one <= x (a 5-step shuffle search), and every lane keeps
+// eight independent 16-byte loads in flight before storing (the kernel is bound
+// by host-memory latency, and beside the persistent DP kernels it gets few warps
+// per SM).  The destinations are consecutive: lane l's job lands at
+// seq + base_l with base_l = base_0 + 16 * (words of lanes < l) -- the layout an
+// exclusive scan of 16 * (qw + tw) over consecutive jobs gives -- so flat word x
+// is stored at seq + base_0 + 16 x.  All 32 lanes must call it, and lane 0 must
+// carry a job (possibly empty).
 __device__ __forceinline__ void warp_gather_slices(uint64_t qa, uint64_t ta, uint64_t base, uint32_t qw, uint32_t tw,
                                                    uint8_t *seq)
 {
@@ -112,10 +116,10 @@ __device__ __forceinline__ void warp_gather_slices(uint64_t qa, uint64_t ta, uin
     }
     const uint32_t total = __shfl_sync(0xffffffffu, pre, 31);
     pre -= wc;
+    uint4 *dst = reinterpret_cast<uint4 *>(seq + __shfl_sync(0xffffffffu, base, 0));
     constexpr int U = 8;
     for (uint32_t x0 = 0; x0 < total; x0 += 32u * U) {
         uint4 v[U];
-        uint4 *dst[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const uint32_t x = x0 + (uint32_t)u * 32u + lane;
@@ -129,16 +133,16 @@ __device__ __forceinline__ void warp_gather_slices(uint64_t qa, uint64_t ta, uin
             const uint32_t qw_j = __shfl_sync(0xffffffffu, qw, j);
             const uint64_t qa_j = __shfl_sync(0xffffffffu, qa, j);
             const uint64_t ta_j = __shfl_sync(0xffffffffu, ta, j);
-            const uint64_t b_j = __shfl_sync(0xffffffffu, base, j);
             const uint32_t wi = x - pre_j;
-            dst[u] = reinterpret_cast<uint4 *>(seq + b_j) + wi;
             if (x < total)
                 v[u] = wi < qw_j ? reinterpret_cast<const uint4 *>(qa_j)[wi]
                                  : reinterpret_cast<const uint4 *>(ta_j)[wi - qw_j];
         }
 #pragma unroll
-        for (int u = 0; u < U; ++u)
-            if (x0 + (uint32_t)u * 32u + lane < total) *dst[u] = v[u];
+        for (int u = 0; u < U; ++u) {
+            const uint32_t x = x0 + (uint32_t)u * 32u + lane;
+            if (x < total) dst[x] = v[u];
+        }
     }
 }
 #endif

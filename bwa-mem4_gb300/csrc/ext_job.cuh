@@ -66,6 +66,35 @@ __host__ __device__ inline bool ext_pair_lanes_ok(int o_del, int e_del, int o_in
     return (long long)o_del + e_del <= 16384 && (long long)o_ins + e_ins <= 16384;
 }
 
+// Target bases of a job read as aligned 32-bit words, the next word loaded a word
+// ahead (four to seven rows of prefetch for the row loop).  A word is read only
+// when it holds at least one byte of the target, so it lies in mapped memory.
+struct TargetStream {
+    const uint32_t *w;
+    uint32_t cur, nxt;
+    int b, end;  // byte index of the current row from w, and one past the last
+    __device__ __forceinline__ void init(const uint8_t *t, int tlen)
+    {
+        const uintptr_t a = reinterpret_cast<uintptr_t>(t);
+        w = reinterpret_cast<const uint32_t *>(a & ~(uintptr_t)3);
+        b = (int)(a & 3);
+        end = b + tlen;
+        cur = tlen > 0 ? w[0] : 0u;
+        nxt = end > 4 ? w[1] : 0u;
+    }
+    __device__ __forceinline__ uint32_t next()
+    {
+        const uint32_t c = (cur >> ((b & 3) * 8)) & 0xffu;
+        ++b;
+        if ((b & 3) == 0) {
+            cur = nxt;
+            const int k = (b >> 2) + 1;
+            if (k * 4 < end) nxt = w[k];
+        }
+        return c;
+    }
+};
+
 // Runs job J; returns the ExtendResult, adds the inner-loop iterations to ncells.
 template <class F, int TB>
 __device__ __forceinline__ bwacuda_ext_result ext_run_job(typename F::T *__restrict__ cell,
@@ -109,10 +138,10 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job(typename F::T *__restr
     const int w = clamp_band(J.w < 0 ? 0 : J.w, qlen, P.sc.max_sc, P.end_bonus, o_ins, e_ins, o_del, e_del);
     int best = h0, best_i = -1, best_j = -1, best_ie = -1, gscore = -1, max_off = 0;
     int beg = 0, end = qlen;
-    uint32_t tnext = tlen > 0 ? t[0] : 0u;
+    TargetStream ts;
+    ts.init(t, tlen);
     for (int i = 0; i < tlen; ++i) {
-        uint32_t tc = tnext;
-        if (i + 1 < tlen) tnext = t[i + 1];
+        uint32_t tc = ts.next();
         bad |= tc >= (uint32_t)m;
         tc &= 7u;
         const uint32_t plo = P.sc.prof[tc][0], phi = P.sc.prof[tc][1];
@@ -370,7 +399,8 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
     const int w = clamp_band(J.w < 0 ? 0 : J.w, qlen, P.sc.max_sc, P.end_bonus, o_ins, e_ins, o_del, e_del);
     int best = h0, best_i = -1, best_j = -1, best_ie = -1, gscore = -1, max_off = 0;
     int beg = 0, end = qlen;
-    uint32_t tnext = tlen > 0 ? t[0] : 0u;
+    TargetStream ts;
+    ts.init(t, tlen);
     // 16x2 broadcasts of the negated gap costs
     const uint32_t noe_ins2 = (uint32_t)(-oe_ins & 0xffff) * 0x10001u;
     const uint32_t noe_del2 = (uint32_t)(-oe_del & 0xffff) * 0x10001u;
@@ -378,8 +408,7 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
     const uint32_t ne_ins2 = (uint32_t)(-e_ins & 0xffff) * 0x10001u;
     const uint32_t fsel2 = 0x8000u | ((uint32_t)(-e_ins & 0xffff) << 16);
     for (int i = 0; i < tlen; ++i) {
-        uint32_t tc = tnext;
-        if (i + 1 < tlen) tnext = t[i + 1];
+        uint32_t tc = ts.next();
         bad |= tc >= (uint32_t)m;
         tc &= 7u;
         const uint32_t plo = P.sc.prof[tc][0], phi = P.sc.prof[tc][1];

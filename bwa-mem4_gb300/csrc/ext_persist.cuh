@@ -7,6 +7,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "common.cuh"
 #include "ext_job.cuh"
 #include "kernels.h"
@@ -120,6 +122,26 @@ ext_persist_pair_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_j
 
 constexpr size_t SMEM_MAX = 227u * 1024u;
 
+// Resident blocks per SM of a persistent launch: the occupancy limit, lowered so
+// that L.reserve_regs registers and L.reserve_threads threads stay free (at least
+// one block).  Registers are allocated per warp in steps of 256.
+template <class K>
+cudaError_t persist_blocks_per_sm(K kern, int tb, size_t smem, const PersistLaunch &L, int &per_sm)
+{
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tb, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidValue;
+    if (L.reserve_regs > 0 || L.reserve_threads > 0) {
+        cudaFuncAttributes fa;
+        if ((e = cudaFuncGetAttributes(&fa, kern)) != cudaSuccess) return e;
+        const int regs_block = ((fa.numRegs * 32 + 255) / 256) * 256 * (tb / 32);
+        const int cap_r = regs_block > 0 ? (L.sm_regs - L.reserve_regs) / regs_block : per_sm;
+        const int cap_t = (L.sm_threads - L.reserve_threads) / tb;
+        per_sm = std::max(1, std::min(per_sm, std::min(cap_r, cap_t)));
+    }
+    return cudaSuccess;
+}
+
 template <class F, int TB, int GRAB>
 cudaError_t launch_persist_tb(const PersistLaunch &L, const ExtBucketDef &d, uint32_t *table, int nsm)
 {
@@ -129,9 +151,7 @@ cudaError_t launch_persist_tb(const PersistLaunch &L, const ExtBucketDef &d, uin
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TB, smem);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) return cudaErrorInvalidValue;
+    if ((e = persist_blocks_per_sm(kern, TB, smem, L, per_sm)) != cudaSuccess) return e;
     const int grid = per_sm * nsm;
     kern<<<grid, TB, smem, L.stream>>>(L.seq, L.jobs, L.order, table, L.P, d.qcap, L.out, L.err, L.cells);
     return cudaGetLastError();
@@ -151,9 +171,7 @@ cudaError_t launch_persist_pair_tb(const PersistLaunch &L, const ExtBucketDef &d
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TB, smem);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) return cudaErrorInvalidValue;
+    if ((e = persist_blocks_per_sm(kern, TB, smem, L, per_sm)) != cudaSuccess) return e;
     kern<<<per_sm * nsm, TB, smem, L.stream>>>(L.seq, L.jobs, L.order, table, L.P, d.qcap, L.out, L.err, L.cells);
     return cudaGetLastError();
 }

@@ -29,6 +29,10 @@ struct PersistLaunch {
     unsigned long long *cells;
     int grab;  // 32-job rounds a warp takes per work-counter grab
     cudaStream_t stream;
+    // registers and threads per SM the persistent blocks leave free for kernels
+    // that run beside them (0: fill the SM); sm_regs / sm_threads are the SM's
+    int reserve_regs = 0, reserve_threads = 0;
+    int sm_regs = 65536, sm_threads = 2048;
 };
 
 int ext_bucket_defs(ExtBucketDef *defs, int max_defs, int step);
