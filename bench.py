@@ -74,6 +74,8 @@ def parse():
     ap.add_argument("--case", choices=["ext-batched", "ext-plain", "ext-mixed", "ext-gather", "rescue", "global"],
                     help="profiling case: run the small workload twice through one path, no timing")
     ap.add_argument("--lanes", type=int, default=8, help="rescue case: wavefront lanes per job")
+    ap.add_argument("--h0-add", type=int, default=0,
+                    help="extension cases: add this to every h0 (300 moves read pairs into the 16-bit cell class)")
     return ap.parse_args()
 
 
@@ -488,6 +490,7 @@ def run_case(args):
     ctx.set_option(B.OPT_GRAPHS, 0)  # plain stream launches (no graph nodes) under the profiler
     if args.case in ("ext-batched", "ext-plain", "ext-mixed"):
         js = B.synth_ext(3 if args.case == "ext-mixed" else 2, args.jobs, seed=0)
+        js.h0 = js.h0 + args.h0_add
         d_seq = torch.from_numpy(js.seq).cuda()
         d_jobs = torch.from_numpy(js.dev_ext_jobs().view(np.uint8)).cuda()
         d_out = torch.zeros(len(js) * 24, dtype=torch.uint8, device="cuda")
