@@ -652,7 +652,7 @@ def main():
             ctx.reset_stats()
             barrier()
             t0 = time.perf_counter()
-            esteps = max(1, min(args.steps, 5))
+            esteps = max(1, min(args.steps, 10))
             for _ in range(esteps):
                 call()
             barrier()

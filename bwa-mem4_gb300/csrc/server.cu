@@ -153,8 +153,10 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // 16-byte words, then scans the copied bases and sets *status if any code is
 // >= m (the request then fails alone instead of failing its wave).  Both job
 // structs begin with query, target, qlen, tlen.
+constexpr int SRV_GATHER_THREADS = 128;
+
 template <int KIND>
-__global__ void __launch_bounds__(256) srv_gather_kernel(const void *__restrict__ hjobs, uint32_t n,
+__global__ void __launch_bounds__(SRV_GATHER_THREADS, 8) srv_gather_kernel(const void *__restrict__ hjobs, uint32_t n,
                                                          const uint64_t *__restrict__ goff,
                                                          const uint64_t *__restrict__ gsoff, uint8_t *__restrict__ arena,
                                                          uint64_t desc_abs, uint64_t soff_abs, uint64_t seq_abs,
@@ -378,14 +380,16 @@ void admit(ServerState *S)
             // once its event fires and its status word is still 0
             int nsm = 0;
             if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, S->c->device) != cudaSuccess || nsm < 1) nsm = 1;
-            const uint32_t grid = (uint32_t)std::min<size_t>((r->n * 32 + 255) / 256, (size_t)nsm * 2);
+            // one block per SM, in the room the waves' bucket kernels leave free
+            const uint32_t grid =
+                (uint32_t)std::min<size_t>((r->n * 32 + SRV_GATHER_THREADS - 1) / SRV_GATHER_THREADS, (size_t)nsm);
             const uint64_t scr_base = (r->off + r->scr_at) / 8;  // uint2 index from the arena base
             if (r->kind == 0)
-                srv_gather_kernel<0><<<grid, 256, 0, S->copy_stream>>>(r->ejobs, (uint32_t)r->n, r->goff.data(), nullptr,
+                srv_gather_kernel<0><<<grid, SRV_GATHER_THREADS, 0, S->copy_stream>>>(r->ejobs, (uint32_t)r->n, r->goff.data(), nullptr,
                                                                       S->d_arena, r->off + r->desc_at, 0,
                                                                       r->off + r->seq_at, 0, r->w, mm, &r->status);
             else
-                srv_gather_kernel<1><<<grid, 256, 0, S->copy_stream>>>(r->rjobs, (uint32_t)r->n, r->goff.data(),
+                srv_gather_kernel<1><<<grid, SRV_GATHER_THREADS, 0, S->copy_stream>>>(r->rjobs, (uint32_t)r->n, r->goff.data(),
                                                                       r->gsoff.data(), S->d_arena, r->off + r->desc_at,
                                                                       r->off + r->soff_at, r->off + r->seq_at, scr_base,
                                                                       0, mm, &r->status);
@@ -674,6 +678,8 @@ extern "C" int bwacuda_server_start(bwacuda_ctx *c, const bwacuda_server_config 
         if (e == cudaSuccess) e = w.h_flags.ensure(64);
         if (e == cudaSuccess) w.bb = batchbufs_create();
         if (e == cudaSuccess && !w.bb) e = cudaErrorMemoryAllocation;
+        // room for one admission-gather block per SM beside the wave's bucket kernels
+        if (e == cudaSuccess) batched_set_reserve(w.bb, SRV_GATHER_THREADS * 64, SRV_GATHER_THREADS);
     }
     if (e != cudaSuccess) {
         c->server = S;
