@@ -46,10 +46,31 @@ struct GlobalDevJob {
 };
 static_assert(sizeof(GlobalDevJob) == 48, "descriptor layout");
 
-// Shared memory of a block: bcap band slots of {H, E} and qcap query codes per thread.
-__host__ __device__ inline size_t global_smem(int bcap, int qcap, int tb)
+// Shared memory of a block: bcap band slots of {H, E} (two int32, or two int16 for
+// narrow jobs) and qcap query codes per thread.
+__host__ __device__ inline size_t global_smem(int bcap, int qcap, int tb, bool narrow = false)
 {
-    return (size_t)tb * ((size_t)bcap * 8 + (size_t)qcap);
+    return (size_t)tb * ((size_t)bcap * (narrow ? 4 : 8) + (size_t)qcap);
+}
+
+// 16-bit cells.  Every value of ksw_global2's DP is either reachable (a path score)
+// or derived from the MINUS_INF sentinel by adding scores and gap costs.  Path
+// scores of a job lie in [-D, D] and sentinel-derived values in MINUS_INF + [-D, D],
+// with D = (qlen + tlen) * max(o + e of either gap, -min score, max score) +
+// o_del + o_ins + o_del + e_del + o_ins + e_ins.  When D <= GLB_NARROW_D the int16
+// cells hold path scores as they are and sentinel-derived values as
+// GLB_NEG16 + (v - MINUS_INF): every sum, maximum and comparison of the recurrence
+// gives the same result in both forms (the two ranges stay apart and inside int16),
+// so traceback bytes and scores are identical.
+constexpr int GLB_NEG16 = -24576;
+constexpr int GLB_NARROW_D = 8000;
+struct GlbNarrowRule {
+    int cost;  // max(o_del + e_del, o_ins + e_ins, -min score, max score)
+    int base;  // o_del + o_ins + o_del + e_del + o_ins + e_ins
+};
+__host__ __device__ inline bool global_narrow(int qlen, int tlen, const GlbNarrowRule &r)
+{
+    return (long long)(qlen + (long long)tlen) * r.cost + r.base <= GLB_NARROW_D;
 }
 
 // Traceback bytes per row.
@@ -85,7 +106,27 @@ __device__ __forceinline__ void cigar_push(uint32_t *cig, int &n, uint32_t op, u
     cig[n++] = (len << 4) | op;
 }
 
-template <int TB>
+template <bool NARROW>
+struct GlbCell {
+    using T = int2;
+    static constexpr int NEG = MINUS_INF;
+    __device__ static __forceinline__ T pack(int h, int e) { return make_int2(h, e); }
+    __device__ static __forceinline__ int h(T c) { return c.x; }
+    __device__ static __forceinline__ int e(T c) { return c.y; }
+    __device__ static __forceinline__ int score32(int v) { return v; }
+};
+template <>
+struct GlbCell<true> {
+    using T = uint32_t;
+    static constexpr int NEG = GLB_NEG16;
+    __device__ static __forceinline__ T pack(int h, int e) { return ((uint32_t)h & 0xffffu) | ((uint32_t)e << 16); }
+    __device__ static __forceinline__ int h(T c) { return (int)(int16_t)(c & 0xffffu); }
+    __device__ static __forceinline__ int e(T c) { return (int)c >> 16; }
+    // sentinel-derived values sit below -16384, path scores above
+    __device__ static __forceinline__ int score32(int v) { return v < -16384 ? MINUS_INF + (v - GLB_NEG16) : v; }
+};
+
+template <int TB, bool NARROW>
 __global__ void __launch_bounds__(TB)
 global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restrict__ jobs,
                   const uint32_t *__restrict__ order, uint32_t base, uint32_t count,
@@ -99,8 +140,11 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
     unsigned long long ncells = 0;
     if (t >= count) return;
     const uint32_t k = order ? order[base + t] : base + t;
-    int2 *cell = reinterpret_cast<int2 *>(smem_raw) + tid;        // cell[x * TB]: {H, E} of band slot x
-    uint8_t *qs = smem_raw + (size_t)bcap * 8 * TB + tid;          // qs[j * TB]: query code
+    using C = GlbCell<NARROW>;
+    using CellT = typename C::T;
+    constexpr int NEG = C::NEG;  // MINUS_INF in this cell form
+    CellT *cell = reinterpret_cast<CellT *>(smem_raw) + tid;       // cell[x * TB]: {H, E} of band slot x
+    uint8_t *qs = smem_raw + (size_t)bcap * sizeof(CellT) * TB + tid;  // qs[j * TB]: query code
     const GlobalDevJob J = jobs[k];
     const int qlen = J.qlen, tlen = J.tlen;
     const int w = J.w < 0 ? 0 : J.w;
@@ -125,16 +169,16 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
     // row -1: the origin, a leading insertion over columns 1..w, unreachable beyond
     // (slots 0..B-1 hold columns 0..B-1, which covers every column row 0 reads)
     for (int j = 0; j < B; ++j) {
-        int h = MINUS_INF;
+        int h = NEG;
         if (j == 0) h = 0;
         else if (j <= w) h = -(sc.o_ins + sc.e_ins * j);
-        cell[(size_t)j * TB] = make_int2(h, MINUS_INF);
+        cell[(size_t)j * TB] = C::pack(h, NEG);
     }
     for (int i = 0; i < tlen; ++i) {
-        int f = MINUS_INF;
+        int f = NEG;
         const int beg = i > w ? i - w : 0;
         const int end = i + w + 1 < qlen ? i + w + 1 : qlen;
-        int h1 = beg == 0 ? -(sc.o_del + sc.e_del * (i + 1)) : MINUS_INF;
+        int h1 = beg == 0 ? -(sc.o_del + sc.e_del * (i + 1)) : NEG;
         uint32_t tc = tg[i];
         bad |= tc >= (uint32_t)sc.m;
         tc = tc < (uint32_t)sc.m ? tc : (uint32_t)PAD_CODE;
@@ -143,9 +187,9 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
         uint32_t word[4] = {0u, 0u, 0u, 0u};
         int x = beg % (B > 0 ? B : 1);  // slot of column j
         for (int j = beg; j < end; ++j) {
-            int2 *cp = cell + (size_t)x * TB;
-            const int2 he = *cp;
-            int mm = he.x, e = he.y;
+            CellT *cp = cell + (size_t)x * TB;
+            const CellT he = *cp;
+            int mm = C::h(he), e = C::e(he);
             mm += prof_score(plo, phi, qs[(size_t)j * TB]);
             uint32_t d = mm < e ? 1u : 0u;
             int h = mm >= e ? mm : e;
@@ -154,7 +198,7 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
             e -= sc.e_del;
             if (e > tt) d |= 1u << 2;
             else e = tt;
-            *cp = make_int2(h1, e);  // H(i, j-1) for the next row's diagonal; E(i+1, j)
+            *cp = C::pack(h1, e);  // H(i, j-1) for the next row's diagonal; E(i+1, j)
             h1 = h;
             tt = mm - oe_ins;
             f -= sc.e_ins;
@@ -168,7 +212,7 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
             }
             if (++x == B) x = 0;
         }
-        if (B > 0) cell[(size_t)(end % B) * TB] = make_int2(h1, MINUS_INF);
+        if (B > 0) cell[(size_t)(end % B) * TB] = C::pack(h1, NEG);
         // band cells this row did not reach read as 0, as in the reference's zeroed matrix
         for (int ci = end > beg ? (end - beg + 15) >> 4 : 0; ci < (n_col + 15) >> 4; ++ci)
             zr[ci] = make_uint4(0u, 0u, 0u, 0u);
@@ -178,7 +222,7 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
     // column, else still its row -1 value (the bands' ends never decrease)
     const int end_last = tlen > 0 ? (tlen + w < qlen ? tlen + w : qlen) : -1;
     int score;
-    if (end_last == qlen) score = cell[(size_t)(qlen % B) * TB].x;
+    if (end_last == qlen) score = C::score32(C::h(cell[(size_t)(qlen % B) * TB]));
     else score = qlen == 0 ? 0 : (qlen <= w ? -(sc.o_ins + sc.e_ins * qlen) : MINUS_INF);
     score_out[k] = score;
     // traceback from the band's last cell of the last row
@@ -243,15 +287,15 @@ __device__ __forceinline__ bool gjob_ok(const bwacuda_global_job &J)
 // bucket.  flags[0]: input error bits.  bstat[2b], bstat[2b+1]: bucket b's max
 // band slots and max query length.
 __global__ void glb_plan_kernel(const bwacuda_global_job *__restrict__ hj, uint32_t n, int qlim,
-                                uint64_t *__restrict__ seq_sz, uint64_t *__restrict__ cig_sz,
+                                GlbNarrowRule nr, uint64_t *__restrict__ seq_sz, uint64_t *__restrict__ cig_sz,
                                 uint64_t *__restrict__ z_sz, uint32_t *__restrict__ keys, uint32_t *__restrict__ idx,
-                                uint32_t *__restrict__ flags, uint32_t *__restrict__ bstat)
+                                uint32_t *__restrict__ flags, uint32_t *__restrict__ bstat, uint32_t *__restrict__ bwide)
 {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t k0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); k0 < n; k0 += stride) {
         const uint32_t k = k0 + (threadIdx.x & 31u);
         int ql = 0, tl = 0, bs = 0, bucket = 0;
-        bool bad = false;
+        bool bad = false, wide = false;
         if (k < n) {
             const bwacuda_global_job J = hj[k];
             const bool ok = gjob_ok(J);
@@ -263,6 +307,7 @@ __global__ void glb_plan_kernel(const bwacuda_global_job *__restrict__ hj, uint3
             z_sz[k] = (uint64_t)tl * (uint64_t)global_zrow(ql, J.w);
             bs = global_band_slots(ql, J.w);
             bucket = global_bucket(ql);
+            wide = !global_narrow(ql, tl, nr);
             const uint32_t qk = ql > 1023 ? 0u : 1023u - (uint32_t)ql;
             const uint32_t tk = tl > 4095 ? 0u : 4095u - (uint32_t)tl;
             keys[k] = ((uint32_t)bucket << 22) | (qk << 12) | tk;
@@ -275,9 +320,11 @@ __global__ void glb_plan_kernel(const bwacuda_global_job *__restrict__ hj, uint3
         if (k < n) {
             const unsigned bmax = __reduce_max_sync(grp, (unsigned)bs);
             const unsigned qmax = __reduce_max_sync(grp, (unsigned)ql);
+            const unsigned anyw = __reduce_or_sync(grp, wide ? 1u : 0u);
             if ((int)(threadIdx.x & 31u) == __ffs(grp) - 1) {
                 atomicMax(bstat + 2 * bucket, bmax);
                 atomicMax(bstat + 2 * bucket + 1, qmax);
+                if (anyw) atomicOr(bwide + bucket, 1u);
             }
         }
     }
@@ -360,13 +407,13 @@ __global__ void glb_store_kernel(const GlobalDevJob *__restrict__ dj, uint32_t n
     }
 }
 
-template <int TB>
+template <int TB, bool NARROW>
 cudaError_t launch_global_tb(const uint8_t *seq, const GlobalDevJob *jobs, const uint32_t *order, uint32_t base,
                              uint32_t count, const Scoring &sc, int bcap, int qcap, uint8_t *z, uint32_t *cig,
                              int32_t *score, int32_t *ncig, uint32_t *err, unsigned long long *cells, cudaStream_t s)
 {
-    const size_t smem = global_smem(bcap, qcap, TB);
-    auto kern = global_tpj_kernel<TB>;
+    const size_t smem = global_smem(bcap, qcap, TB, NARROW);
+    auto kern = global_tpj_kernel<TB, NARROW>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<(count + TB - 1) / TB, TB, smem, s>>>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig,
@@ -374,19 +421,48 @@ cudaError_t launch_global_tb(const uint8_t *seq, const GlobalDevJob *jobs, const
     return cudaGetLastError();
 }
 
+template <bool NARROW>
+cudaError_t launch_global_form(const uint8_t *seq, const GlobalDevJob *jobs, const uint32_t *order, uint32_t base,
+                               uint32_t count, const Scoring &sc, int bcap, int qcap, uint8_t *z, uint32_t *cig,
+                               int32_t *score, int32_t *ncig, uint32_t *err, unsigned long long *cells, cudaStream_t s)
+{
+    if (global_smem(bcap, qcap, 128, NARROW) <= SMEM_LIMIT / 2)
+        return launch_global_tb<128, NARROW>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig, err,
+                                             cells, s);
+    if (global_smem(bcap, qcap, 64, NARROW) <= SMEM_LIMIT)
+        return launch_global_tb<64, NARROW>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig, err,
+                                            cells, s);
+    return launch_global_tb<32, NARROW>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig, err,
+                                        cells, s);
+}
+
 // Jobs order[base .. base + count) (or base .. base + count without an order); bcap / qcap:
-// their largest band-slot count and query length.
+// their largest band-slot count and query length; narrow: every one of them fits the
+// 16-bit cells (global_narrow).
 cudaError_t launch_global(const uint8_t *seq, const GlobalDevJob *jobs, const uint32_t *order, uint32_t base,
-                          uint32_t count, const Scoring &sc, int bcap, int qcap, uint8_t *z, uint32_t *cig,
+                          uint32_t count, const Scoring &sc, int bcap, int qcap, bool narrow, uint8_t *z, uint32_t *cig,
                           int32_t *score, int32_t *ncig, uint32_t *err, unsigned long long *cells, cudaStream_t s)
 {
     if (count == 0) return cudaSuccess;
     if (bcap < 1) bcap = 1;
-    if (global_smem(bcap, qcap, 128) <= SMEM_LIMIT / 2)
-        return launch_global_tb<128>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig, err, cells, s);
-    if (global_smem(bcap, qcap, 64) <= SMEM_LIMIT)
-        return launch_global_tb<64>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig, err, cells, s);
-    return launch_global_tb<32>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig, err, cells, s);
+    if (narrow)
+        return launch_global_form<true>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig, err,
+                                        cells, s);
+    return launch_global_form<false>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig, err, cells,
+                                     s);
+}
+
+GlbNarrowRule global_narrow_rule(const Scoring &sc, int m, const int8_t *mat)
+{
+    int mn = 0, mx = 0;
+    for (int i = 0; i < m * m; ++i) {
+        mn = std::min(mn, (int)mat[i]);
+        mx = std::max(mx, (int)mat[i]);
+    }
+    GlbNarrowRule r;
+    r.cost = std::max(std::max(sc.o_del + sc.e_del, sc.o_ins + sc.e_ins), std::max(-mn, mx));
+    r.base = sc.o_del + sc.o_ins + sc.o_del + sc.e_del + sc.o_ins + sc.e_ins;
+    return r;
 }
 
 // Longest query a 32-thread block holds (its band slots are at most qlen + 1).
@@ -432,8 +508,9 @@ namespace {
 // The device-gather route: planning, gather, DP, compaction and the result stores
 // run as kernels that read and write the caller's host arrays through the host
 // page tables; the host launches and reads back four words per chunk.
-int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n, const Scoring &sc, int32_t *score,
-                        uint64_t *cigar_off, uint32_t *cigar, size_t cigar_cap)
+int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n, const Scoring &sc,
+                        const GlbNarrowRule &nrule, int32_t *score, uint64_t *cigar_off, uint32_t *cigar,
+                        size_t cigar_cap)
 {
     GlobalBufs &b = c->global->b;
     cudaStream_t s = c->stream;
@@ -462,8 +539,9 @@ int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n
         uint64_t *z_sz = cig_off + n1, *z_off = z_sz + n1;
         uint32_t *keys = reinterpret_cast<uint32_t *>(z_off + n1), *keys2 = keys + n1;
         uint32_t *idx = keys2 + n1, *order = idx + n1;
-        uint32_t *flags = static_cast<uint32_t *>(b.d_flags.p);  // [0] errors, [16..31] bucket stats, [32..47] bounds
-        uint32_t *bstat = flags + 16, *bounds = flags + 32;
+        // [0] errors, [16..31] bucket stats, [32..47] bounds, [48..55] bucket holds a job too wide for 16-bit cells
+        uint32_t *flags = static_cast<uint32_t *>(b.d_flags.p);
+        uint32_t *bstat = flags + 16, *bounds = flags + 32, *bwide = flags + 48;
         size_t t1 = 0, t2 = 0, t3 = 0;
         cub::DeviceScan::ExclusiveSum(nullptr, t1, (const uint64_t *)nullptr, (uint64_t *)nullptr, (int)cn + 1);
         cub::DeviceScan::ExclusiveSum(nullptr, t2, (const int32_t *)nullptr, (uint64_t *)nullptr, (int)cn + 1);
@@ -475,7 +553,8 @@ int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n
         if ((e = cudaMemsetAsync(cig_sz + cn, 0, 8, s)) != cudaSuccess) break;
         if ((e = cudaMemsetAsync(z_sz + cn, 0, 8, s)) != cudaSuccess) break;
         uint32_t grid = (uint32_t)std::min<size_t>((cn + 255) / 256, (size_t)nsm * 8);
-        glb_plan_kernel<<<grid, 256, 0, s>>>(hj, (uint32_t)cn, qlim, seq_sz, cig_sz, z_sz, keys, idx, flags, bstat);
+        glb_plan_kernel<<<grid, 256, 0, s>>>(hj, (uint32_t)cn, qlim, nrule, seq_sz, cig_sz, z_sz, keys, idx, flags,
+                                             bstat, bwide);
         if ((e = cudaGetLastError()) != cudaSuccess) break;
         if ((e = cub::DeviceScan::ExclusiveSum(b.d_tmp.p, t1, seq_sz, seq_off, (int)cn + 1, s)) != cudaSuccess) break;
         if ((e = cub::DeviceScan::ExclusiveSum(b.d_tmp.p, t1, cig_sz, cig_off, (int)cn + 1, s)) != cudaSuccess) break;
@@ -512,13 +591,13 @@ int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n
         uint64_t *d_doff = static_cast<uint64_t *>(b.d_doff.p);
         if ((e = cudaMemsetAsync(d_ncig + cn, 0, 4, s)) != cudaSuccess) break;
         // one launch per non-empty length bucket, sized by the bucket's own maxima
-        const uint32_t *hb = hf + 16, *hbd = hf + 32;
+        const uint32_t *hb = hf + 16, *hbd = hf + 32, *hbw = hf + 48;
         for (int bk = 0; bk < GLB_NBUCKETS && e == cudaSuccess; ++bk) {
             const uint32_t b0 = hbd[2 * bk], b1 = hbd[2 * bk + 1];
             if (b1 <= b0) continue;
             e = launch_global(static_cast<const uint8_t *>(b.d_seq.p), dj, order, b0, b1 - b0, sc, (int)hb[2 * bk],
-                              (int)hb[2 * bk + 1], static_cast<uint8_t *>(b.d_z.p), static_cast<uint32_t *>(b.d_cig.p),
-                              d_score, d_ncig, d_err, d_cells, s);
+                              (int)hb[2 * bk + 1], hbw[bk] == 0u, static_cast<uint8_t *>(b.d_z.p),
+                              static_cast<uint32_t *>(b.d_cig.p), d_score, d_ncig, d_err, d_cells, s);
             c->stats.kernel_launches += 1;
         }
         if (e != cudaSuccess) break;
@@ -568,8 +647,9 @@ extern "C" int bwacuda_ksw_global2_batch(bwacuda_ctx *c, const bwacuda_global_jo
                                (c->host_gather == BWACUDA_GATHER_AUTO && c->pageable_access);
     if (device_gather) {
         if (!c->pageable_access) return BWACUDA_EUNSUPPORTED;
-        return global_batch_device(c, jobs, n, make_scoring(m, mat, o_del, e_del, o_ins, e_ins), score, cigar_off,
-                                   cigar, cigar_cap);
+        const Scoring scd = make_scoring(m, mat, o_del, e_del, o_ins, e_ins);
+        return global_batch_device(c, jobs, n, scd, global_narrow_rule(scd, m, mat), score, cigar_off, cigar,
+                                   cigar_cap);
     }
     const int qlim = global_max_qlen();
     for (size_t k = 0; k < n; ++k) {
@@ -584,6 +664,7 @@ extern "C" int bwacuda_ksw_global2_batch(bwacuda_ctx *c, const bwacuda_global_jo
     }
     GlobalBufs &b = c->global->b;
     const Scoring sc = make_scoring(m, mat, o_del, e_del, o_ins, e_ins);
+    const GlbNarrowRule nrule = global_narrow_rule(sc, m, mat);
     cudaStream_t s = c->stream;
     uint32_t *d_err = static_cast<uint32_t *>(c->d_misc.p);
     // chunks bounded in jobs and in traceback bytes
@@ -596,8 +677,10 @@ extern "C" int bwacuda_ksw_global2_batch(bwacuda_ctx *c, const bwacuda_global_jo
         size_t cn = 0;
         uint64_t zbytes = 0, cigw = 0, bytes = 0;
         int qmax = 0, bmax = 1;
+        bool narrow = true;
         while (c0 + cn < n && cn < kMaxJobs) {
             const bwacuda_global_job &J = jobs[c0 + cn];
+            narrow = narrow && global_narrow(J.qlen, J.tlen, nrule);
             const uint64_t jz = (uint64_t)J.tlen * (uint64_t)global_zrow(J.qlen, J.w);
             if (cn > 0 && zbytes + jz > kMaxZBytes) break;
             zbytes += jz;
@@ -650,7 +733,7 @@ extern "C" int bwacuda_ksw_global2_batch(bwacuda_ctx *c, const bwacuda_global_jo
         if ((e = cudaMemsetAsync(d_ncig + cn, 0, 4, s)) != cudaSuccess) break;
         c->stats.h2d_bytes += bytes + cn * sizeof(GlobalDevJob);
         e = launch_global(static_cast<const uint8_t *>(b.d_seq.p), static_cast<const GlobalDevJob *>(b.d_jobs.p),
-                          nullptr, 0, (uint32_t)cn, sc, bmax, qmax, static_cast<uint8_t *>(b.d_z.p),
+                          nullptr, 0, (uint32_t)cn, sc, bmax, qmax, narrow, static_cast<uint8_t *>(b.d_z.p),
                           static_cast<uint32_t *>(b.d_cig.p), d_score, d_ncig, d_err,
                           reinterpret_cast<unsigned long long *>((char *)c->d_misc.p + 8), s);
         if (e != cudaSuccess) break;

@@ -87,6 +87,45 @@ def test_random_lengths_bands_and_scoring(gctx):
     _check(gctx, js, mat, 7, 1, 5, 2)
 
 
+def _pairs_with_edits(rng, lengths, ends=20):
+    qs, ts = [], []
+    for L in lengths:
+        t = rng.integers(0, 4, int(L)).tolist()
+        q = list(t)
+        for _ in range(int(rng.integers(0, 8))):
+            p = int(rng.integers(0, max(1, len(q))))
+            r = rng.random()
+            if r < 0.5 and q:
+                q[p] = int(rng.integers(0, 4))
+            elif r < 0.75:
+                del q[p:p + int(rng.integers(1, 4))]
+            else:
+                q[p:p] = rng.integers(0, 4, int(rng.integers(1, 4))).tolist()
+        ts.append(t + rng.integers(0, 4, int(rng.integers(0, ends))).tolist())
+        qs.append(q)
+    return qs, ts
+
+
+def test_narrow_and_wide_cells(gctx):
+    # Jobs whose (qlen + tlen) x (largest per-step cost) stays small run in 16-bit cells, the
+    # rest in 32-bit cells; a batch mixes both (long reads in their own buckets, and one
+    # length bucket holding both kinds through long targets), and large gap costs make every
+    # job wide.  Sentinel values enter every band edge (H left of the band, E entering it), so
+    # the traceback bytes compare sentinel-derived values in both cell forms.
+    rng = np.random.default_rng(23)
+    lengths = np.concatenate([rng.integers(40, 250, 300), rng.integers(560, 760, 60), rng.integers(260, 320, 60)])
+    qs, ts = _pairs_with_edits(rng, lengths)
+    for k in range(360, 390):  # same query-length bucket as the next 30, targets long enough to be wide
+        ts[k] = ts[k] + rng.integers(0, 4, 1200).tolist()
+    ws = [int(rng.choice([3, 12, 40, 150])) for _ in qs]
+    js = B.JobSet.from_lists(qs, ts, w=ws)
+    keep = np.array([k for k in range(len(qs)) if oracle.global2(qs[k], ts[k], ws[k]) is not None])
+    js = js.take(keep)
+    _check(gctx, js)
+    _check(gctx, js, oracle.scmat(2, 5), 5, 2, 4, 3)
+    _check(gctx, js, oracle.scmat(1, 4), 3000, 1, 2000, 1)
+
+
 def test_edge_conventions(gctx):
     # empty query, empty target, both empty, narrow bands that cannot reach the corner
     qs = [[], [1, 2, 3], [], [0, 1, 2, 3] * 10, [0] * 30, [1, 2]]
