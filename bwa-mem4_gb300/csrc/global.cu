@@ -386,23 +386,23 @@ __global__ void __launch_bounds__(256) glb_gather_kernel(const bwacuda_global_jo
 }
 
 // Results straight into the caller's arrays: score[k], cigar_off[k + 1] = base + doff[k + 1],
-// and (when the chunk's runs fit the caller's capacity) the runs themselves, one warp per job.
+// and (when the chunk's runs fit the caller's capacity) the runs themselves.  One thread per
+// job: consecutive jobs' scores, offsets and runs lie at consecutive host addresses, so a
+// warp's stores coalesce.
 __global__ void glb_store_kernel(const GlobalDevJob *__restrict__ dj, uint32_t n, const int32_t *__restrict__ dscore,
                                  const uint32_t *__restrict__ cig, const int32_t *__restrict__ ncig,
                                  const uint64_t *__restrict__ doff, uint64_t out_base, size_t cap,
                                  int32_t *__restrict__ hscore, uint64_t *__restrict__ hoff, uint32_t *__restrict__ hcig)
 {
     const bool fits = hcig != nullptr && out_base + doff[n] <= cap;
-    const uint32_t lane = threadIdx.x & 31u;
-    for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < n; k += (gridDim.x * blockDim.x) >> 5) {
-        if (lane == 0) {
-            hscore[k] = dscore[k];
-            hoff[k + 1] = out_base + doff[k + 1];
-        }
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        hscore[k] = dscore[k];
+        hoff[k + 1] = out_base + doff[k + 1];
         if (fits) {
             const uint32_t *src = cig + dj[k].cig_off;
             uint32_t *dst = hcig + out_base + doff[k];
-            for (int x = (int)lane; x < ncig[k]; x += 32) dst[x] = src[x];
+            const int nk = ncig[k];
+            for (int x = 0; x < nk; ++x) dst[x] = src[x];
         }
     }
 }
@@ -602,7 +602,7 @@ int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n
         }
         if (e != cudaSuccess) break;
         if ((e = cub::DeviceScan::ExclusiveSum(b.d_tmp.p, t2, d_ncig, d_doff, (int)cn + 1, s)) != cudaSuccess) break;
-        grid = (uint32_t)std::min<size_t>((cn * 32 + 255) / 256, (size_t)nsm * 8);
+        grid = (uint32_t)std::min<size_t>((cn + 255) / 256, (size_t)nsm * 8);
         glb_store_kernel<<<grid, 256, 0, s>>>(dj, (uint32_t)cn, d_score, static_cast<const uint32_t *>(b.d_cig.p), d_ncig,
                                              d_doff, out_base, cigar ? cigar_cap : 0, score + c0, cigar_off + c0, cigar);
         if ((e = cudaGetLastError()) != cudaSuccess) break;
