@@ -184,13 +184,23 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
         tc = tc < (uint32_t)sc.m ? tc : (uint32_t)PAD_CODE;
         const uint32_t plo = sc.prof[tc & 7u][0], phi = sc.prof[tc & 7u][1];
         uint4 *zr = reinterpret_cast<uint4 *>(zj + (size_t)i * zrow);
-        uint32_t word[4] = {0u, 0u, 0u, 0u};
+        // direction bytes of the current 16-column group, in two 64-bit registers
+        uint64_t zlo = 0, zhi = 0;
         int x = beg % (B > 0 ? B : 1);  // slot of column j
+        // Software pipelined: column j+1's slot and query code load while column j computes.
+        // A row's columns occupy distinct slots (end - beg < B), so the look-ahead reads the
+        // previous row's value of that slot, as the in-order read would.
+        CellT cn = cell[(size_t)x * TB];
+        uint32_t qn = beg < end ? qs[(size_t)beg * TB] : 0u;
         for (int j = beg; j < end; ++j) {
             CellT *cp = cell + (size_t)x * TB;
-            const CellT he = *cp;
+            const CellT he = cn;
+            const uint32_t qc = qn;
+            if (++x == B) x = 0;
+            cn = cell[(size_t)x * TB];
+            if (j + 1 < end) qn = qs[(size_t)(j + 1) * TB];
             int mm = C::h(he), e = C::e(he);
-            mm += prof_score(plo, phi, qs[(size_t)j * TB]);
+            mm += prof_score(plo, phi, qc);
             uint32_t d = mm < e ? 1u : 0u;
             int h = mm >= e ? mm : e;
             if (!(h >= f)) { d = 2u; h = f; }
@@ -205,12 +215,13 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
             if (f > tt) d |= 2u << 4;
             else f = tt;
             const int jj = j - beg;
-            word[(jj >> 2) & 3] |= d << ((jj & 3) * 8);
-            if ((jj & 15) == 15 || j == end - 1) {
-                zr[jj >> 4] = make_uint4(word[0], word[1], word[2], word[3]);
-                word[0] = word[1] = word[2] = word[3] = 0u;
+            const int p = jj & 15;
+            if (p < 8) zlo |= (uint64_t)d << (8 * p);
+            else zhi |= (uint64_t)d << (8 * (p - 8));
+            if (p == 15 || j == end - 1) {
+                zr[jj >> 4] = make_uint4((uint32_t)zlo, (uint32_t)(zlo >> 32), (uint32_t)zhi, (uint32_t)(zhi >> 32));
+                zlo = zhi = 0;
             }
-            if (++x == B) x = 0;
         }
         if (B > 0) cell[(size_t)(end % B) * TB] = C::pack(h1, NEG);
         // band cells this row did not reach read as 0, as in the reference's zeroed matrix
@@ -426,10 +437,23 @@ cudaError_t launch_global_form(const uint8_t *seq, const GlobalDevJob *jobs, con
                                uint32_t count, const Scoring &sc, int bcap, int qcap, uint8_t *z, uint32_t *cig,
                                int32_t *score, int32_t *ncig, uint32_t *err, unsigned long long *cells, cudaStream_t s)
 {
-    if (global_smem(bcap, qcap, 128, NARROW) <= SMEM_LIMIT / 2)
+    // the block size that keeps the most warps resident (shared memory bounds this kernel;
+    // 228 KB per SM, 1 KB of it reserved per block), larger blocks on ties
+    int best_tb = 32, best_warps = 0;
+    for (int tb = 128; tb >= 32; tb >>= 1) {
+        const size_t sm = global_smem(bcap, qcap, tb, NARROW);
+        if (sm > SMEM_LIMIT) continue;
+        const int blocks = std::min<int>(32, (int)((228u * 1024u) / (sm + 1024u)));
+        const int warps = std::min(64, blocks * tb / 32);
+        if (warps > best_warps) {
+            best_warps = warps;
+            best_tb = tb;
+        }
+    }
+    if (best_tb == 128)
         return launch_global_tb<128, NARROW>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig, err,
                                              cells, s);
-    if (global_smem(bcap, qcap, 64, NARROW) <= SMEM_LIMIT)
+    if (best_tb == 64)
         return launch_global_tb<64, NARROW>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig, err,
                                             cells, s);
     return launch_global_tb<32, NARROW>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig, err,
