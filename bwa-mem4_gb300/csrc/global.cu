@@ -47,10 +47,10 @@ struct GlobalDevJob {
 static_assert(sizeof(GlobalDevJob) == 48, "descriptor layout");
 
 // Shared memory of a block: bcap band slots of {H, E} (two int32, or two int16 for
-// narrow jobs) and qcap query codes per thread.
+// narrow jobs) and qcap + 1 query codes per thread (one spare for the look-ahead).
 __host__ __device__ inline size_t global_smem(int bcap, int qcap, int tb, bool narrow = false)
 {
-    return (size_t)tb * ((size_t)bcap * (narrow ? 4 : 8) + (size_t)qcap);
+    return (size_t)tb * ((size_t)bcap * (narrow ? 4 : 8) + (size_t)qcap + 1);
 }
 
 // 16-bit cells.  Every value of ksw_global2's DP is either reachable (a path score)
@@ -184,21 +184,21 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
         tc = tc < (uint32_t)sc.m ? tc : (uint32_t)PAD_CODE;
         const uint32_t plo = sc.prof[tc & 7u][0], phi = sc.prof[tc & 7u][1];
         uint4 *zr = reinterpret_cast<uint4 *>(zj + (size_t)i * zrow);
-        // direction bytes of the current 16-column group, in two 64-bit registers
-        uint64_t zlo = 0, zhi = 0;
+        // direction bytes: four columns gather in acc, four words make a 16-column store
+        uint32_t acc = 0, zw0 = 0, zw1 = 0, zw2 = 0, zw3 = 0;
         int x = beg % (B > 0 ? B : 1);  // slot of column j
         // Software pipelined: column j+1's slot and query code load while column j computes.
         // A row's columns occupy distinct slots (end - beg < B), so the look-ahead reads the
         // previous row's value of that slot, as the in-order read would.
         CellT cn = cell[(size_t)x * TB];
-        uint32_t qn = beg < end ? qs[(size_t)beg * TB] : 0u;
+        uint32_t qn = qs[(size_t)beg * TB];  // beg <= qlen: inside the qcap + 1 codes
         for (int j = beg; j < end; ++j) {
             CellT *cp = cell + (size_t)x * TB;
             const CellT he = cn;
             const uint32_t qc = qn;
             if (++x == B) x = 0;
             cn = cell[(size_t)x * TB];
-            if (j + 1 < end) qn = qs[(size_t)(j + 1) * TB];
+            qn = qs[(size_t)(j + 1) * TB];  // j + 1 <= qlen
             int mm = C::h(he), e = C::e(he);
             mm += prof_score(plo, phi, qc);
             uint32_t d = mm < e ? 1u : 0u;
@@ -215,12 +215,19 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
             if (f > tt) d |= 2u << 4;
             else f = tt;
             const int jj = j - beg;
-            const int p = jj & 15;
-            if (p < 8) zlo |= (uint64_t)d << (8 * p);
-            else zhi |= (uint64_t)d << (8 * (p - 8));
-            if (p == 15 || j == end - 1) {
-                zr[jj >> 4] = make_uint4((uint32_t)zlo, (uint32_t)(zlo >> 32), (uint32_t)zhi, (uint32_t)(zhi >> 32));
-                zlo = zhi = 0;
+            acc |= d << (8 * (jj & 3));
+            const bool last = j == end - 1;
+            if ((jj & 3) == 3 || last) {
+                const int g = (jj >> 2) & 3;
+                zw0 = g == 0 ? acc : zw0;
+                zw1 = g == 1 ? acc : zw1;
+                zw2 = g == 2 ? acc : zw2;
+                zw3 = g == 3 ? acc : zw3;
+                acc = 0;
+                if (g == 3 || last) {
+                    zr[jj >> 4] = make_uint4(zw0, zw1, zw2, zw3);
+                    zw0 = zw1 = zw2 = zw3 = 0;
+                }
             }
         }
         if (B > 0) cell[(size_t)(end % B) * TB] = C::pack(h1, NEG);
@@ -540,7 +547,10 @@ int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n
     cudaStream_t s = c->stream;
     uint32_t *d_err = static_cast<uint32_t *>(c->d_misc.p);
     unsigned long long *d_cells = reinterpret_cast<unsigned long long *>((char *)c->d_misc.p + 8);
-    const size_t kChunk = 262144;
+    // chunks of 4 x BWACUDA_OPT_CHUNK_JOBS jobs, at most 1M (several waves of the longest
+    // bucket per launch), halved while a chunk's traceback matrices would exceed 16 GiB of HBM
+    const size_t kMaxZBytes = size_t(16) << 30;
+    size_t chunk = std::min(size_t(1) << 20, std::max<size_t>(c->chunk_jobs, 1) * 4);
     const int qlim = global_max_qlen();
     int nsm = 0;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || nsm < 1) nsm = 1;
@@ -551,8 +561,8 @@ int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n
     if ((e = b.d_flags.ensure(256)) != cudaSuccess) return cuda_status(e);
     if ((e = b.h_tot.ensure(512)) != cudaSuccess) return cuda_status(e);
     uint64_t *ht = static_cast<uint64_t *>(b.h_tot.p);
-    for (size_t c0 = 0; c0 < n && rc == BWACUDA_OK; c0 += kChunk) {
-        const size_t cn = std::min(kChunk, n - c0);
+    for (size_t c0 = 0, cn = 0; c0 < n && rc == BWACUDA_OK; c0 += cn) {
+        cn = std::min(chunk, n - c0);
         const bwacuda_global_job *hj = jobs + c0;
         // planning arrays: seq / cig / z sizes and offsets (cn + 1 each), keys and indices (two
         // copies each for the sort)
@@ -599,6 +609,11 @@ int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n
             for (size_t k = 0; k < cn; ++k)
                 if (hj[k].qlen > qlim && hj[k].qlen >= 0 && hj[k].tlen >= 0) rc = BWACUDA_EUNSUPPORTED;
             break;
+        }
+        if (ht[2] > kMaxZBytes && cn > 1024) {  // plan this range again in halves
+            chunk = cn / 2;
+            cn = 0;
+            continue;
         }
         if ((e = b.d_seq.ensure(ht[0] + 16)) != cudaSuccess) break;
         if ((e = b.d_cig.ensure(ht[1] * 4 + 16)) != cudaSuccess) break;

@@ -146,6 +146,17 @@ def test_edge_conventions(gctx):
         assert e.value.code == B.EUNSUPPORTED
 
 
+def test_many_chunks(gctx):
+    # small chunks (4 x 777 jobs on the device route, 262,144 on the host route) exercise the
+    # per-chunk output offsets and the narrow / wide choice per chunk and bucket
+    js = B.synth_global(20000, seed=6)
+    gctx.set_option(B.OPT_CHUNK_JOBS, 777)
+    try:
+        _check(gctx, js)
+    finally:
+        gctx.set_option(B.OPT_CHUNK_JOBS, 262144)
+
+
 def test_short_buffer_reports_sizes(gctx):
     js = B.synth_global(5000, seed=4)
     wsc, woffs, wwords = oracle.global2_batch(js)
