@@ -70,15 +70,17 @@ struct GlbNarrowRule {
 };
 __host__ __device__ inline bool global_narrow(int qlen, int tlen, const GlbNarrowRule &r)
 {
-    return (long long)(qlen + (long long)tlen) * r.cost + r.base <= GLB_NARROW_D;
+    // two steps of margin: the pair kernel also forms F and E one column / row past the matrix
+    return (long long)(qlen + (long long)tlen + 2) * r.cost + r.base <= GLB_NARROW_D;
 }
 
-// Traceback bytes per row.
+// Traceback bytes per row: the band's columns plus one (the pair kernel keeps a row's
+// bytes at column - (beg & ~1), so column pairs sit at even offsets), rounded up to 16.
 __host__ __device__ inline int global_zrow(int qlen, int w)
 {
     if (w < 0) w = 0;
     const long long nc = qlen < 2LL * w + 1 ? qlen : 2LL * w + 1;
-    return (int)((nc + 15) & ~15LL);
+    return (int)((nc + 1 + 15) & ~15LL);
 }
 
 // Query-length buckets of the device route (upper bounds, inclusive).
@@ -104,6 +106,40 @@ __device__ __forceinline__ void cigar_push(uint32_t *cig, int &n, uint32_t op, u
         return;
     }
     cig[n++] = (len << 4) | op;
+}
+
+// The reference's traceback (sw.rs:700-738) from the band's last cell of the last row over a
+// job's direction bytes; the CIGAR runs, reversed, into cg.  Returns the run count, or -1
+// where the reference's flat index leaves the matrix (its panic).  PAIR: the pair kernel's
+// row layout, a row's bytes starting at column beg & ~1.
+template <bool PAIR>
+__device__ int global_traceback(const uint8_t *zj, size_t zrow, int n_col, int qlen, int tlen, int w, uint32_t *cg)
+{
+    int nc = 0;
+    long i = (long)tlen - 1;
+    long kk = ((long)tlen - 1 + w + 1 < qlen ? (long)tlen - 1 + w + 1 : (long)qlen) - 1;
+    uint32_t which = 0;
+    while (i >= 0 && kk >= 0) {
+        const long beg = i > w ? i - w : 0;
+        // the reference reads the flat row-major matrix: an offset past the row lands in a later row
+        const long flat = i * (long)n_col + (kk - beg);
+        if (kk < beg || flat >= (long)n_col * tlen) return -1;
+        const long row = flat / n_col, col = flat - row * n_col;
+        const long shift = PAIR ? ((row > w ? row - w : 0) & 1) : 0;
+        const uint32_t d = zj[(size_t)row * zrow + (size_t)(col + shift)];
+        which = (d >> (which << 1)) & 3u;
+        if (which == 0) { cigar_push(cg, nc, 0, 1); --i; --kk; }
+        else if (which == 1) { cigar_push(cg, nc, 2, 1); --i; }
+        else { cigar_push(cg, nc, 1, 1); --kk; }
+    }
+    if (i >= 0) cigar_push(cg, nc, 2, (uint32_t)(i + 1));
+    if (kk >= 0) cigar_push(cg, nc, 1, (uint32_t)(kk + 1));
+    for (int a = 0, b = nc - 1; a < b; ++a, --b) {
+        const uint32_t x = cg[a];
+        cg[a] = cg[b];
+        cg[b] = x;
+    }
+    return nc;
 }
 
 template <bool NARROW>
@@ -243,38 +279,264 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
     if (end_last == qlen) score = C::score32(C::h(cell[(size_t)(qlen % B) * TB]));
     else score = qlen == 0 ? 0 : (qlen <= w ? -(sc.o_ins + sc.e_ins * qlen) : MINUS_INF);
     score_out[k] = score;
-    // traceback from the band's last cell of the last row
-    uint32_t *cg = cig + J.cig_off;
-    int nc = 0;
-    long i = (long)tlen - 1;
-    long kk = ((long)tlen - 1 + w + 1 < qlen ? (long)tlen - 1 + w + 1 : (long)qlen) - 1;
-    uint32_t which = 0;
-    bool range = false;
-    while (i >= 0 && kk >= 0) {
-        const long beg = i > w ? i - w : 0;
-        // the reference reads the flat row-major matrix: an offset past the row lands in a later row
-        const long flat = i * (long)n_col + (kk - beg);
-        if (kk < beg || flat >= (long)n_col * tlen) { range = true; break; }
-        const long row = flat / n_col, col = flat - row * n_col;
-        const uint32_t d = zj[(size_t)row * zrow + (size_t)col];
-        which = (d >> (which << 1)) & 3u;
-        if (which == 0) { cigar_push(cg, nc, 0, 1); --i; --kk; }
-        else if (which == 1) { cigar_push(cg, nc, 2, 1); --i; }
-        else { cigar_push(cg, nc, 1, 1); --kk; }
+    const int nc = global_traceback<false>(zj, zrow, n_col, qlen, tlen, w, cig + J.cig_off);
+    if (nc < 0) atomicOr(err, ERR_RANGE);
+    ncig_out[k] = nc < 0 ? 0 : nc;
+    if (bad) atomicOr(err, ERR_BASE);
+    atomicAdd(cells_total, ncells);
+}
+
+// Shared memory of a block for the pair kernel: the band slots as 8-byte pair words (bcap
+// rounded up to even) and the query as 16-bit selector pairs (one spare pair for the look-ahead).
+__host__ __device__ inline size_t global_smem_pair(int bcap, int qcap, int tb)
+{
+    return (size_t)tb * ((size_t)((bcap + 1) / 2) * 8 + (size_t)((qcap + 2) / 2 + 1) * 2);
+}
+
+// One column of the recurrence in 32-bit registers (the head / tail columns of a row in the pair
+// kernel), the scalar kernel's cell: in hd = H(i-1, j-1), e = E(i, j), f = F(i, j); out h, e =
+// E(i+1, j), f = F(i, j+1) and the direction byte.
+__device__ __forceinline__ uint32_t glb_cell(int hd, int &e, int &f, int s, int oe_del, int e_del, int oe_ins,
+                                             int e_ins, int &h)
+{
+    const int mm = hd + s;
+    uint32_t d = mm < e ? 1u : 0u;
+    h = mm >= e ? mm : e;
+    if (!(h >= f)) { d = 2u; h = f; }
+    int tt = mm - oe_del;
+    e -= e_del;
+    if (e > tt) d |= 1u << 2;
+    else e = tt;
+    tt = mm - oe_ins;
+    f -= e_ins;
+    if (f > tt) d |= 2u << 4;
+    else f = tt;
+    return d;
+}
+
+// Direction bytes of one row, kept at offset column - (beg & ~1) so column pairs land on
+// even offsets: 16-bit units gather into words, four words make a 16-byte store.
+struct GlbRowBytes {
+    uint4 *zr;
+    uint32_t cur = 0, w0 = 0, w1 = 0, w2 = 0, w3 = 0;
+    int last = -1;  // offset of the last byte put, -1: none
+    __device__ __forceinline__ void put(int off, uint32_t v, int nbytes)
+    {
+        cur |= v << (8 * (off & 3));
+        last = off + nbytes - 1;
+        if ((last & 3) == 3) flush_word();
     }
-    if (!range) {
-        if (i >= 0) cigar_push(cg, nc, 2, (uint32_t)(i + 1));
-        if (kk >= 0) cigar_push(cg, nc, 1, (uint32_t)(kk + 1));
-        for (int a = 0, b = nc - 1; a < b; ++a, --b) {
-            const uint32_t x = cg[a];
-            cg[a] = cg[b];
-            cg[b] = x;
+    __device__ __forceinline__ void flush_word()
+    {
+        const int g = (last >> 2) & 3;
+        w0 = g == 0 ? cur : w0;
+        w1 = g == 1 ? cur : w1;
+        w2 = g == 2 ? cur : w2;
+        w3 = g == 3 ? cur : w3;
+        cur = 0;
+        if (g == 3) {
+            zr[last >> 4] = make_uint4(w0, w1, w2, w3);
+            w0 = w1 = w2 = w3 = 0;
         }
-    } else {
-        nc = 0;
-        atomicOr(err, ERR_RANGE);
     }
-    ncig_out[k] = nc;
+    // the row's open word and group, then zero groups up to ngroups
+    __device__ __forceinline__ void finish(int ngroups)
+    {
+        int next = 0;
+        if (last >= 0) {
+            if ((last & 3) != 3) flush_word_partial();
+            if ((last & 15) != 15) zr[last >> 4] = make_uint4(w0, w1, w2, w3);
+            next = (last >> 4) + 1;
+        }
+        for (int g = next; g < ngroups; ++g) zr[g] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    __device__ __forceinline__ void flush_word_partial()
+    {
+        const int g = (last >> 2) & 3;
+        w0 = g == 0 ? cur : w0;
+        w1 = g == 1 ? cur : w1;
+        w2 = g == 2 ? cur : w2;
+        w3 = g == 3 ? cur : w3;
+        cur = 0;
+    }
+};
+
+// ksw_global2 on 16-bit pair cells (jobs that pass global_narrow): two columns per lane
+// operation, direction bits from the DPX max-with-predicate instructions.  Slot x of the
+// band (x = column mod B2, B2 the band slots rounded up to even) is lane x & 1 of pair word
+// x / 2: .x = (H, H), .y = (E, E).  Sentinel-derived values are kept as in GlbCell<true>.
+// All lane sums stay inside int16: values lie in [GLB_NEG16 - D, D] with D <= GLB_NARROW_D.
+template <int TB>
+__global__ void __launch_bounds__(TB)
+global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restrict__ jobs,
+                   const uint32_t *__restrict__ order, uint32_t base, uint32_t count,
+                   const __grid_constant__ Scoring sc, int bcap, int qcap, uint8_t *__restrict__ z,
+                   uint32_t *__restrict__ cig, int32_t *__restrict__ score_out, int32_t *__restrict__ ncig_out,
+                   uint32_t *__restrict__ err, unsigned long long *__restrict__ cells_total)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    using C = GlbCell<true>;
+    constexpr int NEG = GLB_NEG16;
+    const int tid = threadIdx.x;
+    const uint32_t t = blockIdx.x * TB + tid;
+    unsigned long long ncells = 0;
+    if (t >= count) return;
+    const uint32_t k = order ? order[base + t] : base + t;
+    const int bpairs = (bcap + 1) / 2;
+    uint2 *cell2 = reinterpret_cast<uint2 *>(smem_raw) + tid;                          // cell2[p * TB]
+    uint16_t *qs2 = reinterpret_cast<uint16_t *>(smem_raw + (size_t)bpairs * 8 * TB) + tid;  // qs2[jp * TB]
+    const GlobalDevJob J = jobs[k];
+    const int qlen = J.qlen, tlen = J.tlen;
+    const int w = J.w < 0 ? 0 : J.w;
+    const int n_col = qlen < 2 * w + 1 ? qlen : 2 * w + 1;
+    const int B = global_band_slots(qlen, w);
+    const int B2 = B + (B & 1), P2 = B2 / 2;
+    const int oe_del = sc.o_del + sc.e_del, oe_ins = sc.o_ins + sc.e_ins;
+    const uint8_t *q = seq + J.q_off;
+    const uint8_t *tg = seq + J.t_off;
+    uint8_t *zj = z + J.z_off;
+    const size_t zrow = (size_t)J.zrow;
+    bool bad = false;
+    if (P2 > bpairs || qlen > qcap) {  // the host sizes bcap / qcap from the launch's jobs
+        atomicOr(err, ERR_RANGE);
+        ncig_out[k] = 0;
+        return;
+    }
+    // query codes as prmt selector bytes 0x80 | c * 0x11 (two sign-extended 16-bit scores per
+    // prmt), two columns per 16-bit word; columns >= qlen are padding
+    for (int jp = 0; 2 * jp <= qlen; ++jp) {
+        uint32_t v = 0;
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int j = 2 * jp + u;
+            uint32_t c = j < qlen ? (uint32_t)q[j] : (uint32_t)PAD_CODE;
+            if (j < qlen) bad |= c >= (uint32_t)sc.m;
+            c = c < (uint32_t)sc.m || j >= qlen ? c : (uint32_t)PAD_CODE;
+            v |= (0x80u | (c & 7u) * 0x11u) << (8 * u);
+        }
+        qs2[(size_t)jp * TB] = (uint16_t)v;
+    }
+    // row -1 (as the scalar kernel): slot x holds column x
+    for (int p = 0; p < P2; ++p) {
+        uint32_t hx = 0;
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int j = 2 * p + u;
+            const int h = j == 0 ? 0 : (j <= w ? -(sc.o_ins + sc.e_ins * j) : NEG);
+            hx |= ((uint32_t)h & 0xffffu) << (16 * u);
+        }
+        cell2[(size_t)p * TB] = make_uint2(hx, ((uint32_t)NEG & 0xffffu) * 0x10001u);
+    }
+    const uint32_t MIN2 = 0x80008000u;
+    const uint32_t noe_ins2 = ((uint32_t)(-oe_ins) & 0xffffu) * 0x10001u;
+    const uint32_t noe_del2 = ((uint32_t)(-oe_del) & 0xffffu) * 0x10001u;
+    const uint32_t ne_ins2 = ((uint32_t)(-sc.e_ins) & 0xffffu) * 0x10001u;
+    const uint32_t ne_del2 = ((uint32_t)(-sc.e_del) & 0xffffu) * 0x10001u;
+    const int ngroups = (n_col + 1 + 15) >> 4;
+    for (int i = 0; i < tlen; ++i) {
+        const int beg = i > w ? i - w : 0;
+        const int end = i + w + 1 < qlen ? i + w + 1 : qlen;
+        int h1 = beg == 0 ? -(sc.o_del + sc.e_del * (i + 1)) : NEG;  // H(i, beg-1)
+        int f = NEG;                                                   // F(i, beg)
+        uint32_t tc = tg[i];
+        bad |= tc >= (uint32_t)sc.m;
+        tc = tc < (uint32_t)sc.m ? tc : (uint32_t)PAD_CODE;
+        const uint32_t plo = sc.prof[tc & 7u][0], phi = sc.prof[tc & 7u][1];
+        GlbRowBytes zb;
+        zb.zr = reinterpret_cast<uint4 *>(zj + (size_t)i * zrow);
+        const int base_off = beg & ~1;
+        int j = beg;
+        if (j < end && (j & 1)) {  // odd first column: the high lanes of its pair
+            const int x = j % B2;
+            uint2 cw = cell2[(size_t)(x >> 1) * TB];
+            int e = (int)cw.y >> 16, h;
+            const uint32_t sel = (uint32_t)qs2[(size_t)(j >> 1) * TB] >> 8;
+            const uint32_t d = glb_cell((int)cw.x >> 16, e, f, (int)prmt(plo, phi, (sel & 0xffu) * 0x101u | 0x8800u),
+                                        oe_del, sc.e_del, oe_ins, sc.e_ins, h);
+            cw.x = (cw.x & 0xffffu) | ((uint32_t)h1 << 16);
+            cw.y = (cw.y & 0xffffu) | ((uint32_t)e << 16);
+            cell2[(size_t)(x >> 1) * TB] = cw;
+            h1 = h;
+            zb.put(j - base_off, d, 1);
+            ++j;
+        }
+        if (j + 1 < end) {
+            // F(i, j) in fv's high lane, H(i, j-1) in h1v's high lane
+            uint32_t fv = (uint32_t)f << 16, h1v = (uint32_t)h1 << 16;
+            int p = (j % B2) >> 1;
+            uint2 wn = cell2[(size_t)p * TB];
+            uint32_t qn = qs2[(size_t)(j >> 1) * TB];
+            for (; j + 1 < end; j += 2) {
+                const uint2 cw = wn;
+                const uint32_t sel = qn;
+                const int pc = p;
+                if (++p == P2) p = 0;
+                wn = cell2[(size_t)p * TB];               // a row's columns use distinct slots
+                qn = qs2[(size_t)((j >> 1) + 1) * TB];    // j / 2 + 1 <= (qlen + 1) / 2: allocated
+                const uint32_t s2 = prmt(plo, phi, sel);  // (s_j, s_j+1)
+                const uint32_t M2 = __viaddmax_s16x2(cw.x, s2, MIN2);  // H(i-1, .-1) + s
+                bool pm_hi, pm_lo, ph_hi, ph_lo, pf_hi, pf_lo, pe_hi, pe_lo;
+                const uint32_t ME2 = __vibmax_s16x2(M2, cw.y, &pm_hi, &pm_lo);      // M >= E
+                const uint32_t tti2 = __viaddmax_s16x2(M2, noe_ins2, MIN2);         // M - oe_ins
+                // (F(i, j), F(i, j+1)): lane lo passes F(i, j) through, lane hi updates it
+                const uint32_t X = prmt(fv, tti2, 0x5432u);                         // (F(i,j), tti_j)
+                const uint32_t fvm = __viaddmax_s16x2(fv, ne_ins2, MIN2);           // hi: F(i,j) - e_ins
+                const uint32_t A2 = prmt(MIN2, fvm, 0x7610u);                       // (MIN, F(i,j) - e_ins)
+                const uint32_t F2 = __viaddmax_s16x2(X, 0u, A2);                     // max(X, A2)
+                const uint32_t H2 = __vibmax_s16x2(ME2, F2, &ph_hi, &ph_lo);        // max(M, E) >= F
+                const uint32_t F2m = __viaddmax_s16x2(F2, ne_ins2, MIN2);
+                fv = __vibmax_s16x2(tti2, F2m, &pf_hi, &pf_lo);                     // open >= extend
+                const uint32_t ttd2 = __viaddmax_s16x2(M2, noe_del2, MIN2);         // M - oe_del
+                const uint32_t E2m = __viaddmax_s16x2(cw.y, ne_del2, MIN2);
+                const uint32_t En2 = __vibmax_s16x2(ttd2, E2m, &pe_hi, &pe_lo);     // open >= extend
+                cell2[(size_t)pc * TB] = make_uint2(prmt(h1v, H2, 0x5432u), En2);
+                h1v = H2;
+                const uint32_t dlo = (ph_lo ? (pm_lo ? 0u : 1u) : 2u) | (pe_lo ? 0u : 4u) | (pf_lo ? 0u : 32u);
+                const uint32_t dhi = (ph_hi ? (pm_hi ? 0u : 1u) : 2u) | (pe_hi ? 0u : 4u) | (pf_hi ? 0u : 32u);
+                zb.put(j - base_off, dlo | (dhi << 8), 2);
+            }
+            f = (int)fv >> 16;
+            h1 = (int)h1v >> 16;
+        }
+        if (j < end) {  // even last column: the low lanes of its pair
+            const int x = j % B2;
+            uint2 cw = cell2[(size_t)(x >> 1) * TB];
+            int e = (int)(int16_t)(cw.y & 0xffffu), h;
+            const uint32_t sel = (uint32_t)qs2[(size_t)(j >> 1) * TB];
+            const uint32_t d = glb_cell((int)(int16_t)(cw.x & 0xffffu), e, f,
+                                        (int)prmt(plo, phi, (sel & 0xffu) * 0x101u | 0x8800u), oe_del, sc.e_del,
+                                        oe_ins, sc.e_ins, h);
+            cw.x = (cw.x & 0xffff0000u) | ((uint32_t)h1 & 0xffffu);
+            cw.y = (cw.y & 0xffff0000u) | ((uint32_t)e & 0xffffu);
+            cell2[(size_t)(x >> 1) * TB] = cw;
+            h1 = h;
+            zb.put(j - base_off, d, 1);
+            ++j;
+        }
+        {   // sentinel slot of column end: H(i, end-1), E unreachable
+            const int x = end % B2;
+            uint2 cw = cell2[(size_t)(x >> 1) * TB];
+            if (x & 1) cw = make_uint2((cw.x & 0xffffu) | ((uint32_t)h1 << 16), (cw.y & 0xffffu) | ((uint32_t)NEG << 16));
+            else cw = make_uint2((cw.x & 0xffff0000u) | ((uint32_t)h1 & 0xffffu),
+                                 (cw.y & 0xffff0000u) | ((uint32_t)NEG & 0xffffu));
+            cell2[(size_t)(x >> 1) * TB] = cw;
+        }
+        zb.finish(ngroups);
+        ncells += (unsigned long long)(end > beg ? end - beg : 0);
+    }
+    const int end_last = tlen > 0 ? (tlen + w < qlen ? tlen + w : qlen) : -1;
+    int score;
+    if (end_last == qlen) {
+        const int x = qlen % B2;
+        const uint32_t hx = cell2[(size_t)(x >> 1) * TB].x;
+        score = C::score32((x & 1) ? (int)hx >> 16 : (int)(int16_t)(hx & 0xffffu));
+    } else {
+        score = qlen == 0 ? 0 : (qlen <= w ? -(sc.o_ins + sc.e_ins * qlen) : MINUS_INF);
+    }
+    score_out[k] = score;
+    const int nc = global_traceback<true>(zj, zrow, n_col, qlen, tlen, w, cig + J.cig_off);
+    if (nc < 0) atomicOr(err, ERR_RANGE);
+    ncig_out[k] = nc < 0 ? 0 : nc;
     if (bad) atomicOr(err, ERR_BASE);
     atomicAdd(cells_total, ncells);
 }
@@ -430,8 +692,9 @@ cudaError_t launch_global_tb(const uint8_t *seq, const GlobalDevJob *jobs, const
                              uint32_t count, const Scoring &sc, int bcap, int qcap, uint8_t *z, uint32_t *cig,
                              int32_t *score, int32_t *ncig, uint32_t *err, unsigned long long *cells, cudaStream_t s)
 {
-    const size_t smem = global_smem(bcap, qcap, TB, NARROW);
-    auto kern = global_tpj_kernel<TB, NARROW>;
+    // narrow jobs: the 16x2 pair kernel; wide jobs: 32-bit cells, one column at a time
+    const size_t smem = NARROW ? global_smem_pair(bcap, qcap, TB) : global_smem(bcap, qcap, TB, false);
+    auto kern = NARROW ? global_pair_kernel<TB> : global_tpj_kernel<TB, false>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<(count + TB - 1) / TB, TB, smem, s>>>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig,
@@ -448,7 +711,7 @@ cudaError_t launch_global_form(const uint8_t *seq, const GlobalDevJob *jobs, con
     // 228 KB per SM, 1 KB of it reserved per block), larger blocks on ties
     int best_tb = 32, best_warps = 0;
     for (int tb = 128; tb >= 32; tb >>= 1) {
-        const size_t sm = global_smem(bcap, qcap, tb, NARROW);
+        const size_t sm = NARROW ? global_smem_pair(bcap, qcap, tb) : global_smem(bcap, qcap, tb, false);
         if (sm > SMEM_LIMIT) continue;
         const int blocks = std::min<int>(32, (int)((228u * 1024u) / (sm + 1024u)));
         const int warps = std::min(64, blocks * tb / 32);
