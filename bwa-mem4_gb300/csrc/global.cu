@@ -124,7 +124,11 @@ __device__ int global_traceback(const uint8_t *zj, size_t zrow, int n_col, int q
         // the reference reads the flat row-major matrix: an offset past the row lands in a later row
         const long flat = i * (long)n_col + (kk - beg);
         if (kk < beg || flat >= (long)n_col * tlen) return -1;
-        const long row = flat / n_col, col = flat - row * n_col;
+        long row = i, col = kk - beg;
+        if (col >= n_col) {
+            row = flat / n_col;
+            col = flat - row * n_col;
+        }
         const long shift = PAIR ? ((row > w ? row - w : 0) & 1) : 0;
         const uint32_t d = zj[(size_t)row * zrow + (size_t)(col + shift)];
         which = (d >> (which << 1)) & 3u;
@@ -433,12 +437,19 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
     const uint32_t ne_ins2 = ((uint32_t)(-sc.e_ins) & 0xffffu) * 0x10001u;
     const uint32_t ne_del2 = ((uint32_t)(-sc.e_del) & 0xffffu) * 0x10001u;
     const int ngroups = (n_col + 1 + 15) >> 4;
+    // slots of columns beg and end, advanced with the band (each moves by at most one a row)
+    int xbeg = 0, xend = (w + 1 < qlen ? w + 1 : qlen) % B2, prev_end = w + 1 < qlen ? w + 1 : qlen;
+    uint32_t tnext = tlen > 0 ? tg[0] : 0u;
     for (int i = 0; i < tlen; ++i) {
         const int beg = i > w ? i - w : 0;
         const int end = i + w + 1 < qlen ? i + w + 1 : qlen;
+        if (i > w && ++xbeg == B2) xbeg = 0;
+        if (end > prev_end && ++xend == B2) xend = 0;
+        prev_end = end;
         int h1 = beg == 0 ? -(sc.o_del + sc.e_del * (i + 1)) : NEG;  // H(i, beg-1)
         int f = NEG;                                                   // F(i, beg)
-        uint32_t tc = tg[i];
+        uint32_t tc = tnext;
+        if (i + 1 < tlen) tnext = tg[i + 1];
         bad |= tc >= (uint32_t)sc.m;
         tc = tc < (uint32_t)sc.m ? tc : (uint32_t)PAD_CODE;
         const uint32_t plo = sc.prof[tc & 7u][0], phi = sc.prof[tc & 7u][1];
@@ -446,8 +457,9 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
         zb.zr = reinterpret_cast<uint4 *>(zj + (size_t)i * zrow);
         const int base_off = beg & ~1;
         int j = beg;
+        int xj = xbeg;  // slot of column j
         if (j < end && (j & 1)) {  // odd first column: the high lanes of its pair
-            const int x = j % B2;
+            const int x = xj;
             uint2 cw = cell2[(size_t)(x >> 1) * TB];
             int e = (int)cw.y >> 16, h;
             const uint32_t sel = (uint32_t)qs2[(size_t)(j >> 1) * TB] >> 8;
@@ -459,11 +471,12 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
             h1 = h;
             zb.put(j - base_off, d, 1);
             ++j;
+            if (++xj == B2) xj = 0;
         }
         if (j + 1 < end) {
             // F(i, j) in fv's high lane, H(i, j-1) in h1v's high lane
             uint32_t fv = (uint32_t)f << 16, h1v = (uint32_t)h1 << 16;
-            int p = (j % B2) >> 1;
+            int p = xj >> 1;
             uint2 wn = cell2[(size_t)p * TB];
             uint32_t qn = qs2[(size_t)(j >> 1) * TB];
             for (; j + 1 < end; j += 2) {
@@ -497,9 +510,10 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
             }
             f = (int)fv >> 16;
             h1 = (int)h1v >> 16;
+            xj = 2 * p;
         }
         if (j < end) {  // even last column: the low lanes of its pair
-            const int x = j % B2;
+            const int x = xj;
             uint2 cw = cell2[(size_t)(x >> 1) * TB];
             int e = (int)(int16_t)(cw.y & 0xffffu), h;
             const uint32_t sel = (uint32_t)qs2[(size_t)(j >> 1) * TB];
@@ -514,7 +528,7 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
             ++j;
         }
         {   // sentinel slot of column end: H(i, end-1), E unreachable
-            const int x = end % B2;
+            const int x = xend;
             uint2 cw = cell2[(size_t)(x >> 1) * TB];
             if (x & 1) cw = make_uint2((cw.x & 0xffffu) | ((uint32_t)h1 << 16), (cw.y & 0xffffu) | ((uint32_t)NEG << 16));
             else cw = make_uint2((cw.x & 0xffff0000u) | ((uint32_t)h1 & 0xffffu),
