@@ -103,8 +103,10 @@ struct ReqView {
 };
 
 __global__ void win_plan_kernel(const ReqView V, uint32_t n, const RefView R, int min_seed_len,
-                                WinInfo *__restrict__ info, uint64_t *__restrict__ sizes)
+                                WinInfo *__restrict__ info, uint64_t *__restrict__ sizes,
+                                unsigned long long *__restrict__ cells)
 {
+    unsigned long long my_cells = 0;  // qlen x tlen of the accepted windows (the statistics)
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const uint8_t *unused;
         const WinReqDev q = V.get(k, &unused);
@@ -146,7 +148,11 @@ __global__ void win_plan_kernel(const ReqView V, uint32_t n, const RefView R, in
         }
         info[k] = w;
         sizes[k] = (uint64_t)q.l_ms + (w.valid ? (uint64_t)(w.re - w.rb) : 0u);
+        if (w.valid) my_cells += (unsigned long long)q.l_ms * (unsigned long long)(w.re - w.rb);
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) my_cells += __shfl_xor_sync(0xffffffffu, my_cells, o);
+    if ((threadIdx.x & 31u) == 0 && my_cells) atomicAdd(cells, my_cells);
 }
 
 // One warp per request: the mate (reverse-complemented for the reverse orientations)
@@ -191,6 +197,8 @@ __global__ void win_fill_kernel(const ReqView V, uint32_t n, const RefView R, co
 }
 
 // The caller's result records, written in place (window and alignment per request).
+// Records into a device buffer (one thread per request); win_copy_kernel then moves them to
+// the caller's array word by word, so consecutive threads store consecutive host words.
 __global__ void win_store_kernel(const WinInfo *__restrict__ info, const bwacuda_rescue_result *__restrict__ aln,
                                  uint32_t n, bwacuda_window_result *__restrict__ out)
 {
@@ -206,6 +214,12 @@ __global__ void win_store_kernel(const WinInfo *__restrict__ info, const bwacuda
     }
 }
 
+__global__ void win_copy_kernel(const uint32_t *__restrict__ src, size_t words, uint32_t *__restrict__ dst)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < words; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
 }  // namespace
 
 struct RefState {
@@ -213,7 +227,7 @@ struct RefState {
     int64_t l_pac = 0;
     int32_t n = 0;
     // per-call buffers
-    DevBuf reqs, mates, info, sizes, offs, tmp, seq, jobs, res;
+    DevBuf reqs, mates, info, sizes, offs, tmp, seq, jobs, res, outd;
     HostBuf h_reqs, h_tot;
 };
 
@@ -223,7 +237,7 @@ void ref_release(bwacuda_ctx *c)
     RefState &S = *c->ref;
     S.pac.release(); S.off.release(); S.len.release();
     S.reqs.release(); S.mates.release(); S.info.release(); S.sizes.release(); S.offs.release(); S.tmp.release();
-    S.seq.release(); S.jobs.release(); S.res.release(); S.h_reqs.release(); S.h_tot.release();
+    S.seq.release(); S.jobs.release(); S.res.release(); S.outd.release(); S.h_reqs.release(); S.h_tot.release();
     delete c->ref;
     c->ref = nullptr;
 }
@@ -315,7 +329,7 @@ extern "C" int bwacuda_mate_rescue_windows(bwacuda_ctx *c, const bwacuda_window_
     cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, (const uint64_t *)nullptr, (uint64_t *)nullptr, (int)n + 1);
     if (!direct && (e = S.reqs.ensure(rq_bytes + mate_bytes + 16)) != cudaSuccess) return cuda_status(e);
     if ((e = S.info.ensure(n * sizeof(WinInfo))) != cudaSuccess) return cuda_status(e);
-    if ((e = S.sizes.ensure((n + 1) * 8)) != cudaSuccess) return cuda_status(e);
+    if ((e = S.sizes.ensure((n + 2) * 8)) != cudaSuccess) return cuda_status(e);
     if ((e = S.offs.ensure((n + 1) * 8)) != cudaSuccess) return cuda_status(e);
     if ((e = S.tmp.ensure(scan_bytes + 16)) != cudaSuccess) return cuda_status(e);
     if ((e = S.h_tot.ensure(64)) != cudaSuccess) return cuda_status(e);
@@ -338,14 +352,21 @@ extern "C" int bwacuda_mate_rescue_windows(bwacuda_ctx *c, const bwacuda_window_
     int nsm = 0;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || nsm < 1) nsm = 1;
     if ((e = cudaMemsetAsync(sizes + n, 0, 8, s)) != cudaSuccess) return cuda_status(e);
+    // the accepted windows' cells, counted by the plan kernel (sizes[n + 1], after the scan's input)
+    unsigned long long *d_cells = reinterpret_cast<unsigned long long *>(sizes + n + 1);
+    if ((e = cudaMemsetAsync(d_cells, 0, 8, s)) != cudaSuccess) return cuda_status(e);
     uint32_t grid = (uint32_t)std::min<size_t>((n + 255) / 256, (size_t)nsm * 8);
-    win_plan_kernel<<<grid, 256, 0, s>>>(V, (uint32_t)n, R, min_seed_len, info, sizes);
+    win_plan_kernel<<<grid, 256, 0, s>>>(V, (uint32_t)n, R, min_seed_len, info, sizes, d_cells);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
     if ((e = cub::DeviceScan::ExclusiveSum(S.tmp.p, scan_bytes, sizes, offs, (int)n + 1, s)) != cudaSuccess)
         return cuda_status(e);
     if ((e = cudaMemcpyAsync(S.h_tot.p, offs + n, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_status(e);
+    if ((e = cudaMemcpyAsync(static_cast<uint64_t *>(S.h_tot.p) + 1, d_cells, 8, cudaMemcpyDeviceToHost, s)) !=
+        cudaSuccess)
+        return cuda_status(e);
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_status(e);
     const uint64_t total = *static_cast<const uint64_t *>(S.h_tot.p);
+    const uint64_t cells = static_cast<const uint64_t *>(S.h_tot.p)[1];
     if ((e = S.seq.ensure(total + 16)) != cudaSuccess) return cuda_status(e);
     grid = (uint32_t)std::min<size_t>((n * 32 + 255) / 256, (size_t)nsm * 16);
     win_fill_kernel<<<grid, 256, 0, s>>>(V, (uint32_t)n, R, info, offs, static_cast<uint8_t *>(S.seq.p),
@@ -361,17 +382,20 @@ extern "C" int bwacuda_mate_rescue_windows(bwacuda_ctx *c, const bwacuda_window_
                                   static_cast<const bwacuda_dev_rescue_job *>(S.jobs.p), n, &sc, minsc, max_sc, 0, 0,
                                   static_cast<bwacuda_rescue_result *>(S.res.p), s);
     if (rc) return rc;
-    uint64_t cells = 0;
     if (direct) {
-        // the records go straight into the caller's array; the cell count is summed on the host
+        // the records, assembled in HBM, then word by word straight into the caller's array
+        if ((e = S.outd.ensure(n * sizeof(bwacuda_window_result))) != cudaSuccess) return cuda_status(e);
         grid = (uint32_t)std::min<size_t>((n + 255) / 256, (size_t)nsm * 8);
         win_store_kernel<<<grid, 256, 0, s>>>(info, static_cast<const bwacuda_rescue_result *>(S.res.p), (uint32_t)n,
-                                              out);
+                                              static_cast<bwacuda_window_result *>(S.outd.p));
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
+        const size_t words = n * (sizeof(bwacuda_window_result) / 4);
+        grid = (uint32_t)std::min<size_t>((words + 255) / 256, (size_t)nsm * 8);
+        win_copy_kernel<<<grid, 256, 0, s>>>(static_cast<const uint32_t *>(S.outd.p), words,
+                                             reinterpret_cast<uint32_t *>(out));
         if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
         uint64_t dummy = 0;
         if ((rc = collect_device_status(c, s, &dummy)) != BWACUDA_OK) return rc;  // synchronises
-        for (size_t k = 0; k < n; ++k)
-            if (out[k].valid) cells += (uint64_t)reqs[k].l_ms * (uint64_t)(out[k].re - out[k].rb);
     } else {
         // windows and alignments back through the staging buffer, then into the caller's records
         if ((e = S.h_reqs.ensure(n * (sizeof(WinInfo) + sizeof(bwacuda_rescue_result)) + 16)) != cudaSuccess)
@@ -392,7 +416,6 @@ extern "C" int bwacuda_mate_rescue_windows(bwacuda_ctx *c, const bwacuda_window_
             o.rid = hi[k].rid;
             o.valid = hi[k].valid;
             o.aln = ha[k];
-            if (hi[k].valid) cells += (uint64_t)reqs[k].l_ms * (uint64_t)(hi[k].re - hi[k].rb);
         }
     }
     c->stats.d2h_bytes += n * (sizeof(WinInfo) + sizeof(bwacuda_rescue_result));
