@@ -186,6 +186,15 @@ int ats_init(bwacuda_ctx *c)
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r.gathered, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r.done, cudaEventDisableTiming);
     }
+    // These kernels use no shared memory, but an SM takes the shared-memory carveout of the
+    // first kernel placed on it while empty: with the default (small shared memory) an SM
+    // that one gather block lands on cannot take the bucket kernels' blocks until it leaves.
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(ats_lengths_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                   cudaSharedmemCarveoutMaxShared);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(ats_gather_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                   cudaSharedmemCarveoutMaxShared);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(ats_scatter_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                   cudaSharedmemCarveoutMaxShared);
     c->ats = A;
     if (e != cudaSuccess) {
         ats_release(c);

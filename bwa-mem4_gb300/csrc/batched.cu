@@ -56,6 +56,7 @@ static int batched_init(bwacuda_ctx *c)
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&B->sm_regs, cudaDevAttrMaxRegistersPerMultiprocessor, c->device);
     if (e == cudaSuccess)
         e = cudaDeviceGetAttribute(&B->sm_threads, cudaDevAttrMaxThreadsPerMultiProcessor, c->device);
+    if (e == cudaSuccess) e = ext_sort_prefer_shared();
     if (e != cudaSuccess) { delete B; return cuda_status(e); }
     B->nb = ext_bucket_defs(B->defs, EXT_MAX_BUCKETS, B->step);
     if ((e = B->d_defs.ensure(sizeof(B->defs))) != cudaSuccess) { delete B; return cuda_status(e); }

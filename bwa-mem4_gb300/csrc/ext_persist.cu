@@ -176,6 +176,18 @@ int ext_bucket_defs(ExtBucketDef *defs, int max_defs, int step)
     return nb;
 }
 
+cudaError_t ext_sort_prefer_shared()
+{
+    // no shared memory used, but an SM takes the carveout of the first kernel placed on it
+    // while empty: prefer the bucket kernels' (maximum shared memory) configuration
+    cudaError_t e = cudaFuncSetAttribute(ext_keys_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         cudaSharedmemCarveoutMaxShared);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(ext_bucket_bounds_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared);
+    return e;
+}
+
 size_t ext_sort_temp_bytes(size_t n)
 {
     size_t bytes = 0;

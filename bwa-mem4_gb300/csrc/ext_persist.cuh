@@ -120,7 +120,7 @@ ext_persist_pair_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_j
     if (lane == 0 && ncells) atomicAdd(cells_total, ncells);
 }
 
-constexpr size_t SMEM_MAX = 227u * 1024u;
+constexpr size_t SMEM_MAX = EXT_SMEM_BLOCK_MAX;
 
 // Resident blocks per SM of a persistent launch: the occupancy limit, lowered so
 // that L.reserve_regs registers and L.reserve_threads threads stay free (at least

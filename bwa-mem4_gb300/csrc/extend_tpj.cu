@@ -63,7 +63,7 @@ ext_tpj_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *__res
     if ((tid & 31) == 0 && ncells) atomicAdd(cells_total, ncells);
 }
 
-constexpr size_t SMEM_MAX = 227u * 1024u;
+constexpr size_t SMEM_MAX = EXT_SMEM_BLOCK_MAX;
 
 template <class F, int TB>
 cudaError_t launch_ext_tb(const ExtLaunch &L)

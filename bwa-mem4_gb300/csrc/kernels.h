@@ -9,6 +9,12 @@
 
 namespace bwacuda {
 
+// Largest shared memory of one extension block.  An SM holds 228 KB and reserves 1 KB per
+// resident block, so a block of at most 225 KB still lets one small block (a gather, a
+// length pass, another stream's kernel) run beside it; a 227 KB block would hold its SM
+// alone, and a bucket launch of such blocks waits for every other kernel to leave an SM.
+constexpr size_t EXT_SMEM_BLOCK_MAX = 225u * 1024u;
+
 struct ExtLaunch {
     const uint8_t *seq;
     const bwacuda_dev_ext_job *jobs;

@@ -37,6 +37,8 @@ struct PersistLaunch {
 
 int ext_bucket_defs(ExtBucketDef *defs, int max_defs, int step);
 size_t ext_sort_temp_bytes(size_t n);
+// the sort's own kernels prefer the maximum shared-memory carveout (once per device)
+cudaError_t ext_sort_prefer_shared();
 // keys + radix sort + bucket bounds; d_table holds 4 words per bucket
 // (start, end, work counter, spare).
 // With P.ug enabled the key kernel also settles ungapped hits (results written to out).

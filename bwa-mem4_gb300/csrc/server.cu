@@ -665,6 +665,14 @@ extern "C" int bwacuda_server_start(bwacuda_ctx *c, const bwacuda_server_config 
     if (e == cudaSuccess && !S->dev)
         e = cudaHostAlloc(reinterpret_cast<void **>(&S->h_arena), S->budget, cudaHostAllocDefault);
     int lo_prio = 0, hi_prio = 0;
+    // admission gathers use no shared memory but should leave an empty SM configured for the
+    // waves' bucket kernels (maximum shared memory)
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(srv_gather_kernel<0>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(srv_gather_kernel<1>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared);
     if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
     // admission copies run beside the waves' persistent kernels: highest priority
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&S->copy_stream, cudaStreamNonBlocking, hi_prio);
