@@ -342,8 +342,11 @@ int extend_batch_ats(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int 
     uint32_t input_flags = 0;
     size_t k = 0;
     for (size_t c0 = 0, cn = 0; c0 < n && rc == BWACUDA_OK; c0 += cn, ++k) {
-        // a short first chunk: the extension starts after a short gather, later gathers hide behind it
-        cn = std::min(k == 0 ? std::max(CH / 8, std::min(CH, (size_t)65536)) : CH, n - c0);
+        // chunks ramp up from 64k jobs, doubling: the extension starts after a short gather, and
+        // each gather (about 2.5x faster than the extension of as many jobs) ends before the
+        // extension of the chunks ahead of it
+        const size_t ramp = std::min(CH, (size_t)65536 << (k < 16 ? k : 16));
+        cn = std::min(ramp, n - c0);
         AtsChunk &R = c->ats->ring[k % ATS_RING];
         if ((rc = ats_retire(c, R, &input_flags)) != BWACUDA_OK) break;
         cudaError_t e = ats_gather_chunk(c, R, jobs + c0, cn, br, w);
