@@ -523,7 +523,7 @@ class Context:
         return s
 
     def extend_device(self, d_seq, d_jobs, n, d_out, sc: Scoring = None, end_bonus=5, zdrop=100,
-                      path=PATH_PLAIN, stream=None):
+                      path=PATH_BATCHED, stream=None):
         sc = sc or self.scoring()
         rc = lib().bwacuda_extend_device(self.h, C.c_void_p(d_seq), C.c_void_p(d_jobs), n, C.byref(sc),
                                          end_bonus, zdrop, path, C.c_void_p(d_out),

@@ -87,7 +87,7 @@ struct bwacuda_ctx {
     bwacuda::DevBuf d_dev_aux, d_dev_scratch;
     bwacuda::WorkerPool pool;
     bwacuda_stats stats{};
-    int ext_path = BWACUDA_PATH_PLAIN;
+    int ext_path = BWACUDA_PATH_BATCHED;
     bool use_graphs = true;
     int rescue_kernel = BWACUDA_RESCUE_AUTO;
     int rescue_lanes = 16;  // lanes per job of the register wavefront (8, 16, 32)
