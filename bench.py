@@ -277,6 +277,12 @@ def other_configs(args, B, ctx, st, barrier, max_over_ranks, world, rank):
     d_seq = torch.from_numpy(js.seq).cuda()
     d_jobs = torch.from_numpy(js.dev_ext_jobs().view(np.uint8)).cuda()
     d_out = torch.zeros(n * 24, dtype=torch.uint8, device="cuda")
+    # the reference's 8/16-bit kernel choice for these jobs (crates/bwa-neon/src/batched.rs:846-866:
+    # both lengths < 256 and h0 + min(qlen, tlen) * a + max(b, N penalty) + a < 256); this
+    # library picks its cell width from the value bound alone, with the same results
+    mn = np.minimum(js.qlen, js.tlen).astype(np.int64)
+    u8 = (js.qlen < 256) & (js.tlen < 256) & (js.h0.astype(np.int64) + mn * 1 + 5 < 256)
+    ref_bins = {"8-bit": round(float(u8.mean()), 4), "16-bit": round(float(1 - u8.mean()), 4)}
     tuning_mixed = ctx.autotune_extend(d_seq.data_ptr(), d_jobs.data_ptr(), n)
     ms, stt = timed(lambda: ctx.extend_device(d_seq.data_ptr(), d_jobs.data_ptr(), n, d_out.data_ptr(),
                                               path=B.PATH_BATCHED, stream=stream))
@@ -296,7 +302,8 @@ def other_configs(args, B, ctx, st, barrier, max_over_ranks, world, rank):
                     "{50, 100, 200}, h0 <= 250; one batched call",
         "value": round(cells * world / (ms / 1e3) / 1e9, 2), "unit": "GCUPS", "ms_per_step": round(ms, 2),
         "plain": {"value": round(ctx.stats()["ext_cells"] * world / tp / 1e9, 2), "unit": "GCUPS"},
-        "plain_equals_batched": bool(np.array_equal(batched, d_out.cpu().numpy())), "tuning": tuning_mixed}
+        "plain_equals_batched": bool(np.array_equal(batched, d_out.cpu().numpy())), "tuning": tuning_mixed,
+        "reference_bins": ref_bins}
     del d_seq, d_jobs, d_out, js
     torch.cuda.empty_cache()
 
