@@ -307,6 +307,31 @@ def other_configs(args, B, ctx, st, barrier, max_over_ranks, world, rank):
     del d_seq, d_jobs, d_out, js
     torch.cuda.empty_cache()
 
+    # the 16-bit cell class: read-pair jobs with 300 added to every h0 (256 <= h0 + min(qlen, tlen)
+    # < 32768), batched, device-resident; the plain path checks the results
+    n = args.mixed_jobs // 8
+    js = B.synth_ext(2, n, seed=6000 + rank)
+    js.h0 = js.h0 + 300
+    d_seq = torch.from_numpy(js.seq).cuda()
+    d_jobs = torch.from_numpy(js.dev_ext_jobs().view(np.uint8)).cuda()
+    d_out = torch.zeros(n * 24, dtype=torch.uint8, device="cuda")
+    ms, stt = timed(lambda: ctx.extend_device(d_seq.data_ptr(), d_jobs.data_ptr(), n, d_out.data_ptr(),
+                                              path=B.PATH_BATCHED, stream=stream))
+    batched = d_out.cpu().numpy().copy()
+    for c0 in range(0, n, 262144):
+        cn = min(262144, n - c0)
+        ctx.extend_device(d_seq.data_ptr(), d_jobs.data_ptr() + c0 * 32, cn, d_out.data_ptr() + c0 * 24,
+                          path=B.PATH_PLAIN, stream=stream)
+    ctx.sync()
+    res["sixteen_bit_cells"] = {
+        "workload": f"ksw_extend2, {n} read-pair jobs per GPU with h0 + 300 (every job in the 16-bit cell "
+                    "class); one batched call",
+        "value": round(stt["ext_cells"] / 3 * world / (ms / 1e3) / 1e9, 2), "unit": "GCUPS",
+        "ms_per_step": round(ms, 2),
+        "plain_equals_batched": bool(np.array_equal(batched, d_out.cpu().numpy()))}
+    del d_seq, d_jobs, d_out, js
+    torch.cuda.empty_cache()
+
     # mate rescue: 150 bp query vs 750 bp window, minsc 20
     n = args.rescue_jobs
     js = B.synth_rescue(n, seed=3000 + rank)

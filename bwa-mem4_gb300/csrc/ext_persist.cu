@@ -178,14 +178,11 @@ int ext_bucket_defs(ExtBucketDef *defs, int max_defs, int step)
 
 cudaError_t ext_sort_prefer_shared()
 {
-    // no shared memory used, but an SM takes the carveout of the first kernel placed on it
-    // while empty: prefer the bucket kernels' (maximum shared memory) configuration
-    cudaError_t e = cudaFuncSetAttribute(ext_keys_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                         cudaSharedmemCarveoutMaxShared);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(ext_bucket_bounds_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 cudaSharedmemCarveoutMaxShared);
-    return e;
+    // The bucket-bound kernel (one block, no shared memory) prefers the bucket kernels'
+    // maximum shared-memory carveout.  The key kernel keeps the default: its blocks live for
+    // one pass only, and with the ungapped rule it reads every job's bases through L1.
+    return cudaFuncSetAttribute(ext_bucket_bounds_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                cudaSharedmemCarveoutMaxShared);
 }
 
 size_t ext_sort_temp_bytes(size_t n)
