@@ -71,7 +71,8 @@ def parse():
     ap.add_argument("--window-jobs", type=int, default=1024 * 1024)
     ap.add_argument("--serve-rates", default="50,500,2000", help="Poisson arrival rates (requests/s)")
     ap.add_argument("--serve-requests", type=int, default=600, help="requests per arrival rate")
-    ap.add_argument("--case", choices=["ext-batched", "ext-plain", "ext-mixed", "ext-gather", "rescue", "global"],
+    ap.add_argument("--case", choices=["ext-batched", "ext-plain", "ext-mixed", "ext-gather", "rescue", "global",
+                                       "windows", "retry"],
                     help="profiling case: run the small workload twice through one path, no timing")
     ap.add_argument("--lanes", type=int, default=8, help="rescue case: wavefront lanes per job")
     ap.add_argument("--h0-add", type=int, default=0,
@@ -575,6 +576,24 @@ def run_case(args):
         js = B.synth_global(args.jobs, seed=0)
         for _ in range(2):
             ctx.ksw_global2_batch(js)
+    elif args.case == "windows":
+        # mate rescue with the windows planned, clamped and unpacked on the device
+        rw = B.RescueWindows(args.jobs, seed=0)
+        ctx.ref_set(rw)
+        reqs = rw.requests()
+        for _ in range(2):
+            ctx.mate_rescue_windows(reqs, minsc=20)
+    elif args.case == "retry":
+        # run_side's band-doubling loop on the device, starting at w = 20 so a share of the jobs
+        # is rejected and re-run at 40
+        js = B.synth_ext(2, args.jobs, seed=0)
+        js.w = np.full(len(js), 20, dtype=np.int32)
+        d_seq = torch.from_numpy(js.seq).cuda()
+        d_jobs = torch.from_numpy(js.dev_ext_jobs().view(np.uint8)).cuda()
+        d_out = torch.zeros(len(js) * 24, dtype=torch.uint8, device="cuda")
+        for _ in range(2):
+            ctx.extend_retry_device(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), d_out.data_ptr())
+            ctx.sync()
     else:
         js = B.synth_rescue(args.jobs, seed=0)
         ctx.set_option(B.OPT_RESCUE_LANES, args.lanes)
