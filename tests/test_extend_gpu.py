@@ -297,6 +297,31 @@ def test_pair_cell_classes_swept(ctx, scoring):
                      what=f"classes {scoring} w={w}")
 
 
+@pytest.mark.parametrize("scoring", [(1, 4, 6, 1, 6, 1, 5, 100), (2, 3, 5, 2, 4, 3, 0, 40)])
+def test_long_queries_short_targets(ctx, scoring):
+    # queries past 512 columns against short targets stay in the 8-bit class (the value bound
+    # follows min(qlen, tlen)): the open-ended 8-bit bucket, whose rows keep 32-bit maxima;
+    # longer targets put the same queries in the 16-bit class
+    a, b, od, ed, oi, ei, eb, zd = scoring
+    rng = np.random.default_rng(31 + a)
+    qs, ts, h0s = [], [], []
+    for k in range(600):
+        ql = int(rng.integers(513, 1400))
+        q = rng.integers(0, 4, ql)
+        tl = int(rng.integers(1, 120)) if k % 3 else int(rng.integers(200, 400))
+        start = int(rng.integers(0, 8))
+        t = q[start:start + tl].copy()
+        for _ in range(int(rng.integers(0, 4))):
+            if len(t):
+                t[int(rng.integers(0, len(t)))] = int(rng.integers(0, 5))
+        qs.append(q.tolist())
+        ts.append(t.tolist())
+        h0s.append(int(rng.integers(1, 40)))
+    for w in (5, 100):
+        _check_batch(ctx, qs, ts, h0s, a, b, od, ed, oi, ei, w, eb, zd, path=(B.PATH_BATCHED, B.GATHER_HOST),
+                     what=f"long queries {scoring} w={w}")
+
+
 @pytest.mark.parametrize("path", PATHS)
 def test_wide_cells_for_large_scores(ctx, path):
     # h0 + min(q,t)*a >= 32768 needs int32 cells (the reference's scalar bin)
