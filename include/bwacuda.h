@@ -100,7 +100,9 @@ typedef struct bwacuda_ctx bwacuda_ctx;
 #define BWACUDA_OPT_EXT_PATH 1
 #define BWACUDA_PATH_PLAIN 0   /* one launch per chunk, jobs in caller order */
 #define BWACUDA_PATH_BATCHED 1 /* length-bucketed, persistent, graph-replayed (default) */
-/* Jobs per device chunk (pipelining granularity of the host-buffer calls). */
+/* Jobs per device chunk (pipelining granularity of the host-buffer calls; default 262144).
+ * Device-gather extension calls ramp up to it from 65536 jobs, doubling chunk by chunk;
+ * bwacuda_ksw_global2_batch takes 4 x this many jobs per chunk, at most 1,048,576. */
 #define BWACUDA_OPT_CHUNK_JOBS 2
 /* Batched device calls: replay a captured CUDA graph (1, default) or enqueue every call (0). */
 #define BWACUDA_OPT_GRAPHS 3
