@@ -148,7 +148,9 @@ cudaError_t launch_persist_tb(const PersistLaunch &L, const ExtBucketDef &d, uin
     const size_t smem = ext_block_smem(d.qcap, TB, sizeof(typename F::T));
     if (smem > SMEM_MAX) return cudaErrorInvalidValue;
     auto kern = ext_persist_kernel<F, TB, GRAB>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // process-wide per kernel: always the ceiling, so a launch on another context (another
+    // host thread) never shrinks it under this one
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_MAX);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
     if ((e = persist_blocks_per_sm(kern, TB, smem, L, per_sm)) != cudaSuccess) return e;
@@ -168,7 +170,9 @@ cudaError_t launch_persist_pair_tb(const PersistLaunch &L, const ExtBucketDef &d
     const size_t smem = pair_block_smem(d.qcap, TB, W16);
     if (smem > SMEM_MAX) return cudaErrorInvalidValue;
     auto kern = ext_persist_pair_kernel<TB, GRAB, W16>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // process-wide per kernel: always the ceiling, so a launch on another context (another
+    // host thread) never shrinks it under this one
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_MAX);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
     if ((e = persist_blocks_per_sm(kern, TB, smem, L, per_sm)) != cudaSuccess) return e;

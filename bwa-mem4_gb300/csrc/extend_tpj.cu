@@ -69,8 +69,10 @@ template <class F, int TB>
 cudaError_t launch_ext_tb(const ExtLaunch &L)
 {
     const size_t smem = ext_block_smem(L.qcap, TB, sizeof(typename F::T));
+    // the attribute is process-wide per kernel: always its ceiling, so calls on other
+    // contexts (other host threads) never shrink it under this launch
     cudaError_t e = cudaFuncSetAttribute(ext_tpj_kernel<F, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+                                         (int)SMEM_MAX);
     if (e != cudaSuccess) return e;
     const uint32_t grid = (uint32_t)((L.n + TB - 1) / TB);
     if (grid == 0) return cudaSuccess;

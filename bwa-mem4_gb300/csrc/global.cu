@@ -709,7 +709,8 @@ cudaError_t launch_global_tb(const uint8_t *seq, const GlobalDevJob *jobs, const
     // narrow jobs: the 16x2 pair kernel; wide jobs: 32-bit cells, one column at a time
     const size_t smem = NARROW ? global_smem_pair(bcap, qcap, TB) : global_smem(bcap, qcap, TB, false);
     auto kern = NARROW ? global_pair_kernel<TB> : global_tpj_kernel<TB, false>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // process-wide per kernel: always the ceiling (concurrent contexts must not shrink it)
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT);
     if (e != cudaSuccess) return e;
     kern<<<(count + TB - 1) / TB, TB, smem, s>>>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig,
                                                  err, cells);

@@ -17,8 +17,10 @@
 //
 // The array is shared by all calls on a device, and it keeps the previous call's
 // contents.  The error word and the length maxima are cleared at the start of
-// every call; tracker entries are always written before they are read.  Calls
-// that overlap on the GPU (from several threads or streams) race on the array.
+// every call; tracker entries are always written before they are read.  A call
+// returns only after its kernels finish, and calls from several host threads
+// (on one context or several) take a process-wide lock for their whole length,
+// so they never overlap on the array.
 //
 // The first call on a device looks the array up with cudaGetSymbolAddress,
 // which needs that device to be current; make that first call before any
@@ -128,6 +130,8 @@ extern "C" int bwacuda_ksw_align2_device_noalloc(bwacuda_ctx *c, const uint8_t *
 {
     if (!c || !scp) return BWACUDA_EINVAL;
     std::lock_guard<std::mutex> g(c->mu);
+    static std::mutex array_mu;  // the static arrays are shared by every context of the process
+    std::lock_guard<std::mutex> ga(array_mu);
     int rc = validate_scoring(scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
     if (rc) return rc;
     if (max_sc < 1 || (mode != 0 && mode != 1) || (lanes != 0 && lanes != 8 && lanes != 16)) return BWACUDA_EINVAL;

@@ -282,8 +282,9 @@ template <bool WIDE, int TB>
 cudaError_t launch_res_tb(const RescueLaunch &L)
 {
     size_t smem = res_smem_bytes<WIDE>(L.qcap, TB);
+    // process-wide per kernel: always the ceiling (concurrent contexts must not shrink it)
     cudaError_t e = cudaFuncSetAttribute(rescue_tpj_kernel<WIDE, TB>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_MAX);
     if (e != cudaSuccess) return e;
     uint32_t grid = (uint32_t)((L.n + TB - 1) / TB);
     if (grid == 0) return cudaSuccess;
