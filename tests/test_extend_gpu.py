@@ -395,6 +395,38 @@ def test_invalid_inputs_fail_loudly(ctx, path):
         ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_AUTO)
 
 
+@pytest.mark.parametrize("path", PATHS)
+def test_invalid_job_in_a_later_chunk(ctx, path):
+    # many small chunks (the device gather's ring wraps several times); an invalid job or a bad
+    # base code late in the batch fails the call, and the context then runs the batch cleanly
+    _set_path(ctx, path)
+    js = B.synth_ext(2, 9000, seed=22)
+    want, _ = oracle.extend_batch(js)
+    out = np.zeros(len(js), dtype=B.EXT_RES)
+    ctx.set_option(B.OPT_CHUNK_JOBS, 700)
+    try:
+        jobs = ctx._host_jobs(js, B.EXT_JOB)
+        jobs[8000]["qlen"] = -3
+        assert _raw_extend(ctx, jobs, out) == B.EINVAL
+        import copy
+
+        bad = copy.copy(js)  # same offsets, its own copy of the bases
+        bad.seq = js.seq.copy()
+        seq = bad.seq
+        k = 7777
+        if js.qlen[k] == 0:
+            k += 1
+        seq[js.q_off[k]] = 6  # a base code >= m
+        with pytest.raises(B.BwaCudaError) as e:
+            ctx.extend_batch(bad)
+        assert e.value.code == B.EBASE
+        got = ctx.extend_batch(js)
+        assert np.array_equal(got, want)
+    finally:
+        ctx.set_option(B.OPT_CHUNK_JOBS, 262144)
+        ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_AUTO)
+
+
 def test_device_gather_equals_host_packing(ctx):
     # the two feeds of the batched kernels agree on results, cell counts and bin statistics,
     # and the device gather writes every result word of the caller's array
