@@ -63,6 +63,9 @@ __host__ __device__ inline size_t global_smem(int bcap, int qcap, int tb, bool n
 // gives the same result in both forms (the two ranges stay apart and inside int16),
 // so traceback bytes and scores are identical.
 constexpr int GLB_NEG16 = -24576;
+// what a DP kernel leaves in ncig[k] for the traceback kernel: the direction-byte layout
+constexpr int GLB_TB_ROWS = -1;   // a row's bytes from column beg (32-bit cell kernel)
+constexpr int GLB_TB_PAIRS = -2;  // from column beg & ~1 (pair kernel)
 constexpr int GLB_NARROW_D = 8000;
 struct GlbNarrowRule {
     int cost;  // max(o_del + e_del, o_ins + e_ins, -min score, max score)
@@ -283,9 +286,7 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
     if (end_last == qlen) score = C::score32(C::h(cell[(size_t)(qlen % B) * TB]));
     else score = qlen == 0 ? 0 : (qlen <= w ? -(sc.o_ins + sc.e_ins * qlen) : MINUS_INF);
     score_out[k] = score;
-    const int nc = global_traceback<false>(zj, zrow, n_col, qlen, tlen, w, cig + J.cig_off);
-    if (nc < 0) atomicOr(err, ERR_RANGE);
-    ncig_out[k] = nc < 0 ? 0 : nc;
+    ncig_out[k] = GLB_TB_ROWS;  // glb_traceback_kernel follows (this layout)
     if (bad) atomicOr(err, ERR_BASE);
     atomicAdd(cells_total, ncells);
 }
@@ -548,11 +549,32 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
         score = qlen == 0 ? 0 : (qlen <= w ? -(sc.o_ins + sc.e_ins * qlen) : MINUS_INF);
     }
     score_out[k] = score;
-    const int nc = global_traceback<true>(zj, zrow, n_col, qlen, tlen, w, cig + J.cig_off);
-    if (nc < 0) atomicOr(err, ERR_RANGE);
-    ncig_out[k] = nc < 0 ? 0 : nc;
+    ncig_out[k] = GLB_TB_PAIRS;  // glb_traceback_kernel follows (the column-pair layout)
     if (bad) atomicOr(err, ERR_BASE);
     atomicAdd(cells_total, ncells);
+}
+
+// The traceback of every job whose DP ran (one thread per job, no shared memory, so the SMs
+// hold many warps and the walk's dependent HBM reads overlap across jobs).  ncig[k] carries the
+// layout the DP kernel wrote the direction bytes in (0: the job was rejected, no walk) and
+// leaves with the run count.
+__global__ void __launch_bounds__(256) glb_traceback_kernel(const GlobalDevJob *__restrict__ jobs, uint32_t n,
+                                                            const uint8_t *__restrict__ z, uint32_t *__restrict__ cig,
+                                                            int32_t *__restrict__ ncig, uint32_t *__restrict__ err)
+{
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int layout = ncig[k];
+        if (layout != GLB_TB_ROWS && layout != GLB_TB_PAIRS) continue;
+        const GlobalDevJob J = jobs[k];
+        const int w = J.w < 0 ? 0 : J.w;
+        const int n_col = J.qlen < 2 * w + 1 ? J.qlen : 2 * w + 1;
+        const uint8_t *zj = z + J.z_off;
+        const int nc = layout == GLB_TB_PAIRS
+                           ? global_traceback<true>(zj, (size_t)J.zrow, n_col, J.qlen, J.tlen, w, cig + J.cig_off)
+                           : global_traceback<false>(zj, (size_t)J.zrow, n_col, J.qlen, J.tlen, w, cig + J.cig_off);
+        if (nc < 0) atomicOr(err, ERR_RANGE);
+        ncig[k] = nc < 0 ? 0 : nc;
+    }
 }
 
 // dense[doff[k] ..] = cig[cig_off[k] .. + ncig[k]]: one warp per job.
@@ -761,6 +783,16 @@ cudaError_t launch_global(const uint8_t *seq, const GlobalDevJob *jobs, const ui
                                      s);
 }
 
+// The traceback of jobs 0 .. n after every DP launch of the chunk.
+cudaError_t launch_global_traceback(const GlobalDevJob *jobs, uint32_t n, const uint8_t *z, uint32_t *cig,
+                                    int32_t *ncig, uint32_t *err, int nsm, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    const uint32_t grid = (uint32_t)std::min<size_t>((n + 255) / 256, (size_t)nsm * 8);
+    glb_traceback_kernel<<<grid, 256, 0, s>>>(jobs, n, z, cig, ncig, err);
+    return cudaGetLastError();
+}
+
 GlbNarrowRule global_narrow_rule(const Scoring &sc, int m, const int8_t *mat)
 {
     int mn = 0, mx = 0;
@@ -918,6 +950,9 @@ int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n
             c->stats.kernel_launches += 1;
         }
         if (e != cudaSuccess) break;
+        if ((e = launch_global_traceback(dj, (uint32_t)cn, static_cast<const uint8_t *>(b.d_z.p),
+                                         static_cast<uint32_t *>(b.d_cig.p), d_ncig, d_err, nsm, s)) != cudaSuccess)
+            break;
         if ((e = cub::DeviceScan::ExclusiveSum(b.d_tmp.p, t2, d_ncig, d_doff, (int)cn + 1, s)) != cudaSuccess) break;
         grid = (uint32_t)std::min<size_t>((cn + 255) / 256, (size_t)nsm * 8);
         glb_store_kernel<<<grid, 256, 0, s>>>(dj, (uint32_t)cn, d_score, static_cast<const uint32_t *>(b.d_cig.p), d_ncig,
@@ -927,7 +962,7 @@ int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) break;
         if (!cigar || out_base + ht[40] > cigar_cap) short_buf = true;
         out_base += ht[40];
-        c->stats.kernel_launches += 10;
+        c->stats.kernel_launches += 11;
     }
     if (e != cudaSuccess) return cuda_status(e);
     if (rc) {
@@ -982,6 +1017,8 @@ extern "C" int bwacuda_ksw_global2_batch(bwacuda_ctx *c, const bwacuda_global_jo
     GlobalBufs &b = c->global->b;
     const Scoring sc = make_scoring(m, mat, o_del, e_del, o_ins, e_ins);
     const GlbNarrowRule nrule = global_narrow_rule(sc, m, mat);
+    int nsm = 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || nsm < 1) nsm = 1;
     cudaStream_t s = c->stream;
     uint32_t *d_err = static_cast<uint32_t *>(c->d_misc.p);
     // chunks bounded in jobs and in traceback bytes
@@ -1054,6 +1091,10 @@ extern "C" int bwacuda_ksw_global2_batch(bwacuda_ctx *c, const bwacuda_global_jo
                           static_cast<uint32_t *>(b.d_cig.p), d_score, d_ncig, d_err,
                           reinterpret_cast<unsigned long long *>((char *)c->d_misc.p + 8), s);
         if (e != cudaSuccess) break;
+        if ((e = launch_global_traceback(static_cast<const GlobalDevJob *>(b.d_jobs.p), (uint32_t)cn,
+                                         static_cast<const uint8_t *>(b.d_z.p), static_cast<uint32_t *>(b.d_cig.p),
+                                         d_ncig, d_err, nsm, s)) != cudaSuccess)
+            break;
         if ((e = cub::DeviceScan::ExclusiveSum(b.d_tmp.p, scan_bytes, d_ncig, d_doff, (int)cn + 1, s)) != cudaSuccess) break;
         // scores and run counts back; the host derives the offsets the device scan also made
         int32_t *hr = static_cast<int32_t *>(b.h_res.p);
@@ -1080,7 +1121,7 @@ extern "C" int bwacuda_ksw_global2_batch(bwacuda_ctx *c, const bwacuda_global_jo
             short_buf = true;
         }
         c->stats.d2h_bytes += cn * 8;
-        c->stats.kernel_launches += 3;
+        c->stats.kernel_launches += 4;
         out_base += tot;
         c0 += cn;
     }
