@@ -66,6 +66,7 @@ constexpr int GLB_NEG16 = -24576;
 // what a DP kernel leaves in ncig[k] for the traceback kernel: the direction-byte layout
 constexpr int GLB_TB_ROWS = -1;   // a row's bytes from column beg (32-bit cell kernel)
 constexpr int GLB_TB_PAIRS = -2;  // from column beg & ~1 (pair kernel)
+constexpr int GLB_SIDE_STREAMS = 2;  // streams beside the context's for the bucket DP launches
 constexpr int GLB_NARROW_D = 8000;
 struct GlbNarrowRule {
     int cost;  // max(o_del + e_del, o_ins + e_ins, -min score, max score)
@@ -554,15 +555,19 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
     atomicAdd(cells_total, ncells);
 }
 
-// The traceback of every job whose DP ran (one thread per job, no shared memory, so the SMs
-// hold many warps and the walk's dependent HBM reads overlap across jobs).  ncig[k] carries the
-// layout the DP kernel wrote the direction bytes in (0: the job was rejected, no walk) and
-// leaves with the run count.
-__global__ void __launch_bounds__(256) glb_traceback_kernel(const GlobalDevJob *__restrict__ jobs, uint32_t n,
-                                                            const uint8_t *__restrict__ z, uint32_t *__restrict__ cig,
-                                                            int32_t *__restrict__ ncig, uint32_t *__restrict__ err)
+// The traceback of jobs order[base .. base + count) (base .. base + count without an order)
+// whose DP ran: one thread per job, no shared memory, so its warps fit beside the
+// shared-memory-bound DP kernel of another bucket and the walk's dependent HBM reads overlap
+// that kernel's ALU work.  ncig[k] carries the layout the DP kernel wrote the direction bytes in
+// (0: the job was rejected, no walk) and leaves with the run count.
+__global__ void __launch_bounds__(256) glb_traceback_kernel(const GlobalDevJob *__restrict__ jobs,
+                                                            const uint32_t *__restrict__ order, uint32_t base,
+                                                            uint32_t count, const uint8_t *__restrict__ z,
+                                                            uint32_t *__restrict__ cig, int32_t *__restrict__ ncig,
+                                                            uint32_t *__restrict__ err)
 {
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+        const uint32_t k = order ? order[base + t] : base + t;
         const int layout = ncig[k];
         if (layout != GLB_TB_ROWS && layout != GLB_TB_PAIRS) continue;
         const GlobalDevJob J = jobs[k];
@@ -783,13 +788,14 @@ cudaError_t launch_global(const uint8_t *seq, const GlobalDevJob *jobs, const ui
                                      s);
 }
 
-// The traceback of jobs 0 .. n after every DP launch of the chunk.
-cudaError_t launch_global_traceback(const GlobalDevJob *jobs, uint32_t n, const uint8_t *z, uint32_t *cig,
-                                    int32_t *ncig, uint32_t *err, int nsm, cudaStream_t s)
+// The traceback of jobs order[base .. base + count), after their DP launches.
+cudaError_t launch_global_traceback(const GlobalDevJob *jobs, const uint32_t *order, uint32_t base, uint32_t count,
+                                    const uint8_t *z, uint32_t *cig, int32_t *ncig, uint32_t *err, int nsm,
+                                    cudaStream_t s)
 {
-    if (n == 0) return cudaSuccess;
-    const uint32_t grid = (uint32_t)std::min<size_t>((n + 255) / 256, (size_t)nsm * 8);
-    glb_traceback_kernel<<<grid, 256, 0, s>>>(jobs, n, z, cig, ncig, err);
+    if (count == 0) return cudaSuccess;
+    const uint32_t grid = (uint32_t)std::min<size_t>((count + 255) / 256, (size_t)nsm * 8);
+    glb_traceback_kernel<<<grid, 256, 0, s>>>(jobs, order, base, count, z, cig, ncig, err);
     return cudaGetLastError();
 }
 
@@ -826,6 +832,19 @@ struct GlobalBufs {
 
 struct GlobalState {
     GlobalBufs b;
+    static constexpr int NSIDE = GLB_SIDE_STREAMS;
+    cudaStream_t side[NSIDE] = {};  // bucket DP launches beside the context's stream
+    cudaEvent_t ready = nullptr, done[NSIDE] = {};
+    cudaError_t init_streams()
+    {
+        cudaError_t e = cudaSuccess;
+        if (!ready) e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
+        for (int x = 0; x < NSIDE && e == cudaSuccess; ++x) {
+            if (!side[x]) e = cudaStreamCreateWithFlags(&side[x], cudaStreamNonBlocking);
+            if (e == cudaSuccess && !done[x]) e = cudaEventCreateWithFlags(&done[x], cudaEventDisableTiming);
+        }
+        return e;
+    }
 };
 
 void global_release(bwacuda_ctx *c)
@@ -836,6 +855,14 @@ void global_release(bwacuda_ctx *c)
     b.d_seq.release(); b.d_jobs.release(); b.d_z.release(); b.d_cig.release(); b.d_res.release();
     b.d_doff.release(); b.d_dense.release(); b.d_tmp.release();
     b.d_sz.release(); b.d_flags.release(); b.h_tot.release();
+    for (int x = 0; x < GlobalState::NSIDE; ++x) {
+        if (c->global->side[x]) {
+            cudaStreamSynchronize(c->global->side[x]);
+            cudaStreamDestroy(c->global->side[x]);
+        }
+        if (c->global->done[x]) cudaEventDestroy(c->global->done[x]);
+    }
+    if (c->global->ready) cudaEventDestroy(c->global->ready);
     delete c->global;
     c->global = nullptr;
 }
@@ -853,8 +880,10 @@ int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n
                         const GlbNarrowRule &nrule, int32_t *score, uint64_t *cigar_off, uint32_t *cigar,
                         size_t cigar_cap)
 {
-    GlobalBufs &b = c->global->b;
+    GlobalState &G = *c->global;
+    GlobalBufs &b = G.b;
     cudaStream_t s = c->stream;
+    if (cudaError_t e0 = G.init_streams()) return cuda_status(e0);
     uint32_t *d_err = static_cast<uint32_t *>(c->d_misc.p);
     unsigned long long *d_cells = reinterpret_cast<unsigned long long *>((char *)c->d_misc.p + 8);
     // chunks of 4 x BWACUDA_OPT_CHUNK_JOBS jobs, at most 1M (several waves of the longest
@@ -939,18 +968,34 @@ int global_batch_device(bwacuda_ctx *c, const bwacuda_global_job *jobs, size_t n
         int32_t *d_ncig = d_score + cn + 1;
         uint64_t *d_doff = static_cast<uint64_t *>(b.d_doff.p);
         if ((e = cudaMemsetAsync(d_ncig + cn, 0, 4, s)) != cudaSuccess) break;
-        // one launch per non-empty length bucket, sized by the bucket's own maxima
+        // one DP launch per non-empty length bucket, sized by the bucket's own maxima, longest
+        // queries first, round-robin over the context's stream and the side streams so a
+        // bucket's blocks fill the last partial wave of the ones before it; the tracebacks
+        // follow all of them
         const uint32_t *hb = hf + 16, *hbd = hf + 32, *hbw = hf + 48;
-        for (int bk = 0; bk < GLB_NBUCKETS && e == cudaSuccess; ++bk) {
+        if ((e = cudaEventRecord(G.ready, s)) != cudaSuccess) break;
+        for (int x = 0; x < GlobalState::NSIDE && e == cudaSuccess; ++x) e = cudaStreamWaitEvent(G.side[x], G.ready, 0);
+        if (e != cudaSuccess) break;
+        int nl = 0;
+        for (int bk = GLB_NBUCKETS - 1; bk >= 0 && e == cudaSuccess; --bk) {
             const uint32_t b0 = hbd[2 * bk], b1 = hbd[2 * bk + 1];
             if (b1 <= b0) continue;
             e = launch_global(static_cast<const uint8_t *>(b.d_seq.p), dj, order, b0, b1 - b0, sc, (int)hb[2 * bk],
                               (int)hb[2 * bk + 1], hbw[bk] == 0u, static_cast<uint8_t *>(b.d_z.p),
-                              static_cast<uint32_t *>(b.d_cig.p), d_score, d_ncig, d_err, d_cells, s);
+                              static_cast<uint32_t *>(b.d_cig.p), d_score, d_ncig, d_err, d_cells,
+                              nl % (GlobalState::NSIDE + 1) ? G.side[nl % (GlobalState::NSIDE + 1) - 1] : s);
+            ++nl;
             c->stats.kernel_launches += 1;
         }
-        if (e != cudaSuccess) break;
-        if ((e = launch_global_traceback(dj, (uint32_t)cn, static_cast<const uint8_t *>(b.d_z.p),
+        for (int x = 0; x < GlobalState::NSIDE && e == cudaSuccess; ++x) {
+            e = cudaEventRecord(G.done[x], G.side[x]);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(s, G.done[x], 0);
+        }
+        if (e != cudaSuccess) {
+            for (int x = 0; x < GlobalState::NSIDE; ++x) cudaStreamSynchronize(G.side[x]);  // nothing runs on
+            break;
+        }
+        if ((e = launch_global_traceback(dj, nullptr, 0, (uint32_t)cn, static_cast<const uint8_t *>(b.d_z.p),
                                          static_cast<uint32_t *>(b.d_cig.p), d_ncig, d_err, nsm, s)) != cudaSuccess)
             break;
         if ((e = cub::DeviceScan::ExclusiveSum(b.d_tmp.p, t2, d_ncig, d_doff, (int)cn + 1, s)) != cudaSuccess) break;
@@ -1091,7 +1136,7 @@ extern "C" int bwacuda_ksw_global2_batch(bwacuda_ctx *c, const bwacuda_global_jo
                           static_cast<uint32_t *>(b.d_cig.p), d_score, d_ncig, d_err,
                           reinterpret_cast<unsigned long long *>((char *)c->d_misc.p + 8), s);
         if (e != cudaSuccess) break;
-        if ((e = launch_global_traceback(static_cast<const GlobalDevJob *>(b.d_jobs.p), (uint32_t)cn,
+        if ((e = launch_global_traceback(static_cast<const GlobalDevJob *>(b.d_jobs.p), nullptr, 0, (uint32_t)cn,
                                          static_cast<const uint8_t *>(b.d_z.p), static_cast<uint32_t *>(b.d_cig.p),
                                          d_ncig, d_err, nsm, s)) != cudaSuccess)
             break;
