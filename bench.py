@@ -548,6 +548,8 @@ def run_reference(args, rank, world):
 
 def run_case(args):
     """Small fixed case for ncu captures: two calls of one path, nothing timed."""
+    import ctypes as C
+
     import numpy as np
     import torch
 
@@ -574,9 +576,25 @@ def run_case(args):
         for _ in range(2):
             ctx.extend_batch(js)
     elif args.case == "global":
+        # through the C ABI with the host arrays held across calls, as the timed CIGAR stage
+        # (the first call touches the output pages; the second is the one to read)
         js = B.synth_global(args.jobs, seed=0)
+        n = len(js)
+        gjobs = np.zeros(n, dtype=B.GLOBAL_JOB)
+        gjobs["query"] = js.seq.ctypes.data + js.q_off.astype(np.uint64)
+        gjobs["target"] = js.seq.ctypes.data + js.t_off.astype(np.uint64)
+        gjobs["qlen"], gjobs["tlen"], gjobs["w"] = js.qlen, js.tlen, js.w
+        gmat = B.scmat()
+        gscore = np.zeros(n, np.int32)
+        offs = np.zeros(n + 1, np.uint64)
+        words = np.zeros(8 * n, np.uint32)
         for _ in range(2):
-            ctx.ksw_global2_batch(js)
+            rc = B.lib().bwacuda_ksw_global2_batch(ctx.h, C.c_void_p(gjobs.ctypes.data), n, 5,
+                                                   C.c_void_p(gmat.ctypes.data), 6, 1, 6, 1,
+                                                   C.c_void_p(gscore.ctypes.data), C.c_void_p(offs.ctypes.data),
+                                                   C.c_void_p(words.ctypes.data), len(words))
+            if rc != B.OK:
+                raise B.BwaCudaError(rc, "bwacuda_ksw_global2_batch")
     elif args.case == "windows":
         # mate rescue with the windows planned, clamped and unpacked on the device
         rw = B.RescueWindows(args.jobs, seed=0)
