@@ -22,7 +22,7 @@ OPT_EXT_PATH, OPT_CHUNK_JOBS, OPT_GRAPHS, OPT_PERSIST_BLOCK, OPT_RESCUE_KERNEL =
 RESCUE_AUTO, RESCUE_TPJ = 0, 1
 OPT_HOST_GATHER = 6
 GATHER_AUTO, GATHER_HOST, GATHER_DEVICE = 0, 1, 2
-OPT_GRAB, OPT_BUCKET_STEP, OPT_RESCUE_LANES, OPT_UNGAPPED = 7, 8, 9, 10
+OPT_GRAB, OPT_BUCKET_STEP, OPT_RESCUE_LANES, OPT_UNGAPPED, OPT_DEVICE_PIECE = 7, 8, 9, 10, 11
 PATH_PLAIN, PATH_BATCHED = 0, 1
 INT_MAX = 2**31 - 1
 

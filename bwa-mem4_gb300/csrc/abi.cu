@@ -302,6 +302,10 @@ extern "C" int bwacuda_set_option(bwacuda_ctx *c, int option, int64_t value)
         if (value != 8 && value != 16 && value != 32) return BWACUDA_EINVAL;
         c->rescue_lanes = (int)value;
         return BWACUDA_OK;
+    case BWACUDA_OPT_DEVICE_PIECE:
+        if (value < 1 || value > ((int64_t)1 << 30)) return BWACUDA_EINVAL;
+        c->dev_piece = (size_t)value;
+        return BWACUDA_OK;
     default:
         return BWACUDA_EINVAL;
     }
@@ -926,26 +930,11 @@ int device_qmax(bwacuda_ctx *c, const J *jobs, size_t n, cudaStream_t s, int *qm
     return BWACUDA_OK;
 }
 
-}  // namespace
-
-extern "C" int bwacuda_extend_device(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_dev_ext_job *d_jobs,
-                                     size_t n, const bwacuda_scoring *scp, int end_bonus, int zdrop, int path,
-                                     bwacuda_ext_result *d_out, void *stream)
+// The plain path over n device-resident jobs (n <= the context's piece size).
+int extend_device_plain(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_dev_ext_job *d_jobs, size_t n,
+                        const ExtParams &P, bwacuda_ext_result *d_out, cudaStream_t s)
 {
-    if (!c || !scp) return BWACUDA_EINVAL;
-    std::lock_guard<std::mutex> g(c->mu);
-    int rc = validate_scoring(scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
-    if (rc) return rc;
-    if (n == 0) return BWACUDA_OK;
-    if (!d_seq || !d_jobs || !d_out) return BWACUDA_EINVAL;
-    if (cudaSetDevice(c->device) != cudaSuccess) return BWACUDA_ECUDA;
-    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
-    ExtParams P;
-    P.sc = make_scoring(scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
-    P.end_bonus = end_bonus;
-    P.zdrop = zdrop;
-    P.ug = ungapped_rule(c, scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
-    if (path == BWACUDA_PATH_BATCHED) return extend_device_batched(c, d_seq, d_jobs, n, P, d_out, s);
+    int rc;
     int qmax = 0;
     if ((rc = device_qmax(c, d_jobs, n, s, &qmax)) != BWACUDA_OK) return rc;
     if ((size_t)qmax + 1 > ext_tpj_smem_limit_qcap(false)) return BWACUDA_EUNSUPPORTED;
@@ -978,6 +967,35 @@ extern "C" int bwacuda_extend_device(bwacuda_ctx *c, const uint8_t *d_seq, const
     return BWACUDA_OK;
 }
 
+}  // namespace
+
+extern "C" int bwacuda_extend_device(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_dev_ext_job *d_jobs,
+                                     size_t n, const bwacuda_scoring *scp, int end_bonus, int zdrop, int path,
+                                     bwacuda_ext_result *d_out, void *stream)
+{
+    if (!c || !scp) return BWACUDA_EINVAL;
+    std::lock_guard<std::mutex> g(c->mu);
+    int rc = validate_scoring(scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
+    if (rc) return rc;
+    if (n == 0) return BWACUDA_OK;
+    if (!d_seq || !d_jobs || !d_out) return BWACUDA_EINVAL;
+    if (cudaSetDevice(c->device) != cudaSuccess) return BWACUDA_ECUDA;
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+    ExtParams P;
+    P.sc = make_scoring(scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
+    P.end_bonus = end_bonus;
+    P.zdrop = zdrop;
+    P.ug = ungapped_rule(c, scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
+    // consecutive pieces on the stream: the sort, scans and kernels index a piece in 32 bits
+    for (size_t off = 0; off < n; off += c->dev_piece) {
+        const size_t m = std::min(c->dev_piece, n - off);
+        rc = path == BWACUDA_PATH_BATCHED ? extend_device_batched(c, d_seq, d_jobs + off, m, P, d_out + off, s)
+                                          : extend_device_plain(c, d_seq, d_jobs + off, m, P, d_out + off, s);
+        if (rc) return rc;
+    }
+    return BWACUDA_OK;
+}
+
 extern "C" int bwacuda_ksw_align2_device(bwacuda_ctx *c, const uint8_t *d_seq,
                                          const bwacuda_dev_rescue_job *d_jobs, size_t n,
                                          const bwacuda_scoring *scp, int minsc, int max_sc, int mode,
@@ -990,20 +1008,12 @@ extern "C" int bwacuda_ksw_align2_device(bwacuda_ctx *c, const uint8_t *d_seq,
 
 namespace bwacuda {
 
-// bwacuda_ksw_align2_device with the context lock already held.
-int ksw_align2_device_locked(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_dev_rescue_job *d_jobs, size_t n,
-                             const bwacuda_scoring *scp, int minsc, int max_sc, int mode, int lanes,
-                             bwacuda_rescue_result *d_out, void *stream)
+// One piece of a device-resident rescue call (n <= the context's piece size).
+static int ksw_align2_device_piece(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_dev_rescue_job *d_jobs, size_t n,
+                                   const Scoring &sc, int minsc, int mode, int lanes, bwacuda_rescue_result *d_out,
+                                   cudaStream_t s)
 {
-    int rc = validate_scoring(scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
-    if (rc) return rc;
-    if (max_sc < 1 || (mode != 0 && mode != 1) || (lanes != 0 && lanes != 8 && lanes != 16)) return BWACUDA_EINVAL;
-    if (n == 0) return BWACUDA_OK;
-    if (!d_seq || !d_jobs || !d_out) return BWACUDA_EINVAL;
-    if (cudaSetDevice(c->device) != cudaSuccess) return BWACUDA_ECUDA;
-    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
-    Scoring sc = make_scoring(scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
-    sc.max_sc = max_sc;
+    int rc;
     int qmax = 0;
     if ((rc = device_qmax(c, d_jobs, n, s, &qmax)) != BWACUDA_OK) return rc;
     const int qcap = (qmax + 15) / 16 * 16 + 16;
@@ -1053,6 +1063,29 @@ int ksw_align2_device_locked(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda
     c->stats.kernel_launches += 4;
     c->stats.rescue_jobs += n;
     c->dev_pending_stream = s;
+    return BWACUDA_OK;
+}
+
+// bwacuda_ksw_align2_device with the context lock already held.
+int ksw_align2_device_locked(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_dev_rescue_job *d_jobs, size_t n,
+                             const bwacuda_scoring *scp, int minsc, int max_sc, int mode, int lanes,
+                             bwacuda_rescue_result *d_out, void *stream)
+{
+    int rc = validate_scoring(scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
+    if (rc) return rc;
+    if (max_sc < 1 || (mode != 0 && mode != 1) || (lanes != 0 && lanes != 8 && lanes != 16)) return BWACUDA_EINVAL;
+    if (n == 0) return BWACUDA_OK;
+    if (!d_seq || !d_jobs || !d_out) return BWACUDA_EINVAL;
+    if (cudaSetDevice(c->device) != cudaSuccess) return BWACUDA_ECUDA;
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+    Scoring sc = make_scoring(scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
+    sc.max_sc = max_sc;
+    // consecutive pieces on the stream: the scans and kernels index a piece in 32 bits
+    for (size_t off = 0; off < n; off += c->dev_piece) {
+        const size_t m = std::min(c->dev_piece, n - off);
+        if ((rc = ksw_align2_device_piece(c, d_seq, d_jobs + off, m, sc, minsc, mode, lanes, d_out + off, s)))
+            return rc;
+    }
     return BWACUDA_OK;
 }
 

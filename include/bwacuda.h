@@ -136,6 +136,11 @@ typedef struct bwacuda_ctx bwacuda_ctx;
  * uniform 5x5 matrices only).  Results are identical with it on or off; 0 = off
  * (default), 1 = on. */
 #define BWACUDA_OPT_UNGAPPED 10
+/* Device-resident calls (bwacuda_extend_device, bwacuda_ksw_align2_device): jobs per
+ * launch sequence, 1 .. 1,073,741,824 (default, the maximum: the sorts, scans and kernels
+ * index a sequence's jobs in 32 bits).  A larger batch runs as consecutive sequences on
+ * the call's stream, with the same results. */
+#define BWACUDA_OPT_DEVICE_PIECE 11
 
 int bwacuda_ctx_create(int device, bwacuda_ctx **out);
 void bwacuda_ctx_destroy(bwacuda_ctx *ctx);

@@ -186,6 +186,24 @@ def test_device_entry_equals_oracle(ctx, path):
         assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("path", DEVICE_PATHS)
+def test_device_batch_in_pieces(ctx, path):
+    # a device-resident batch larger than the piece size runs as consecutive launch sequences
+    # (each piece sorted and bucketed on its own, a ragged last piece), with the same results
+    js = B.synth_ext(3, 20000, seed=15)
+    want, _ = oracle.extend_batch(js)
+    ctx.set_option(B.OPT_DEVICE_PIECE, 6007)
+    try:
+        outs = _device_run(ctx, js, path, reps=2)
+    finally:
+        ctx.set_option(B.OPT_DEVICE_PIECE, 1 << 30)
+    for got in outs:
+        assert np.array_equal(got, want)
+    for bad in (0, -1, (1 << 30) + 1):
+        with pytest.raises(B.BwaCudaError):
+            ctx.set_option(B.OPT_DEVICE_PIECE, bad)
+
+
 @pytest.mark.parametrize("block", [32, 64, 128, 256])
 def test_persistent_block_sizes(ctx, block):
     js = B.synth_ext(2, 20000, seed=13)

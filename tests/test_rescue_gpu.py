@@ -100,6 +100,23 @@ def test_device_entry(rctx):
     assert np.array_equal(d_out.cpu().numpy().view(B.ALN_RES), want)
 
 
+def test_device_entry_in_pieces(rctx):
+    import torch
+
+    js = B.synth_rescue(5000, seed=16)
+    want, _ = oracle.align2_batch(js, minsc=20)
+    d_seq = torch.from_numpy(js.seq).cuda()
+    d_jobs = torch.from_numpy(js.dev_res_jobs().view(np.uint8)).cuda()
+    d_out = torch.zeros(len(js) * 28, dtype=torch.uint8, device="cuda")
+    rctx.set_option(B.OPT_DEVICE_PIECE, 1201)  # four whole pieces and a ragged one
+    try:
+        rctx.ksw_align2_device(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), d_out.data_ptr(), minsc=20)
+        rctx.sync()
+    finally:
+        rctx.set_option(B.OPT_DEVICE_PIECE, 1 << 30)
+    assert np.array_equal(d_out.cpu().numpy().view(B.ALN_RES), want)
+
+
 def test_edge_cases(rctx):
     pairs = [([], [0, 1, 2]), ([0, 1], []), ([], []), ([4, 4, 4], [4, 4, 4]), ([0] * 300, [0] * 400),
              ([1, 2, 3, 0] * 70, [1, 2, 3, 0] * 100), ([2], [2])]
