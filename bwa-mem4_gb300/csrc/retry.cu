@@ -171,7 +171,12 @@ extern "C" int bwacuda_extend_retry_device(bwacuda_ctx *c, const uint8_t *d_seq,
     P.end_bonus = end_bonus;
     P.zdrop = zdrop;
     P.ug = ungapped_rule(c, scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
-    rc = retry_rounds(c, d_seq, d_jobs, n, P, max_tries, d_prev, d_out, d_w_used, s);
+    // consecutive pieces on the stream (every job's rounds are its own)
+    for (size_t off = 0; off < n && rc == BWACUDA_OK; off += c->dev_piece) {
+        const size_t m = std::min(c->dev_piece, n - off);
+        rc = retry_rounds(c, d_seq, d_jobs + off, m, P, max_tries, d_prev ? d_prev + off : nullptr, d_out + off,
+                          d_w_used ? d_w_used + off : nullptr, s);
+    }
     c->stats.ext_jobs += n;
     c->dev_pending_stream = s;
     return rc;
@@ -188,7 +193,7 @@ extern "C" int bwacuda_extend_batch_retry(bwacuda_ctx *c, const bwacuda_ext_job 
     if (rc) return rc;
     if (w < 0 || max_tries < 1 || max_tries > 8 || (n && (!jobs || !out))) return BWACUDA_EINVAL;
     if (n == 0) return BWACUDA_OK;
-    if (n > ((size_t)1 << 31)) return BWACUDA_EUNSUPPORTED;
+    if (n > ((size_t)1 << 28)) return BWACUDA_EUNSUPPORTED;  // one gather of 16 chunks at most
     if (cudaSetDevice(c->device) != cudaSuccess) return BWACUDA_ECUDA;
     if ((rc = retry_prepare(c)) != BWACUDA_OK) return rc;
     RetryState &R = *c->retry;

@@ -136,7 +136,8 @@ typedef struct bwacuda_ctx bwacuda_ctx;
  * uniform 5x5 matrices only).  Results are identical with it on or off; 0 = off
  * (default), 1 = on. */
 #define BWACUDA_OPT_UNGAPPED 10
-/* Device-resident calls (bwacuda_extend_device, bwacuda_ksw_align2_device): jobs per
+/* Device-resident calls (bwacuda_extend_device, bwacuda_ksw_align2_device,
+ * bwacuda_extend_retry_device): jobs per
  * launch sequence, 1 .. 1,073,741,824 (default, the maximum: the sorts, scans and kernels
  * index a sequence's jobs in 32 bits).  A larger batch runs as consecutive sequences on
  * the call's stream, with the same results. */
@@ -170,7 +171,8 @@ int bwacuda_extend_batch(bwacuda_ctx *ctx, const bwacuda_ext_job *jobs, size_t n
  * out[k] is the accepted round's result, w_used[k] (may be NULL) its band.  The
  * jobs stay on the GPU across rounds (one count readback per round).  No
  * single-call counterpart in the reference, which loops on the host around
- * SwBackend::extend_batch. */
+ * SwBackend::extend_batch.  At most 268,435,456 jobs per call (BWACUDA_EUNSUPPORTED
+ * above). */
 int bwacuda_extend_batch_retry(bwacuda_ctx *ctx, const bwacuda_ext_job *jobs, size_t n, int m,
                                const int8_t *mat, int o_del, int e_del, int o_ins, int e_ins, int w,
                                int end_bonus, int zdrop, int max_tries, const int32_t *prev,
@@ -286,7 +288,8 @@ int bwacuda_extend_device(bwacuda_ctx *ctx, const uint8_t *d_seq, const bwacuda_
                           int path, bwacuda_ext_result *d_out, void *stream);
 /* bwacuda_extend_batch_retry on device-resident jobs: round 0 uses each job's own
  * w (doubled per round); d_prev as prev above (NULL: -1); returns after the last
- * round is enqueued on stream (bwacuda_ctx_sync waits and reports errors). */
+ * round is enqueued on stream (bwacuda_ctx_sync waits and reports errors).  Runs in
+ * pieces of BWACUDA_OPT_DEVICE_PIECE jobs, as bwacuda_extend_device. */
 int bwacuda_extend_retry_device(bwacuda_ctx *ctx, const uint8_t *d_seq, const bwacuda_dev_ext_job *d_jobs,
                                 size_t n, const bwacuda_scoring *sc, int end_bonus, int zdrop, int max_tries,
                                 const int32_t *d_prev, bwacuda_ext_result *d_out, int32_t *d_w_used,

@@ -60,7 +60,8 @@ def test_host_retry_matches_run_side(ctx, route, w0, max_tries):
         assert ctx.stats()["ext_retry_jobs"] > 0  # narrow bands do send jobs round again
 
 
-def test_device_retry_per_job_bands(ctx):
+@pytest.mark.parametrize("piece", [1 << 30, 7001])
+def test_device_retry_per_job_bands(ctx, piece):
     import torch
 
     js = B.synth_ext(3, 30000, seed=61)
@@ -72,9 +73,13 @@ def test_device_retry_per_job_bands(ctx):
     d_out = torch.zeros(len(js) * 24, dtype=torch.uint8, device="cuda")
     d_w = torch.zeros(len(js), dtype=torch.int32, device="cuda")
     d_prev = torch.from_numpy(prev).cuda()
-    ctx.extend_retry_device(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), d_out.data_ptr(), d_w.data_ptr(),
-                            d_prev.data_ptr(), max_tries=3)
-    ctx.sync()
+    ctx.set_option(B.OPT_DEVICE_PIECE, piece)  # 7001: four whole pieces and a ragged one
+    try:
+        ctx.extend_retry_device(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), d_out.data_ptr(), d_w.data_ptr(),
+                                d_prev.data_ptr(), max_tries=3)
+        ctx.sync()
+    finally:
+        ctx.set_option(B.OPT_DEVICE_PIECE, 1 << 30)
     assert np.array_equal(d_out.cpu().numpy().view(B.EXT_RES), want)
     assert np.array_equal(d_w.cpu().numpy(), want_w)
 
