@@ -66,6 +66,7 @@ constexpr int GLB_NEG16 = -24576;
 // what a DP kernel leaves in ncig[k] for the traceback kernel: the direction-byte layout
 constexpr int GLB_TB_ROWS = -1;   // a row's bytes from column beg (32-bit cell kernel)
 constexpr int GLB_TB_PAIRS = -2;  // from column beg & ~1 (pair kernel)
+constexpr int GLB_TB_AHEAD = 4;     // traceback cells loaded together down the diagonal
 constexpr int GLB_SIDE_STREAMS = 2;  // streams beside the context's for the bucket DP launches
 constexpr int GLB_NARROW_D = 8000;
 struct GlbNarrowRule {
@@ -123,22 +124,52 @@ __device__ int global_traceback(const uint8_t *zj, size_t zrow, int n_col, int q
     long i = (long)tlen - 1;
     long kk = ((long)tlen - 1 + w + 1 < qlen ? (long)tlen - 1 + w + 1 : (long)qlen) - 1;
     uint32_t which = 0;
+    const long total = (long)n_col * tlen;
     while (i >= 0 && kk >= 0) {
-        const long beg = i > w ? i - w : 0;
-        // the reference reads the flat row-major matrix: an offset past the row lands in a later row
-        const long flat = i * (long)n_col + (kk - beg);
-        if (kk < beg || flat >= (long)n_col * tlen) return -1;
-        long row = i, col = kk - beg;
-        if (col >= n_col) {
-            row = flat / n_col;
-            col = flat - row * n_col;
+        // In state M the walk usually stays on the diagonal: the next GLB_TB_AHEAD cells down it
+        // are loaded together (independent loads, their latencies overlap), then consumed while
+        // every step is diagonal; a step off the diagonal, or state E / F, loads afresh.
+        const int ahead = which == 0 ? GLB_TB_AHEAD : 1;
+        uint32_t dv[GLB_TB_AHEAD];
+        bool okv[GLB_TB_AHEAD];
+#pragma unroll
+        for (int t = 0; t < GLB_TB_AHEAD; ++t) {
+            const long ii = i - t, kt = kk - t;
+            dv[t] = 0;
+            okv[t] = false;
+            if (t < ahead && ii >= 0 && kt >= 0) {
+                const long beg = ii > w ? ii - w : 0;
+                // the reference reads the flat row-major matrix: an offset past the row lands in a
+                // later row; one before the band or past the matrix is its panic
+                const long flat = ii * (long)n_col + (kt - beg);
+                if (kt >= beg && flat < total) {
+                    long row = ii, col = kt - beg;
+                    if (col >= n_col) {
+                        row = flat / n_col;
+                        col = flat - row * n_col;
+                    }
+                    const long shift = PAIR ? ((row > w ? row - w : 0) & 1) : 0;
+                    dv[t] = zj[(size_t)row * zrow + (size_t)(col + shift)];
+                    okv[t] = true;
+                }
+            }
         }
-        const long shift = PAIR ? ((row > w ? row - w : 0) & 1) : 0;
-        const uint32_t d = zj[(size_t)row * zrow + (size_t)(col + shift)];
-        which = (d >> (which << 1)) & 3u;
-        if (which == 0) { cigar_push(cg, nc, 0, 1); --i; --kk; }
-        else if (which == 1) { cigar_push(cg, nc, 2, 1); --i; }
-        else { cigar_push(cg, nc, 1, 1); --kk; }
+#pragma unroll
+        for (int t = 0; t < GLB_TB_AHEAD; ++t) {
+            // (i, kk) is cell t down the diagonal from where the loads started
+            if (t >= ahead || i < 0 || kk < 0) break;
+            if (!okv[t]) return -1;
+            which = (dv[t] >> (which << 1)) & 3u;
+            if (which == 0) {
+                cigar_push(cg, nc, 0, 1);
+                --i;
+                --kk;
+                continue;
+            }
+            if (which == 1) { cigar_push(cg, nc, 2, 1); --i; }
+            else { cigar_push(cg, nc, 1, 1); --kk; }
+            break;
+        }
     }
     if (i >= 0) cigar_push(cg, nc, 2, (uint32_t)(i + 1));
     if (kk >= 0) cigar_push(cg, nc, 1, (uint32_t)(kk + 1));
