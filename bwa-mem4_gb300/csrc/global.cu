@@ -67,7 +67,8 @@ constexpr int GLB_NEG16 = -24576;
 constexpr int GLB_TB_ROWS = -1;   // a row's bytes from column beg (32-bit cell kernel)
 constexpr int GLB_TB_PAIRS = -2;  // from column beg & ~1 (pair kernel)
 constexpr int GLB_TB_AHEAD = 4;     // traceback cells loaded together down the diagonal
-constexpr int GLB_SIDE_STREAMS = 2;  // streams beside the context's for the bucket DP launches
+constexpr int GLB_SIDE_STREAMS = 2;
+constexpr int GLB_Q4_BELOW_WARPS = 12;  // pair kernel: 4-bit query codes below this many resident warps  // streams beside the context's for the bucket DP launches
 constexpr int GLB_NARROW_D = 8000;
 struct GlbNarrowRule {
     int cost;  // max(o_del + e_del, o_ins + e_ins, -min score, max score)
@@ -324,10 +325,18 @@ global_tpj_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restric
 }
 
 // Shared memory of a block for the pair kernel: the band slots as 8-byte pair words (bcap
-// rounded up to even) and the query as 16-bit selector pairs (one spare pair for the look-ahead).
-__host__ __device__ inline size_t global_smem_pair(int bcap, int qcap, int tb)
+// rounded up to even) and the query per column pair (one spare pair for the look-ahead) as a
+// 16-bit prmt selector, or (q4) as two 4-bit codes.
+__host__ __device__ inline size_t global_smem_pair(int bcap, int qcap, int tb, bool q4 = false)
 {
-    return (size_t)tb * ((size_t)((bcap + 1) / 2) * 8 + (size_t)((qcap + 2) / 2 + 1) * 2);
+    return (size_t)tb * ((size_t)((bcap + 1) / 2) * 8 + (size_t)((qcap + 2) / 2 + 1) * (q4 ? 1 : 2));
+}
+
+// A column pair's codes c0 | c1 << 4 as the prmt selector (0x80 | c0 * 0x11) | (0x80 | c1 * 0x11) << 8:
+// c0 | c1 << 8 by one mask and one multiply-add, then * 0x11 + 0x8080 (c <= 7: no carries).
+__device__ __forceinline__ uint32_t glb_q4_sel(uint32_t b)
+{
+    return (b + (b & 0xf0u) * 15u) * 0x11u + 0x8080u;
 }
 
 // One column of the recurrence in 32-bit registers (the head / tail columns of a row in the pair
@@ -403,7 +412,9 @@ struct GlbRowBytes {
 // band (x = column mod B2, B2 the band slots rounded up to even) is lane x & 1 of pair word
 // x / 2: .x = (H, H), .y = (E, E).  Sentinel-derived values are kept as in GlbCell<true>.
 // All lane sums stay inside int16: values lie in [GLB_NEG16 - D, D] with D <= GLB_NARROW_D.
-template <int TB>
+// Q4: the query as 4-bit code pairs (half the query's shared memory, more jobs resident, one
+// ALU and two multiply-add instructions per column pair to rebuild the selector).
+template <int TB, bool Q4>
 __global__ void __launch_bounds__(TB)
 global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restrict__ jobs,
                    const uint32_t *__restrict__ order, uint32_t base, uint32_t count,
@@ -421,7 +432,12 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
     const uint32_t k = order ? order[base + t] : base + t;
     const int bpairs = (bcap + 1) / 2;
     uint2 *cell2 = reinterpret_cast<uint2 *>(smem_raw) + tid;                          // cell2[p * TB]
-    uint16_t *qs2 = reinterpret_cast<uint16_t *>(smem_raw + (size_t)bpairs * 8 * TB) + tid;  // qs2[jp * TB]
+    // query word of column pair jp at [jp * TB]
+    uint16_t *qs2 = reinterpret_cast<uint16_t *>(smem_raw + (size_t)bpairs * 8 * TB) + tid;
+    uint8_t *qs1 = smem_raw + (size_t)bpairs * 8 * TB + tid;
+    auto qsel = [&](int jp) -> uint32_t {
+        return Q4 ? glb_q4_sel(qs1[(size_t)jp * TB]) : (uint32_t)qs2[(size_t)jp * TB];
+    };
     const GlobalDevJob J = jobs[k];
     const int qlen = J.qlen, tlen = J.tlen;
     const int w = J.w < 0 ? 0 : J.w;
@@ -440,9 +456,10 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
         return;
     }
     // query codes as prmt selector bytes 0x80 | c * 0x11 (two sign-extended 16-bit scores per
-    // prmt), two columns per 16-bit word; columns >= qlen are padding
+    // prmt), two columns per 16-bit word, or as two 4-bit codes per byte; columns >= qlen are
+    // padding
     for (int jp = 0; 2 * jp <= qlen; ++jp) {
-        uint32_t v = 0;
+        uint32_t v = 0, v4 = 0;
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
             const int j = 2 * jp + u;
@@ -450,8 +467,10 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
             if (j < qlen) bad |= c >= (uint32_t)sc.m;
             c = c < (uint32_t)sc.m || j >= qlen ? c : (uint32_t)PAD_CODE;
             v |= (0x80u | (c & 7u) * 0x11u) << (8 * u);
+            v4 |= (c & 7u) << (4 * u);
         }
-        qs2[(size_t)jp * TB] = (uint16_t)v;
+        if (Q4) qs1[(size_t)jp * TB] = (uint8_t)v4;
+        else qs2[(size_t)jp * TB] = (uint16_t)v;
     }
     // row -1 (as the scalar kernel): slot x holds column x
     for (int p = 0; p < P2; ++p) {
@@ -495,7 +514,7 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
             const int x = xj;
             uint2 cw = cell2[(size_t)(x >> 1) * TB];
             int e = (int)cw.y >> 16, h;
-            const uint32_t sel = (uint32_t)qs2[(size_t)(j >> 1) * TB] >> 8;
+            const uint32_t sel = qsel(j >> 1) >> 8;
             const uint32_t d = glb_cell((int)cw.x >> 16, e, f, (int)prmt(plo, phi, (sel & 0xffu) * 0x101u | 0x8800u),
                                         oe_del, sc.e_del, oe_ins, sc.e_ins, h);
             cw.x = (cw.x & 0xffffu) | ((uint32_t)h1 << 16);
@@ -511,14 +530,14 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
             uint32_t fv = (uint32_t)f << 16, h1v = (uint32_t)h1 << 16;
             int p = xj >> 1;
             uint2 wn = cell2[(size_t)p * TB];
-            uint32_t qn = qs2[(size_t)(j >> 1) * TB];
+            uint32_t qn = qsel(j >> 1);
             for (; j + 1 < end; j += 2) {
                 const uint2 cw = wn;
                 const uint32_t sel = qn;
                 const int pc = p;
                 if (++p == P2) p = 0;
                 wn = cell2[(size_t)p * TB];               // a row's columns use distinct slots
-                qn = qs2[(size_t)((j >> 1) + 1) * TB];    // j / 2 + 1 <= (qlen + 1) / 2: allocated
+                qn = qsel((j >> 1) + 1);                  // j / 2 + 1 <= (qlen + 1) / 2: allocated
                 const uint32_t s2 = prmt(plo, phi, sel);  // (s_j, s_j+1)
                 const uint32_t M2 = __viaddmax_s16x2(cw.x, s2, MIN2);  // H(i-1, .-1) + s
                 bool pm_hi, pm_lo, ph_hi, ph_lo, pf_hi, pf_lo, pe_hi, pe_lo;
@@ -549,7 +568,7 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
             const int x = xj;
             uint2 cw = cell2[(size_t)(x >> 1) * TB];
             int e = (int)(int16_t)(cw.y & 0xffffu), h;
-            const uint32_t sel = (uint32_t)qs2[(size_t)(j >> 1) * TB];
+            const uint32_t sel = qsel(j >> 1);
             const uint32_t d = glb_cell((int)(int16_t)(cw.x & 0xffffu), e, f,
                                         (int)prmt(plo, phi, (sel & 0xffu) * 0x101u | 0x8800u), oe_del, sc.e_del,
                                         oe_ins, sc.e_ins, h);
@@ -759,14 +778,14 @@ __global__ void glb_store_kernel(const GlobalDevJob *__restrict__ dj, uint32_t n
     }
 }
 
-template <int TB, bool NARROW>
+template <int TB, bool NARROW, bool Q4 = false>
 cudaError_t launch_global_tb(const uint8_t *seq, const GlobalDevJob *jobs, const uint32_t *order, uint32_t base,
                              uint32_t count, const Scoring &sc, int bcap, int qcap, uint8_t *z, uint32_t *cig,
                              int32_t *score, int32_t *ncig, uint32_t *err, unsigned long long *cells, cudaStream_t s)
 {
     // narrow jobs: the 16x2 pair kernel; wide jobs: 32-bit cells, one column at a time
-    const size_t smem = NARROW ? global_smem_pair(bcap, qcap, TB) : global_smem(bcap, qcap, TB, false);
-    auto kern = NARROW ? global_pair_kernel<TB> : global_tpj_kernel<TB, false>;
+    const size_t smem = NARROW ? global_smem_pair(bcap, qcap, TB, Q4) : global_smem(bcap, qcap, TB, false);
+    auto kern = NARROW ? global_pair_kernel<TB, Q4> : global_tpj_kernel<TB, false>;
     // process-wide per kernel: always the ceiling (concurrent contexts must not shrink it)
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT);
     if (e != cudaSuccess) return e;
@@ -782,16 +801,33 @@ cudaError_t launch_global_form(const uint8_t *seq, const GlobalDevJob *jobs, con
 {
     // the block size that keeps the most warps resident (shared memory bounds this kernel;
     // 228 KB per SM, 1 KB of it reserved per block), larger blocks on ties
-    int best_tb = 32, best_warps = 0;
-    for (int tb = 128; tb >= 32; tb >>= 1) {
-        const size_t sm = NARROW ? global_smem_pair(bcap, qcap, tb) : global_smem(bcap, qcap, tb, false);
-        if (sm > SMEM_LIMIT) continue;
-        const int blocks = std::min<int>(32, (int)((228u * 1024u) / (sm + 1024u)));
-        const int warps = std::min(64, blocks * tb / 32);
-        if (warps > best_warps) {
-            best_warps = warps;
-            best_tb = tb;
+    auto resident = [&](bool q4, int &best_tb) {
+        int best_warps = 0;
+        best_tb = 32;
+        for (int tb = 128; tb >= 32; tb >>= 1) {
+            const size_t sm = NARROW ? global_smem_pair(bcap, qcap, tb, q4) : global_smem(bcap, qcap, tb, false);
+            if (sm > SMEM_LIMIT) continue;
+            const int blocks = std::min<int>(32, (int)((228u * 1024u) / (sm + 1024u)));
+            const int warps = std::min(64, blocks * tb / 32);
+            if (warps > best_warps) {
+                best_warps = warps;
+                best_tb = tb;
+            }
         }
+        return best_warps;
+    };
+    int best_tb = 32, tb4 = 32;
+    const int warps = resident(false, best_tb);
+    // 4-bit query codes where the 16-bit selectors leave few warps resident and the codes add some
+    if (NARROW && warps < GLB_Q4_BELOW_WARPS && resident(true, tb4) > warps) {
+        if (tb4 == 128)
+            return launch_global_tb<128, NARROW, true>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score,
+                                                       ncig, err, cells, s);
+        if (tb4 == 64)
+            return launch_global_tb<64, NARROW, true>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score,
+                                                      ncig, err, cells, s);
+        return launch_global_tb<32, NARROW, true>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig,
+                                                  err, cells, s);
     }
     if (best_tb == 128)
         return launch_global_tb<128, NARROW>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score, ncig, err,
