@@ -67,8 +67,7 @@ constexpr int GLB_NEG16 = -24576;
 constexpr int GLB_TB_ROWS = -1;   // a row's bytes from column beg (32-bit cell kernel)
 constexpr int GLB_TB_PAIRS = -2;  // from column beg & ~1 (pair kernel)
 constexpr int GLB_TB_AHEAD = 4;     // traceback cells loaded together down the diagonal
-constexpr int GLB_SIDE_STREAMS = 2;
-constexpr int GLB_Q4_BELOW_WARPS = 12;  // pair kernel: 4-bit query codes below this many resident warps  // streams beside the context's for the bucket DP launches
+constexpr int GLB_SIDE_STREAMS = 2;  // streams beside the context's for the bucket DP launches
 constexpr int GLB_NARROW_D = 8000;
 struct GlbNarrowRule {
     int cost;  // max(o_del + e_del, o_ins + e_ins, -min score, max score)
@@ -818,8 +817,10 @@ cudaError_t launch_global_form(const uint8_t *seq, const GlobalDevJob *jobs, con
     };
     int best_tb = 32, tb4 = 32;
     const int warps = resident(false, best_tb);
-    // 4-bit query codes where the 16-bit selectors leave few warps resident and the codes add some
-    if (NARROW && warps < GLB_Q4_BELOW_WARPS && resident(true, tb4) > warps) {
+    // 4-bit query codes wherever they keep more warps resident (measured on the CIGAR-stage
+    // buckets: the extra instructions cost less than the added warps bring, also in the
+    // ALU-bound 100 and 150 bp buckets)
+    if (NARROW && resident(true, tb4) > warps) {
         if (tb4 == 128)
             return launch_global_tb<128, NARROW, true>(seq, jobs, order, base, count, sc, bcap, qcap, z, cig, score,
                                                        ncig, err, cells, s);
