@@ -227,10 +227,11 @@ def run_plain_fifo(B, pools, trace):
 
 def serve_bench(B, rates, count, seed=5, budget=8 << 30, tuning=None):
     pools = ServePools(B, seed)
-    # warm both sides (allocations, module loading) on a short trace
-    warm = serve_trace(1000.0, 8, seed + 99)
-    run_served(B, pools, warm, budget, tuning)
-    run_plain_fifo(B, pools, warm)
+    # warm both sides (allocations, module loading) on short traces: the served side's covers the
+    # request mix (read-pair and mixed-length extension, rescue) so that every kernel variant its
+    # waves use is loaded (CUDA loads a kernel's module at its first launch in the process)
+    run_served(B, pools, serve_trace(2000.0, 64, seed + 99), budget, tuning)
+    run_plain_fifo(B, pools, serve_trace(1000.0, 8, seed + 99))
     rows = []
     for rate in rates:
         # at most ~4 s of arrivals per rate (and at least 100 requests)

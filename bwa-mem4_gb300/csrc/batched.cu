@@ -31,7 +31,17 @@ struct BatchBufs {
     ExtParams g_P{};
     // per-SM room the bucket kernels leave for kernels running beside them
     int reserve_regs = 0, reserve_threads = 0;
+    size_t jobs_cap = 0;  // jobs the work buffers are sized for (batched_enqueue, batched_reserve)
 };
+
+// Jobs to size a reused slot's work buffers for, n or more: they grow at least twofold (every
+// regrowth frees a buffer, and cudaFree waits for the whole device, stalling the work of the
+// other streams, e.g. the serving loop's other waves).
+static size_t batched_grow_jobs(BatchBufs &bb, size_t n)
+{
+    if (n > bb.jobs_cap) bb.jobs_cap = std::max(n, bb.jobs_cap * 2);
+    return bb.jobs_cap;
+}
 
 struct BatchedState {
     int nsm = 0;
@@ -292,9 +302,17 @@ cudaError_t batched_enqueue(bwacuda_ctx *c, BatchBufs *bb, const uint8_t *d_seq,
                             size_t n, const ExtParams &P, bwacuda_ext_result *d_out, cudaStream_t s, uint32_t *err,
                             unsigned long long *cells)
 {
-    cudaError_t e = ensure_bufs(*bb, n);
+    cudaError_t e = ensure_bufs(*bb, batched_grow_jobs(*bb, n));
     if (e != cudaSuccess) return e;
     return enqueue_batched(c, *bb, d_seq, d_jobs, n, P, d_out, s, err, cells);
+}
+
+// Work buffers of a slot for n jobs ahead of its first batch (the serving loop's wave slots).
+cudaError_t batched_reserve(BatchBufs *bb, size_t n)
+{
+    cudaError_t e = ensure_bufs(*bb, n);
+    if (e == cudaSuccess) bb->jobs_cap = std::max(bb->jobs_cap, n);
+    return e;
 }
 
 // Host-buffer form: the plain path's packing pipeline, each chunk run batched.

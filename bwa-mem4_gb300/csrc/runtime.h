@@ -150,6 +150,7 @@ cudaError_t batched_enqueue(bwacuda_ctx *c, BatchBufs *bb, const uint8_t *d_seq,
                             size_t n, const ExtParams &P, bwacuda_ext_result *d_out, cudaStream_t s, uint32_t *err,
                             unsigned long long *cells);
 BatchBufs *batched_slot_bufs(bwacuda_ctx *c, int slot);  // work buffers of host-pipeline slot 0 or 1
+cudaError_t batched_reserve(BatchBufs *bb, size_t n);
 // registers / threads per SM that bb's bucket kernels leave free (0, 0: none)
 void batched_set_reserve(BatchBufs *bb, int regs, int threads);
 int batched_nsm(bwacuda_ctx *c);

@@ -447,6 +447,13 @@ bool settle_admitted(ServerState *S)
     return any;
 }
 
+// A wave slot's buffer: at least twofold growth, since every regrowth frees the old buffer and
+// cudaFree waits for the whole device (the other slots' waves and the admission copies).
+cudaError_t srv_grow(DevBuf &b, size_t bytes)
+{
+    return bytes <= b.cap ? cudaSuccess : b.ensure(std::max(bytes, b.cap * 2));
+}
+
 // Launch one wave on a free slot from the admitted requests of one group.
 bool launch_wave(ServerState *S)
 {
@@ -473,9 +480,9 @@ bool launch_wave(ServerState *S)
     for (Request *r : group)
         if ((e = cudaStreamWaitEvent(s, r->h2d, 0)) != cudaSuccess) return fail(e);
     const size_t rsz = lead->kind == 0 ? sizeof(bwacuda_ext_result) : sizeof(bwacuda_rescue_result);
-    if ((e = slot->desc.ensure(n * 32 + 64)) != cudaSuccess) return fail(e);
-    if ((e = slot->out.ensure(n * rsz + 64)) != cudaSuccess) return fail(e);
-    if (lead->kind == 1 && (e = slot->soff.ensure(n * 8 + 64)) != cudaSuccess) return fail(e);
+    if ((e = srv_grow(slot->desc, n * 32 + 64)) != cudaSuccess) return fail(e);
+    if ((e = srv_grow(slot->out, n * rsz + 64)) != cudaSuccess) return fail(e);
+    if (lead->kind == 1 && (e = srv_grow(slot->soff, n * 8 + 64)) != cudaSuccess) return fail(e);
     // gather descriptors (and tracker offsets) of the wave
     size_t at = 0;
     int qmax = 0;
@@ -688,6 +695,13 @@ extern "C" int bwacuda_server_start(bwacuda_ctx *c, const bwacuda_server_config 
         if (e == cudaSuccess && !w.bb) e = cudaErrorMemoryAllocation;
         // room for one admission-gather block per SM beside the wave's bucket kernels
         if (e == cudaSuccess) batched_set_reserve(w.bb, SRV_GATHER_THREADS * 64, SRV_GATHER_THREADS);
+        // buffers sized ahead for waves of budget / 1024 jobs (at most 8M): growing them while
+        // other waves run would wait for the whole device at every regrowth
+        const size_t n0 = std::min<size_t>(S->budget / 1024, size_t(1) << 23);
+        if (e == cudaSuccess) e = w.desc.ensure(n0 * 32 + 64);
+        if (e == cudaSuccess) e = w.out.ensure(n0 * sizeof(bwacuda_rescue_result) + 64);
+        if (e == cudaSuccess) e = w.soff.ensure(n0 * 8 + 64);
+        if (e == cudaSuccess) e = batched_reserve(w.bb, n0);
     }
     if (e != cudaSuccess) {
         c->server = S;

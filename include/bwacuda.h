@@ -331,8 +331,11 @@ int bwacuda_ksw_align2_device_noalloc(bwacuda_ctx *ctx, const uint8_t *d_seq,
  * device; each result equals what the batch calls return for the same jobs.
  * ------------------------------------------------------------------------ */
 typedef struct {
-    uint64_t hbm_budget_bytes; /* device arena for admitted requests (0 = 4 GiB); a pinned host arena of the same size mirrors it */
-    int32_t max_waves;         /* waves in flight (0 = 3) */
+    uint64_t hbm_budget_bytes; /* device arena for admitted requests (0 = 4 GiB); a pinned host arena of the same size mirrors it
+                                  where the device cannot read pageable host memory.  Each wave slot also holds work buffers
+                                  sized at start for waves of min(budget / 1024, 8M) jobs (about 80 bytes a job), grown
+                                  twofold past that */
+    int32_t max_waves;         /* waves in flight (0 = 3), one work-buffer slot each */
     int32_t max_requests;      /* requests held (queued, running or unread; 0 = 4096) */
 } bwacuda_server_config;
 
