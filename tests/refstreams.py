@@ -280,3 +280,32 @@ def rescue_bench_jobs(n):
             q[p] = nx() % 4
         out.append((q, t))
     return out
+
+
+def third_party_oracle_pairs():
+    """crates/bwa-extend/tests/third_party_oracle.rs:246-298 -- 300 local-SW pairs per scoring:
+    qlen 1..160 over the full alphabet (N at ~3%), the target a noisy relative of the query
+    (8% substitutions / indels, N injected), tlen = qlen + 0..199.  One stream per scoring,
+    restarted from the same seed for each of (1, 4, 6, 1) and (2, 3, 5, 2)."""
+    nx = Lcg(0x51D39CF10BADC0DE)
+    out = []
+    for _ in range(300):
+        qlen = 1 + nx() % 160
+        q = [4 if nx() % 100 < 3 else nx() % 4 for _ in range(qlen)]
+        tlen = qlen + nx() % 200
+        t = []
+        qi = 0
+        while len(t) < tlen:
+            if qi < len(q) and nx() % 100 >= 8:
+                t.append(q[qi])
+                qi += 1
+            elif nx() % 100 < 3:
+                t.append(4)
+                if nx() % 2 == 0:
+                    qi += 1
+            else:
+                t.append(nx() % 4)
+                if nx() % 2 == 0:
+                    qi += 1
+        out.append((q, t))
+    return out
