@@ -904,29 +904,39 @@ extern "C" int bwacuda_ksw_local_fwd_batch(bwacuda_ctx *c, const bwacuda_fwd_job
 
 namespace {
 
-// Max query length over device jobs (synchronous: sizes the shared memory).
+// Max query length over device jobs (synchronous: sizes the shared memory), and whether any
+// job carries a negative length (out[1] != 0).
 template <typename J>
 __global__ void qmax_kernel(const J *__restrict__ jobs, uint32_t n, int *__restrict__ out)
 {
-    int mx = 0;
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    int mx = 0, neg = 0;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         mx = max(mx, jobs[k].qlen);
+        neg |= jobs[k].qlen < 0 || jobs[k].tlen < 0;
+    }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(out, mx);
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        neg |= __shfl_xor_sync(0xffffffffu, neg, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(out, mx);
+        if (neg) atomicOr(out + 1, 1);
+    }
 }
 
 template <typename J>
-int device_qmax(bwacuda_ctx *c, const J *jobs, size_t n, cudaStream_t s, int *qmax)
+int device_qmax(bwacuda_ctx *c, const J *jobs, size_t n, cudaStream_t s, int *qmax, bool *negative = nullptr)
 {
     int *d = reinterpret_cast<int *>((char *)c->d_misc.p + 32);
-    cudaError_t e = cudaMemsetAsync(d, 0, 4, s);
+    cudaError_t e = cudaMemsetAsync(d, 0, 8, s);
     if (e != cudaSuccess) return cuda_status(e);
     uint32_t grid = (uint32_t)std::min<size_t>((n + 255) / 256, 1024);
     if (grid) qmax_kernel<J><<<grid, 256, 0, s>>>(jobs, (uint32_t)n, d);
-    if ((e = cudaMemcpyAsync((char *)c->h_misc.p + 32, d, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_status(e);
+    if ((e = cudaMemcpyAsync((char *)c->h_misc.p + 32, d, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_status(e);
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_status(e);
     *qmax = *reinterpret_cast<int *>((char *)c->h_misc.p + 32);
+    if (negative) *negative = *reinterpret_cast<int *>((char *)c->h_misc.p + 36) != 0;
     return BWACUDA_OK;
 }
 
@@ -1015,7 +1025,9 @@ static int ksw_align2_device_piece(bwacuda_ctx *c, const uint8_t *d_seq, const b
 {
     int rc;
     int qmax = 0;
-    if ((rc = device_qmax(c, d_jobs, n, s, &qmax)) != BWACUDA_OK) return rc;
+    bool negative = false;
+    if ((rc = device_qmax(c, d_jobs, n, s, &qmax, &negative)) != BWACUDA_OK) return rc;
+    if (negative) return BWACUDA_EINVAL;  // a negative length would size the tracker scratch wrongly
     const int qcap = (qmax + 15) / 16 * 16 + 16;
     if ((size_t)qcap > rescue_tpj_smem_limit_qcap(false)) return BWACUDA_EUNSUPPORTED;
     // tracker scratch: exclusive scan of per-job capacities, total read back to size the pool

@@ -29,7 +29,7 @@ ext_tpj_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *__res
     CellT *cell = reinterpret_cast<CellT *>(smem_raw) + tid;
     uint32_t *qw = reinterpret_cast<uint32_t *>(reinterpret_cast<CellT *>(smem_raw) + (size_t)qcap * TB) + tid;
 
-    const uint32_t lim = count_ptr ? *count_ptr : n;
+    const uint32_t lim = count_ptr ? min(*count_ptr, n) : n;  // a device count never exceeds the launch's n
     const uint32_t k = blockIdx.x * TB + tid;
     bool active = k < lim;
     const uint32_t jid = active ? (order ? order[k] : k) : 0u;

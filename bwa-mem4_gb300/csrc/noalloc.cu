@@ -24,7 +24,8 @@
 //
 // The first call on a device looks the array up with cudaGetSymbolAddress,
 // which needs that device to be current; make that first call before any
-// stream capture.
+// stream capture.  Every call synchronises its stream before it returns, on
+// error paths too once a kernel may have been launched.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -117,6 +118,17 @@ int read_status(const NoallocPtrs &p, cudaStream_t s, NoallocStatus *h)
     return cuda_status(e);
 }
 
+// Waits for the call's stream on every return once a kernel may be in flight, so no kernel of
+// this call still writes the static arrays after the process-wide lock is released.
+struct StreamDrain {
+    cudaStream_t s;
+    bool armed = false;
+    ~StreamDrain()
+    {
+        if (armed) cudaStreamSynchronize(s);
+    }
+};
+
 }  // namespace
 
 }  // namespace bwacuda
@@ -142,10 +154,12 @@ extern "C" int bwacuda_ksw_align2_device_noalloc(bwacuda_ctx *c, const uint8_t *
     NoallocPtrs p;
     if ((rc = noalloc_setup(c->device, &p)) != BWACUDA_OK) return rc;
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+    StreamDrain drain{s};  // declared after the locks: runs before they are released
 
     // clear the status block, then find the longest query and target
     cudaError_t e = cudaMemsetAsync(p.status, 0, sizeof(NoallocStatus), s);
     if (e != cudaSuccess) return cuda_status(e);
+    drain.armed = true;
     uint32_t grid = (uint32_t)((n + 255) / 256);
     if (grid > 1024) grid = 1024;
     noalloc_scan_kernel<<<grid, 256, 0, s>>>(d_jobs, (uint32_t)n, p.status);
@@ -182,10 +196,13 @@ extern "C" int bwacuda_ksw_align2_device_noalloc(bwacuda_ctx *c, const uint8_t *
     L.err = &p.status->err;
     L.stream = s;
     if ((e = rescue_narrow_launch(c, L)) != cudaSuccess) return cuda_status(e);
+    c->stats.kernel_launches += 3;
     if (wide_fits) {
         L.only_wide = 1;
         if ((e = rescue_tpj_launch(L, true)) != cudaSuccess) return cuda_status(e);
+        c->stats.kernel_launches += 1;
     }
+    c->stats.rescue_jobs += n;
     if ((rc = read_status(p, s, &h)) != BWACUDA_OK) return rc;
     if (h.err & ERR_BASE) return BWACUDA_EBASE;
     if (h.err & (ERR_RANGE | ERR_SCRATCH)) return BWACUDA_EUNSUPPORTED;

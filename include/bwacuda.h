@@ -311,10 +311,10 @@ int bwacuda_ctx_sync(bwacuda_ctx *ctx);
  * 4 MiB of offsets, held by every GPU that loads the library until exit).
  * A call may hold at most 524288 jobs and n * (max tlen / 2 + 2) <= 16 Mi
  * tracker entries, else it returns BWACUDA_EUNSUPPORTED without launching.
- * Synchronous: returns after the results are written (errors included).
- * Calls share the static array: calls that overlap on the GPU race.  The first
- * call on a device resolves the array's address (cudaGetSymbolAddress) and must
- * come before any stream capture. */
+ * Synchronous: every call synchronises its stream before returning (errors
+ * included).  Calls share the static array: calls that overlap on the GPU race.
+ * The first call on a device resolves the array's address (cudaGetSymbolAddress)
+ * and must come before any stream capture. */
 int bwacuda_ksw_align2_device_noalloc(bwacuda_ctx *ctx, const uint8_t *d_seq,
                                       const bwacuda_dev_rescue_job *d_jobs, size_t n,
                                       const bwacuda_scoring *sc, int minsc, int max_sc, int mode,

@@ -48,3 +48,40 @@ def test_noalloc_rejects_oversized_calls(ctx):
     with pytest.raises(B.BwaCudaError) as e:
         ctx.ksw_align2_device_noalloc(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), out.data_ptr(), minsc=20)
     assert e.value.code == B.EUNSUPPORTED
+
+
+def test_noalloc_error_call_then_clean_call(ctx):
+    import torch
+
+    # a bad base code in the last job's target makes the call fail with BWACUDA_EBASE; the next
+    # call on clean input must not see that call's error flag or its scratch
+    n = 2000
+    js = B.synth_rescue(n, seed=24)
+    bad = js.seq.copy()
+    bad[int(js.t_off[-1]) + int(js.tlen[-1]) - 1] = 9
+    d_bad = torch.from_numpy(bad).cuda()
+    d_seq, d_jobs = _device_jobs(js)
+    out = torch.zeros(n * 28, dtype=torch.uint8, device="cuda")
+    with pytest.raises(B.BwaCudaError) as e:
+        ctx.ksw_align2_device_noalloc(d_bad.data_ptr(), d_jobs.data_ptr(), n, out.data_ptr(), minsc=20)
+    assert e.value.code == B.EBASE
+    want = torch.zeros(n * 28, dtype=torch.uint8, device="cuda")
+    got = torch.full((n * 28,), 0xCD, dtype=torch.uint8, device="cuda")
+    ctx.ksw_align2_device(d_seq.data_ptr(), d_jobs.data_ptr(), n, want.data_ptr(), minsc=20)
+    ctx.sync()
+    ctx.ksw_align2_device_noalloc(d_seq.data_ptr(), d_jobs.data_ptr(), n, got.data_ptr(), minsc=20)
+    torch.cuda.synchronize()
+    assert torch.equal(got, want)
+
+
+def test_noalloc_rejects_more_than_max_jobs(ctx):
+    import torch
+
+    # 524,289 jobs is one past the offsets array: rejected before anything is read or launched
+    n = (512 << 10) + 1
+    d_seq = torch.zeros(16, dtype=torch.uint8, device="cuda")
+    d_jobs = torch.zeros(n * 32, dtype=torch.uint8, device="cuda")
+    out = torch.zeros(n * 28, dtype=torch.uint8, device="cuda")
+    with pytest.raises(B.BwaCudaError) as e:
+        ctx.ksw_align2_device_noalloc(d_seq.data_ptr(), d_jobs.data_ptr(), n, out.data_ptr(), minsc=20)
+    assert e.value.code == B.EUNSUPPORTED
