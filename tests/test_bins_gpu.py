@@ -49,13 +49,16 @@ def test_per_job_labels_at_thresholds(ctx):
     mat = oracle.scmat(1, 4)
     for ql, tl, h0 in _boundary_jobs():
         t = rng.integers(0, 4, tl).astype(np.uint8)
-        q = t[:ql].copy()
+        q = rng.integers(0, 4, ql).astype(np.uint8)
+        k = min(ql, tl)
+        q[:k] = t[:k]
         js = B.JobSet.from_lists([q], [t], h0=[h0])
         before = np.array(_bins(ctx.stats()))
         got = ctx.extend_batch(js, mat)
         after = np.array(_bins(ctx.stats()))
         label = int(np.nonzero(after - before)[0][0])
         assert (after - before).sum() == 1
+        assert len(q) == ql and len(t) == tl
         assert label == oracle.ext_bin(ql, tl, h0, mat), (ql, tl, h0)
         assert np.array_equal(got, oracle.extend_batch(js, mat)[0])
 
