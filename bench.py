@@ -130,6 +130,8 @@ def apply_tuning(B, ctx, t):
         ctx.set_option(B.OPT_BUCKET_STEP, t["bucket_step"])
         ctx.set_option(B.OPT_RESCUE_KERNEL, t["rescue_kernel"])
         ctx.set_option(B.OPT_RESCUE_LANES, t["rescue_lanes"])
+        ctx.set_option(B.OPT_LONG_QLEN, t.get("long_qlen", 0))
+        ctx.set_option(B.OPT_LONG_LANES, t.get("long_lanes", 16))
 
 
 def run_served(B, pools, trace, budget, tuning=None):

@@ -206,6 +206,8 @@ pub mod ffi {
         pub candidates: i32,
         pub ext_gcups: f64,
         pub rescue_gcups: f64,
+        pub long_qlen: i32,
+        pub long_lanes: i32,
     }
 
     extern "C" {

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <atomic>
 #include <condition_variable>
 #include <cstring>
@@ -244,6 +245,7 @@ extern "C" void bwacuda_ctx_destroy(bwacuda_ctx *c)
         sl.h_seq.release(); sl.h_jobs.release(); sl.h_out.release(); sl.h_aux.release();
         sl.d_seq.release(); sl.d_jobs.release(); sl.d_out.release(); sl.d_aux.release();
         sl.d_scratch.release();
+        sl.d_xl.release();
         if (sl.done) cudaEventDestroy(sl.done);
         if (sl.stream) cudaStreamDestroy(sl.stream);
     }
@@ -251,6 +253,7 @@ extern "C" void bwacuda_ctx_destroy(bwacuda_ctx *c)
     c->h_misc.release();
     c->d_dev_aux.release();
     c->d_dev_scratch.release();
+    c->d_dev_xl.release();
     ats_release(c);
     global_release(c);
     retry_release(c);
@@ -302,6 +305,13 @@ extern "C" int bwacuda_set_option(bwacuda_ctx *c, int option, int64_t value)
         if (value != 8 && value != 16 && value != 32) return BWACUDA_EINVAL;
         c->rescue_lanes = (int)value;
         return BWACUDA_OK;
+    case BWACUDA_OPT_LONG_QLEN:
+        if (value < 0 || value > (1 << 30)) return BWACUDA_EINVAL;
+        if (cudaSetDevice(c->device) != cudaSuccess) return BWACUDA_ECUDA;
+        return batched_set_long(c, value == 0 ? INT_MAX : (int)value);
+    case BWACUDA_OPT_LONG_LANES:
+        if (value != 8 && value != 16 && value != 32) return BWACUDA_EINVAL;
+        return batched_set_long_lanes(c, (int)value);
     case BWACUDA_OPT_DEVICE_PIECE:
         if (value < 1 || value > ((int64_t)1 << 30)) return BWACUDA_EINVAL;
         c->dev_piece = (size_t)value;
@@ -379,13 +389,14 @@ struct ExtChunk {
     uint64_t bytes;     // sequence bytes
     int qmax;
     uint32_t nwide;
+    int w;              // the call's band
 };
 
 // Gather jobs [c0, c0+cn) into the slot's pinned buffers.  Returns the chunk summary.
 ExtChunk pack_ext_chunk(bwacuda_ctx *c, Slot &sl, const bwacuda_ext_job *jobs, size_t c0, size_t cn,
                         int w, int max_sc, int m, const int8_t *mat, int *rc)
 {
-    ExtChunk ch{c0, cn, 0, 0, 0};
+    ExtChunk ch{c0, cn, 0, 0, 0, w};
     *rc = BWACUDA_OK;
     const int P = c->pool.size();
     std::vector<uint64_t> part_bytes(P, 0);
@@ -485,6 +496,7 @@ int run_ext_chunk(bwacuda_ctx *c, int slot_i, const ExtChunk &ch, const ExtParam
     info.n = ch.cn;
     info.nwide = ch.nwide;
     info.qmax = ch.qmax;
+    info.w = ch.w;
     info.P = P;
     info.d_out = static_cast<bwacuda_ext_result *>(sl.d_out.p);
     int rc = run(slot_i, info, s);
@@ -496,10 +508,12 @@ int run_ext_chunk(bwacuda_ctx *c, int slot_i, const ExtChunk &ch, const ExtParam
 }
 
 // The plain path: narrow launch over the chunk in caller order, wide jobs from
-// the host-built list.
-int run_plain(bwacuda_ctx *c, const ExtChunkInfo &I, cudaStream_t s)
+// the host-built list; queries too long for a thread's shared-memory row go to the
+// group-per-job kernel.
+int run_plain(bwacuda_ctx *c, int slot_i, const ExtChunkInfo &I, cudaStream_t s)
 {
-    if ((size_t)I.qmax + 1 > ext_tpj_smem_limit_qcap(I.nwide > 0)) return BWACUDA_EUNSUPPORTED;
+    const int lim16 = (int)ext_tpj_smem_limit_qcap(false), lim32 = (int)ext_tpj_smem_limit_qcap(true);
+    const bool long16 = I.qmax + 1 > lim16, long32 = I.nwide > 0 && I.qmax + 1 > lim32;
     ExtLaunch L;
     L.seq = I.d_seq;
     L.jobs = I.d_jobs;
@@ -507,8 +521,9 @@ int run_plain(bwacuda_ctx *c, const ExtChunkInfo &I, cudaStream_t s)
     L.count_ptr = nullptr;
     L.n = I.n;
     L.P = I.P;
-    L.qcap = I.qmax + 1;
+    L.qcap = std::min(I.qmax + 1, lim16);
     L.only_wide = 0;
+    L.long_follows = long16;
     L.out = I.d_out;
     L.err = d_err(c);
     L.cells = d_cells(c);
@@ -521,9 +536,15 @@ int run_plain(bwacuda_ctx *c, const ExtChunkInfo &I, cudaStream_t s)
     if (I.nwide) {
         L.order = I.d_wide;
         L.n = I.nwide;
+        L.qcap = std::min(I.qmax + 1, lim32);
+        L.long_follows = long32;
         if ((e = ext_tpj_launch(L, true)) != cudaSuccess) return cuda_status(e);
         c->stats.kernel_launches++;
     }
+    if (long16 || long32)
+        return launch_long_unbucketed(c, c->slot[slot_i].d_xl, I.d_seq, I.d_jobs, I.n, I.P, I.d_out,
+                                      long16 ? lim16 : INT_MAX, long32 ? lim32 : INT_MAX, ext_long_ring_for_band(I.w),
+                                      s);
     return BWACUDA_OK;
 }
 
@@ -591,7 +612,7 @@ int extend_batch_host(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int
         return extend_batch_host_batched(c, jobs, n, m, mat, P, w, out);
     }
     return extend_host_pipeline(c, jobs, n, m, mat, P, w, out,
-                                [c](int, const ExtChunkInfo &I, cudaStream_t s) { return run_plain(c, I, s); });
+                                [c](int slot, const ExtChunkInfo &I, cudaStream_t s) { return run_plain(c, slot, I, s); });
 }
 
 }  // namespace bwacuda
@@ -617,6 +638,53 @@ extern "C" int bwacuda_extend(bwacuda_ctx *c, const uint8_t *query, int32_t qlen
     J.h0 = h0;
     return bwacuda_extend_batch(c, &J, 1, m, mat, o_del, e_del, o_ins, e_ins, w, end_bonus, zdrop, out);
 }
+
+// ------------------------------------------------------------------ long queries
+
+namespace bwacuda {
+
+int launch_long_unbucketed(bwacuda_ctx *c, DevBuf &xl, const uint8_t *seq, const bwacuda_dev_ext_job *jobs, size_t n,
+                           const ExtParams &P, bwacuda_ext_result *out, int min16, int min32, int ring, cudaStream_t s)
+{
+    int rc = batched_prepare(c);  // the SM count
+    if (rc) return rc;
+    cudaError_t e;
+    if ((e = xl.ensure(((size_t)XL_WORK_WORDS + n) * 4)) != cudaSuccess) return cuda_status(e);
+    uint32_t *work = static_cast<uint32_t *>(xl.p);
+    if ((e = cudaMemsetAsync(work, 0, XL_WORK_WORDS * 4, s)) != cudaSuccess) return cuda_status(e);
+    ExtLongLaunch X;
+    X.seq = seq;
+    X.jobs = jobs;
+    X.order = nullptr;
+    X.bounds = nullptr;
+    X.njobs = (uint32_t)n;
+    X.lanes = c->long_lanes;
+    X.ring_cols = ring;
+    X.P = P;
+    X.out = out;
+    X.err = d_err(c);
+    X.cells = d_cells(c);
+    X.defer = work + XL_WORK_WORDS;
+    X.defer_count = work + XL_WORK_DCOUNT;
+    X.stream = s;
+    const int nsm = batched_nsm(c);
+    for (int w32 = 0; w32 < 2; ++w32) {
+        const int mq = w32 ? min32 : min16;
+        if (mq == INT_MAX) continue;
+        X.min_qlen = mq;
+        X.counter = work + (w32 ? XL_WORK_COUNTER32 : XL_WORK_COUNTER16);
+        if ((e = ext_long_launch(X, w32 != 0, nsm)) != cudaSuccess) return cuda_status(e);
+        c->stats.kernel_launches++;
+    }
+    for (int w32 = 0; w32 < 2; ++w32) {
+        if ((w32 ? min32 : min16) == INT_MAX) continue;
+        if ((e = ext_long_deferred_launch(X, w32 != 0, work, nsm)) != cudaSuccess) return cuda_status(e);
+        c->stats.kernel_launches++;
+    }
+    return BWACUDA_OK;
+}
+
+}  // namespace bwacuda
 
 // ------------------------------------------------------------------ rescue
 
@@ -947,7 +1015,8 @@ int extend_device_plain(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_dev_
     int rc;
     int qmax = 0;
     if ((rc = device_qmax(c, d_jobs, n, s, &qmax)) != BWACUDA_OK) return rc;
-    if ((size_t)qmax + 1 > ext_tpj_smem_limit_qcap(false)) return BWACUDA_EUNSUPPORTED;
+    const int lim16 = (int)ext_tpj_smem_limit_qcap(false), lim32 = (int)ext_tpj_smem_limit_qcap(true);
+    const bool long16 = qmax + 1 > lim16, long32 = qmax + 1 > lim32;
     cudaError_t e;
     ExtLaunch L;
     L.seq = d_seq;
@@ -956,22 +1025,26 @@ int extend_device_plain(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_dev_
     L.count_ptr = nullptr;
     L.n = n;
     L.P = P;
-    L.qcap = qmax + 1;
-    L.only_wide = 0;
+    L.qcap = std::min(qmax + 1, lim16);
+    L.long_follows = long16;
     L.out = d_out;
     L.err = d_err(c);
     L.cells = d_cells(c);
     L.stream = s;
-    // wide cells need twice the shared memory: run them only if the block fits
-    const bool wide_fits = (size_t)qmax + 1 <= ext_tpj_smem_limit_qcap(true);
-    L.only_wide = wide_fits ? 0 : 2;
+    // narrow launch, then the wide one over the jobs needing 32-bit cells; queries too long for
+    // either go to the group-per-job kernel
+    L.only_wide = 0;
     if ((e = ext_tpj_launch(L, false)) != cudaSuccess) return cuda_status(e);
-    if (wide_fits) {
-        L.only_wide = 1;
-        if ((e = ext_tpj_launch(L, true)) != cudaSuccess) return cuda_status(e);
-        c->stats.kernel_launches += 1;
+    L.only_wide = 1;
+    L.qcap = std::min(qmax + 1, lim32);
+    L.long_follows = long32;
+    if ((e = ext_tpj_launch(L, true)) != cudaSuccess) return cuda_status(e);
+    c->stats.kernel_launches += 3;
+    if (long16 || long32) {
+        rc = launch_long_unbucketed(c, c->d_dev_xl, d_seq, d_jobs, n, P, d_out, long16 ? lim16 : INT_MAX,
+                                    long32 ? lim32 : INT_MAX, XL_RING_DEFAULT, s);
+        if (rc) return rc;
     }
-    c->stats.kernel_launches += 2;
     c->stats.ext_jobs += n;
     c->dev_pending_stream = s;
     return BWACUDA_OK;

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cstring>
 #include <vector>
 
@@ -19,6 +20,7 @@ constexpr int FAN = 4;  // bucket streams
 // Device work buffers of one in-flight batch.
 struct BatchBufs {
     DevBuf keys_in, keys_out, idx_in, idx_out, tmp, table;
+    DevBuf xl;  // group-per-job buckets: work words and the deferred-job list
     cudaStream_t fan[FAN] = {};
     cudaEvent_t fork = nullptr, join[FAN] = {};
     // graph cache for device-resident replays
@@ -51,6 +53,7 @@ struct BatchedState {
     int tb = 128;    // threads per block of the persistent kernels
     int grab = 1;    // 32-job rounds per work-counter grab
     int step = 32;   // query-length bucket width below 257 columns
+    int long_qlo = INT_MAX;  // buckets from this query length up use the group-per-job kernel
     uint64_t gen = 1;
     ExtBucketDef defs[EXT_MAX_BUCKETS];
     DevBuf d_defs;
@@ -68,7 +71,7 @@ static int batched_init(bwacuda_ctx *c)
         e = cudaDeviceGetAttribute(&B->sm_threads, cudaDevAttrMaxThreadsPerMultiProcessor, c->device);
     if (e == cudaSuccess) e = ext_sort_prefer_shared();
     if (e != cudaSuccess) { delete B; return cuda_status(e); }
-    B->nb = ext_bucket_defs(B->defs, EXT_MAX_BUCKETS, B->step);
+    B->nb = ext_bucket_defs(B->defs, EXT_MAX_BUCKETS, B->step, B->long_qlo);
     if ((e = B->d_defs.ensure(sizeof(B->defs))) != cudaSuccess) { delete B; return cuda_status(e); }
     if ((e = cudaMemcpy(B->d_defs.p, B->defs, sizeof(ExtBucketDef) * B->nb, cudaMemcpyHostToDevice)) != cudaSuccess) {
         delete B;
@@ -102,7 +105,7 @@ void batched_release(bwacuda_ctx *c)
         }
         if (bb.fork) cudaEventDestroy(bb.fork);
         bb.keys_in.release(); bb.keys_out.release(); bb.idx_in.release(); bb.idx_out.release();
-        bb.tmp.release(); bb.table.release();
+        bb.tmp.release(); bb.table.release(); bb.xl.release();
     }
     B->d_defs.release();
     delete B;
@@ -137,10 +140,42 @@ int batched_set_bucket_step(bwacuda_ctx *c, int step)
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return cuda_status(e);
     B->step = step;
-    B->nb = ext_bucket_defs(B->defs, EXT_MAX_BUCKETS, step);
+    B->nb = ext_bucket_defs(B->defs, EXT_MAX_BUCKETS, step, B->long_qlo);
     if ((e = cudaMemcpy(B->d_defs.p, B->defs, sizeof(ExtBucketDef) * B->nb, cudaMemcpyHostToDevice)) != cudaSuccess)
         return cuda_status(e);
     B->gen++;
+    return BWACUDA_OK;
+}
+
+// Query length from which the buckets use the group-per-job kernel (INT_MAX: only the
+// open-ended buckets); waits for in-flight batches like batched_set_bucket_step.
+int batched_set_long(bwacuda_ctx *c, int long_qlo)
+{
+    int rc = batched_init(c);
+    if (rc) return rc;
+    BatchedState *B = c->batched;
+    if (B->long_qlo == long_qlo) return BWACUDA_OK;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_status(e);
+    B->long_qlo = long_qlo;
+    B->nb = ext_bucket_defs(B->defs, EXT_MAX_BUCKETS, B->step, long_qlo);
+    if ((e = cudaMemcpy(B->d_defs.p, B->defs, sizeof(ExtBucketDef) * B->nb, cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cuda_status(e);
+    B->gen++;
+    return BWACUDA_OK;
+}
+
+int batched_get_long(bwacuda_ctx *c) { return c->batched ? c->batched->long_qlo : INT_MAX; }
+
+// Lanes per job of the group-per-job kernel; a new value invalidates captured graphs.
+int batched_set_long_lanes(bwacuda_ctx *c, int lanes)
+{
+    int rc = batched_init(c);
+    if (rc) return rc;
+    if (c->long_lanes != lanes) {
+        c->long_lanes = lanes;
+        c->batched->gen++;
+    }
     return BWACUDA_OK;
 }
 
@@ -159,6 +194,7 @@ static cudaError_t ensure_bufs(BatchBufs &bb, size_t n)
     if ((e = bb.keys_out.ensure(n * 2 + 16)) != cudaSuccess) return e;
     if ((e = bb.idx_in.ensure(n * 4 + 16)) != cudaSuccess) return e;
     if ((e = bb.idx_out.ensure(n * 4 + 16)) != cudaSuccess) return e;
+    if ((e = bb.xl.ensure(((size_t)XL_WORK_WORDS + n) * 4 + 16)) != cudaSuccess) return e;
     return bb.tmp.ensure(ext_sort_temp_bytes(n) + 256);
 }
 
@@ -177,9 +213,46 @@ static cudaError_t enqueue_batched(bwacuda_ctx *c, BatchBufs &bb, const uint8_t 
                                         static_cast<const ExtBucketDef *>(B->d_defs.p), B->nb,
                                         static_cast<uint32_t *>(bb.table.p), s);
     if (e != cudaSuccess) return e;
+    uint32_t *work = static_cast<uint32_t *>(bb.xl.p);
+    if ((e = cudaMemsetAsync(work, 0, XL_WORK_WORDS * 4, s)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(bb.fork, s)) != cudaSuccess) return e;
     for (int f = 0; f < FAN; ++f)
         if ((e = cudaStreamWaitEvent(bb.fan[f], bb.fork, 0)) != cudaSuccess) return e;
+    // Group-per-job buckets (the open-ended ones take queries of any length) one after
+    // another on the first stream, then the deferred launches over the jobs whose bands
+    // needed a larger ring; empty buckets exit at once.
+    ExtLongLaunch X;
+    X.seq = d_seq;
+    X.jobs = d_jobs;
+    X.order = static_cast<const uint32_t *>(bb.idx_out.p);
+    X.njobs = (uint32_t)n;
+    X.min_qlen = 0;
+    X.lanes = c->long_lanes;
+    X.ring_cols = XL_RING_DEFAULT;
+    X.P = P;
+    X.out = d_out;
+    X.err = err ? err : reinterpret_cast<uint32_t *>(c->d_misc.p);
+    X.cells = cells ? cells : reinterpret_cast<unsigned long long *>((char *)c->d_misc.p + 8);
+    X.defer = work + XL_WORK_WORDS;
+    X.defer_count = work + XL_WORK_DCOUNT;
+    X.reserve_regs = bb.reserve_regs;
+    X.reserve_threads = bb.reserve_threads;
+    X.sm_regs = B->sm_regs;
+    X.sm_threads = B->sm_threads;
+    X.stream = bb.fan[0];
+    bool long16 = false, long32 = false;
+    for (int b = B->nb - 1; b >= 0; --b) {
+        if (B->defs[b].kernel != 1) continue;
+        uint32_t *tab = static_cast<uint32_t *>(bb.table.p) + 4 * b;
+        X.bounds = tab;
+        X.counter = tab + 2;
+        const bool w32 = B->defs[b].cls == 2;
+        if ((e = ext_long_launch(X, w32, B->nsm)) != cudaSuccess) return e;
+        long16 |= !w32;
+        long32 |= w32;
+    }
+    if (long16 && (e = ext_long_deferred_launch(X, false, work, B->nsm)) != cudaSuccess) return e;
+    if (long32 && (e = ext_long_deferred_launch(X, true, work, B->nsm)) != cudaSuccess) return e;
     PersistLaunch L;
     L.seq = d_seq;
     L.jobs = d_jobs;
@@ -194,9 +267,10 @@ static cudaError_t enqueue_batched(bwacuda_ctx *c, BatchBufs &bb, const uint8_t 
     L.reserve_threads = bb.reserve_threads;
     L.sm_regs = B->sm_regs;
     L.sm_threads = B->sm_threads;
-    // largest buckets first: they hold the long jobs
-    for (int b = B->nb - 1, k = 0; b >= 0; --b, ++k) {
-        L.stream = bb.fan[k % FAN];
+    // thread-per-job buckets, largest first: they hold the long jobs
+    for (int b = B->nb - 1, k = 1; b >= 0; --b) {
+        if (B->defs[b].kernel == 1) continue;
+        L.stream = bb.fan[k++ % FAN];
         uint32_t *tab = static_cast<uint32_t *>(bb.table.p) + 4 * b;
         if ((e = ext_persist_launch(L, B->defs[b], tab, B->nsm, B->tb)) != cudaSuccess) return e;
     }
@@ -244,7 +318,7 @@ int extend_device_batched(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_de
     } else if ((e = enqueue_batched(c, bb, d_seq, d_jobs, n, P, d_out, s)) != cudaSuccess) {
         return cuda_status(e);
     }
-    c->stats.kernel_launches += 3 + c->batched->nb;
+    c->stats.kernel_launches += 3 + (uint64_t)batched_bucket_count(c);
     c->stats.ext_jobs += n;
     c->dev_pending_stream = s;
     return BWACUDA_OK;
@@ -258,7 +332,8 @@ void batched_set_reserve(BatchBufs *bb, int regs, int threads)
 }
 BatchBufs *batched_slot_bufs(bwacuda_ctx *c, int slot) { return &c->batched->bufs[slot & 1]; }
 int batched_nsm(bwacuda_ctx *c) { return c->batched->nsm; }
-int batched_bucket_count(bwacuda_ctx *c) { return c->batched->nb; }
+// Launches of the bucket stage: one per bucket and the two deferred group-per-job launches.
+int batched_bucket_count(bwacuda_ctx *c) { return c->batched->nb + 2; }
 
 static cudaError_t bufs_streams(BatchBufs &bb)
 {
@@ -294,7 +369,7 @@ void batchbufs_destroy(BatchBufs *bb)
     if (bb->fork) cudaEventDestroy(bb->fork);
     if (bb->graph) cudaGraphExecDestroy(bb->graph);
     bb->keys_in.release(); bb->keys_out.release(); bb->idx_in.release(); bb->idx_out.release();
-    bb->tmp.release(); bb->table.release();
+    bb->tmp.release(); bb->table.release(); bb->xl.release();
     delete bb;
 }
 
@@ -326,7 +401,7 @@ int extend_batch_host_batched(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_
         BatchBufs &bb = c->batched->bufs[slot];
         cudaError_t e = ensure_bufs(bb, I.n);
         if (e == cudaSuccess) e = enqueue_batched(c, bb, I.d_seq, I.d_jobs, I.n, I.P, I.d_out, s);
-        c->stats.kernel_launches += 3 + c->batched->nb;
+        c->stats.kernel_launches += 3 + (uint64_t)batched_bucket_count(c);
         return cuda_status(e);
     });
 }

@@ -144,7 +144,7 @@ static int max_qcap_of_class(int cls)
     return (int)ext_tpj_smem_limit_qcap(cls == 2);
 }
 
-int ext_bucket_defs(ExtBucketDef *defs, int max_defs, int step)
+int ext_bucket_defs(ExtBucketDef *defs, int max_defs, int step, int long_qlo)
 {
     if (step != 16 && step != 32 && step != 64) step = 32;
     int nb = 0;
@@ -160,6 +160,7 @@ int ext_bucket_defs(ExtBucketDef *defs, int max_defs, int step)
             d.qlo = lo;
             d.qhi = caps[c] - 1;
             d.qcap = caps[c];
+            d.kernel = d.qhi >= long_qlo ? 1 : 0;  // the bucket holds queries of long_qlo or more
             defs[nb++] = d;
             lo = caps[c];
         }
@@ -170,6 +171,7 @@ int ext_bucket_defs(ExtBucketDef *defs, int max_defs, int step)
             d.qlo = lo;
             d.qhi = 1 << 30;
             d.qcap = cls == 0 ? (int)ext_tpj_smem_limit_qcap(false) : max_qcap_of_class(cls);
+            d.kernel = 1;  // any query length
             defs[nb++] = d;
         }
     }

@@ -18,7 +18,7 @@ template <class F, int TB>
 __global__ void __launch_bounds__(TB)
 ext_tpj_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *__restrict__ jobs,
                const uint32_t *__restrict__ order, const uint32_t *__restrict__ count_ptr, uint32_t n,
-               const __grid_constant__ ExtParams P, int qcap, int only_wide,
+               const __grid_constant__ ExtParams P, int qcap, int only_wide, int long_follows,
                bwacuda_ext_result *__restrict__ out, uint32_t *__restrict__ err,
                unsigned long long *__restrict__ cells_total)
 {
@@ -47,7 +47,9 @@ ext_tpj_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *__res
             active = false;
         }
     }
-    if (active && (J.qlen < 0 || J.qlen + 1 > qcap)) {
+    if (active && J.qlen + 1 > qcap && J.qlen >= 0 && long_follows) {
+        active = false;  // the group-per-job launch that follows takes it
+    } else if (active && (J.qlen < 0 || J.qlen + 1 > qcap)) {
         atomicOr(err, ERR_RANGE);
         active = false;
     }
@@ -77,7 +79,8 @@ cudaError_t launch_ext_tb(const ExtLaunch &L)
     const uint32_t grid = (uint32_t)((L.n + TB - 1) / TB);
     if (grid == 0) return cudaSuccess;
     ext_tpj_kernel<F, TB><<<grid, TB, smem, L.stream>>>(L.seq, L.jobs, L.order, L.count_ptr, (uint32_t)L.n,
-                                                       L.P, L.qcap, L.only_wide, L.out, L.err, L.cells);
+                                                       L.P, L.qcap, L.only_wide, L.long_follows, L.out, L.err,
+                                                       L.cells);
     return cudaGetLastError();
 }
 

@@ -25,6 +25,7 @@ struct ExtLaunch {
     int qcap;                   // >= max qlen + 1 over the launch
     int only_wide;              // wide launch: 1 = skip jobs that fit narrow cells;
                                 // narrow launch: 2 = report wide jobs (no wide launch follows)
+    int long_follows = 0;       // 1: jobs with qlen + 1 > qcap are left to a group-per-job launch
     bwacuda_ext_result *out;
     uint32_t *err;
     unsigned long long *cells;
@@ -33,6 +34,41 @@ struct ExtLaunch {
 
 cudaError_t ext_tpj_launch(const ExtLaunch &L, bool wide);
 size_t ext_tpj_smem_limit_qcap(bool wide);
+
+// Group-per-job extension of any query length (ext_long.cu, ext_long.cuh).  Every call site
+// owns XL_WORK_WORDS device words, zeroed before its launches, and a deferred-job list of
+// njobs entries.
+constexpr int XL_WORK_DCOUNT = 1;                              // [0] stays 0, [1] deferred jobs
+constexpr int XL_WORK_DCOUNTER16 = 2, XL_WORK_DCOUNTER32 = 3;  // work counters of the deferred launches
+constexpr int XL_WORK_COUNTER16 = 4, XL_WORK_COUNTER32 = 5;    // work counters of unbucketed first launches
+constexpr int XL_WORK_WORDS = 8;
+constexpr int XL_RING_MIN = 256, XL_RING_FIRST_MAX = 4096;
+constexpr int XL_RING_DEFAULT = 512;  // first-launch ring when the bands are not known on the host
+
+struct ExtLongLaunch {
+    const uint8_t *seq;
+    const bwacuda_dev_ext_job *jobs;
+    const uint32_t *order;   // job index list (nullptr: the identity)
+    const uint32_t *bounds;  // [start, stop) of positions in order, device words (nullptr: [0, njobs))
+    uint32_t *counter;       // zeroed work counter of the first launch
+    uint32_t njobs;          // jobs of the call: bounds every position and job index
+    int min_qlen;            // shorter jobs belong to another launch
+    int lanes;               // lanes per job: 8, 16 or 32
+    int ring_cols;           // first launch's ring columns per job (a power of two)
+    ExtParams P;
+    bwacuda_ext_result *out;
+    uint32_t *err;
+    unsigned long long *cells;
+    uint32_t *defer;         // njobs entries: jobs set aside for the deferred launch
+    uint32_t *defer_count;   // work + XL_WORK_DCOUNT
+    int reserve_regs = 0, reserve_threads = 0, sm_regs = 65536, sm_threads = 2048;
+    cudaStream_t stream;
+};
+
+cudaError_t ext_long_launch(const ExtLongLaunch &X, bool w32, int nsm);
+cudaError_t ext_long_deferred_launch(const ExtLongLaunch &X, bool w32, uint32_t *work, int nsm);
+// First-launch ring for bands up to w (XL_RING_MIN .. XL_RING_FIRST_MAX columns).
+int ext_long_ring_for_band(int w);
 
 // Rescue (ksw_local_fwd / ksw_align2).  mode: 0 = batched_ksw_align2,
 // 1 = scalar ksw_align2, 2 = forward pass only (per-job minsc / endsc).

@@ -10,11 +10,14 @@
 namespace bwacuda {
 
 // One bucket: jobs of cell class `cls` (0 = 8-bit pairs, 1 = 16-bit, 2 = 32-bit)
-// with qlen in [qlo, qhi], run with qcap cell columns per thread.
+// with qlen in [qlo, qhi], run with qcap cell columns per thread (kernel 0) or by the
+// group-per-job kernel (kernel 1: the open-ended buckets, whose queries may exceed any
+// thread's shared-memory row, and the buckets from the tuned query length up).
 struct ExtBucketDef {
     int32_t cls;
     int32_t qlo, qhi;
     int32_t qcap;
+    int32_t kernel;
 };
 
 constexpr int EXT_MAX_BUCKETS = 64;  // one thread each in the bucket-bounds kernel
@@ -36,7 +39,9 @@ struct PersistLaunch {
     int sm_regs = 65536, sm_threads = 2048;
 };
 
-int ext_bucket_defs(ExtBucketDef *defs, int max_defs, int step);
+// long_qlo: buckets holding queries of this length or longer use the group-per-job kernel
+// (INT_MAX: only the open-ended ones).
+int ext_bucket_defs(ExtBucketDef *defs, int max_defs, int step, int long_qlo);
 size_t ext_sort_temp_bytes(size_t n);
 // the sort's own kernels prefer the maximum shared-memory carveout (once per device)
 cudaError_t ext_sort_prefer_shared();

@@ -58,6 +58,7 @@ struct Slot {
     cudaEvent_t done = nullptr;
     HostBuf h_seq, h_jobs, h_out, h_aux;
     DevBuf d_seq, d_jobs, d_out, d_aux, d_scratch;
+    DevBuf d_xl;  // group-per-job extension: work words and the deferred-job list
 };
 
 struct BatchedState;  // batched path (batched.cu)
@@ -85,6 +86,7 @@ struct bwacuda_ctx {
     bwacuda::DevBuf d_misc;   // error flags, counters
     bwacuda::HostBuf h_misc;
     bwacuda::DevBuf d_dev_aux, d_dev_scratch;
+    bwacuda::DevBuf d_dev_xl;  // group-per-job extension of device-resident plain calls
     bwacuda::WorkerPool pool;
     bwacuda_stats stats{};
     int ext_path = BWACUDA_PATH_BATCHED;
@@ -92,6 +94,7 @@ struct bwacuda_ctx {
     int rescue_kernel = BWACUDA_RESCUE_AUTO;
     int rescue_lanes = 16;  // lanes per job of the register wavefront (8, 16, 32)
     bool ungapped = false;  // ungapped-diagonal fast path on the batched extension path
+    int long_lanes = 16;    // lanes per job of the group-per-job extension kernel (8, 16, 32)
     int tune_candidates = 0;        // last autotune call
     double tuned_ext_gcups = 0.0;   // best candidates' rates on their samples
     double tuned_rescue_gcups = 0.0;
@@ -121,6 +124,7 @@ struct ExtChunkInfo {
     size_t n;
     uint32_t nwide;
     int qmax;
+    int w;  // the call's band
     ExtParams P;
     bwacuda_ext_result *d_out;
 };
@@ -141,6 +145,9 @@ int batched_set_block(bwacuda_ctx *c, int tb);
 int batched_set_grab(bwacuda_ctx *c, int grab);
 int batched_set_bucket_step(bwacuda_ctx *c, int step);
 void batched_get_tuning(bwacuda_ctx *c, int *tb, int *grab, int *step);
+int batched_set_long(bwacuda_ctx *c, int long_qlo);
+int batched_get_long(bwacuda_ctx *c);
+int batched_set_long_lanes(bwacuda_ctx *c, int lanes);
 
 struct BatchBufs;
 int batched_prepare(bwacuda_ctx *c);
@@ -174,6 +181,11 @@ void global_release(bwacuda_ctx *c);
 
 // server.cu
 void server_shutdown(bwacuda_ctx *c);
+
+// abi.cu: group-per-job launches over the jobs of one call that the thread-per-job kernels
+// leave (qlen >= min16 in 16-bit cells, qlen >= min32 in 32-bit cells; INT_MAX: none)
+int launch_long_unbucketed(bwacuda_ctx *c, DevBuf &xl, const uint8_t *seq, const bwacuda_dev_ext_job *jobs, size_t n,
+                           const ExtParams &P, bwacuda_ext_result *out, int min16, int min32, int ring, cudaStream_t s);
 
 // abi.cu (device-resident rescue with the context lock held)
 int ksw_align2_device_locked(bwacuda_ctx *c, const uint8_t *d_seq, const bwacuda_dev_rescue_job *d_jobs, size_t n,

@@ -265,8 +265,7 @@ int plan_request(Request *r, int m)
     r->scr_at = at;
     at = align256(at + scr * 8);
     r->bytes = at;
-    // the kernels' per-launch limits
-    if (r->kind == 0 && (size_t)qmax + 1 > ext_tpj_smem_limit_qcap(false)) return BWACUDA_EUNSUPPORTED;
+    // the rescue kernels' per-launch limit (extension takes any query length)
     if (r->kind == 1 && (size_t)((qmax + 15) / 16 * 16 + 16) > rescue_tpj_smem_limit_qcap(wide)) return BWACUDA_EUNSUPPORTED;
     return BWACUDA_OK;
 }

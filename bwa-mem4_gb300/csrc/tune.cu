@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 
 #include "kernels.h"
 #include "runtime.h"
@@ -104,6 +105,9 @@ extern "C" int bwacuda_get_tuning(bwacuda_ctx *c, bwacuda_tuning *out)
     out->candidates = c->tune_candidates;
     out->ext_gcups = c->tuned_ext_gcups;
     out->rescue_gcups = c->tuned_rescue_gcups;
+    const int lq = batched_get_long(c);
+    out->long_qlen = lq == INT_MAX ? 0 : lq;
+    out->long_lanes = c->long_lanes;
     return BWACUDA_OK;
 }
 
@@ -187,12 +191,46 @@ extern "C" int bwacuda_autotune_extend(bwacuda_ctx *c, const uint8_t *d_seq, con
             }
         }
         best_ms = chosen_ms;
-        uint64_t dummy = 0;
-        const int st = collect_device_status(c, s, &dummy);
-        if (!rc) rc = st;
         if (!rc) rc = batched_set_bucket_step(c, best[2]);
         if (!rc) rc = batched_set_block(c, best[0]);
         if (!rc) rc = batched_set_grab(c, best[1]);
+        // Then the group-per-job kernel against thread-per-job on the longer buckets: the query
+        // length from which buckets switch kernels (225, 193 or 129) by lanes per job (8, 16 or
+        // 32), kept only when more than 1.5% faster than thread-per-job at the chosen shape.
+        const int long0 = batched_get_long(c), lanes0 = c->long_lanes;
+        if (!rc) rc = batched_set_long(c, INT_MAX);
+        double tpj_ms = rc ? 0 : time_runs(T, s, 2, run);
+        if (tpj_ms < 0) rc = (int)tpj_ms;
+        int long_best = INT_MAX, lanes_best = lanes0;
+        double long_ms = 0;
+        static const int kLongQ[] = {225, 193, 129}, kLanes[] = {8, 16, 32};
+        for (int lq : kLongQ) {
+            if (rc) break;
+            if ((rc = batched_set_long(c, lq)) != BWACUDA_OK) break;
+            for (int ln : kLanes) {
+                batched_set_long_lanes(c, ln);
+                const double ms = time_runs(T, s, 2, run);
+                if (ms < 0) { rc = (int)ms; break; }
+                ++ncand;
+                if (long_ms == 0 || ms < long_ms) { long_ms = ms; long_best = lq; lanes_best = ln; }
+            }
+        }
+        if (!rc && long_ms > 0 && long_ms * 1.015 < tpj_ms) {
+            best_ms = long_ms;
+        } else {
+            long_best = INT_MAX;
+            lanes_best = lanes0;
+            if (tpj_ms > 0) best_ms = std::min(best_ms, tpj_ms);
+        }
+        if (!rc) rc = batched_set_long(c, long_best);
+        if (!rc) rc = batched_set_long_lanes(c, lanes_best);
+        if (rc) {
+            batched_set_long(c, long0);
+            batched_set_long_lanes(c, lanes0);
+        }
+        uint64_t dummy = 0;
+        const int st = collect_device_status(c, s, &dummy);
+        if (!rc) rc = st;
         c->use_graphs = graphs;
         c->stats = saved;
         tmp.release();

@@ -142,6 +142,13 @@ typedef struct bwacuda_ctx bwacuda_ctx;
  * index a sequence's jobs in 32 bits).  A larger batch runs as consecutive sequences on
  * the call's stream, with the same results. */
 #define BWACUDA_OPT_DEVICE_PIECE 11
+/* Batched extension: query length from which the length buckets run the group-per-job
+ * kernel (a group of 8, 16 or 32 lanes per job, the DP row processed in parallel across
+ * the group) instead of thread-per-job; 0 (default) = only the open-ended buckets, which
+ * hold the queries too long for a thread's shared-memory row.  Results never depend on it. */
+#define BWACUDA_OPT_LONG_QLEN 12
+/* Lanes per job of the group-per-job extension kernel: 8, 16 (default) or 32. */
+#define BWACUDA_OPT_LONG_LANES 13
 
 int bwacuda_ctx_create(int device, bwacuda_ctx **out);
 void bwacuda_ctx_destroy(bwacuda_ctx *ctx);
@@ -396,6 +403,9 @@ typedef struct {
     int32_t candidates;     /* candidates timed by the last autotune call */
     double ext_gcups;       /* best extension candidate on its sample (0 if not tuned) */
     double rescue_gcups;    /* best rescue candidate on its sample (0 if not tuned) */
+    int32_t long_qlen;      /* batched extension: buckets from this query length up use the group-per-job
+                               kernel (0: only the open-ended buckets, queries beyond the thread-per-job rows) */
+    int32_t long_lanes;     /* lanes per job of the group-per-job kernel: 8, 16 or 32 */
 } bwacuda_tuning;
 
 int bwacuda_get_tuning(bwacuda_ctx *ctx, bwacuda_tuning *out);
