@@ -25,7 +25,10 @@ cudaError_t launch_first(const ExtLongLaunch &X, int nsm)
 {
     auto kern = xl::ext_long_kernel<W32, L, XL_C>;
     const int groups = XL_BLOCK / L;
-    const size_t smem = (size_t)groups * xl::ring_words(X.ring_cols, W32) * 4;
+    // the largest ring up to the requested one whose block fits (jobs needing more are deferred)
+    int ring = X.ring_cols;
+    while (ring > XL_RING_MIN && (size_t)groups * xl::ring_words(ring, W32) * 4 > EXT_SMEM_BLOCK_MAX) ring >>= 1;
+    const size_t smem = (size_t)groups * xl::ring_words(ring, W32) * 4;
     if (smem > EXT_SMEM_BLOCK_MAX) return cudaErrorInvalidValue;
     // process-wide per kernel: always the ceiling (see the persistent kernels)
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)EXT_SMEM_BLOCK_MAX);
@@ -42,8 +45,8 @@ cudaError_t launch_first(const ExtLongLaunch &X, int nsm)
         per_sm = std::max(1, std::min(per_sm, std::min(cap_r, cap_t)));
     }
     kern<<<per_sm * nsm, XL_BLOCK, smem, X.stream>>>(X.seq, X.jobs, X.order, X.bounds, X.counter, X.njobs,
-                                                    X.min_qlen, X.ring_cols, X.defer, X.defer_count, X.P, X.out,
-                                                    X.err, X.cells);
+                                                    X.min_qlen, ring, X.defer, X.defer_count, X.P, X.out, X.err,
+                                                    X.cells);
     return cudaGetLastError();
 }
 

@@ -241,9 +241,11 @@ def test_autotune_extend_keeps_results(ctx):
     d_jobs = torch.from_numpy(js.dev_ext_jobs().view(np.uint8)).cuda()
     try:
         t = ctx.autotune_extend(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), sample=20000)
-        assert t["candidates"] == 36 and t["ext_gcups"] > 0
+        # 36 launch shapes, then 9 group-per-job settings (3 query lengths x 3 lane counts)
+        assert t["candidates"] == 45 and t["ext_gcups"] > 0
         assert t["persist_block"] in (32, 64, 128, 256) and t["grab"] in (1, 2, 4)
         assert t["bucket_step"] in (16, 32, 64)
+        assert t["long_qlen"] in (0, 129, 193, 225) and t["long_lanes"] in (8, 16, 32)
         assert ctx.tuning() == t
         got = _device_run(ctx, js, B.PATH_BATCHED)[0]
         assert np.array_equal(got, want)
@@ -253,6 +255,8 @@ def test_autotune_extend_keeps_results(ctx):
         ctx.set_option(B.OPT_PERSIST_BLOCK, 128)
         ctx.set_option(B.OPT_BUCKET_STEP, 32)
         ctx.set_option(B.OPT_GRAB, 1)
+        ctx.set_option(B.OPT_LONG_QLEN, 0)
+        ctx.set_option(B.OPT_LONG_LANES, 16)
 
 
 @pytest.mark.parametrize("path", PATHS)
