@@ -278,6 +278,11 @@ pub mod ffi {
         pub fn bwacuda_server_submit_rescue(ctx: *mut bwacuda_ctx, jobs: *const bwacuda_rescue_job, n: usize,
                                             sc: *const bwacuda_scoring, minsc: c_int, max_sc: c_int,
                                             req_id: *mut u64) -> c_int;
+        pub fn bwacuda_server_submit_mixed(ctx: *mut bwacuda_ctx, ext_jobs: *const bwacuda_ext_job, n_ext: usize,
+                                           rescue_jobs: *const bwacuda_rescue_job, n_rescue: usize,
+                                           sc: *const bwacuda_scoring, w: c_int, end_bonus: c_int, zdrop: c_int,
+                                           minsc: c_int, max_sc: c_int, req_id: *mut u64) -> c_int;
+        pub fn bwacuda_server_cells(ctx: *mut bwacuda_ctx, ext_cells: *mut u64, rescue_cells: *mut u64) -> c_int;
         pub fn bwacuda_server_wait(ctx: *mut bwacuda_ctx, req_id: u64, out: *mut c_void, timeout_us: i64,
                                    latency_ns: *mut i64) -> c_int;
         pub fn bwacuda_server_stats(ctx: *mut bwacuda_ctx, served_jobs: *mut u64, waves: *mut u64,

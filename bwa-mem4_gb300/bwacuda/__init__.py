@@ -87,7 +87,8 @@ EXPORTS = ("bwacuda_ctx_create", "bwacuda_ctx_destroy", "bwacuda_set_option", "b
            "bwacuda_server_submit_extend", "bwacuda_server_submit_rescue", "bwacuda_server_wait",
            "bwacuda_server_stats", "bwacuda_measure_alu_peak", "bwacuda_get_tuning", "bwacuda_autotune_extend",
            "bwacuda_autotune_rescue", "bwacuda_ksw_global2_batch", "bwacuda_extend_batch_retry",
-           "bwacuda_extend_retry_device", "bwacuda_ref_set", "bwacuda_mate_rescue_windows")
+           "bwacuda_extend_retry_device", "bwacuda_ref_set", "bwacuda_mate_rescue_windows",
+           "bwacuda_server_submit_mixed", "bwacuda_server_cells")
 
 _lib = None
 _synth = None
@@ -139,6 +140,9 @@ def lib():
     L.bwacuda_server_submit_rescue.argtypes = [vp, vp, sz, C.POINTER(Scoring), I, I, C.POINTER(C.c_uint64)]
     L.bwacuda_server_wait.argtypes = [vp, C.c_uint64, vp, C.c_int64, C.POINTER(C.c_int64)]
     L.bwacuda_server_stats.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+    L.bwacuda_server_submit_mixed.argtypes = [vp, vp, sz, vp, sz, C.POINTER(Scoring), I, I, I, I, I,
+                                              C.POINTER(C.c_uint64)]
+    L.bwacuda_server_cells.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     L.bwacuda_ctx_sync.argtypes = [vp]
     L.bwacuda_get_stats.argtypes = [vp, C.POINTER(Stats)]
     L.bwacuda_reset_stats.argtypes = [vp]
@@ -580,17 +584,45 @@ class Context:
         self._held[rid.value] = (js, jobs, ALN_RES)
         return rid.value
 
+    def submit_mixed(self, ejs: JobSet, rjs: JobSet, sc: Scoring = None, w=100, end_bonus=5, zdrop=100, minsc=19,
+                     max_sc=1) -> int:
+        """Queue one request holding extension jobs ejs and rescue jobs rjs."""
+        ejobs = self._host_jobs(ejs, EXT_JOB)
+        rjobs = self._host_jobs(rjs, RES_JOB)
+        rid = C.c_uint64()
+        sc = sc or self.scoring()
+        rc = lib().bwacuda_server_submit_mixed(self.h, _ptr(ejobs), len(ejs), _ptr(rjobs), len(rjs), C.byref(sc), w,
+                                               end_bonus, zdrop, minsc, max_sc, C.byref(rid))
+        self._check(rc, "bwacuda_server_submit_mixed")
+        self._held[rid.value] = ((ejs, rjs), (ejobs, rjobs), None)
+        return rid.value
+
     def wait(self, rid, timeout_us=-1):
-        """Results of a request and its submit-to-completion latency in seconds."""
+        """Results of a request and its submit-to-completion latency in seconds (a mixed
+        request's results as (extension results, rescue results))."""
         js, jobs, dt = self._held[rid]
-        out = np.zeros(len(js), dtype=dt)
+        if dt is None:
+            ne, nr = len(js[0]), len(js[1])
+            raw = np.zeros(ne * EXT_RES.itemsize + nr * ALN_RES.itemsize + 1, dtype=np.uint8)
+            out = raw
+        else:
+            out = np.zeros(len(js), dtype=dt)
         lat = C.c_int64()
         rc = lib().bwacuda_server_wait(self.h, rid, _ptr(out), timeout_us, C.byref(lat))
         if rc == EAGAIN or rc == ETIMEOUT:
             raise BwaCudaError(rc, "bwacuda_server_wait")
         del self._held[rid]
         self._check(rc, "bwacuda_server_wait")
+        if dt is None:
+            cut = ne * EXT_RES.itemsize
+            out = (raw[:cut].view(EXT_RES).copy(), raw[cut:cut + nr * ALN_RES.itemsize].view(ALN_RES).copy())
         return out, lat.value * 1e-9
+
+    def server_cells(self):
+        """(extension cells, rescue cells) served since the loop started."""
+        a, b = C.c_uint64(), C.c_uint64()
+        self._check(lib().bwacuda_server_cells(self.h, C.byref(a), C.byref(b)), "bwacuda_server_cells")
+        return a.value, b.value
 
     def server_stats(self):
         a, b, q = C.c_uint64(), C.c_uint64(), C.c_uint64()

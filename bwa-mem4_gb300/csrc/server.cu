@@ -136,10 +136,12 @@ struct ServerState {
     std::deque<Request *> pending;
     std::vector<Request *> admitted;
     std::unordered_map<uint64_t, Request *> reqs;
+    // mixed requests: id -> (extension part, rescue part), both in reqs
+    std::unordered_map<uint64_t, std::pair<uint64_t, uint64_t>> mixed;
     std::vector<WaveSlot> slots;
     cudaStream_t copy_stream = nullptr, read_stream = nullptr;
     WorkerPool *pool = nullptr;
-    uint64_t served_jobs = 0, served_cells = 0, waves = 0;
+    uint64_t served_jobs = 0, served_ext_cells = 0, served_rescue_cells = 0, waves = 0;
     bool dev = false;  // admission by device gather (the device reads pageable host memory)
 };
 
@@ -561,9 +563,9 @@ bool retire(ServerState *S)
             S->served_jobs += r->n;
             if (r->kind == 1)
                 for (size_t k = 0; k < r->n; ++k)
-                    S->served_cells += (uint64_t)r->rjobs[k].qlen * (uint64_t)r->rjobs[k].tlen;
+                    S->served_rescue_cells += (uint64_t)r->rjobs[k].qlen * (uint64_t)r->rjobs[k].tlen;
         }
-        S->served_cells += cells;
+        S->served_ext_cells += cells;  // extension waves count their inner-loop cells on the device
         w.reqs.clear();
         w.busy = false;
         any = true;
@@ -723,23 +725,73 @@ extern "C" int bwacuda_server_stop(bwacuda_ctx *c)
     return BWACUDA_OK;
 }
 
-static int submit(bwacuda_ctx *c, Request *r)
+// Queues the requests together (all or none; r[1] may be null).  *mixed_id, when given,
+// receives one id naming both.
+static int submit_all(bwacuda_ctx *c, Request *r0, Request *r1, uint64_t *mixed_id)
 {
     ServerState *S = c->server;
-    if (!S) { delete r; return BWACUDA_EINVAL; }
-    r->dev = S->dev;
-    int rc = plan_request(r, r->kind == 0 ? r->P.sc.m : r->sc.m);
-    if (rc == BWACUDA_OK && r->bytes > S->budget) rc = BWACUDA_ENOMEM;  // could never be admitted
-    if (rc != BWACUDA_OK) { delete r; return rc; }
+    Request *rs[2] = {r0, r1};
+    auto drop = [&]() { delete r0; delete r1; };
+    if (!S) { drop(); return BWACUDA_EINVAL; }
+    size_t bytes = 0;
+    for (Request *r : rs) {
+        if (!r) continue;
+        r->dev = S->dev;
+        int rc = plan_request(r, r->kind == 0 ? r->P.sc.m : r->sc.m);
+        if (rc != BWACUDA_OK) { drop(); return rc; }
+        bytes += r->bytes;
+    }
+    if (bytes > S->budget) { drop(); return BWACUDA_ENOMEM; }  // could never be admitted
     std::lock_guard<std::mutex> g(S->mu);
-    if (S->stop) { delete r; return BWACUDA_EBUSY; }
-    if (S->reqs.size() >= S->max_requests) { delete r; return BWACUDA_EBUSY; }
-    r->id = S->next_id++;
-    r->t_submit = Clock::now();
-    S->reqs[r->id] = r;
-    S->pending.push_back(r);
+    if (S->stop) { drop(); return BWACUDA_EBUSY; }
+    if (S->reqs.size() + (r1 ? 2 : 1) > S->max_requests) { drop(); return BWACUDA_EBUSY; }
+    const auto now = Clock::now();
+    for (Request *r : rs) {
+        if (!r) continue;
+        r->id = S->next_id++;
+        r->t_submit = now;
+        S->reqs[r->id] = r;
+        S->pending.push_back(r);
+    }
+    if (mixed_id) {
+        *mixed_id = S->next_id++;
+        S->mixed[*mixed_id] = {r0->id, r1->id};
+    }
     S->cv_work.notify_one();
     return BWACUDA_OK;
+}
+
+static int submit(bwacuda_ctx *c, Request *r) { return submit_all(c, r, nullptr, nullptr); }
+
+static Request *new_ext_request(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, const bwacuda_scoring *sc,
+                                int w, int end_bonus, int zdrop)
+{
+    Request *r = new (std::nothrow) Request();
+    if (!r) return nullptr;
+    r->kind = 0;
+    r->ejobs = jobs;
+    r->n = n;
+    r->w = w;
+    r->P.sc = make_scoring(sc->m, sc->mat, sc->o_del, sc->e_del, sc->o_ins, sc->e_ins);
+    r->P.end_bonus = end_bonus;
+    r->P.zdrop = zdrop;
+    r->P.ug = ungapped_rule(c, sc->m, sc->mat, sc->o_del, sc->e_del, sc->o_ins, sc->e_ins);
+    return r;
+}
+
+static Request *new_rescue_request(const bwacuda_rescue_job *jobs, size_t n, const bwacuda_scoring *sc, int minsc,
+                                   int max_sc)
+{
+    Request *r = new (std::nothrow) Request();
+    if (!r) return nullptr;
+    r->kind = 1;
+    r->rjobs = jobs;
+    r->n = n;
+    r->minsc = minsc;
+    r->max_sc = max_sc;
+    r->sc = make_scoring(sc->m, sc->mat, sc->o_del, sc->e_del, sc->o_ins, sc->e_ins);
+    r->sc.max_sc = max_sc;
+    return r;
 }
 
 extern "C" int bwacuda_server_submit_extend(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n,
@@ -749,16 +801,8 @@ extern "C" int bwacuda_server_submit_extend(bwacuda_ctx *c, const bwacuda_ext_jo
     if (!c || !sc || !req_id || (n && !jobs) || n == 0 || w < 0) return BWACUDA_EINVAL;
     int rc = validate_scoring(sc->m, sc->mat, sc->o_del, sc->e_del, sc->o_ins, sc->e_ins);
     if (rc) return rc;
-    Request *r = new (std::nothrow) Request();
+    Request *r = new_ext_request(c, jobs, n, sc, w, end_bonus, zdrop);
     if (!r) return BWACUDA_ENOMEM;
-    r->kind = 0;
-    r->ejobs = jobs;
-    r->n = n;
-    r->w = w;
-    r->P.sc = make_scoring(sc->m, sc->mat, sc->o_del, sc->e_del, sc->o_ins, sc->e_ins);
-    r->P.end_bonus = end_bonus;
-    r->P.zdrop = zdrop;
-    r->P.ug = ungapped_rule(c, sc->m, sc->mat, sc->o_del, sc->e_del, sc->o_ins, sc->e_ins);
     rc = submit(c, r);
     if (rc == BWACUDA_OK) *req_id = r->id;
     return rc;
@@ -770,18 +814,33 @@ extern "C" int bwacuda_server_submit_rescue(bwacuda_ctx *c, const bwacuda_rescue
     if (!c || !sc || !req_id || (n && !jobs) || n == 0 || max_sc < 1) return BWACUDA_EINVAL;
     int rc = validate_scoring(sc->m, sc->mat, sc->o_del, sc->e_del, sc->o_ins, sc->e_ins);
     if (rc) return rc;
-    Request *r = new (std::nothrow) Request();
+    Request *r = new_rescue_request(jobs, n, sc, minsc, max_sc);
     if (!r) return BWACUDA_ENOMEM;
-    r->kind = 1;
-    r->rjobs = jobs;
-    r->n = n;
-    r->minsc = minsc;
-    r->max_sc = max_sc;
-    r->sc = make_scoring(sc->m, sc->mat, sc->o_del, sc->e_del, sc->o_ins, sc->e_ins);
-    r->sc.max_sc = max_sc;
     rc = submit(c, r);
     if (rc == BWACUDA_OK) *req_id = r->id;
     return rc;
+}
+
+extern "C" int bwacuda_server_submit_mixed(bwacuda_ctx *c, const bwacuda_ext_job *ext_jobs, size_t n_ext,
+                                           const bwacuda_rescue_job *rescue_jobs, size_t n_rescue,
+                                           const bwacuda_scoring *sc, int w, int end_bonus, int zdrop, int minsc,
+                                           int max_sc, uint64_t *req_id)
+{
+    if (!c || !sc || !req_id || (n_ext && !ext_jobs) || (n_rescue && !rescue_jobs) || n_ext + n_rescue == 0 ||
+        w < 0 || max_sc < 1)
+        return BWACUDA_EINVAL;
+    int rc = validate_scoring(sc->m, sc->mat, sc->o_del, sc->e_del, sc->o_ins, sc->e_ins);
+    if (rc) return rc;
+    if (n_rescue == 0) return bwacuda_server_submit_extend(c, ext_jobs, n_ext, sc, w, end_bonus, zdrop, req_id);
+    if (n_ext == 0) return bwacuda_server_submit_rescue(c, rescue_jobs, n_rescue, sc, minsc, max_sc, req_id);
+    Request *re = new_ext_request(c, ext_jobs, n_ext, sc, w, end_bonus, zdrop);
+    Request *rr = new_rescue_request(rescue_jobs, n_rescue, sc, minsc, max_sc);
+    if (!re || !rr) {
+        delete re;
+        delete rr;
+        return BWACUDA_ENOMEM;
+    }
+    return submit_all(c, re, rr, req_id);
 }
 
 extern "C" int bwacuda_server_wait(bwacuda_ctx *c, uint64_t req_id, void *out, int64_t timeout_us,
@@ -790,38 +849,75 @@ extern "C" int bwacuda_server_wait(bwacuda_ctx *c, uint64_t req_id, void *out, i
     if (!c || !c->server || !out) return BWACUDA_EINVAL;
     ServerState *S = c->server;
     std::unique_lock<std::mutex> lk(S->mu);
-    auto it = S->reqs.find(req_id);
-    if (it == S->reqs.end()) return BWACUDA_EINVAL;
-    Request *r = it->second;
-    if (r->state != DONE) {
+    // a mixed request is its extension part then its rescue part, results in that order
+    Request *parts[2] = {nullptr, nullptr};
+    const auto mit = S->mixed.find(req_id);
+    if (mit != S->mixed.end()) {
+        auto a = S->reqs.find(mit->second.first), b = S->reqs.find(mit->second.second);
+        if (a == S->reqs.end() || b == S->reqs.end()) return BWACUDA_EINVAL;
+        parts[0] = a->second;
+        parts[1] = b->second;
+    } else {
+        auto it = S->reqs.find(req_id);
+        if (it == S->reqs.end()) return BWACUDA_EINVAL;
+        parts[0] = it->second;
+    }
+    auto all_done = [&]() { return parts[0]->state == DONE && (!parts[1] || parts[1]->state == DONE); };
+    if (!all_done()) {
         if (timeout_us == 0) return BWACUDA_EAGAIN;
         const auto deadline = Clock::now() + std::chrono::microseconds(timeout_us < 0 ? (int64_t)1 << 40 : timeout_us);
-        while (r->state != DONE) {
-            if (S->cv_done.wait_until(lk, deadline) == std::cv_status::timeout && r->state != DONE)
+        while (!all_done()) {
+            if (S->cv_done.wait_until(lk, deadline) == std::cv_status::timeout && !all_done())
                 return BWACUDA_ETIMEOUT;
         }
     }
-    int rc = r->rc;
-    // take the request out of the table, copy its results without holding the
-    // lock, then release its arena range
-    S->reqs.erase(r->id);
+    // take the requests out of the table, copy their results without holding the
+    // lock, then release their arena ranges
+    int rc = BWACUDA_OK;
+    for (Request *r : parts)
+        if (r) {
+            S->reqs.erase(r->id);
+            if (rc == BWACUDA_OK) rc = r->rc;
+        }
+    if (parts[1]) S->mixed.erase(req_id);
     lk.unlock();
     if (rc == BWACUDA_OK) {
-        const size_t rsz = r->kind == 0 ? sizeof(bwacuda_ext_result) : sizeof(bwacuda_rescue_result);
         cudaError_t e = cudaSetDevice(c->device);
         cudaStream_t rs = nullptr;
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&rs, cudaStreamNonBlocking);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(out, S->d_arena + r->off + r->res_at, r->n * rsz, cudaMemcpyDeviceToHost, rs);
+        size_t at = 0;
+        for (Request *r : parts) {
+            if (!r || e != cudaSuccess) continue;
+            const size_t rsz = r->kind == 0 ? sizeof(bwacuda_ext_result) : sizeof(bwacuda_rescue_result);
+            e = cudaMemcpyAsync(static_cast<char *>(out) + at, S->d_arena + r->off + r->res_at, r->n * rsz,
+                                cudaMemcpyDeviceToHost, rs);
+            at += r->n * rsz;
+        }
         if (e == cudaSuccess) e = cudaStreamSynchronize(rs);
         if (rs) cudaStreamDestroy(rs);
         if (e != cudaSuccess) rc = cuda_status(e);
     }
-    if (latency_ns) *latency_ns = std::chrono::duration_cast<std::chrono::nanoseconds>(r->t_done - r->t_submit).count();
+    if (latency_ns) {
+        int64_t ns = 0;
+        for (Request *r : parts)
+            if (r) ns = std::max<int64_t>(ns, std::chrono::duration_cast<std::chrono::nanoseconds>(r->t_done - r->t_submit).count());
+        *latency_ns = ns;
+    }
     lk.lock();
-    release_request(S, r);
+    for (Request *r : parts)
+        if (r) release_request(S, r);
     S->cv_work.notify_one();  // memory freed: admission may proceed
     return rc;
+}
+
+extern "C" int bwacuda_server_cells(bwacuda_ctx *c, uint64_t *ext_cells, uint64_t *rescue_cells)
+{
+    if (!c || !c->server) return BWACUDA_EINVAL;
+    ServerState *S = c->server;
+    std::lock_guard<std::mutex> g(S->mu);
+    if (ext_cells) *ext_cells = S->served_ext_cells;
+    if (rescue_cells) *rescue_cells = S->served_rescue_cells;
+    return BWACUDA_OK;
 }
 
 extern "C" int bwacuda_server_stats(bwacuda_ctx *c, uint64_t *served_jobs, uint64_t *waves, uint64_t *queued)

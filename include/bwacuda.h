@@ -356,6 +356,13 @@ int bwacuda_server_submit_extend(bwacuda_ctx *ctx, const bwacuda_ext_job *jobs, 
                                  uint64_t *req_id);
 int bwacuda_server_submit_rescue(bwacuda_ctx *ctx, const bwacuda_rescue_job *jobs, size_t n,
                                  const bwacuda_scoring *sc, int minsc, int max_sc, uint64_t *req_id);
+/* One request of both kinds (a chunk's extension and rescue jobs together): its wait
+ * writes the n_ext extension results, then the n_rescue rescue results, into out, and
+ * reports the later part's latency.  The parts are admitted together and join the
+ * waves of their kind.  Either count may be 0 (then it is a one-kind request). */
+int bwacuda_server_submit_mixed(bwacuda_ctx *ctx, const bwacuda_ext_job *ext_jobs, size_t n_ext,
+                                const bwacuda_rescue_job *rescue_jobs, size_t n_rescue, const bwacuda_scoring *sc,
+                                int w, int end_bonus, int zdrop, int minsc, int max_sc, uint64_t *req_id);
 /* Waits up to timeout_us (0 = poll: BWACUDA_EAGAIN if not done; < 0 = no
  * limit, BWACUDA_ETIMEOUT when the limit passes), copies the n results into
  * out (bwacuda_ext_result or bwacuda_rescue_result) and releases the request.
@@ -363,6 +370,9 @@ int bwacuda_server_submit_rescue(bwacuda_ctx *ctx, const bwacuda_rescue_job *job
 int bwacuda_server_wait(bwacuda_ctx *ctx, uint64_t req_id, void *out, int64_t timeout_us,
                         int64_t *latency_ns);
 int bwacuda_server_stats(bwacuda_ctx *ctx, uint64_t *served_jobs, uint64_t *waves, uint64_t *queued);
+/* Cells served since the loop started: extension cells as the kernels count them (one
+ * inner-loop iteration of ksw_extend2 each), rescue cells as qlen x tlen per job. */
+int bwacuda_server_cells(bwacuda_ctx *ctx, uint64_t *ext_cells, uint64_t *rescue_cells);
 
 /* Counters accumulated since the context was created (or last reset). */
 typedef struct {

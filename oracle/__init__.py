@@ -96,6 +96,10 @@ def lib():
         L.ko_extend_batch.argtypes = [u8p, C.c_int64, i64p, i64p, i32p, i32p, i32p, i32p, I,
                                       i8p, I, I, I, I, I, I, I, C.c_void_p,
                                       C.POINTER(C.c_uint64)]
+        L.ko_extend_batch_dispatch.restype = None
+        L.ko_extend_batch_dispatch.argtypes = [u8p, C.c_int64, i64p, i64p, i32p, i32p, i32p, i32p, I, i8p, I, I, I,
+                                               I, I, I, I, C.c_void_p, C.POINTER(C.c_uint64),
+                                               C.POINTER(C.c_uint64)]
         L.ko_align2_batch.restype = None
         L.ko_align2_batch.argtypes = [u8p, C.c_int64, i64p, i64p, i32p, i32p, I, i8p, I, I, I,
                                       I, I, I, I, I, I, C.c_void_p, C.POINTER(C.c_uint64)]
@@ -253,6 +257,23 @@ def extend_batch(js, mat=None, o_del=6, e_del=1, o_ins=6, e_ins=1, end_bonus=5, 
                           end_bonus, zdrop, nthreads, out.ctypes.data_as(C.c_void_p),
                           C.byref(cells))
     return out, cells.value
+
+
+def extend_batch_dispatch(js, mat=None, o_del=6, e_del=1, o_ins=6, e_ins=1, end_bonus=5, zdrop=100,
+                          nthreads=0, m=5):
+    """The reference's production flow (ungapped closed form, then the DP) over a JobSet-like
+    object.  Returns (structured results, jobs settled by the closed form, DP cells evaluated)."""
+    mat = _mat(scmat() if mat is None else mat)
+    n = len(js.qlen)
+    out = np.zeros(n, dtype=EXT_DTYPE)
+    settled, cells = C.c_uint64(0), C.c_uint64(0)
+    seq = _u8(js.seq) if len(js.seq) else np.zeros(1, np.uint8)
+    lib().ko_extend_batch_dispatch(_p(seq, C.c_uint8), n, _p(js.q_off, C.c_int64), _p(js.t_off, C.c_int64),
+                                   _p(js.qlen, C.c_int32), _p(js.tlen, C.c_int32), _p(js.h0, C.c_int32),
+                                   _p(js.w, C.c_int32), m, _p(mat, C.c_int8), o_del, e_del, o_ins, e_ins,
+                                   end_bonus, zdrop, nthreads, out.ctypes.data_as(C.c_void_p), C.byref(settled),
+                                   C.byref(cells))
+    return out, settled.value, cells.value
 
 
 def align2_batch(js, mat=None, o_del=6, e_del=1, o_ins=6, e_ins=1, minsc=19, max_sc=1, mode=0,

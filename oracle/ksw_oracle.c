@@ -566,6 +566,41 @@ void ko_extend_batch(const uint8_t *seq, int64_t n, const int64_t *q_off,
     if (cells_out) *cells_out = total;
 }
 
+void ko_extend_batch_dispatch(const uint8_t *seq, int64_t n, const int64_t *q_off,
+                              const int64_t *t_off, const int32_t *qlen, const int32_t *tlen,
+                              const int32_t *h0, const int32_t *w, int m, const int8_t *mat,
+                              int o_del, int e_del, int o_ins, int e_ins, int end_bonus,
+                              int zdrop, int nthreads, ko_ext_result *out, uint64_t *settled_out,
+                              uint64_t *cells_out)
+{
+    /* The reference's production flow for an extension batch, crates/bwa-neon/src/batched.rs:716-775:
+     * with a uniform DNA matrix, every job first tries the ungapped closed form (:773,
+     * ungapped_hit :602-697, threshold :756-764); the jobs it declines run the DP.  The
+     * reference's DP runs lane-parallel bins (:817-925, NEON / AVX2); this restatement runs the
+     * scalar ksw_extend2 per job, whose results the bins equal.  *cells_out counts the DP cells
+     * actually evaluated, *settled_out the jobs the closed form settled. */
+    uint64_t total = 0, settled = 0;
+    int nt = pick_threads(nthreads);
+    (void)nt;
+    const int uniform = m == 5 && is_uniform_dna(m, mat);
+    const int a = mat[0], b = -(int)mat[1];
+    const int x = uniform ? ko_x_threshold(a, b, o_del, e_del, o_ins, e_ins) : -1;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : total, settled) num_threads(nt)
+    for (int64_t k = 0; k < n; ++k) {
+        const uint8_t *q = seq + q_off[k], *t = seq + t_off[k];
+        if (x >= 0 && ko_ungapped_hit(q, qlen[k], t, tlen[k], h0[k], a, b, x, zdrop, &out[k])) {
+            ++settled;
+            continue;
+        }
+        uint64_t c = 0;
+        out[k] = ko_extend2(q, qlen[k], t, tlen[k], m, mat, o_del, e_del, o_ins, e_ins, w[k], end_bonus, zdrop,
+                            h0[k], &c);
+        total += c;
+    }
+    if (cells_out) *cells_out = total;
+    if (settled_out) *settled_out = settled;
+}
+
 void ko_align2_batch(const uint8_t *seq, int64_t n, const int64_t *q_off,
                      const int64_t *t_off, const int32_t *qlen, const int32_t *tlen,
                      int m, const int8_t *mat, int o_del, int e_del, int o_ins,

@@ -140,6 +140,16 @@ int ko_rescue_window(const uint8_t *pac, int64_t l_pac, const int64_t *off, cons
 /* bwa_fill_scmat, crates/bwa-core/src/opt.rs:419-460 (match a, mismatch -b, N -1). */
 void ko_fill_scmat(int a, int b, int8_t mat[25]);
 
+/* The reference's production dispatch for an extension batch (crates/bwa-neon/src/batched.rs:716-775):
+ * the ungapped closed form first (uniform DNA matrices), the scalar DP for the jobs it declines;
+ * OpenMP over jobs.  *settled_out = jobs the closed form settled, *cells_out = DP cells evaluated. */
+void ko_extend_batch_dispatch(const uint8_t *seq, int64_t n, const int64_t *q_off,
+                              const int64_t *t_off, const int32_t *qlen, const int32_t *tlen,
+                              const int32_t *h0, const int32_t *w, int m, const int8_t *mat,
+                              int o_del, int e_del, int o_ins, int e_ins, int end_bonus,
+                              int zdrop, int nthreads, ko_ext_result *out, uint64_t *settled_out,
+                              uint64_t *cells_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -121,3 +121,49 @@ def test_poll_and_bounded_wait(server):
             time.sleep(0.001)
     assert lat > 0
     assert np.array_equal(out, oracle.extend_batch(js)[0])
+
+
+def _mixed_kind_requests(seed, count, lo=500, hi=8000):
+    """Requests that each carry extension and rescue jobs (a chunk's extensions and its rescue
+    windows together), with a rescue share between 0 and 1."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        n = int(rng.integers(lo, hi))
+        nr = int(n * rng.random())
+        ejs = B.synth_ext(int(rng.choice([2, 3])), max(n - nr, 1), seed=seed * 1000 + k)
+        ejs.w[:] = 100
+        rjs = B.synth_rescue(max(nr, 1), seed=seed * 1000 + 500 + k)
+        out.append((ejs, rjs))
+    return out
+
+
+def test_mixed_kind_requests_alone_and_in_the_mix(server):
+    reqs = _mixed_kind_requests(7, 16)
+    alone = [server.wait(server.submit_mixed(e, r, minsc=20))[0] for e, r in reqs]
+    ids = [server.submit_mixed(e, r, minsc=20) for e, r in reqs]
+    mixed = [server.wait(i)[0] for i in ids]
+    for (ae, ar), (me, mr) in zip(alone, mixed):
+        assert np.array_equal(ae, me) and np.array_equal(ar, mr)
+    for (e, r), (oe, orr) in zip(reqs[:6], alone[:6]):
+        assert np.array_equal(oe, oracle.extend_batch(e)[0])
+        assert np.array_equal(orr, oracle.align2_batch(r, minsc=20)[0])
+    ext_cells, res_cells = server.server_cells()
+    assert ext_cells > 0 and res_cells == 2 * sum(int((r.qlen.astype(np.int64) * r.tlen).sum()) for _, r in reqs)
+
+
+def test_mixed_kind_requests_beside_one_kind_requests(server):
+    # mixed-kind, extension-only and rescue-only requests in flight together
+    mk = _mixed_kind_requests(8, 6)
+    one = _mixed_requests(9, 6)
+    ids = [("m", server.submit_mixed(e, r, minsc=20), (e, r)) for e, r in mk]
+    ids += [("1", _submit(server, kind, js), (kind, js)) for kind, js in one]
+    for tag, rid, what in ids:
+        out = server.wait(rid)[0]
+        if tag == "m":
+            assert np.array_equal(out[0], oracle.extend_batch(what[0])[0])
+            assert np.array_equal(out[1], oracle.align2_batch(what[1], minsc=20)[0])
+        else:
+            kind, js = what
+            want = oracle.extend_batch(js)[0] if kind == "extend" else oracle.align2_batch(js, minsc=20)[0]
+            assert np.array_equal(out, want)
