@@ -141,6 +141,7 @@ def apply_tuning(B, ctx, t):
         ctx.set_option(B.OPT_BUCKET_STEP, t["bucket_step"])
         ctx.set_option(B.OPT_RESCUE_KERNEL, t["rescue_kernel"])
         ctx.set_option(B.OPT_RESCUE_LANES, t["rescue_lanes"])
+        ctx.set_option(B.OPT_RESCUE_PAIR, t.get("rescue_pair", 0))
         ctx.set_option(B.OPT_LONG_QLEN, t.get("long_qlen", 0))
         ctx.set_option(B.OPT_LONG_LANES, t.get("long_lanes", 16))
 
@@ -382,7 +383,8 @@ def other_configs(args, B, ctx, st, barrier, max_over_ranks, world, rank):
         "value": round(rcells * world / (ms / 1e3) / 1e9, 2), "unit": "GCUPS",
         "cells": "qlen x tlen of the forward pass per job (padding and reverse pass not counted)",
         "ms_per_step": round(ms, 2), "jobs_per_s": round(n * world / (ms / 1e3), 1),
-        "tuning": {k: tuning_res[k] for k in ("rescue_kernel", "rescue_lanes", "rescue_gcups", "candidates")}}
+        "tuning": {k: tuning_res[k] for k in ("rescue_kernel", "rescue_lanes", "rescue_pair", "rescue_gcups",
+                                            "candidates")}}
     if rank == 0:
         # CPU baseline: the oracle's batched_ksw_align2 (forward pass, truncated reverse pass) on every
         # host core over the first 20,000 jobs of the same workload

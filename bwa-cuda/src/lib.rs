@@ -208,6 +208,8 @@ pub mod ffi {
         pub rescue_gcups: f64,
         pub long_qlen: i32,
         pub long_lanes: i32,
+        pub rescue_pair: i32,
+        pub reserved: i32,
     }
 
     extern "C" {

@@ -23,7 +23,7 @@ RESCUE_AUTO, RESCUE_TPJ = 0, 1
 OPT_HOST_GATHER = 6
 GATHER_AUTO, GATHER_HOST, GATHER_DEVICE = 0, 1, 2
 OPT_GRAB, OPT_BUCKET_STEP, OPT_RESCUE_LANES, OPT_UNGAPPED, OPT_DEVICE_PIECE = 7, 8, 9, 10, 11
-OPT_LONG_QLEN, OPT_LONG_LANES = 12, 13
+OPT_LONG_QLEN, OPT_LONG_LANES, OPT_RESCUE_PAIR = 12, 13, 14
 PATH_PLAIN, PATH_BATCHED = 0, 1
 INT_MAX = 2**31 - 1
 
@@ -68,7 +68,7 @@ class Tuning(C.Structure):
     _fields_ = [("persist_block", C.c_int32), ("grab", C.c_int32), ("bucket_step", C.c_int32),
                 ("rescue_lanes", C.c_int32), ("rescue_kernel", C.c_int32), ("candidates", C.c_int32),
                 ("ext_gcups", C.c_double), ("rescue_gcups", C.c_double), ("long_qlen", C.c_int32),
-                ("long_lanes", C.c_int32)]
+                ("long_lanes", C.c_int32), ("rescue_pair", C.c_int32), ("reserved", C.c_int32)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

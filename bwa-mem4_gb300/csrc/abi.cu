@@ -305,6 +305,10 @@ extern "C" int bwacuda_set_option(bwacuda_ctx *c, int option, int64_t value)
         if (value != 8 && value != 16 && value != 32) return BWACUDA_EINVAL;
         c->rescue_lanes = (int)value;
         return BWACUDA_OK;
+    case BWACUDA_OPT_RESCUE_PAIR:
+        if (value != 0 && value != 1) return BWACUDA_EINVAL;
+        c->rescue_pair = value != 0;
+        return BWACUDA_OK;
     case BWACUDA_OPT_LONG_QLEN:
         if (value < 0 || value > (1 << 30)) return BWACUDA_EINVAL;
         if (cudaSetDevice(c->device) != cudaSuccess) return BWACUDA_ECUDA;
@@ -695,8 +699,16 @@ namespace bwacuda {
 // shared-memory thread-per-job kernel.  Wide jobs always go to the latter.
 cudaError_t rescue_narrow_launch(bwacuda_ctx *c, const RescueLaunch &L)
 {
-    if (c->rescue_kernel == BWACUDA_RESCUE_AUTO && L.qcap <= rescue_wf_max_qpad() && L.only_wide != 2)
-        return rescue_wf_launch(L, L.qcap, c->rescue_lanes);
+    if (c->rescue_kernel == BWACUDA_RESCUE_AUTO && L.qcap <= rescue_wf_max_qpad() && L.only_wide != 2) {
+        if (!c->rescue_pair) return rescue_wf_launch(L, L.qcap, c->rescue_lanes);
+        // jobs whose values fit a byte: two per group; the rest in the 32-bit wavefront
+        int cols = 0;
+        cudaError_t e = rescue_wf2_launch(L, L.qcap, c->rescue_lanes == 16 ? 16 : 8, &cols);
+        if (e != cudaSuccess) return e;
+        RescueLaunch R = L;
+        R.pair_cols = cols;
+        return rescue_wf_launch(R, R.qcap, c->rescue_lanes);
+    }
     return rescue_tpj_launch(L, false);
 }
 

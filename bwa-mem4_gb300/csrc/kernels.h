@@ -84,6 +84,7 @@ struct RescueLaunch {
     int minsc;        // modes 0 and 1
     int qcap;         // >= padded query length + 16
     int only_wide;    // as ExtLaunch::only_wide
+    int pair_cols = 0;  // 32-bit wavefront: skip the jobs the paired wavefront of this many columns took
     uint2 *scratch;   // suboptimal-tracker entries
     const uint64_t *scratch_off;  // per job entry offset into scratch
     bwacuda_rescue_result *out_aln;
@@ -92,8 +93,27 @@ struct RescueLaunch {
     cudaStream_t stream;
 };
 
+// Whether a rescue job runs in the two-jobs-per-group wavefront of `cols` columns
+// (rescue_wf2.cuh): every value fits a byte (min(qlen, tlen) * max_sc <= 255) and the padded
+// query of both passes (bwa's width rule, or lanes_fixed; the reverse pass may pad to 16) fits
+// min(cols, 256) columns.
+__host__ __device__ inline bool rescue_pair_job_ok(int qlen, int tlen, int max_sc, int lanes_fixed, int cols)
+{
+    if (qlen < 0 || tlen < 0 || max_sc < 1 || cols <= 0) return false;
+    const long long mn = qlen < tlen ? qlen : tlen;
+    if (mn * max_sc > 255) return false;
+    const int ln = lanes_fixed ? lanes_fixed : ((long long)qlen * max_sc < 250 ? 16 : 8);
+    const int p1 = (qlen + ln - 1) / ln * ln, p16 = (qlen + 15) / 16 * 16;
+    const int need = p1 > p16 ? p1 : p16;
+    return need <= (cols < 256 ? cols : 256);
+}
+
 cudaError_t rescue_tpj_launch(const RescueLaunch &L, bool wide);
 cudaError_t rescue_wf_launch(const RescueLaunch &L, int qcap, int lanes);  // lanes per job: 8, 16 or 32
+// The paired wavefront (two jobs per group of 8 or 16 lanes) over the jobs rescue_pair_job_ok
+// admits at its column count; *cols receives that count (0: no launch, the matrix or the
+// queries do not suit it).
+cudaError_t rescue_wf2_launch(const RescueLaunch &L, int qcap, int lanes, int *cols);
 int rescue_wf_max_qpad();
 size_t rescue_tpj_smem_limit_qcap(bool wide);
 // Entries the suboptimal tracker may need for a target of tlen rows.

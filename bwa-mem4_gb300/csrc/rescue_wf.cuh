@@ -189,7 +189,7 @@ template <int L, int C>
 __global__ void __launch_bounds__(128)
 rescue_wf_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_rescue_job *__restrict__ jobs,
                  const uint32_t *__restrict__ order, uint32_t n, const __grid_constant__ Scoring sc, int mode,
-                 int lanes_fixed, int minsc_all, uint2 *__restrict__ scratch,
+                 int lanes_fixed, int minsc_all, int pair_cols, uint2 *__restrict__ scratch,
                  const uint64_t *__restrict__ scratch_off, bwacuda_rescue_result *__restrict__ out_aln,
                  bwacuda_fwd_result *__restrict__ out_fwd, uint32_t *__restrict__ err)
 {
@@ -206,8 +206,10 @@ rescue_wf_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_rescue_job *
     if (active) J = jobs[jid];
     const int lanes = lanes_fixed ? lanes_fixed : (J.qlen * sc.max_sc < 250 ? 16 : 8);
     const int qpad = (J.qlen + lanes - 1) / lanes * lanes;
-    // jobs whose scores need int32 cells go to the wide shared-memory launch
+    // jobs whose scores need int32 cells go to the wide shared-memory launch; jobs the paired
+    // wavefront took are done
     if (active && (long long)min(J.qlen, J.tlen) * sc.max_sc >= 32768) active = false;
+    if (active && rescue_pair_job_ok(J.qlen, J.tlen, sc.max_sc, lanes_fixed, pair_cols)) active = false;
     if (active && qpad > L * C) {
         if (W.k == 0) atomicOr(err, ERR_RANGE);  // the host sizes C from the batch
         active = false;
@@ -268,8 +270,8 @@ cudaError_t launch_wf(const RescueLaunch &Lr)
     const uint32_t grid = (uint32_t)((total + threads - 1) / threads);
     if (grid == 0) return cudaSuccess;
     rescue_wf_kernel<L, C><<<grid, threads, 0, Lr.stream>>>(Lr.seq, Lr.jobs, Lr.order, (uint32_t)Lr.n, Lr.sc, Lr.mode,
-                                                            Lr.lanes, Lr.minsc, Lr.scratch, Lr.scratch_off,
-                                                            Lr.out_aln, Lr.out_fwd, Lr.err);
+                                                            Lr.lanes, Lr.minsc, Lr.pair_cols, Lr.scratch,
+                                                            Lr.scratch_off, Lr.out_aln, Lr.out_fwd, Lr.err);
     return cudaGetLastError();
 }
 

@@ -1,0 +1,313 @@
+// rescue_wf2.cuh -- the mate-rescue register wavefront (rescue_wf.cuh) with two jobs per lane
+// group: job A in the low 16-bit lane of every register, job B in the high one, so each DPX
+// instruction (__viaddmax_s16x2_relu, __vimax_s16x2_relu, __vimax3_u16x2) updates one cell
+// of each job.  The recurrences, tie rules and the suboptimal tracker are those of the 32-bit
+// wavefront (ksw_local_fwd, crates/bwa-extend/src/sw.rs:921-1075; start recovery of
+// batched_ksw_align2 / ksw_align2), cell for cell.
+//
+// A job qualifies when every value fits a byte: min(qlen, tlen) * max_sc <= 255 (a local score
+// gains at most max_sc per diagonal step, gaps never add), and its padded query (forward and
+// reverse) fits 256 columns -- the reference's own 8-bit rescue class (min(q, t) * a < 250 and
+// q < 250, crates/bwa-neon/src/matesw.rs:780-795) lies inside it.  Then the row-maximum key
+// of a job is 16 bits, (H << 8) | (255 - column): the largest H, and among equal H the smallest
+// column, as the reference's qe rule wants.
+//
+// Scores.  A target row's four scores for query codes 0..3 are one 32-bit profile word, so one
+// prmt picks (mat[tA][qA], mat[tB][qB]) sign-extended into the two lanes.  Query columns that
+// are N (code 4), ksw padding (score 0) or invalid (score 0, flagged) are patched with one
+// lop3 against per-column keep / fix words; this needs the N column of the matrix to be one
+// value (mat[t][4] equal for every t, as bwa's matrix has), which the host checks.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "rescue_wf.cuh"
+
+namespace bwacuda {
+namespace wf2 {
+
+constexpr uint32_t MIN2 = 0x80008000u;  // (-32768, -32768)
+
+__host__ __device__ inline int ceil_to(int x, int m) { return (x + m - 1) / m * m; }
+
+__host__ __device__ inline bool job_ok(int qlen, int tlen, int max_sc, int lanes_fixed, int cols)
+{
+    return rescue_pair_job_ok(qlen, tlen, max_sc, lanes_fixed, cols);
+}
+
+template <int L, int C>
+struct Lane2 {
+    int k;
+    uint32_t sel[C];   // prmt selectors: low half picks job A's byte from word A, high half job B's from word B
+    uint32_t keep[C];  // 0xffff per half: the prmt score stands; 0: replaced by fix
+    uint32_t fix[C];   // N penalty (query N), 0 (padding or an invalid code)
+    uint32_t ks[C];    // row-key selectors: (H << 8) | column byte, or 0 for a column past the padded query
+};
+
+// Loads the lane's columns of both jobs: forward (query[j]) or the reversed prefix
+// (query[qe0 - j]); columns [qlen, qpad) are ksw padding (score 0, part of the row maxima),
+// columns >= qpad do not exist: their cells are computed but their row keys are 0, so they are
+// never a row maximum (they lie right of every real column and feed no real cell).
+template <int L, int C>
+__device__ __forceinline__ void load_query2(Lane2<L, C> &W, const uint8_t *qa, int qla, int qpa, const uint8_t *qb,
+                                            int qlb, int qpb, bool rev, int qea, int qeb, int m, int npen, bool &bad)
+{
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        const int j = W.k * C + c;
+        // key bytes: the column byte, H; past the padded query two zero bytes (H's high bytes)
+        W.ks[c] = (j < qpa ? 0x0040u : 0x0055u) | (j < qpb ? 0x6000u : 0x7700u);
+        uint32_t ca = 7u, cb = 7u;
+        if (j < qla) {
+            ca = rev ? qa[qea - j] : qa[j];
+            bad |= ca >= (uint32_t)m;
+            ca = ca < (uint32_t)m ? ca : 7u;
+        }
+        if (j < qlb) {
+            cb = rev ? qb[qeb - j] : qb[j];
+            bad |= cb >= (uint32_t)m;
+            cb = cb < (uint32_t)m ? cb : 7u;
+        }
+        const bool sa = ca >= 4u, sb = cb >= 4u;  // N, padding or invalid
+        const uint32_t ba = sa ? 0u : ca, bb = sb ? 4u : 4u + cb;
+        W.sel[c] = ba | ((ba | 8u) << 4) | (bb << 8) | ((bb | 8u) << 12);
+        W.keep[c] = (sa ? 0u : 0xffffu) | (sb ? 0u : 0xffff0000u);
+        const uint32_t fa = ca == 4u ? (uint32_t)(npen & 0xffff) : 0u;
+        const uint32_t fb = cb == 4u ? (uint32_t)(npen & 0xffff) : 0u;
+        W.fix[c] = fa | (fb << 16);
+    }
+}
+
+struct Out2 {
+    int score[2], te[2], qe[2];
+};
+
+// One local-SW pass of both jobs of every group in the warp, in lockstep.  tlen[h] = 0 makes half
+// h inactive; tmap / te0 select the reverse pass's target mapping (rows <= te0 read reversed).
+// stop[h]: the half stops once its score reaches endsc[h].  Returns the results in every lane.
+template <int L, int C>
+__device__ Out2 pass2(const Lane2<L, C> &W, const uint32_t *prof_s, const uint8_t *const t[2], const int tlen[2],
+                      int tmap, const int te0[2], const Scoring &sc, const int minsc[2], const int endsc[2],
+                      bool stop_enabled, wf::WfTracker *trk, bool &bad)
+{
+    const int k = W.k;
+    const uint32_t noe_del2 = (uint32_t)(-(sc.o_del + sc.e_del) & 0xffff) * 0x10001u;
+    const uint32_t noe_ins2 = (uint32_t)(-(sc.o_ins + sc.e_ins) & 0xffff) * 0x10001u;
+    const uint32_t ne_del2 = (uint32_t)(-sc.e_del & 0xffff) * 0x10001u;
+    const uint32_t ne_ins2 = (uint32_t)(-sc.e_ins & 0xffff) * 0x10001u;
+    uint32_t Hp[C], E[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) { Hp[c] = 0u; E[c] = 0u; }
+    const int tl_max = tlen[0] > tlen[1] ? tlen[0] : tlen[1];
+    int steps = tl_max > 0 ? tl_max + L - 1 : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) steps = max(steps, __shfl_xor_sync(0xffffffffu, steps, o));
+
+    int gmax[2] = {0, 0}, te[2] = {-1, -1}, qe[2] = {-1, -1};
+    bool done[2] = {tlen[0] <= 0, tlen[1] <= 0};
+    uint32_t send_hf = 0u;   // bytes H_A, F_A, H_B, F_B of this lane's last column
+    uint32_t send_key = 0u;
+    uint32_t hprev_in = 0u;  // (H_A, H_B) of row i-1 at the column left of this lane's first
+    const uint32_t ccb = 255u - (uint32_t)(k * C);  // key column byte of the lane's first column
+    uint32_t tn[2] = {0u, 0u};
+    {
+        const int i0 = -k;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            if (i0 >= 0 && i0 < tlen[h]) tn[h] = (tmap && i0 <= te0[h]) ? t[h][te0[h] - i0] : t[h][i0];
+    }
+    for (int s = 0; s < steps; ++s) {
+        const uint32_t rhf = __shfl_up_sync(0xffffffffu, send_hf, 1, L);
+        const uint32_t rkey = __shfl_up_sync(0xffffffffu, send_key, 1, L);
+        const int i = s - k;
+        const uint32_t tca = tn[0], tcb = tn[1];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int in = i + 1;
+            if (in >= 0 && in < tlen[h] && !done[h]) tn[h] = (tmap && in <= te0[h]) ? t[h][te0[h] - in] : t[h][in];
+        }
+        const uint32_t h_in = k == 0 ? 0u : prmt(rhf, 0u, 0x4240u);
+        uint32_t f = k == 0 ? 0u : prmt(rhf, 0u, 0x4341u);
+        uint32_t key = k == 0 ? 0u : rkey;
+        const bool live_a = !done[0] && i >= 0 && i < tlen[0];
+        const bool live_b = !done[1] && i >= 0 && i < tlen[1];
+        if (live_a || live_b) {
+            if (live_a) bad |= tca >= (uint32_t)sc.m;
+            if (live_b) bad |= tcb >= (uint32_t)sc.m;
+            const uint32_t wa = prof_s[2 * (tca & 7u)], wb = prof_s[2 * (tcb & 7u)];
+            uint32_t hd = hprev_in;
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                uint32_t s2 = prmt(wa, wb, W.sel[c]);
+                s2 = (s2 & W.keep[c]) | W.fix[c];
+                const uint32_t m0 = __viaddmax_s16x2_relu(hd, s2, E[c]);  // max(H(i-1,j-1) + s, E, 0)
+                const uint32_t h = __vimax_s16x2_relu(m0, f);
+                // row-maximum key per job: (H << 8) | (255 - column)
+                const uint32_t kk = prmt(ccb - (uint32_t)c, h, W.ks[c]);
+                key = __vimax3_u16x2(key, kk, kk);
+                E[c] = __viaddmax_s16x2_relu(E[c], ne_del2, __viaddmax_s16x2(h, noe_del2, MIN2));  // E opens from H
+                f = __viaddmax_s16x2_relu(f, ne_ins2, __viaddmax_s16x2(m0, noe_ins2, MIN2));    // F opens from M0
+                hd = Hp[c];
+                Hp[c] = h;
+            }
+            send_hf = prmt(Hp[C - 1], f, 0x6240u);
+            send_key = key;
+            if (k == L - 1) {  // row i of both jobs is complete in this lane
+#pragma unroll
+                for (int hh = 0; hh < 2; ++hh) {
+                    if (!(hh == 0 ? live_a : live_b)) continue;
+                    const uint32_t kh = hh == 0 ? (key & 0xffffu) : (key >> 16);
+                    const int rmax = (int)(kh >> 8);
+                    if (trk) trk[hh].push(i, rmax, minsc[hh]);
+                    if (rmax > gmax[hh]) {
+                        gmax[hh] = rmax;
+                        te[hh] = i;
+                        qe[hh] = 255 - (int)(kh & 0xffu);
+                        if (gmax[hh] >= endsc[hh]) done[hh] = true;
+                    }
+                }
+            }
+        }
+        hprev_in = h_in;
+        if (stop_enabled) {  // warp-uniform early stop; the last lane tells its group
+            done[0] = __shfl_sync(0xffffffffu, done[0], L - 1, L);
+            done[1] = __shfl_sync(0xffffffffu, done[1], L - 1, L);
+            if (__all_sync(0xffffffffu, done[0] && done[1])) break;
+        }
+    }
+    Out2 r;
+#pragma unroll
+    for (int hh = 0; hh < 2; ++hh) {
+        r.score[hh] = __shfl_sync(0xffffffffu, gmax[hh], L - 1, L);
+        r.te[hh] = __shfl_sync(0xffffffffu, te[hh], L - 1, L);
+        r.qe[hh] = __shfl_sync(0xffffffffu, qe[hh], L - 1, L);
+        if (r.te[hh] < 0) r.qe[hh] = -1;
+    }
+    return r;
+}
+
+// One group of L lanes per pair of jobs (positions 2p and 2p+1 of the launch); a half whose job
+// does not qualify (job_ok) stays idle and is left to the other rescue kernels.
+template <int L, int C>
+__global__ void __launch_bounds__(128)
+rescue_wf2_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_rescue_job *__restrict__ jobs,
+                  const uint32_t *__restrict__ order, uint32_t n, const __grid_constant__ Scoring sc, int mode,
+                  int lanes_fixed, int minsc_all, int npen, uint2 *__restrict__ scratch,
+                  const uint64_t *__restrict__ scratch_off, bwacuda_rescue_result *__restrict__ out_aln,
+                  bwacuda_fwd_result *__restrict__ out_fwd, uint32_t *__restrict__ err)
+{
+    __shared__ uint32_t prof_s[16];
+    if (threadIdx.x < 16) prof_s[threadIdx.x] = sc.prof[threadIdx.x >> 1][threadIdx.x & 1];
+    __syncthreads();
+    const uint32_t pair = (blockIdx.x * blockDim.x + threadIdx.x) / L;
+    Lane2<L, C> W;
+    W.k = threadIdx.x % L;
+    const bool last = W.k == L - 1;
+    bool act[2];
+    uint32_t jid[2] = {0u, 0u};
+    bwacuda_dev_rescue_job J[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const uint32_t pos = 2 * pair + h;
+        act[h] = pos < n;
+        J[h].q_off = 0; J[h].t_off = 0; J[h].qlen = 0; J[h].tlen = 0; J[h].minsc = 0; J[h].endsc = 0;
+        if (act[h]) {
+            jid[h] = order ? order[pos] : pos;
+            J[h] = jobs[jid[h]];
+            act[h] = job_ok(J[h].qlen, J[h].tlen, sc.max_sc, lanes_fixed, L * C);
+        }
+    }
+    const uint8_t *q[2], *t[2];
+    int qlen[2], tlen[2], qpad[2], minsc[2], endsc[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        q[h] = seq + J[h].q_off;
+        t[h] = seq + J[h].t_off;
+        qlen[h] = act[h] ? J[h].qlen : 0;
+        tlen[h] = act[h] ? J[h].tlen : 0;
+        const int ln = lanes_fixed ? lanes_fixed : (J[h].qlen * sc.max_sc < 250 ? 16 : 8);
+        qpad[h] = act[h] ? ceil_to(J[h].qlen, ln) : 0;
+        minsc[h] = mode == 2 ? J[h].minsc : minsc_all;
+        endsc[h] = mode == 2 ? J[h].endsc : 0x7fffffff;
+    }
+    bool bad = false;
+    wf::WfTracker trk[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+        trk[h].init(act[h] ? scratch + scratch_off[jid[h]] : nullptr, act[h] ? (int)rescue_scratch_entries(J[h].tlen) : 0);
+    load_query2<L, C>(W, q[0], qlen[0], qpad[0], q[1], qlen[1], qpad[1], false, 0, 0, sc.m, npen, bad);
+    const int te0z[2] = {0, 0};
+    const Out2 fw = pass2<L, C>(W, prof_s, t, tlen, 0, te0z, sc, minsc, endsc, mode == 2, last ? trk : nullptr, bad);
+    int score2[2] = {-1, -1}, te2[2] = {-1, -1};
+    if (last) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            if (act[h]) {
+                trk[h].finish(fw.score[h], fw.te[h], sc.max_sc, score2[h], te2[h]);
+                if (trk[h].overflow) atomicOr(err, ERR_SCRATCH);
+            }
+    }
+    if (mode == 2) {
+        if (last) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                if (act[h]) {
+                    bwacuda_fwd_result r;
+                    r.score = fw.score[h]; r.te = fw.te[h]; r.qe = fw.qe[h]; r.score2 = score2[h]; r.te2 = te2[h];
+                    out_fwd[jid[h]] = r;
+                }
+        }
+    } else {
+        bool rev[2];
+        int rq[2], rqpad[2], rt[2], te0[2], stopsc[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            rev[h] = act[h] && fw.score[h] >= minsc[h] && fw.qe[h] >= 0 && fw.qe[h] < J[h].qlen;
+            rq[h] = rev[h] ? fw.qe[h] + 1 : 0;
+            // reverse-pass padding: batched_ksw_align2 recomputes the width from qe + 1, the
+            // scalar form keeps the forward one
+            const int ln = lanes_fixed ? lanes_fixed : (J[h].qlen * sc.max_sc < 250 ? 16 : 8);
+            const int rl = mode == 0 ? (rq[h] * sc.max_sc < 250 ? 16 : 8) : ln;
+            rqpad[h] = rev[h] ? ceil_to(rq[h], rl) : 0;
+            rt[h] = rev[h] ? (mode == 0 ? fw.te[h] + 1 : J[h].tlen) : 0;
+            te0[h] = fw.te[h];
+            stopsc[h] = fw.score[h];
+        }
+        int nomin[2] = {0x7fffffff, 0x7fffffff};
+        load_query2<L, C>(W, q[0], rq[0], rqpad[0], q[1], rq[1], rqpad[1], true, fw.qe[0], fw.qe[1], sc.m, npen,
+                          bad);
+        const Out2 rv = pass2<L, C>(W, prof_s, t, rt, 1, te0, sc, nomin, stopsc, true, nullptr, bad);
+        if (last) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                if (act[h]) {
+                    bwacuda_rescue_result r;
+                    r.score = fw.score[h]; r.qb = -1; r.qe = fw.qe[h]; r.tb = -1; r.te = fw.te[h];
+                    r.score2 = score2[h]; r.te2 = te2[h];
+                    if (rev[h] && rv.score[h] == fw.score[h]) {
+                        r.tb = fw.te[h] - rv.te[h];
+                        r.qb = fw.qe[h] - rv.qe[h];
+                    }
+                    out_aln[jid[h]] = r;
+                }
+        }
+    }
+    if (bad) atomicOr(err, ERR_BASE);
+}
+
+template <int L, int C>
+cudaError_t launch_wf2(const RescueLaunch &Lr, int npen)
+{
+    const uint32_t threads = 128;
+    const uint64_t total = (uint64_t)((Lr.n + 1) / 2) * L;
+    const uint32_t grid = (uint32_t)((total + threads - 1) / threads);
+    if (grid == 0) return cudaSuccess;
+    rescue_wf2_kernel<L, C><<<grid, threads, 0, Lr.stream>>>(Lr.seq, Lr.jobs, Lr.order, (uint32_t)Lr.n, Lr.sc,
+                                                             Lr.mode, Lr.lanes, Lr.minsc, npen, Lr.scratch,
+                                                             Lr.scratch_off, Lr.out_aln, Lr.out_fwd, Lr.err);
+    return cudaGetLastError();
+}
+
+}  // namespace wf2
+}  // namespace bwacuda

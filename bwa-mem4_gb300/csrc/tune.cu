@@ -108,6 +108,8 @@ extern "C" int bwacuda_get_tuning(bwacuda_ctx *c, bwacuda_tuning *out)
     const int lq = batched_get_long(c);
     out->long_qlen = lq == INT_MAX ? 0 : lq;
     out->long_lanes = c->long_lanes;
+    out->rescue_pair = c->rescue_pair ? 1 : 0;
+    out->reserved = 0;
     return BWACUDA_OK;
 }
 
@@ -272,6 +274,7 @@ extern "C" int bwacuda_autotune_rescue(bwacuda_ctx *c, const uint8_t *d_seq, con
         if (e != cudaSuccess) { tmp.release(); dout.release(); dcells.release(); return cuda_status(e); }
         const bwacuda_stats saved = c->stats;
         const int kern0 = c->rescue_kernel, lanes0 = c->rescue_lanes;
+        const bool pair0 = c->rescue_pair;
         auto run = [&]() {
             return ksw_align2_device_locked(c, d_seq, static_cast<const bwacuda_dev_rescue_job *>(jp), count, scp,
                                             minsc, max_sc, 0, 0, static_cast<bwacuda_rescue_result *>(dout.p), s);
@@ -280,15 +283,17 @@ extern "C" int bwacuda_autotune_rescue(bwacuda_ctx *c, const uint8_t *d_seq, con
         uint64_t dummy = 0;
         int rc = run();
         if (!rc) rc = collect_device_status(c, s, &dummy);
-        struct Cand { int kernel, lanes; } cands[] = {
-            {BWACUDA_RESCUE_AUTO, 8}, {BWACUDA_RESCUE_AUTO, 16}, {BWACUDA_RESCUE_AUTO, 32}, {BWACUDA_RESCUE_TPJ, 16}};
+        struct Cand { int kernel, lanes; bool pair; } cands[] = {
+            {BWACUDA_RESCUE_AUTO, 8, false}, {BWACUDA_RESCUE_AUTO, 16, false}, {BWACUDA_RESCUE_AUTO, 32, false},
+            {BWACUDA_RESCUE_TPJ, 16, false}, {BWACUDA_RESCUE_AUTO, 8, true}, {BWACUDA_RESCUE_AUTO, 16, true}};
         double best_ms = 0;
-        Cand best = {kern0, lanes0};
+        Cand best = {kern0, lanes0, pair0};
         int ncand = 0;
         for (const Cand &cd : cands) {
             if (rc) break;
             c->rescue_kernel = cd.kernel;
             c->rescue_lanes = cd.lanes;
+            c->rescue_pair = cd.pair;
             const double ms = time_runs(T, s, 2, run);
             if (ms < 0) { rc = (int)ms; break; }
             ++ncand;
@@ -298,6 +303,7 @@ extern "C" int bwacuda_autotune_rescue(bwacuda_ctx *c, const uint8_t *d_seq, con
         if (!rc) rc = st;
         c->rescue_kernel = rc ? kern0 : best.kernel;
         c->rescue_lanes = rc ? lanes0 : best.lanes;
+        c->rescue_pair = rc ? pair0 : best.pair;
         c->stats = saved;
         tmp.release();
         dout.release();

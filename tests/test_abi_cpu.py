@@ -45,7 +45,7 @@ def test_null_context_is_rejected():
 def test_struct_layouts_match_header():
     assert B.EXT_RES.itemsize == 24 and B.ALN_RES.itemsize == 28 and B.FWD_RES.itemsize == 20
     assert ctypes.sizeof(B.Scoring) == 84
-    assert ctypes.sizeof(B.Tuning) == 48
+    assert ctypes.sizeof(B.Tuning) == 56
 
 
 def test_synthetic_workloads_are_deterministic():
@@ -73,5 +73,5 @@ def test_header_constants_match_binding():
         if hasattr(B, name):
             assert getattr(B, name) == val, name
     for name in ("OPT_EXT_PATH", "OPT_CHUNK_JOBS", "OPT_GRAPHS", "OPT_PERSIST_BLOCK", "OPT_RESCUE_KERNEL",
-                 "OPT_HOST_GATHER", "OPT_GRAB", "OPT_BUCKET_STEP", "OPT_RESCUE_LANES", "OPT_UNGAPPED", "OPT_DEVICE_PIECE", "OPT_LONG_QLEN", "OPT_LONG_LANES", "GATHER_AUTO", "GATHER_HOST", "GATHER_DEVICE", "PATH_PLAIN", "PATH_BATCHED"):
+                 "OPT_HOST_GATHER", "OPT_GRAB", "OPT_BUCKET_STEP", "OPT_RESCUE_LANES", "OPT_UNGAPPED", "OPT_DEVICE_PIECE", "OPT_LONG_QLEN", "OPT_LONG_LANES", "OPT_RESCUE_PAIR", "GATHER_AUTO", "GATHER_HOST", "GATHER_DEVICE", "PATH_PLAIN", "PATH_BATCHED"):
         assert getattr(B, name) == defs[name], name

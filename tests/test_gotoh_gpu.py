@@ -14,8 +14,9 @@ import refstreams as R
 
 pytestmark = pytest.mark.gpu
 
-KERNELS = [pytest.param((B.RESCUE_AUTO, 16), id="wavefront16"), pytest.param((B.RESCUE_AUTO, 8), id="wavefront8"),
-           pytest.param((B.RESCUE_AUTO, 32), id="wavefront32"), pytest.param((B.RESCUE_TPJ, 16), id="tpj")]
+KERNELS = [pytest.param((B.RESCUE_AUTO, 16, 0), id="wavefront16"), pytest.param((B.RESCUE_AUTO, 8, 0), id="wavefront8"),
+           pytest.param((B.RESCUE_AUTO, 32, 0), id="wavefront32"), pytest.param((B.RESCUE_TPJ, 16, 0), id="tpj"),
+           pytest.param((B.RESCUE_AUTO, 8, 1), id="paired8"), pytest.param((B.RESCUE_AUTO, 16, 1), id="paired16")]
 SCORINGS = [(1, 4, 6, 1), (2, 3, 5, 2)]
 
 
@@ -32,12 +33,14 @@ def stream():
 
 @pytest.fixture(params=KERNELS)
 def rctx(ctx, request):
-    kernel, lanes = request.param
+    kernel, lanes, pair = request.param
     ctx.set_option(B.OPT_RESCUE_KERNEL, kernel)
     ctx.set_option(B.OPT_RESCUE_LANES, lanes)
+    ctx.set_option(B.OPT_RESCUE_PAIR, pair)
     yield ctx
     ctx.set_option(B.OPT_RESCUE_KERNEL, B.RESCUE_AUTO)
     ctx.set_option(B.OPT_RESCUE_LANES, 16)
+    ctx.set_option(B.OPT_RESCUE_PAIR, 0)
 
 
 def _check(pairs, got, want, score_only=False):

@@ -10,19 +10,22 @@ import refstreams as R
 pytestmark = pytest.mark.gpu
 
 # (kernel family, lanes per job of the register wavefront)
-KERNELS = [pytest.param((B.RESCUE_AUTO, 16), id="wavefront16"), pytest.param((B.RESCUE_AUTO, 8), id="wavefront8"),
-           pytest.param((B.RESCUE_AUTO, 32), id="wavefront32"), pytest.param((B.RESCUE_TPJ, 16), id="tpj")]
+KERNELS = [pytest.param((B.RESCUE_AUTO, 16, 0), id="wavefront16"), pytest.param((B.RESCUE_AUTO, 8, 0), id="wavefront8"),
+           pytest.param((B.RESCUE_AUTO, 32, 0), id="wavefront32"), pytest.param((B.RESCUE_TPJ, 16, 0), id="tpj"),
+           pytest.param((B.RESCUE_AUTO, 8, 1), id="paired8"), pytest.param((B.RESCUE_AUTO, 16, 1), id="paired16")]
 
 
 @pytest.fixture(params=KERNELS)
 def rctx(ctx, request):
     """The context with the rescue kernel family under test selected."""
-    kernel, lanes = request.param
+    kernel, lanes, pair = request.param
     ctx.set_option(B.OPT_RESCUE_KERNEL, kernel)
     ctx.set_option(B.OPT_RESCUE_LANES, lanes)
+    ctx.set_option(B.OPT_RESCUE_PAIR, pair)
     yield ctx
     ctx.set_option(B.OPT_RESCUE_KERNEL, B.RESCUE_AUTO)
     ctx.set_option(B.OPT_RESCUE_LANES, 16)
+    ctx.set_option(B.OPT_RESCUE_PAIR, 0)
 
 
 def _js(pairs):
@@ -159,12 +162,78 @@ def test_autotune_rescue_keeps_results(ctx):
     d_out = torch.zeros(len(js) * 28, dtype=torch.uint8, device="cuda")
     try:
         t = ctx.autotune_rescue(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), minsc=20, max_sc=1, sample=8192)
-        assert t["candidates"] == 4 and t["rescue_gcups"] > 0
-        assert (t["rescue_kernel"], t["rescue_lanes"]) in {(B.RESCUE_AUTO, 8), (B.RESCUE_AUTO, 16),
-                                                           (B.RESCUE_AUTO, 32), (B.RESCUE_TPJ, 16)}
+        # the 32-bit wavefront at 8/16/32 lanes, thread-per-job, the paired wavefront at 8/16 lanes
+        assert t["candidates"] == 6 and t["rescue_gcups"] > 0
+        assert (t["rescue_kernel"], t["rescue_lanes"], t["rescue_pair"]) in {
+            (B.RESCUE_AUTO, 8, 0), (B.RESCUE_AUTO, 16, 0), (B.RESCUE_AUTO, 32, 0), (B.RESCUE_TPJ, 16, 0),
+            (B.RESCUE_AUTO, 8, 1), (B.RESCUE_AUTO, 16, 1)}
         ctx.ksw_align2_device(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), d_out.data_ptr(), minsc=20, max_sc=1)
         ctx.sync()
         assert np.array_equal(d_out.cpu().numpy().view(B.ALN_RES), want)
     finally:
         ctx.set_option(B.OPT_RESCUE_KERNEL, B.RESCUE_AUTO)
+        ctx.set_option(B.OPT_RESCUE_LANES, 16)
+
+
+def _pair_mix(seed, n):
+    """Jobs on both sides of the paired wavefront's limits in one batch: byte-range windows,
+    queries whose score can pass 255 (qlen 260-300 at a = 1), short and empty targets, ragged
+    target lengths inside a pair, N in queries and targets."""
+    rng = np.random.default_rng(seed)
+    pairs = []
+    for k in range(n):
+        kind = k % 5
+        ql = int(rng.integers(100, 160)) if kind < 3 else int(rng.integers(256, 300))
+        tl = int(rng.integers(0, 40)) if kind == 4 else int(rng.integers(200, 900))
+        t = rng.integers(0, 4, tl)
+        q = rng.integers(0, 4, ql)
+        if tl > ql and kind != 2:
+            at = int(rng.integers(0, tl - ql + 1))
+            t[at:at + ql] = q
+            flip = rng.random(ql) < 0.02
+            q[flip] = (q[flip] + 1) % 4
+        q[rng.random(ql) < 0.01] = 4
+        if tl:
+            t[rng.random(tl) < 0.01] = 4
+        pairs.append((q.tolist(), t.tolist()))
+    return pairs
+
+
+@pytest.mark.parametrize("lanes", [8, 16])
+@pytest.mark.parametrize("scoring", [(1, 4, 6, 1), (2, 3, 5, 2)])
+def test_paired_wavefront_limits(ctx, lanes, scoring):
+    a, b, o, e = scoring
+    mat = oracle.scmat(a, b)
+    js = _js(_pair_mix(100 + lanes + a, 3001))  # odd: the last pair has one job
+    ctx.set_option(B.OPT_RESCUE_PAIR, 1)
+    ctx.set_option(B.OPT_RESCUE_LANES, lanes)
+    try:
+        for mode in (0, 1):
+            want, _ = oracle.align2_batch(js, mat, o, e, o, e, 19 * a, a, mode=mode)
+            got = (ctx.ksw_align2_batch(js, mat, o, e, o, e, 19 * a, a) if mode == 0 else
+                   ctx.ksw_align2_scalar_batch(js, mat, o, e, o, e, 19 * a, a, 0))
+            assert np.array_equal(got, want), mode
+        want = oracle.local_fwd_batch(js, 19 * a, 40 * a, mat, o, e, o, e, a)
+        assert np.array_equal(ctx.ksw_local_fwd_batch(js, 19 * a, 40 * a, mat, o, e, o, e, a), want)
+    finally:
+        ctx.set_option(B.OPT_RESCUE_PAIR, 0)
+        ctx.set_option(B.OPT_RESCUE_LANES, 16)
+
+
+def test_paired_wavefront_other_matrices(ctx):
+    # an N column of several values keeps every job in the 32-bit wavefront; an asymmetric 4x4 block
+    # with a constant N column runs paired
+    js = _js(_pair_mix(7, 800))
+    odd = oracle.scmat(1, 4).copy()
+    odd[4] = -2  # mat[0][4]: the N column is no longer one value
+    asym = oracle.scmat(1, 4).copy()
+    asym[1], asym[5 + 2], asym[10 + 3] = -3, -2, -1  # mat[0][1], mat[1][2], mat[2][3]
+    ctx.set_option(B.OPT_RESCUE_PAIR, 1)
+    ctx.set_option(B.OPT_RESCUE_LANES, 8)
+    try:
+        for mat in (odd, asym):
+            want, _ = oracle.align2_batch(js, mat, 6, 1, 6, 1, 19, 1)
+            assert np.array_equal(ctx.ksw_align2_batch(js, mat, 6, 1, 6, 1, 19, 1), want)
+    finally:
+        ctx.set_option(B.OPT_RESCUE_PAIR, 0)
         ctx.set_option(B.OPT_RESCUE_LANES, 16)
