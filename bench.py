@@ -80,6 +80,7 @@ def parse():
                                        "windows", "retry"],
                     help="profiling case: run the small workload twice through one path, no timing")
     ap.add_argument("--lanes", type=int, default=8, help="rescue case: wavefront lanes per job")
+    ap.add_argument("--pair", type=int, default=0, help="rescue case: two byte-range jobs per wavefront group")
     ap.add_argument("--h0-add", type=int, default=0,
                     help="extension cases: add this to every h0 (300 moves read pairs into the 16-bit cell class)")
     return ap.parse_args()
@@ -761,6 +762,7 @@ def run_case(args):
     else:
         js = B.synth_rescue(args.jobs, seed=0)
         ctx.set_option(B.OPT_RESCUE_LANES, args.lanes)
+        ctx.set_option(B.OPT_RESCUE_PAIR, args.pair)
         d_seq = torch.from_numpy(js.seq).cuda()
         d_jobs = torch.from_numpy(js.dev_res_jobs().view(np.uint8)).cuda()
         d_out = torch.zeros(len(js) * 28, dtype=torch.uint8, device="cuda")
