@@ -14,11 +14,18 @@
 //
 // Scores.  A target row's four scores for query codes 0..3 are one 32-bit profile word, so one
 // prmt picks (mat[tA][qA], mat[tB][qB]) sign-extended into the two lanes.  Query columns that
-// are N (code 4), ksw padding (score 0) or invalid (score 0, flagged) are patched with one
-// lop3 against per-column keep / fix words; this needs the N column of the matrix to be one
-// value (mat[t][4] equal for every t, as bwa's matrix has), which the host checks.
+// are N (code 4), ksw padding (score 0) or invalid (score 0, flagged) are patched by a second
+// prmt against a word holding the N penalty and zeros; this needs the N column of the matrix to
+// be one value (mat[t][4] equal for every t, as bwa's matrix has), which the host checks.
+//
+// Per column and row: two prmt for the scores, M0 = max(Hd + s, E, 0), H = max(M0, F), the key
+// prmt and half a 3-way key maximum, and two fused add-max each for E and F -- 9.5 instructions
+// for two cells.  M0 of the next column is computed before H of this one is stored, so the
+// previous row's H is overwritten in place (no register copies per step).
 #pragma once
 #include <cuda_runtime.h>
+
+#include <climits>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -39,10 +46,10 @@ __host__ __device__ inline bool job_ok(int qlen, int tlen, int max_sc, int lanes
 template <int L, int C>
 struct Lane2 {
     int k;
-    uint32_t sel[C];   // prmt selectors: low half picks job A's byte from word A, high half job B's from word B
-    uint32_t keep[C];  // 0xffff per half: the prmt score stands; 0: replaced by fix
-    uint32_t fix[C];   // N penalty (query N), 0 (padding or an invalid code)
-    uint32_t ks[C];    // row-key selectors: (H << 8) | column byte, or 0 for a column past the padded query
+    uint32_t sel[C];          // prmt selectors: low half picks job A's byte from word A, high half job B's from word B
+    uint32_t sf[C];           // prmt selectors patching the score: keep it, the N penalty, or 0
+    uint32_t ks[C];           // row-key selectors: (H << 8) | column byte, or 0 for a column past the padded query
+    uint32_t cw[(C + 3) / 4]; // key column bytes 255 - j, four columns a word
 };
 
 // Loads the lane's columns of both jobs: forward (query[j]) or the reversed prefix
@@ -51,13 +58,16 @@ struct Lane2 {
 // never a row maximum (they lie right of every real column and feed no real cell).
 template <int L, int C>
 __device__ __forceinline__ void load_query2(Lane2<L, C> &W, const uint8_t *qa, int qla, int qpa, const uint8_t *qb,
-                                            int qlb, int qpb, bool rev, int qea, int qeb, int m, int npen, bool &bad)
+                                            int qlb, int qpb, bool rev, int qea, int qeb, int m, bool &bad)
 {
 #pragma unroll
     for (int c = 0; c < C; ++c) {
         const int j = W.k * C + c;
+        const uint32_t b = 4u + (uint32_t)(c & 3);  // this column's byte of cw[c / 4] as a prmt source
         // key bytes: the column byte, H; past the padded query two zero bytes (H's high bytes)
-        W.ks[c] = (j < qpa ? 0x0040u : 0x0055u) | (j < qpb ? 0x6000u : 0x7700u);
+        W.ks[c] = (j < qpa ? b : 0x11u) | (j < qpb ? ((b << 8) | 0x2000u) : 0x3300u);
+        if ((c & 3) == 0) W.cw[c >> 2] = 0u;
+        W.cw[c >> 2] |= ((uint32_t)(255 - j) & 0xffu) << (8 * (c & 3));
         uint32_t ca = 7u, cb = 7u;
         if (j < qla) {
             ca = rev ? qa[qea - j] : qa[j];
@@ -72,10 +82,8 @@ __device__ __forceinline__ void load_query2(Lane2<L, C> &W, const uint8_t *qa, i
         const bool sa = ca >= 4u, sb = cb >= 4u;  // N, padding or invalid
         const uint32_t ba = sa ? 0u : ca, bb = sb ? 4u : 4u + cb;
         W.sel[c] = ba | ((ba | 8u) << 4) | (bb << 8) | ((bb | 8u) << 12);
-        W.keep[c] = (sa ? 0u : 0xffffu) | (sb ? 0u : 0xffff0000u);
-        const uint32_t fa = ca == 4u ? (uint32_t)(npen & 0xffff) : 0u;
-        const uint32_t fb = cb == 4u ? (uint32_t)(npen & 0xffff) : 0u;
-        W.fix[c] = fa | (fb << 16);
+        // patch selectors over (score, Z): Z = (N penalty, 0) as bytes 4-7
+        W.sf[c] = (ca < 4u ? 0x10u : (ca == 4u ? 0x54u : 0x76u)) | (cb < 4u ? 0x3200u : (cb == 4u ? 0x5400u : 0x7600u));
     }
 }
 
@@ -87,9 +95,9 @@ struct Out2 {
 // h inactive; tmap / te0 select the reverse pass's target mapping (rows <= te0 read reversed).
 // stop[h]: the half stops once its score reaches endsc[h].  Returns the results in every lane.
 template <int L, int C>
-__device__ Out2 pass2(const Lane2<L, C> &W, const uint32_t *prof_s, const uint8_t *const t[2], const int tlen[2],
-                      int tmap, const int te0[2], const Scoring &sc, const int minsc[2], const int endsc[2],
-                      bool stop_enabled, wf::WfTracker *trk, bool &bad)
+__device__ Out2 pass2(const Lane2<L, C> &W, const uint32_t *prof_s, uint32_t zw, const uint8_t *const t[2],
+                      const int tlen[2], int tmap, const int te0[2], const Scoring &sc, const int minsc[2],
+                      const int endsc[2], bool stop_enabled, wf::WfTracker *trk, bool &bad)
 {
     const int k = W.k;
     const uint32_t noe_del2 = (uint32_t)(-(sc.o_del + sc.e_del) & 0xffff) * 0x10001u;
@@ -105,11 +113,17 @@ __device__ Out2 pass2(const Lane2<L, C> &W, const uint32_t *prof_s, const uint8_
     for (int o = 16; o > 0; o >>= 1) steps = max(steps, __shfl_xor_sync(0xffffffffu, steps, o));
 
     int gmax[2] = {0, 0}, te[2] = {-1, -1}, qe[2] = {-1, -1};
+    // a row maximum at or below thr[h] changes nothing: below the tracker's minsc and not a new best
+    int mm1[2], thr[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        mm1[h] = minsc[h] > INT_MIN ? minsc[h] - 1 : INT_MIN;
+        thr[h] = mm1[h] < 0 ? mm1[h] : 0;  // min(minsc - 1, best so far = 0)
+    }
     bool done[2] = {tlen[0] <= 0, tlen[1] <= 0};
     uint32_t send_hf = 0u;   // bytes H_A, F_A, H_B, F_B of this lane's last column
     uint32_t send_key = 0u;
     uint32_t hprev_in = 0u;  // (H_A, H_B) of row i-1 at the column left of this lane's first
-    const uint32_t ccb = 255u - (uint32_t)(k * C);  // key column byte of the lane's first column
     uint32_t tn[2] = {0u, 0u};
     {
         const int i0 = -k;
@@ -136,35 +150,41 @@ __device__ Out2 pass2(const Lane2<L, C> &W, const uint32_t *prof_s, const uint8_
             if (live_a) bad |= tca >= (uint32_t)sc.m;
             if (live_b) bad |= tcb >= (uint32_t)sc.m;
             const uint32_t wa = prof_s[2 * (tca & 7u)], wb = prof_s[2 * (tcb & 7u)];
-            uint32_t hd = hprev_in;
+            uint32_t m0 = __viaddmax_s16x2_relu(hprev_in, prmt(prmt(wa, wb, W.sel[0]), zw, W.sf[0]), E[0]);
+            uint32_t kprev = 0u;
 #pragma unroll
             for (int c = 0; c < C; ++c) {
-                uint32_t s2 = prmt(wa, wb, W.sel[c]);
-                s2 = (s2 & W.keep[c]) | W.fix[c];
-                const uint32_t m0 = __viaddmax_s16x2_relu(hd, s2, E[c]);  // max(H(i-1,j-1) + s, E, 0)
-                const uint32_t h = __vimax_s16x2_relu(m0, f);
-                // row-maximum key per job: (H << 8) | (255 - column)
-                const uint32_t kk = prmt(ccb - (uint32_t)c, h, W.ks[c]);
-                key = __vimax3_u16x2(key, kk, kk);
+                const uint32_t h = __vimax_s16x2_relu(m0, f);                 // H = max(M0, F)
+                const uint32_t ti = __viaddmax_s16x2(m0, noe_ins2, MIN2);     // M0 - oe_ins
+                // row-maximum key per job: (H << 8) | (255 - column), two columns per 3-way max
+                const uint32_t kk = prmt(h, W.cw[c >> 2], W.ks[c]);
+                if (c & 1) key = __vimax3_u16x2(key, kprev, kk);
+                else kprev = kk;
                 E[c] = __viaddmax_s16x2_relu(E[c], ne_del2, __viaddmax_s16x2(h, noe_del2, MIN2));  // E opens from H
-                f = __viaddmax_s16x2_relu(f, ne_ins2, __viaddmax_s16x2(m0, noe_ins2, MIN2));    // F opens from M0
-                hd = Hp[c];
+                f = __viaddmax_s16x2_relu(f, ne_ins2, ti);                    // F opens from M0
+                if (c + 1 < C)  // M0 of the next column reads this column's previous-row H before it is replaced
+                    m0 = __viaddmax_s16x2_relu(Hp[c], prmt(prmt(wa, wb, W.sel[c + 1]), zw, W.sf[c + 1]), E[c + 1]);
                 Hp[c] = h;
             }
+            if (C & 1) key = __vimax3_u16x2(key, kprev, kprev);
             send_hf = prmt(Hp[C - 1], f, 0x6240u);
             send_key = key;
             if (k == L - 1) {  // row i of both jobs is complete in this lane
+                const int ra = (int)((key >> 8) & 0xffu), rb = (int)(key >> 24);
+                if ((live_a && ra > thr[0]) || (live_b && rb > thr[1])) {
 #pragma unroll
-                for (int hh = 0; hh < 2; ++hh) {
-                    if (!(hh == 0 ? live_a : live_b)) continue;
-                    const uint32_t kh = hh == 0 ? (key & 0xffffu) : (key >> 16);
-                    const int rmax = (int)(kh >> 8);
-                    if (trk) trk[hh].push(i, rmax, minsc[hh]);
-                    if (rmax > gmax[hh]) {
-                        gmax[hh] = rmax;
-                        te[hh] = i;
-                        qe[hh] = 255 - (int)(kh & 0xffu);
-                        if (gmax[hh] >= endsc[hh]) done[hh] = true;
+                    for (int hh = 0; hh < 2; ++hh) {
+                        if (!(hh == 0 ? live_a : live_b)) continue;
+                        const uint32_t kh = hh == 0 ? (key & 0xffffu) : (key >> 16);
+                        const int rmax = (int)(kh >> 8);
+                        if (trk) trk[hh].push(i, rmax, minsc[hh]);
+                        if (rmax > gmax[hh]) {
+                            gmax[hh] = rmax;
+                            te[hh] = i;
+                            qe[hh] = 255 - (int)(kh & 0xffu);
+                            thr[hh] = mm1[hh] < rmax ? mm1[hh] : rmax;
+                            if (gmax[hh] >= endsc[hh]) done[hh] = true;
+                        }
                     }
                 }
             }
@@ -236,9 +256,11 @@ rescue_wf2_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_rescue_job 
 #pragma unroll
     for (int h = 0; h < 2; ++h)
         trk[h].init(act[h] ? scratch + scratch_off[jid[h]] : nullptr, act[h] ? (int)rescue_scratch_entries(J[h].tlen) : 0);
-    load_query2<L, C>(W, q[0], qlen[0], qpad[0], q[1], qlen[1], qpad[1], false, 0, 0, sc.m, npen, bad);
+    const uint32_t zw = (uint32_t)npen & 0xffffu;  // patch word: bytes N penalty (16-bit), 0, 0
+    load_query2<L, C>(W, q[0], qlen[0], qpad[0], q[1], qlen[1], qpad[1], false, 0, 0, sc.m, bad);
     const int te0z[2] = {0, 0};
-    const Out2 fw = pass2<L, C>(W, prof_s, t, tlen, 0, te0z, sc, minsc, endsc, mode == 2, last ? trk : nullptr, bad);
+    const Out2 fw = pass2<L, C>(W, prof_s, zw, t, tlen, 0, te0z, sc, minsc, endsc, mode == 2, last ? trk : nullptr,
+                                bad);
     int score2[2] = {-1, -1}, te2[2] = {-1, -1};
     if (last) {
 #pragma unroll
@@ -275,9 +297,8 @@ rescue_wf2_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_rescue_job 
             stopsc[h] = fw.score[h];
         }
         int nomin[2] = {0x7fffffff, 0x7fffffff};
-        load_query2<L, C>(W, q[0], rq[0], rqpad[0], q[1], rq[1], rqpad[1], true, fw.qe[0], fw.qe[1], sc.m, npen,
-                          bad);
-        const Out2 rv = pass2<L, C>(W, prof_s, t, rt, 1, te0, sc, nomin, stopsc, true, nullptr, bad);
+        load_query2<L, C>(W, q[0], rq[0], rqpad[0], q[1], rq[1], rqpad[1], true, fw.qe[0], fw.qe[1], sc.m, bad);
+        const Out2 rv = pass2<L, C>(W, prof_s, zw, t, rt, 1, te0, sc, nomin, stopsc, true, nullptr, bad);
         if (last) {
 #pragma unroll
             for (int h = 0; h < 2; ++h)
@@ -299,7 +320,9 @@ rescue_wf2_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_rescue_job 
 template <int L, int C>
 cudaError_t launch_wf2(const RescueLaunch &Lr, int npen)
 {
-    const uint32_t threads = 128;
+    // two-warp blocks: residency is register-bound (about 190 registers at 20 columns a lane), and
+    // small blocks let an SM hold every warp its register file fits
+    const uint32_t threads = 64;
     const uint64_t total = (uint64_t)((Lr.n + 1) / 2) * L;
     const uint32_t grid = (uint32_t)((total + threads - 1) / threads);
     if (grid == 0) return cudaSuccess;
