@@ -20,8 +20,8 @@
 //
 // Per column and row: two prmt for the scores, M0 = max(Hd + s, E, 0), H = max(M0, F), the key
 // prmt and half a 3-way key maximum, and two fused add-max each for E and F -- 9.5 instructions
-// for two cells.  M0 of the next column is computed before H of this one is stored, so the
-// previous row's H is overwritten in place (no register copies per step).
+// for two cells.  M0 of the next column is computed before H of this one, so the previous
+// row's H is overwritten in place (no register copies per step).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -154,6 +154,11 @@ __device__ Out2 pass2(const Lane2<L, C> &W, const uint32_t *prof_s, uint32_t zw,
             uint32_t kprev = 0u;
 #pragma unroll
             for (int c = 0; c < C; ++c) {
+                // M0 of the next column first: it is the last reader of this column's previous-row H,
+                // which H of this row then replaces in the same register
+                uint32_t m0n = 0u;
+                if (c + 1 < C)
+                    m0n = __viaddmax_s16x2_relu(Hp[c], prmt(prmt(wa, wb, W.sel[c + 1]), zw, W.sf[c + 1]), E[c + 1]);
                 const uint32_t h = __vimax_s16x2_relu(m0, f);                 // H = max(M0, F)
                 const uint32_t ti = __viaddmax_s16x2(m0, noe_ins2, MIN2);     // M0 - oe_ins
                 // row-maximum key per job: (H << 8) | (255 - column), two columns per 3-way max
@@ -162,9 +167,8 @@ __device__ Out2 pass2(const Lane2<L, C> &W, const uint32_t *prof_s, uint32_t zw,
                 else kprev = kk;
                 E[c] = __viaddmax_s16x2_relu(E[c], ne_del2, __viaddmax_s16x2(h, noe_del2, MIN2));  // E opens from H
                 f = __viaddmax_s16x2_relu(f, ne_ins2, ti);                    // F opens from M0
-                if (c + 1 < C)  // M0 of the next column reads this column's previous-row H before it is replaced
-                    m0 = __viaddmax_s16x2_relu(Hp[c], prmt(prmt(wa, wb, W.sel[c + 1]), zw, W.sf[c + 1]), E[c + 1]);
                 Hp[c] = h;
+                m0 = m0n;
             }
             if (C & 1) key = __vimax3_u16x2(key, kprev, kprev);
             send_hf = prmt(Hp[C - 1], f, 0x6240u);
