@@ -77,7 +77,7 @@ def parse():
     ap.add_argument("--serve-rates", default="50,500,2000", help="Poisson arrival rates (requests/s)")
     ap.add_argument("--serve-requests", type=int, default=600, help="requests per arrival rate")
     ap.add_argument("--case", choices=["ext-batched", "ext-plain", "ext-mixed", "ext-gather", "rescue", "global",
-                                       "windows", "retry"],
+                                       "windows", "retry", "op-rates"],
                     help="profiling case: run the small workload twice through one path, no timing")
     ap.add_argument("--lanes", type=int, default=8, help="rescue case: wavefront lanes per job")
     ap.add_argument("--pair", type=int, default=0, help="rescue case: two byte-range jobs per wavefront group")
@@ -703,6 +703,14 @@ def run_case(args):
 
     ctx = B.Context(0)
     ctx.set_option(B.OPT_GRAPHS, 0)  # plain stream launches (no graph nodes) under the profiler
+    if args.case == "op-rates":
+        # the instruction-rate microbenchmark: one line per operation (1e9 lane-ops/s); under ncu
+        # each launch's smsp__inst_executed / sm__inst_executed_pipe_alu counts per operation
+        for name, g in ctx.measure_op_rates().items():
+            print(f"{name} {g:.1f}")
+        print("alu_peak", round(ctx.measure_alu_peak(), 1))
+        ctx.close()
+        return
     if args.case in ("ext-batched", "ext-plain", "ext-mixed"):
         js = B.synth_ext(3 if args.case == "ext-mixed" else 2, args.jobs, seed=0)
         js.h0 = js.h0 + args.h0_add

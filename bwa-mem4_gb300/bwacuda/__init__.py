@@ -88,7 +88,12 @@ EXPORTS = ("bwacuda_ctx_create", "bwacuda_ctx_destroy", "bwacuda_set_option", "b
            "bwacuda_server_stats", "bwacuda_measure_alu_peak", "bwacuda_get_tuning", "bwacuda_autotune_extend",
            "bwacuda_autotune_rescue", "bwacuda_ksw_global2_batch", "bwacuda_extend_batch_retry",
            "bwacuda_extend_retry_device", "bwacuda_ref_set", "bwacuda_mate_rescue_windows",
-           "bwacuda_server_submit_mixed", "bwacuda_server_cells")
+           "bwacuda_server_submit_mixed", "bwacuda_server_cells", "bwacuda_measure_op_rate")
+
+# bwacuda_measure_op_rate operations, in header order
+OP_RATE_NAMES = ("viaddmax_s32", "viaddmax_s32_relu", "viaddmax_s16x2", "viaddmax_s16x2_relu", "viaddmin_s16x2",
+                 "vimax3_s16x2", "vimax3_u16x2", "vimax_s16x2_relu", "vimax3_s32", "prmt", "c_add_max", "imad",
+                 "lop3")
 
 _lib = None
 _synth = None
@@ -112,6 +117,7 @@ def lib():
     vp, I, sz = C.c_void_p, C.c_int, C.c_size_t
     L.bwacuda_ctx_create.argtypes = [I, C.POINTER(vp)]
     L.bwacuda_measure_alu_peak.argtypes = [vp, C.POINTER(C.c_double)]
+    L.bwacuda_measure_op_rate.argtypes = [vp, I, C.POINTER(C.c_double)]
     L.bwacuda_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.bwacuda_ksw_global2_batch.argtypes = [vp, vp, sz, I, vp, I, I, I, I, vp, vp, vp, sz]
     L.bwacuda_ref_set.argtypes = [vp, vp, C.c_int64, vp, vp, C.c_int32]
@@ -654,6 +660,15 @@ class Context:
                                            max_sc, sample, C.byref(t))
         self._check(rc, "bwacuda_autotune_rescue")
         return t.as_dict()
+
+    def measure_op_rates(self) -> dict:
+        """Measured throughput (1e9 lane-operations/s) of each integer operation of the DP kernels."""
+        out = {}
+        for k, name in enumerate(OP_RATE_NAMES):
+            g = C.c_double()
+            self._check(lib().bwacuda_measure_op_rate(self.h, k, C.byref(g)), "bwacuda_measure_op_rate")
+            out[name] = g.value
+        return out
 
     def measure_alu_peak(self) -> float:
         """Measured integer ALU-pipe rate of the device, 1e9 fused add-max ops per second."""

@@ -402,6 +402,27 @@ int bwacuda_reset_stats(bwacuda_ctx *ctx);
  * counterpart in the reference. */
 int bwacuda_measure_alu_peak(bwacuda_ctx *ctx, double *gops);
 
+/* Measured throughput of one integer operation the DP kernels are built from, in 1e9
+ * lane-operations per second: every thread of a few short launches runs 8 independent chains
+ * of it, so an operation that is one ALU-pipe instruction runs at bwacuda_measure_alu_peak's
+ * rate and one that takes two instructions at half of it.  Synchronous.  A measurement helper
+ * with no counterpart in the reference. */
+#define BWACUDA_OPR_VIADDMAX_S32 0        /* __viaddmax_s32 */
+#define BWACUDA_OPR_VIADDMAX_S32_RELU 1   /* __viaddmax_s32_relu */
+#define BWACUDA_OPR_VIADDMAX_S16X2 2      /* __viaddmax_s16x2 */
+#define BWACUDA_OPR_VIADDMAX_S16X2_RELU 3 /* __viaddmax_s16x2_relu */
+#define BWACUDA_OPR_VIADDMIN_S16X2 4      /* __viaddmin_s16x2 */
+#define BWACUDA_OPR_VIMAX3_S16X2 5        /* __vimax3_s16x2 */
+#define BWACUDA_OPR_VIMAX3_U16X2 6        /* __vimax3_u16x2 */
+#define BWACUDA_OPR_VIMAX_S16X2_RELU 7    /* __vimax_s16x2_relu */
+#define BWACUDA_OPR_VIMAX3_S32 8          /* __vimax3_s32 */
+#define BWACUDA_OPR_PRMT 9                /* prmt.b32 byte permute */
+#define BWACUDA_OPR_C_ADD_MAX 10          /* max(a + b, c) written in C */
+#define BWACUDA_OPR_IMAD 11               /* a * b + c */
+#define BWACUDA_OPR_LOP3 12               /* (a & b) | c */
+#define BWACUDA_OPR_COUNT 13
+int bwacuda_measure_op_rate(bwacuda_ctx *ctx, int op, double *gops);
+
 /* ------------------------------------------------------------------------
  * Autotuner.  No counterpart in the reference (its NEON kernels have fixed
  * lane counts).  The launch shape of the batched extension path (threads per
