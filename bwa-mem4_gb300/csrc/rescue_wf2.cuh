@@ -93,11 +93,13 @@ struct Out2 {
 
 // One local-SW pass of both jobs of every group in the warp, in lockstep.  tlen[h] = 0 makes half
 // h inactive; tmap / te0 select the reverse pass's target mapping (rows <= te0 read reversed).
-// stop[h]: the half stops once its score reaches endsc[h].  Returns the results in every lane.
-template <int L, int C>
+// stop[h]: the half stops once its score reaches endsc[h].  REC: the group's last lane stores
+// every computed row's maximum key to rk[h][row] (the suboptimal-score scan reads them after the
+// pass).  Returns the results in every lane.
+template <int L, int C, bool REC>
 __device__ Out2 pass2(const Lane2<L, C> &W, const uint32_t *prof_s, uint32_t zw, const uint8_t *const t[2],
-                      const int tlen[2], int tmap, const int te0[2], const Scoring &sc, const int minsc[2],
-                      const int endsc[2], bool stop_enabled, wf::WfTracker *trk, bool &bad)
+                      const int tlen[2], int tmap, const int te0[2], const Scoring &sc, const int endsc[2],
+                      bool stop_enabled, uint16_t *const rk[2], bool &bad)
 {
     const int k = W.k;
     const uint32_t noe_del2 = (uint32_t)(-(sc.o_del + sc.e_del) & 0xffff) * 0x10001u;
@@ -113,13 +115,6 @@ __device__ Out2 pass2(const Lane2<L, C> &W, const uint32_t *prof_s, uint32_t zw,
     for (int o = 16; o > 0; o >>= 1) steps = max(steps, __shfl_xor_sync(0xffffffffu, steps, o));
 
     int gmax[2] = {0, 0}, te[2] = {-1, -1}, qe[2] = {-1, -1};
-    // a row maximum at or below thr[h] changes nothing: below the tracker's minsc and not a new best
-    int mm1[2], thr[2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        mm1[h] = minsc[h] > INT_MIN ? minsc[h] - 1 : INT_MIN;
-        thr[h] = mm1[h] < 0 ? mm1[h] : 0;  // min(minsc - 1, best so far = 0)
-    }
     bool done[2] = {tlen[0] <= 0, tlen[1] <= 0};
     uint32_t send_hf = 0u;   // bytes H_A, F_A, H_B, F_B of this lane's last column
     uint32_t send_key = 0u;
@@ -174,22 +169,18 @@ __device__ Out2 pass2(const Lane2<L, C> &W, const uint32_t *prof_s, uint32_t zw,
             send_hf = prmt(Hp[C - 1], f, 0x6240u);
             send_key = key;
             if (k == L - 1) {  // row i of both jobs is complete in this lane
-                const int ra = (int)((key >> 8) & 0xffu), rb = (int)(key >> 24);
-                if ((live_a && ra > thr[0]) || (live_b && rb > thr[1])) {
+                // predicated updates: the branch-free form keeps the warp's common path short
 #pragma unroll
-                    for (int hh = 0; hh < 2; ++hh) {
-                        if (!(hh == 0 ? live_a : live_b)) continue;
-                        const uint32_t kh = hh == 0 ? (key & 0xffffu) : (key >> 16);
-                        const int rmax = (int)(kh >> 8);
-                        if (trk) trk[hh].push(i, rmax, minsc[hh]);
-                        if (rmax > gmax[hh]) {
-                            gmax[hh] = rmax;
-                            te[hh] = i;
-                            qe[hh] = 255 - (int)(kh & 0xffu);
-                            thr[hh] = mm1[hh] < rmax ? mm1[hh] : rmax;
-                            if (gmax[hh] >= endsc[hh]) done[hh] = true;
-                        }
-                    }
+                for (int hh = 0; hh < 2; ++hh) {
+                    const bool live = hh == 0 ? live_a : live_b;
+                    const uint32_t kh = hh == 0 ? (key & 0xffffu) : (key >> 16);
+                    const int rmax = (int)(kh >> 8);
+                    const bool up = live && rmax > gmax[hh];  // first row reaching the maximum keeps te
+                    gmax[hh] = up ? rmax : gmax[hh];
+                    te[hh] = up ? i : te[hh];
+                    qe[hh] = up ? 255 - (int)(kh & 0xffu) : qe[hh];
+                    done[hh] = done[hh] || (up && rmax >= endsc[hh]);
+                    if (REC && live) rk[hh][i] = (uint16_t)kh;
                 }
             }
         }
@@ -209,6 +200,38 @@ __device__ Out2 pass2(const Lane2<L, C> &W, const uint32_t *prof_s, uint32_t zw,
         if (r.te[hh] < 0) r.qe[hh] = -1;
     }
     return r;
+}
+
+// bwa's second-best rule (the peak list of ksw_align2's tracker, as wf::WfTracker builds it) over
+// the row maxima a forward pass recorded: rows reaching minsc open a peak, the row right after a
+// peak's row replaces it only when strictly higher; the best peak lying more than
+// ceil(score / max_sc) rows from te wins, the earlier one on ties.  Peaks are judged as they
+// close, so no list is kept.  rk is 8-byte aligned; rows are read four at a time.
+__device__ inline void peaks_scan(const uint16_t *rk, int nrows, int minsc, int score, int te, int max_sc,
+                                  int &score2, int &te2)
+{
+    score2 = -1;
+    te2 = -1;
+    if (score <= 0) return;
+    const int hw = (score + max_sc - 1) / max_sc, lo = te - hw, hi = te + hw;
+    bool has = false;
+    int ls = 0, lr = 0;
+    const uint2 *p = reinterpret_cast<const uint2 *>(rk);
+    for (int r0 = 0; r0 < nrows; r0 += 4) {
+        const uint2 v4 = p[r0 >> 2];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int r = r0 + u;
+            const uint32_t w = u < 2 ? v4.x : v4.y;
+            const int v = (int)((w >> (16 * (u & 1) + 8)) & 0xffu);
+            if (r >= nrows || v < minsc) continue;
+            const bool cont = has && lr + 1 == r;
+            if (has && !cont && (lr < lo || lr > hi) && ls > score2) { score2 = ls; te2 = lr; }
+            if (!cont || ls < v) { ls = v; lr = r; }
+            has = true;
+        }
+    }
+    if (has && (lr < lo || lr > hi) && ls > score2) { score2 = ls; te2 = lr; }
 }
 
 // One group of L lanes per pair of jobs (positions 2p and 2p+1 of the launch); a half whose job
@@ -256,23 +279,33 @@ rescue_wf2_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_rescue_job 
         endsc[h] = mode == 2 ? J[h].endsc : 0x7fffffff;
     }
     bool bad = false;
-    wf::WfTracker trk[2];
+    // row-maximum keys, 2 bytes a row, in the job's tracker scratch (4 * tlen + 16 bytes)
+    uint16_t *rk[2];
 #pragma unroll
-    for (int h = 0; h < 2; ++h)
-        trk[h].init(act[h] ? scratch + scratch_off[jid[h]] : nullptr, act[h] ? (int)rescue_scratch_entries(J[h].tlen) : 0);
+    for (int h = 0; h < 2; ++h) rk[h] = reinterpret_cast<uint16_t *>(scratch + (act[h] ? scratch_off[jid[h]] : 0));
     const uint32_t zw = (uint32_t)npen & 0xffffu;  // patch word: bytes N penalty (16-bit), 0, 0
     load_query2<L, C>(W, q[0], qlen[0], qpad[0], q[1], qlen[1], qpad[1], false, 0, 0, sc.m, bad);
     const int te0z[2] = {0, 0};
-    const Out2 fw = pass2<L, C>(W, prof_s, zw, t, tlen, 0, te0z, sc, minsc, endsc, mode == 2, last ? trk : nullptr,
-                                bad);
+    const Out2 fw = pass2<L, C, true>(W, prof_s, zw, t, tlen, 0, te0z, sc, endsc, mode == 2, rk, bad);
+    __syncwarp();  // the last lane's key stores before the scans of lanes L - 1 (job A) and L - 2 (job B)
     int score2[2] = {-1, -1}, te2[2] = {-1, -1};
-    if (last) {
-#pragma unroll
-        for (int h = 0; h < 2; ++h)
-            if (act[h]) {
-                trk[h].finish(fw.score[h], fw.te[h], sc.max_sc, score2[h], te2[h]);
-                if (trk[h].overflow) atomicOr(err, ERR_SCRATCH);
-            }
+    {
+        // lane L - 1 scans job A, lane L - 2 job B (selects, not a dynamic index, keep this in registers)
+        const bool b = !last;
+        const bool a_h = b ? act[1] : act[0];
+        const int sc_h = b ? fw.score[1] : fw.score[0], te_h = b ? fw.te[1] : fw.te[0];
+        const int end_h = b ? endsc[1] : endsc[0];
+        int s2 = -1, t2 = -1;
+        if ((last || W.k == L - 2) && a_h) {
+            // a forward pass that stopped (mode 2, score reached endsc) recorded rows up to te
+            const int nrows = mode == 2 && sc_h >= end_h ? te_h + 1 : (b ? tlen[1] : tlen[0]);
+            peaks_scan(b ? rk[1] : rk[0], nrows, b ? minsc[1] : minsc[0], sc_h, te_h, sc.max_sc, s2, t2);
+        }
+        // job B's result to the last lane, which writes both
+        score2[0] = s2;
+        te2[0] = t2;
+        score2[1] = __shfl_sync(0xffffffffu, s2, L - 2, L);
+        te2[1] = __shfl_sync(0xffffffffu, t2, L - 2, L);
     }
     if (mode == 2) {
         if (last) {
@@ -300,9 +333,8 @@ rescue_wf2_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_rescue_job 
             te0[h] = fw.te[h];
             stopsc[h] = fw.score[h];
         }
-        int nomin[2] = {0x7fffffff, 0x7fffffff};
         load_query2<L, C>(W, q[0], rq[0], rqpad[0], q[1], rq[1], rqpad[1], true, fw.qe[0], fw.qe[1], sc.m, bad);
-        const Out2 rv = pass2<L, C>(W, prof_s, zw, t, rt, 1, te0, sc, nomin, stopsc, true, nullptr, bad);
+        const Out2 rv = pass2<L, C, false>(W, prof_s, zw, t, rt, 1, te0, sc, stopsc, true, rk, bad);
         if (last) {
 #pragma unroll
             for (int h = 0; h < 2; ++h)
