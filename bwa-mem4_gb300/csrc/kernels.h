@@ -96,10 +96,10 @@ struct RescueLaunch {
 // Whether a rescue job runs in the two-jobs-per-group wavefront of `cols` columns
 // (rescue_wf2.cuh): every value fits a byte (min(qlen, tlen) * max_sc <= 255) and the padded
 // query of both passes (bwa's width rule, or lanes_fixed; the reverse pass may pad to 16) fits
-// min(cols, 256) columns.
+// min(cols, 256) columns; the target has fewer than 2^20 rows (the kernel's row field).
 __host__ __device__ inline bool rescue_pair_job_ok(int qlen, int tlen, int max_sc, int lanes_fixed, int cols)
 {
-    if (qlen < 0 || tlen < 0 || max_sc < 1 || cols <= 0) return false;
+    if (qlen < 0 || tlen < 0 || tlen >= (1 << 20) || max_sc < 1 || cols <= 0) return false;
     const long long mn = qlen < tlen ? qlen : tlen;
     if (mn * max_sc > 255) return false;
     const int ln = lanes_fixed ? lanes_fixed : ((long long)qlen * max_sc < 250 ? 16 : 8);

@@ -12,16 +12,28 @@
 // of a job is 16 bits, (H << 8) | (255 - column): the largest H, and among equal H the smallest
 // column, as the reference's qe rule wants.
 //
-// Scores.  A target row's four scores for query codes 0..3 are one 32-bit profile word, so one
-// prmt picks (mat[tA][qA], mat[tB][qB]) sign-extended into the two lanes.  Query columns that
-// are N (code 4), ksw padding (score 0) or invalid (score 0, flagged) are patched by a second
-// prmt against a word holding the N penalty and zeros; this needs the N column of the matrix to
-// be one value (mat[t][4] equal for every t, as bwa's matrix has), which the host checks.
+// Scores.  Each lane holds, per column and job, the column's query-profile word: byte t is
+// mat[t][q_j] for target codes 0..3 (ksw's padding columns: 0; an N column: the N score).  One
+// prmt with a per-row selector picks (mat[tA][qA_j], mat[tB][qB_j]) sign-extended into the two
+// lanes.  A target N row (code 4) scores the N value on every real column, so the matrix's N row
+// and column must be one value (bwa's matrix is); such rows take a second prmt per column, on a
+// warp-uniform branch.
 //
-// Per column and row: two prmt for the scores, M0 = max(Hd + s, E, 0), H = max(M0, F), the key
-// prmt and half a 3-way key maximum, and two fused add-max each for E and F -- 9.5 instructions
-// for two cells.  M0 of the next column is computed before H of this one, so the previous
-// row's H is overwritten in place (no register copies per step).
+// Columns past the padded query do not exist for the job; they are computed with score -128.
+// Their H then never exceeds the row's largest real H (a diagonal step from a real cell loses
+// 128 >= o_del + e_del, at least the E step below that real cell loses; E and F only decay), and
+// their key's column byte is below every real column's, so they are never a row maximum.
+//
+// Per column and row: the score prmt, M0 = max(Hd + s, E, 0), H = max(M0, F), the key prmt and
+// half a 3-way key maximum, and E, F: with o_del + e_del == o_ins + e_ins both open from the
+// shared H - (o + e) (F opening from H equals F opening from M0 for o >= 0), 7.5 instructions
+// for two cells; otherwise F opens from M0 - (o_ins + e_ins), 8.5.  M0 of the next column is
+// computed before H of this one, so the previous row's H is overwritten in place.
+//
+// The group's last lane stores each row's two keys (2 bytes a job and row, in the job's tracker
+// scratch) and keeps max(rmax << 20 | (2^20 - 1 - row)) -- score and first row -- per job; after
+// the forward pass the suboptimal-score rule runs over the stored keys (peaks_scan), and qe is
+// read from the key of row te.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -29,12 +41,14 @@
 
 #include "common.cuh"
 #include "kernels.h"
-#include "rescue_wf.cuh"
 
 namespace bwacuda {
 namespace wf2 {
 
-constexpr uint32_t MIN2 = 0x80008000u;  // (-32768, -32768)
+constexpr uint32_t MIN2 = 0x80008000u;   // (-32768, -32768)
+constexpr uint32_t NOCOL = 0x80808080u;  // score -128 for every target code: a column past the query
+constexpr int ROW_BITS = 20;             // rows of a target (rescue_pair_job_ok keeps tlen below 2^20)
+constexpr uint32_t ROW_MASK = (1u << ROW_BITS) - 1u;
 
 __host__ __device__ inline int ceil_to(int x, int m) { return (x + m - 1) / m * m; }
 
@@ -45,45 +59,68 @@ __host__ __device__ inline bool job_ok(int qlen, int tlen, int max_sc, int lanes
 
 template <int L, int C>
 struct Lane2 {
-    int k;
-    uint32_t sel[C];          // prmt selectors: low half picks job A's byte from word A, high half job B's from word B
-    uint32_t sf[C];           // prmt selectors patching the score: keep it, the N penalty, or 0
-    uint32_t ks[C];           // row-key selectors: (H << 8) | column byte, or 0 for a column past the padded query
+    int k;                    // lane index within the group
+    uint32_t nf;              // 0 in the group's first lane, 1 elsewhere (zeroes the values it receives)
+    uint32_t qa[C], qb[C];    // query-profile words of jobs A and B
     uint32_t cw[(C + 3) / 4]; // key column bytes 255 - j, four columns a word
 };
 
+// Gap constants, each 16-bit value in both lanes.
+struct Gap2 {
+    uint32_t noe_del, noe_ins, ne_del, ne_ins;
+};
+
+__device__ __forceinline__ Gap2 gap2(const Scoring &sc)
+{
+    Gap2 g;
+    g.noe_del = (uint32_t)(-(sc.o_del + sc.e_del) & 0xffff) * 0x10001u;
+    g.noe_ins = (uint32_t)(-(sc.o_ins + sc.e_ins) & 0xffff) * 0x10001u;
+    g.ne_del = (uint32_t)(-sc.e_del & 0xffff) * 0x10001u;
+    g.ne_ins = (uint32_t)(-sc.e_ins & 0xffff) * 0x10001u;
+    return g;
+}
+
+// Query-profile words in shared memory: qp[q] for query codes 0..3 holds mat[t][q] in byte t,
+// qp[4] the N score in every byte, qp[5..7] 0 (codes the matrix does not have; flagged).
+__device__ __forceinline__ void build_qprof(uint32_t *qp, const Scoring &sc, int npen)
+{
+    const int q = threadIdx.x;
+    if (q < 4) {
+        uint32_t w = 0u;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) w |= ((sc.prof[t][0] >> (8 * q)) & 0xffu) << (8 * t);
+        qp[q] = w;
+    } else if (q < 8) {
+        qp[q] = q == 4 ? ((uint32_t)npen & 0xffu) * 0x01010101u : 0u;
+    }
+}
+
 // Loads the lane's columns of both jobs: forward (query[j]) or the reversed prefix
 // (query[qe0 - j]); columns [qlen, qpad) are ksw padding (score 0, part of the row maxima),
-// columns >= qpad do not exist: their cells are computed but their row keys are 0, so they are
-// never a row maximum (they lie right of every real column and feed no real cell).
+// columns >= qpad do not exist (score -128, never a row maximum).
 template <int L, int C>
-__device__ __forceinline__ void load_query2(Lane2<L, C> &W, const uint8_t *qa, int qla, int qpa, const uint8_t *qb,
-                                            int qlb, int qpb, bool rev, int qea, int qeb, int m, bool &bad)
+__device__ __forceinline__ void load_query2(Lane2<L, C> &W, const uint32_t *qp, const uint8_t *qa, int qla, int qpa,
+                                            const uint8_t *qb, int qlb, int qpb, bool rev, int qea, int qeb, int m,
+                                            bool &bad)
 {
 #pragma unroll
     for (int c = 0; c < C; ++c) {
         const int j = W.k * C + c;
-        const uint32_t b = 4u + (uint32_t)(c & 3);  // this column's byte of cw[c / 4] as a prmt source
-        // key bytes: the column byte, H; past the padded query two zero bytes (H's high bytes)
-        W.ks[c] = (j < qpa ? b : 0x11u) | (j < qpb ? ((b << 8) | 0x2000u) : 0x3300u);
         if ((c & 3) == 0) W.cw[c >> 2] = 0u;
         W.cw[c >> 2] |= ((uint32_t)(255 - j) & 0xffu) << (8 * (c & 3));
-        uint32_t ca = 7u, cb = 7u;
+        uint32_t wa = j < qpa ? 0u : NOCOL, wb = j < qpb ? 0u : NOCOL;
         if (j < qla) {
-            ca = rev ? qa[qea - j] : qa[j];
+            const uint32_t ca = rev ? qa[qea - j] : qa[j];
             bad |= ca >= (uint32_t)m;
-            ca = ca < (uint32_t)m ? ca : 7u;
+            wa = qp[ca & 7u];
         }
         if (j < qlb) {
-            cb = rev ? qb[qeb - j] : qb[j];
+            const uint32_t cb = rev ? qb[qeb - j] : qb[j];
             bad |= cb >= (uint32_t)m;
-            cb = cb < (uint32_t)m ? cb : 7u;
+            wb = qp[cb & 7u];
         }
-        const bool sa = ca >= 4u, sb = cb >= 4u;  // N, padding or invalid
-        const uint32_t ba = sa ? 0u : ca, bb = sb ? 4u : 4u + cb;
-        W.sel[c] = ba | ((ba | 8u) << 4) | (bb << 8) | ((bb | 8u) << 12);
-        // patch selectors over (score, Z): Z = (N penalty, 0) as bytes 4-7
-        W.sf[c] = (ca < 4u ? 0x10u : (ca == 4u ? 0x54u : 0x76u)) | (cb < 4u ? 0x3200u : (cb == 4u ? 0x5400u : 0x7600u));
+        W.qa[c] = wa;
+        W.qb[c] = wb;
     }
 }
 
@@ -91,21 +128,75 @@ struct Out2 {
     int score[2], te[2], qe[2];
 };
 
+// Score of column c for both jobs.  SLOW: some row of the warp is a target N (or a code outside
+// 0..3): selN keeps a job's profile score (0x10 / 0x3200) or takes its N-row score from nz, which
+// is the N value on real columns, 0 on padding and -128 past the padded query.
+template <bool SLOW>
+__device__ __forceinline__ uint32_t score2(uint32_t qa, uint32_t qb, uint32_t selT, int c, uint32_t selN, int ra,
+                                           int pa, int rb, int pb, uint32_t npa, uint32_t npb)
+{
+    const uint32_t s = prmt(qa, qb, selT);
+    if constexpr (!SLOW) {
+        return s;
+    } else {
+        const uint32_t za = c < ra ? npa : (c < pa ? 0u : 0xff80u);
+        const uint32_t zb = c < rb ? npb : (c < pb ? 0u : 0xff800000u);
+        return prmt(s, za | zb, selN);
+    }
+}
+
+// One row of the lane's C columns for both jobs.  hd: H of row i-1 at the column left of the
+// lane's first; f, key: F and the row key entering from the left; on return f, key leave to the
+// right and Hp holds row i.
+template <int C, bool SYM, bool SLOW>
+__device__ __forceinline__ void row2(const uint32_t (&qa)[C], const uint32_t (&qb)[C], const uint32_t *cw,
+                                     uint32_t (&Hp)[C], uint32_t (&E)[C], uint32_t &f, uint32_t &key, uint32_t hd,
+                                     uint32_t selT, const Gap2 &g, uint32_t selN, int ra, int pa, int rb, int pb,
+                                     uint32_t npa, uint32_t npb)
+{
+    uint32_t m0 =
+        __viaddmax_s16x2_relu(hd, score2<SLOW>(qa[0], qb[0], selT, 0, selN, ra, pa, rb, pb, npa, npb), E[0]);
+    uint32_t kprev = 0u;
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        // M0 of the next column first: it is the last reader of this column's previous-row H,
+        // which H of this row then replaces in the same register
+        uint32_t m0n = 0u;
+        if (c + 1 < C)
+            m0n = __viaddmax_s16x2_relu(
+                Hp[c], score2<SLOW>(qa[c + 1], qb[c + 1], selT, c + 1, selN, ra, pa, rb, pb, npa, npb), E[c + 1]);
+        const uint32_t h = __vimax_s16x2_relu(m0, f);  // H = max(M0, F)
+        // row-maximum key per job: (H << 8) | (255 - column); selector bytes: column, H_A, column, H_B
+        const uint32_t kk = prmt(h, cw[c >> 2], (uint32_t)((4 + (c & 3)) * 0x101 + 0x2000));
+        if (c & 1) key = __vimax3_u16x2(key, kprev, kk);
+        else kprev = kk;
+        if constexpr (SYM) {
+            const uint32_t t = __viaddmax_s16x2(h, g.noe_del, MIN2);  // H - (o + e), both gaps open from it
+            E[c] = __viaddmax_s16x2_relu(E[c], g.ne_del, t);
+            f = __viaddmax_s16x2_relu(f, g.ne_ins, t);
+        } else {
+            const uint32_t ti = __viaddmax_s16x2(m0, g.noe_ins, MIN2);  // F opens from M0
+            const uint32_t td = __viaddmax_s16x2(h, g.noe_del, MIN2);   // E opens from H
+            E[c] = __viaddmax_s16x2_relu(E[c], g.ne_del, td);
+            f = __viaddmax_s16x2_relu(f, g.ne_ins, ti);
+        }
+        Hp[c] = h;
+        m0 = m0n;
+    }
+    if (C & 1) key = __vimax3_u16x2(key, kprev, kprev);
+}
+
 // One local-SW pass of both jobs of every group in the warp, in lockstep.  tlen[h] = 0 makes half
-// h inactive; tmap / te0 select the reverse pass's target mapping (rows <= te0 read reversed).
-// stop[h]: the half stops once its score reaches endsc[h].  REC: the group's last lane stores
-// every computed row's maximum key to rk[h][row] (the suboptimal-score scan reads them after the
-// pass).  Returns the results in every lane.
-template <int L, int C, bool REC>
-__device__ Out2 pass2(const Lane2<L, C> &W, const uint32_t *prof_s, uint32_t zw, const uint8_t *const t[2],
-                      const int tlen[2], int tmap, const int te0[2], const Scoring &sc, const int endsc[2],
-                      bool stop_enabled, uint16_t *const rk[2], bool &bad)
+// h inactive.  TMAP: the reverse pass's target mapping (row r reads t[te0 - r] while r <= te0,
+// t[r] after).  stop: half h stops at its first row whose maximum reaches endsc[h] (at least 1).
+// The last lane stores every computed row's key to rk[h][row].  ql / qp: the pass's query length
+// and padded length per job.  Returns the results in every lane.
+template <int L, int C, bool SYM, bool TMAP>
+__device__ Out2 pass2(const Lane2<L, C> &W, const uint8_t *const t[2], const int tlen[2], const int te0[2],
+                      const Gap2 &g, int npen, int m, bool stop, const int endsc[2], uint16_t *const rk[2],
+                      const int ql[2], const int qp[2], bool &bad)
 {
     const int k = W.k;
-    const uint32_t noe_del2 = (uint32_t)(-(sc.o_del + sc.e_del) & 0xffff) * 0x10001u;
-    const uint32_t noe_ins2 = (uint32_t)(-(sc.o_ins + sc.e_ins) & 0xffff) * 0x10001u;
-    const uint32_t ne_del2 = (uint32_t)(-sc.e_del & 0xffff) * 0x10001u;
-    const uint32_t ne_ins2 = (uint32_t)(-sc.e_ins & 0xffff) * 0x10001u;
     uint32_t Hp[C], E[C];
 #pragma unroll
     for (int c = 0; c < C; ++c) { Hp[c] = 0u; E[c] = 0u; }
@@ -113,100 +204,98 @@ __device__ Out2 pass2(const Lane2<L, C> &W, const uint32_t *prof_s, uint32_t zw,
     int steps = tl_max > 0 ? tl_max + L - 1 : 0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) steps = max(steps, __shfl_xor_sync(0xffffffffu, steps, o));
+    // slow-row parameters: the lane's real / padded column counts per job, the N value per lane
+    const int ra = ql[0] - k * C, pa = qp[0] - k * C, rb = ql[1] - k * C, pb = qp[1] - k * C;
+    const uint32_t npa = (uint32_t)npen & 0xffffu, npb = (uint32_t)npen << 16;
+    const uint32_t thr = (uint32_t)(m < 4 ? m : 4);  // codes from thr on take the slow rows
+    const int end_a = endsc[0] > 1 ? endsc[0] : 1, end_b = endsc[1] > 1 ? endsc[1] : 1;
 
-    int gmax[2] = {0, 0}, te[2] = {-1, -1}, qe[2] = {-1, -1};
-    bool done[2] = {tlen[0] <= 0, tlen[1] <= 0};
-    uint32_t send_hf = 0u;   // bytes H_A, F_A, H_B, F_B of this lane's last column
-    uint32_t send_key = 0u;
-    uint32_t hprev_in = 0u;  // (H_A, H_B) of row i-1 at the column left of this lane's first
+    uint32_t ga = 0u, gb = 0u;  // (rmax << 20) | (2^20 - 1 - row), best so far
+    bool done_a = tlen[0] <= 0, done_b = tlen[1] <= 0;
+    uint32_t send_h = 0u, send_f = 0u, send_key = 0u;
+    uint32_t hprev = 0u;  // (H_A, H_B) of row i-1 at the column left of this lane's first
     uint32_t tn[2] = {0u, 0u};
     {
         const int i0 = -k;
 #pragma unroll
         for (int h = 0; h < 2; ++h)
-            if (i0 >= 0 && i0 < tlen[h]) tn[h] = (tmap && i0 <= te0[h]) ? t[h][te0[h] - i0] : t[h][i0];
+            if (i0 >= 0 && i0 < tlen[h]) tn[h] = (TMAP && i0 <= te0[h]) ? t[h][te0[h] - i0] : t[h][i0];
     }
     for (int s = 0; s < steps; ++s) {
-        const uint32_t rhf = __shfl_up_sync(0xffffffffu, send_hf, 1, L);
-        const uint32_t rkey = __shfl_up_sync(0xffffffffu, send_key, 1, L);
+        const uint32_t rh = __shfl_up_sync(0xffffffffu, send_h, 1, L) * W.nf;
+        uint32_t f = __shfl_up_sync(0xffffffffu, send_f, 1, L) * W.nf;
+        uint32_t key = __shfl_up_sync(0xffffffffu, send_key, 1, L) * W.nf;
         const int i = s - k;
         const uint32_t tca = tn[0], tcb = tn[1];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
+        {
             const int in = i + 1;
-            if (in >= 0 && in < tlen[h] && !done[h]) tn[h] = (tmap && in <= te0[h]) ? t[h][te0[h] - in] : t[h][in];
-        }
-        const uint32_t h_in = k == 0 ? 0u : prmt(rhf, 0u, 0x4240u);
-        uint32_t f = k == 0 ? 0u : prmt(rhf, 0u, 0x4341u);
-        uint32_t key = k == 0 ? 0u : rkey;
-        const bool live_a = !done[0] && i >= 0 && i < tlen[0];
-        const bool live_b = !done[1] && i >= 0 && i < tlen[1];
-        if (live_a || live_b) {
-            if (live_a) bad |= tca >= (uint32_t)sc.m;
-            if (live_b) bad |= tcb >= (uint32_t)sc.m;
-            const uint32_t wa = prof_s[2 * (tca & 7u)], wb = prof_s[2 * (tcb & 7u)];
-            uint32_t m0 = __viaddmax_s16x2_relu(hprev_in, prmt(prmt(wa, wb, W.sel[0]), zw, W.sf[0]), E[0]);
-            uint32_t kprev = 0u;
 #pragma unroll
-            for (int c = 0; c < C; ++c) {
-                // M0 of the next column first: it is the last reader of this column's previous-row H,
-                // which H of this row then replaces in the same register
-                uint32_t m0n = 0u;
-                if (c + 1 < C)
-                    m0n = __viaddmax_s16x2_relu(Hp[c], prmt(prmt(wa, wb, W.sel[c + 1]), zw, W.sf[c + 1]), E[c + 1]);
-                const uint32_t h = __vimax_s16x2_relu(m0, f);                 // H = max(M0, F)
-                const uint32_t ti = __viaddmax_s16x2(m0, noe_ins2, MIN2);     // M0 - oe_ins
-                // row-maximum key per job: (H << 8) | (255 - column), two columns per 3-way max
-                const uint32_t kk = prmt(h, W.cw[c >> 2], W.ks[c]);
-                if (c & 1) key = __vimax3_u16x2(key, kprev, kk);
-                else kprev = kk;
-                E[c] = __viaddmax_s16x2_relu(E[c], ne_del2, __viaddmax_s16x2(h, noe_del2, MIN2));  // E opens from H
-                f = __viaddmax_s16x2_relu(f, ne_ins2, ti);                    // F opens from M0
-                Hp[c] = h;
-                m0 = m0n;
+            for (int h = 0; h < 2; ++h)
+                if ((unsigned)in < (unsigned)tlen[h]) tn[h] = (TMAP && in <= te0[h]) ? t[h][te0[h] - in] : t[h][in];
+        }
+        const bool live_a = !done_a && (unsigned)i < (unsigned)tlen[0];
+        const bool live_b = !done_b && (unsigned)i < (unsigned)tlen[1];
+        // the vote runs in every lane of the warp, before the branch on this lane's rows
+        const bool any_slow = __any_sync(0xffffffffu, (live_a && tca >= thr) || (live_b && tcb >= thr));
+        if (live_a || live_b) {
+            const uint32_t ta = tca & 3u, tb = tcb & 3u;
+            // selector bytes: A's score and its sign from word A, B's score and its sign from word B
+            const uint32_t selT = ta * 0x11u + 0x80u + tb * 0x1100u + 0xC400u;
+            if (any_slow) {
+                if (live_a) bad |= tca >= (uint32_t)m;
+                if (live_b) bad |= tcb >= (uint32_t)m;
+                const uint32_t selN = (live_a && tca >= 4u ? 0x54u : 0x10u) | (live_b && tcb >= 4u ? 0x7600u : 0x3200u);
+                row2<C, SYM, true>(W.qa, W.qb, W.cw, Hp, E, f, key, hprev, selT, g, selN, ra, pa, rb, pb, npa, npb);
+            } else {
+                row2<C, SYM, false>(W.qa, W.qb, W.cw, Hp, E, f, key, hprev, selT, g, 0u, 0, 0, 0, 0, 0u, 0u);
             }
-            if (C & 1) key = __vimax3_u16x2(key, kprev, kprev);
-            send_hf = prmt(Hp[C - 1], f, 0x6240u);
+            send_h = Hp[C - 1];
+            send_f = f;
             send_key = key;
             if (k == L - 1) {  // row i of both jobs is complete in this lane
-                // predicated updates: the branch-free form keeps the warp's common path short
-#pragma unroll
-                for (int hh = 0; hh < 2; ++hh) {
-                    const bool live = hh == 0 ? live_a : live_b;
-                    const uint32_t kh = hh == 0 ? (key & 0xffffu) : (key >> 16);
-                    const int rmax = (int)(kh >> 8);
-                    const bool up = live && rmax > gmax[hh];  // first row reaching the maximum keeps te
-                    gmax[hh] = up ? rmax : gmax[hh];
-                    te[hh] = up ? i : te[hh];
-                    qe[hh] = up ? 255 - (int)(kh & 0xffu) : qe[hh];
-                    done[hh] = done[hh] || (up && rmax >= endsc[hh]);
-                    if (REC && live) rk[hh][i] = (uint16_t)kh;
+                const uint32_t rowinv = ROW_MASK - (uint32_t)i;
+                const uint32_t rma = (key >> 8) & 0xffu, rmb = key >> 24;
+                if (live_a) {
+                    ga = max(ga, (rma << ROW_BITS) | rowinv);
+                    rk[0][i] = (uint16_t)key;
+                }
+                if (live_b) {
+                    gb = max(gb, (rmb << ROW_BITS) | rowinv);
+                    rk[1][i] = (uint16_t)(key >> 16);
+                }
+                if (stop) {
+                    done_a = done_a || (live_a && (int)rma >= end_a);
+                    done_b = done_b || (live_b && (int)rmb >= end_b);
                 }
             }
         }
-        hprev_in = h_in;
-        if (stop_enabled) {  // warp-uniform early stop; the last lane tells its group
-            done[0] = __shfl_sync(0xffffffffu, done[0], L - 1, L);
-            done[1] = __shfl_sync(0xffffffffu, done[1], L - 1, L);
-            if (__all_sync(0xffffffffu, done[0] && done[1])) break;
+        hprev = rh;
+        if (stop) {  // warp-uniform early stop; the last lane tells its group
+            done_a = __shfl_sync(0xffffffffu, done_a, L - 1, L);
+            done_b = __shfl_sync(0xffffffffu, done_b, L - 1, L);
+            if (__all_sync(0xffffffffu, done_a && done_b)) break;
         }
     }
     Out2 r;
+    const uint32_t gg[2] = {ga, gb};
 #pragma unroll
     for (int hh = 0; hh < 2; ++hh) {
-        r.score[hh] = __shfl_sync(0xffffffffu, gmax[hh], L - 1, L);
-        r.te[hh] = __shfl_sync(0xffffffffu, te[hh], L - 1, L);
-        r.qe[hh] = __shfl_sync(0xffffffffu, qe[hh], L - 1, L);
-        if (r.te[hh] < 0) r.qe[hh] = -1;
+        const int sc = (int)(gg[hh] >> ROW_BITS);
+        const int te = sc > 0 ? (int)(ROW_MASK - (gg[hh] & ROW_MASK)) : -1;
+        // qe: the key column of row te (the last lane wrote it)
+        const int qe = (k == L - 1 && te >= 0) ? 255 - (int)(rk[hh][te] & 0xffu) : -1;
+        r.score[hh] = __shfl_sync(0xffffffffu, sc, L - 1, L);
+        r.te[hh] = __shfl_sync(0xffffffffu, te, L - 1, L);
+        r.qe[hh] = __shfl_sync(0xffffffffu, qe, L - 1, L);
     }
     return r;
 }
 
-// bwa's second-best rule (the peak list of ksw_align2's tracker, as wf::WfTracker builds it) over
-// the row maxima a forward pass recorded: rows reaching minsc open a peak, the row right after a
-// peak's row replaces it only when strictly higher; the best peak lying more than
-// ceil(score / max_sc) rows from te wins, the earlier one on ties.  Peaks are judged as they
-// close, so no list is kept.  rk is 8-byte aligned; rows are read four at a time.
+// bwa's second-best rule (the peak list of ksw_align2's tracker, as the 32-bit wavefront's
+// tracker builds it) over the row maxima a forward pass recorded: rows reaching minsc open a
+// peak, the row right after a peak's row replaces it only when strictly higher; the best peak
+// lying more than ceil(score / max_sc) rows from te wins, the earlier one on ties.  Peaks are
+// judged as they close, so no list is kept.  rk is 8-byte aligned; rows are read four at a time.
 __device__ inline void peaks_scan(const uint16_t *rk, int nrows, int minsc, int score, int te, int max_sc,
                                   int &score2, int &te2)
 {
@@ -236,20 +325,21 @@ __device__ inline void peaks_scan(const uint16_t *rk, int nrows, int minsc, int 
 
 // One group of L lanes per pair of jobs (positions 2p and 2p+1 of the launch); a half whose job
 // does not qualify (job_ok) stays idle and is left to the other rescue kernels.
-template <int L, int C>
-__global__ void __launch_bounds__(128)
+template <int L, int C, bool SYM>
+__global__ void __launch_bounds__(64)
 rescue_wf2_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_rescue_job *__restrict__ jobs,
                   const uint32_t *__restrict__ order, uint32_t n, const __grid_constant__ Scoring sc, int mode,
                   int lanes_fixed, int minsc_all, int npen, uint2 *__restrict__ scratch,
                   const uint64_t *__restrict__ scratch_off, bwacuda_rescue_result *__restrict__ out_aln,
                   bwacuda_fwd_result *__restrict__ out_fwd, uint32_t *__restrict__ err)
 {
-    __shared__ uint32_t prof_s[16];
-    if (threadIdx.x < 16) prof_s[threadIdx.x] = sc.prof[threadIdx.x >> 1][threadIdx.x & 1];
+    __shared__ uint32_t qp_s[8];
+    build_qprof(qp_s, sc, npen);
     __syncthreads();
     const uint32_t pair = (blockIdx.x * blockDim.x + threadIdx.x) / L;
     Lane2<L, C> W;
     W.k = threadIdx.x % L;
+    W.nf = W.k != 0 ? 1u : 0u;
     const bool last = W.k == L - 1;
     bool act[2];
     uint32_t jid[2] = {0u, 0u};
@@ -279,14 +369,14 @@ rescue_wf2_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_rescue_job 
         endsc[h] = mode == 2 ? J[h].endsc : 0x7fffffff;
     }
     bool bad = false;
+    const Gap2 g = gap2(sc);
     // row-maximum keys, 2 bytes a row, in the job's tracker scratch (4 * tlen + 16 bytes)
     uint16_t *rk[2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) rk[h] = reinterpret_cast<uint16_t *>(scratch + (act[h] ? scratch_off[jid[h]] : 0));
-    const uint32_t zw = (uint32_t)npen & 0xffffu;  // patch word: bytes N penalty (16-bit), 0, 0
-    load_query2<L, C>(W, q[0], qlen[0], qpad[0], q[1], qlen[1], qpad[1], false, 0, 0, sc.m, bad);
+    load_query2<L, C>(W, qp_s, q[0], qlen[0], qpad[0], q[1], qlen[1], qpad[1], false, 0, 0, sc.m, bad);
     const int te0z[2] = {0, 0};
-    const Out2 fw = pass2<L, C, true>(W, prof_s, zw, t, tlen, 0, te0z, sc, endsc, mode == 2, rk, bad);
+    const Out2 fw = pass2<L, C, SYM, false>(W, t, tlen, te0z, g, npen, sc.m, mode == 2, endsc, rk, qlen, qpad, bad);
     __syncwarp();  // the last lane's key stores before the scans of lanes L - 1 (job A) and L - 2 (job B)
     int score2[2] = {-1, -1}, te2[2] = {-1, -1};
     {
@@ -298,7 +388,7 @@ rescue_wf2_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_rescue_job 
         int s2 = -1, t2 = -1;
         if ((last || W.k == L - 2) && a_h) {
             // a forward pass that stopped (mode 2, score reached endsc) recorded rows up to te
-            const int nrows = mode == 2 && sc_h >= end_h ? te_h + 1 : (b ? tlen[1] : tlen[0]);
+            const int nrows = mode == 2 && sc_h >= (end_h > 1 ? end_h : 1) ? te_h + 1 : (b ? tlen[1] : tlen[0]);
             peaks_scan(b ? rk[1] : rk[0], nrows, b ? minsc[1] : minsc[0], sc_h, te_h, sc.max_sc, s2, t2);
         }
         // job B's result to the last lane, which writes both
@@ -333,8 +423,10 @@ rescue_wf2_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_rescue_job 
             te0[h] = fw.te[h];
             stopsc[h] = fw.score[h];
         }
-        load_query2<L, C>(W, q[0], rq[0], rqpad[0], q[1], rq[1], rqpad[1], true, fw.qe[0], fw.qe[1], sc.m, bad);
-        const Out2 rv = pass2<L, C, false>(W, prof_s, zw, t, rt, 1, te0, sc, stopsc, true, rk, bad);
+        load_query2<L, C>(W, qp_s, q[0], rq[0], rqpad[0], q[1], rq[1], rqpad[1], true, fw.qe[0], fw.qe[1], sc.m,
+                          bad);
+        __syncwarp();  // the scans' reads of the keys before the reverse pass rewrites them
+        const Out2 rv = pass2<L, C, SYM, true>(W, t, rt, te0, g, npen, sc.m, true, stopsc, rk, rq, rqpad, bad);
         if (last) {
 #pragma unroll
             for (int h = 0; h < 2; ++h)
@@ -353,20 +445,55 @@ rescue_wf2_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_rescue_job 
     if (bad) atomicOr(err, ERR_BASE);
 }
 
-template <int L, int C>
+template <int L, int C, bool SYM>
 cudaError_t launch_wf2(const RescueLaunch &Lr, int npen)
 {
-    // two-warp blocks: residency is register-bound (about 190 registers at 20 columns a lane), and
-    // small blocks let an SM hold every warp its register file fits
+    // two-warp blocks: residency is register-bound, and small blocks let an SM hold every warp its
+    // register file fits
     const uint32_t threads = 64;
     const uint64_t total = (uint64_t)((Lr.n + 1) / 2) * L;
     const uint32_t grid = (uint32_t)((total + threads - 1) / threads);
     if (grid == 0) return cudaSuccess;
-    rescue_wf2_kernel<L, C><<<grid, threads, 0, Lr.stream>>>(Lr.seq, Lr.jobs, Lr.order, (uint32_t)Lr.n, Lr.sc,
-                                                             Lr.mode, Lr.lanes, Lr.minsc, npen, Lr.scratch,
-                                                             Lr.scratch_off, Lr.out_aln, Lr.out_fwd, Lr.err);
+    rescue_wf2_kernel<L, C, SYM><<<grid, threads, 0, Lr.stream>>>(Lr.seq, Lr.jobs, Lr.order, (uint32_t)Lr.n, Lr.sc,
+                                                                  Lr.mode, Lr.lanes, Lr.minsc, npen, Lr.scratch,
+                                                                  Lr.scratch_off, Lr.out_aln, Lr.out_fwd, Lr.err);
     return cudaGetLastError();
 }
+
+// Column counts built per lane count (L * C covers queries padded to 256 columns).
+constexpr int C8[] = {4, 8, 12, 16, 20, 24, 32};
+constexpr int C16[] = {4, 6, 8, 10, 12, 16};
+
+template <bool SYM>
+cudaError_t launch_shape(const RescueLaunch &Lr, int lanes, int c, int npen)
+{
+    if (lanes == 16) {
+        switch (c) {
+        case 4: return launch_wf2<16, 4, SYM>(Lr, npen);
+        case 6: return launch_wf2<16, 6, SYM>(Lr, npen);
+        case 8: return launch_wf2<16, 8, SYM>(Lr, npen);
+        case 10: return launch_wf2<16, 10, SYM>(Lr, npen);
+        case 12: return launch_wf2<16, 12, SYM>(Lr, npen);
+        case 16: return launch_wf2<16, 16, SYM>(Lr, npen);
+        default: return cudaErrorInvalidValue;
+        }
+    }
+    switch (c) {
+    case 4: return launch_wf2<8, 4, SYM>(Lr, npen);
+    case 8: return launch_wf2<8, 8, SYM>(Lr, npen);
+    case 12: return launch_wf2<8, 12, SYM>(Lr, npen);
+    case 16: return launch_wf2<8, 16, SYM>(Lr, npen);
+    case 20: return launch_wf2<8, 20, SYM>(Lr, npen);
+    case 24: return launch_wf2<8, 24, SYM>(Lr, npen);
+    case 32: return launch_wf2<8, 32, SYM>(Lr, npen);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+// The launches of one gap class, each in its own translation unit (rescue_wf2.cu:
+// o_del + e_del == o_ins + e_ins; rescue_wf2a.cu: the rest).
+cudaError_t launch_sym(const RescueLaunch &Lr, int lanes, int c, int npen);
+cudaError_t launch_asym(const RescueLaunch &Lr, int lanes, int c, int npen);
 
 }  // namespace wf2
 }  // namespace bwacuda

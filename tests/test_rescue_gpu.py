@@ -221,19 +221,26 @@ def test_paired_wavefront_limits(ctx, lanes, scoring):
 
 
 def test_paired_wavefront_other_matrices(ctx):
-    # an N column of several values keeps every job in the 32-bit wavefront; an asymmetric 4x4 block
-    # with a constant N column runs paired
+    # an N column or N row of several values, or o_del + e_del above 128, keeps every job in the
+    # 32-bit wavefront; an asymmetric 4x4 block with a constant N row and column runs paired, and
+    # so do gap costs whose two opens differ (F then opens from M0, not from the shared H - o - e)
     js = _js(_pair_mix(7, 800))
     odd = oracle.scmat(1, 4).copy()
     odd[4] = -2  # mat[0][4]: the N column is no longer one value
+    odd_row = oracle.scmat(1, 4).copy()
+    odd_row[20 + 1] = -2  # mat[4][1]: the N row is no longer one value
     asym = oracle.scmat(1, 4).copy()
     asym[1], asym[5 + 2], asym[10 + 3] = -3, -2, -1  # mat[0][1], mat[1][2], mat[2][3]
     ctx.set_option(B.OPT_RESCUE_PAIR, 1)
     ctx.set_option(B.OPT_RESCUE_LANES, 8)
     try:
-        for mat in (odd, asym):
+        for mat in (odd, odd_row, asym):
             want, _ = oracle.align2_batch(js, mat, 6, 1, 6, 1, 19, 1)
             assert np.array_equal(ctx.ksw_align2_batch(js, mat, 6, 1, 6, 1, 19, 1), want)
+        mat = oracle.scmat(1, 4)
+        for gaps in ((5, 2, 4, 3), (6, 1, 4, 1), (4, 1, 6, 1), (0, 1, 0, 1), (127, 1, 6, 1), (128, 1, 6, 1)):
+            want, _ = oracle.align2_batch(js, mat, *gaps, 19, 1)
+            assert np.array_equal(ctx.ksw_align2_batch(js, mat, *gaps, 19, 1), want), gaps
     finally:
         ctx.set_option(B.OPT_RESCUE_PAIR, 0)
         ctx.set_option(B.OPT_RESCUE_LANES, 16)
