@@ -76,11 +76,15 @@ def parse():
     ap.add_argument("--window-jobs", type=int, default=1024 * 1024)
     ap.add_argument("--serve-rates", default="50,500,2000", help="Poisson arrival rates (requests/s)")
     ap.add_argument("--serve-requests", type=int, default=600, help="requests per arrival rate")
-    ap.add_argument("--case", choices=["ext-batched", "ext-plain", "ext-mixed", "ext-gather", "rescue", "global",
-                                       "windows", "retry", "op-rates"],
+    ap.add_argument("--case", choices=["ext-batched", "ext-plain", "ext-mixed", "ext-gather", "ext-long", "rescue",
+                                       "global", "windows", "retry", "serve", "op-rates"],
                     help="profiling case: run the small workload twice through one path, no timing")
     ap.add_argument("--lanes", type=int, default=8, help="rescue case: wavefront lanes per job")
     ap.add_argument("--pair", type=int, default=0, help="rescue case: two byte-range jobs per wavefront group")
+    ap.add_argument("--rescue-kernel", choices=["auto", "tpj"], default="auto",
+                    help="rescue case: the wavefronts where the jobs fit (auto) or thread-per-job for all")
+    ap.add_argument("--gaps", default="6,1,6,1", help="extension cases: o_del,e_del,o_ins,e_ins")
+    ap.add_argument("--ungapped", type=int, default=0, help="extension cases: the ungapped pre-pass on (1)")
     ap.add_argument("--h0-add", type=int, default=0,
                     help="extension cases: add this to every h0 (300 moves read pairs into the 16-bit cell class)")
     return ap.parse_args()
@@ -484,12 +488,9 @@ def other_configs(args, B, ctx, st, barrier, max_over_ranks, world, rank):
     return res
 
 
-def long_query_config(B, ctx, st, stream, timed, world, m=20000, seed=7000):
-    """ksw_extend2 on m queries of 2,000-10,000 bases (1% substitutions), tlen = qlen + 100,
-    w = 100, device-resident; plain path (the long queries go straight to the group-per-job
-    kernel) at 8, 16 and 32 lanes per job, and the batched path."""
-    import torch
-
+def long_query_jobs(B, m, seed):
+    """m extension jobs with queries of 2,000-10,000 bases (1% substitutions), tlen = qlen + 100,
+    w = 100, h0 20-60."""
     rng = np.random.default_rng(seed)
     ql = rng.integers(2000, 10001, m).astype(np.int32)
     tl = (ql + 100).astype(np.int32)
@@ -502,7 +503,16 @@ def long_query_config(B, ctx, st, stream, timed, world, m=20000, seed=7000):
         q_[mk] = (q_[mk] + 1) % 4
         seq[qo[k]:qo[k] + ql[k]] = q_
         seq[to[k]:to[k] + tl[k]] = t_
-    js = B.JobSet(seq, qo, to, ql, tl, rng.integers(20, 61, m).astype(np.int32), np.full(m, 100, np.int32))
+    return B.JobSet(seq, qo, to, ql, tl, rng.integers(20, 61, m).astype(np.int32), np.full(m, 100, np.int32))
+
+
+def long_query_config(B, ctx, st, stream, timed, world, m=20000, seed=7000):
+    """ksw_extend2 on m queries of 2,000-10,000 bases (1% substitutions), tlen = qlen + 100,
+    w = 100, device-resident; plain path (the long queries go straight to the group-per-job
+    kernel) at 8, 16 and 32 lanes per job, and the batched path."""
+    import torch
+
+    js = long_query_jobs(B, m, seed)
     d_seq = torch.from_numpy(js.seq).cuda()
     d_jobs = torch.from_numpy(js.dev_ext_jobs().view(np.uint8)).cuda()
     d_out = torch.zeros(m * 24, dtype=torch.uint8, device="cuda")
@@ -711,15 +721,21 @@ def run_case(args):
         print("alu_peak", round(ctx.measure_alu_peak(), 1))
         ctx.close()
         return
-    if args.case in ("ext-batched", "ext-plain", "ext-mixed"):
-        js = B.synth_ext(3 if args.case == "ext-mixed" else 2, args.jobs, seed=0)
+    if args.case in ("ext-batched", "ext-plain", "ext-mixed", "ext-long"):
+        if args.case == "ext-long":
+            js = long_query_jobs(B, args.jobs, seed=0)
+        else:
+            js = B.synth_ext(3 if args.case == "ext-mixed" else 2, args.jobs, seed=0)
         js.h0 = js.h0 + args.h0_add
+        od, ed, oi, ei = (int(x) for x in args.gaps.split(","))
+        sc = ctx.scoring(o_del=od, e_del=ed, o_ins=oi, e_ins=ei)
+        ctx.set_option(B.OPT_UNGAPPED, args.ungapped)
         d_seq = torch.from_numpy(js.seq).cuda()
         d_jobs = torch.from_numpy(js.dev_ext_jobs().view(np.uint8)).cuda()
         d_out = torch.zeros(len(js) * 24, dtype=torch.uint8, device="cuda")
         path = B.PATH_PLAIN if args.case == "ext-plain" else B.PATH_BATCHED
         for _ in range(2):
-            ctx.extend_device(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), d_out.data_ptr(), path=path)
+            ctx.extend_device(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), d_out.data_ptr(), sc=sc, path=path)
             ctx.sync()
     elif args.case == "ext-gather":
         # host buffers, batched path fed by the device gather (one chunk per call)
@@ -767,10 +783,25 @@ def run_case(args):
         for _ in range(2):
             ctx.extend_retry_device(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), d_out.data_ptr())
             ctx.sync()
+    elif args.case == "serve":
+        # the serving loop: mixed requests (extension and rescue jobs) from host buffers, the
+        # gather kernel packing each request's slices on the device
+        pools = ServePools(B, seed=0)
+        ctx.server_start(hbm_budget_bytes=1 << 30, max_waves=4)
+        try:
+            for t in serve_trace(1000.0, 8, seed=0):
+                _, cfg, es, ne, w, rs, nr = t
+                ne, nr = min(ne, args.jobs), min(nr, args.jobs)
+                ej = pools.ext[cfg].take(np.arange(es, es + ne))
+                rj = pools.res.take(np.arange(rs, rs + nr))
+                ctx.wait(ctx.submit_mixed(ej, rj, w=w, minsc=20))
+        finally:
+            ctx.server_stop()
     else:
         js = B.synth_rescue(args.jobs, seed=0)
         ctx.set_option(B.OPT_RESCUE_LANES, args.lanes)
         ctx.set_option(B.OPT_RESCUE_PAIR, args.pair)
+        ctx.set_option(B.OPT_RESCUE_KERNEL, B.RESCUE_TPJ if args.rescue_kernel == "tpj" else B.RESCUE_AUTO)
         d_seq = torch.from_numpy(js.seq).cuda()
         d_jobs = torch.from_numpy(js.dev_res_jobs().view(np.uint8)).cuda()
         d_out = torch.zeros(len(js) * 28, dtype=torch.uint8, device="cuda")

@@ -57,11 +57,14 @@ __host__ __device__ inline bool job_ok(int qlen, int tlen, int max_sc, int lanes
     return rescue_pair_job_ok(qlen, tlen, max_sc, lanes_fixed, cols);
 }
 
+constexpr int WF2_THREADS = 64;  // threads a block: two warps
+
 template <int L, int C>
 struct Lane2 {
     int k;                    // lane index within the group
     uint32_t nf;              // 0 in the group's first lane, 1 elsewhere (zeroes the values it receives)
-    uint32_t qa[C], qb[C];    // query-profile words of jobs A and B
+    uint2 *qw;                // the lane's query-profile words of jobs A and B in shared memory, column c
+                              // at qw[c * WF2_THREADS] (read once per row; registers hold the DP state)
     uint32_t cw[(C + 3) / 4]; // key column bytes 255 - j, four columns a word
 };
 
@@ -95,32 +98,29 @@ __device__ __forceinline__ void build_qprof(uint32_t *qp, const Scoring &sc, int
     }
 }
 
-// Loads the lane's columns of both jobs: forward (query[j]) or the reversed prefix
-// (query[qe0 - j]); columns [qlen, qpad) are ksw padding (score 0, part of the row maxima),
-// columns >= qpad do not exist (score -128, never a row maximum).
+// Loads the lane's columns of job h (0: A, the low 16-bit lanes; 1: B, the high ones): forward
+// (query[j]) or the reversed prefix (query[qe0 - j]); columns [qlen, qpad) are ksw padding
+// (score 0, part of the row maxima), columns >= qpad do not exist (score -128, never a row
+// maximum).  Job A's call also writes the key column bytes.
 template <int L, int C>
-__device__ __forceinline__ void load_query2(Lane2<L, C> &W, const uint32_t *qp, const uint8_t *qa, int qla, int qpa,
-                                            const uint8_t *qb, int qlb, int qpb, bool rev, int qea, int qeb, int m,
-                                            bool &bad)
+__device__ __forceinline__ void load_query2_half(Lane2<L, C> &W, const uint32_t *qp, const uint8_t *q, int ql, int qpd,
+                                                 bool rev, int qe0, int h, int m, bool &bad)
 {
 #pragma unroll
     for (int c = 0; c < C; ++c) {
         const int j = W.k * C + c;
-        if ((c & 3) == 0) W.cw[c >> 2] = 0u;
-        W.cw[c >> 2] |= ((uint32_t)(255 - j) & 0xffu) << (8 * (c & 3));
-        uint32_t wa = j < qpa ? 0u : NOCOL, wb = j < qpb ? 0u : NOCOL;
-        if (j < qla) {
-            const uint32_t ca = rev ? qa[qea - j] : qa[j];
-            bad |= ca >= (uint32_t)m;
-            wa = qp[ca & 7u];
+        if (h == 0) {
+            if ((c & 3) == 0) W.cw[c >> 2] = 0u;
+            W.cw[c >> 2] |= ((uint32_t)(255 - j) & 0xffu) << (8 * (c & 3));
         }
-        if (j < qlb) {
-            const uint32_t cb = rev ? qb[qeb - j] : qb[j];
-            bad |= cb >= (uint32_t)m;
-            wb = qp[cb & 7u];
+        uint32_t w = j < qpd ? 0u : NOCOL;
+        if (j < ql) {
+            const uint32_t code = rev ? q[qe0 - j] : q[j];
+            bad |= code >= (uint32_t)m;
+            w = qp[code & 7u];
         }
-        W.qa[c] = wa;
-        W.qb[c] = wb;
+        if (h == 0) W.qw[c * WF2_THREADS].x = w;
+        else W.qw[c * WF2_THREADS].y = w;
     }
 }
 
@@ -132,10 +132,10 @@ struct Out2 {
 // 0..3): selN keeps a job's profile score (0x10 / 0x3200) or takes its N-row score from nz, which
 // is the N value on real columns, 0 on padding and -128 past the padded query.
 template <bool SLOW>
-__device__ __forceinline__ uint32_t score2(uint32_t qa, uint32_t qb, uint32_t selT, int c, uint32_t selN, int ra,
-                                           int pa, int rb, int pb, uint32_t npa, uint32_t npb)
+__device__ __forceinline__ uint32_t score2(uint2 q, uint32_t selT, int c, uint32_t selN, int ra, int pa, int rb,
+                                           int pb, uint32_t npa, uint32_t npb)
 {
-    const uint32_t s = prmt(qa, qb, selT);
+    const uint32_t s = prmt(q.x, q.y, selT);
     if constexpr (!SLOW) {
         return s;
     } else {
@@ -149,13 +149,11 @@ __device__ __forceinline__ uint32_t score2(uint32_t qa, uint32_t qb, uint32_t se
 // lane's first; f, key: F and the row key entering from the left; on return f, key leave to the
 // right and Hp holds row i.
 template <int C, bool SYM, bool SLOW>
-__device__ __forceinline__ void row2(const uint32_t (&qa)[C], const uint32_t (&qb)[C], const uint32_t *cw,
-                                     uint32_t (&Hp)[C], uint32_t (&E)[C], uint32_t &f, uint32_t &key, uint32_t hd,
-                                     uint32_t selT, const Gap2 &g, uint32_t selN, int ra, int pa, int rb, int pb,
-                                     uint32_t npa, uint32_t npb)
+__device__ __forceinline__ void row2(const uint2 *qw, const uint32_t *cw, uint32_t (&Hp)[C], uint32_t (&E)[C],
+                                     uint32_t &f, uint32_t &key, uint32_t hd, uint32_t selT, const Gap2 &g,
+                                     uint32_t selN, int ra, int pa, int rb, int pb, uint32_t npa, uint32_t npb)
 {
-    uint32_t m0 =
-        __viaddmax_s16x2_relu(hd, score2<SLOW>(qa[0], qb[0], selT, 0, selN, ra, pa, rb, pb, npa, npb), E[0]);
+    uint32_t m0 = __viaddmax_s16x2_relu(hd, score2<SLOW>(qw[0], selT, 0, selN, ra, pa, rb, pb, npa, npb), E[0]);
     uint32_t kprev = 0u;
 #pragma unroll
     for (int c = 0; c < C; ++c) {
@@ -164,7 +162,7 @@ __device__ __forceinline__ void row2(const uint32_t (&qa)[C], const uint32_t (&q
         uint32_t m0n = 0u;
         if (c + 1 < C)
             m0n = __viaddmax_s16x2_relu(
-                Hp[c], score2<SLOW>(qa[c + 1], qb[c + 1], selT, c + 1, selN, ra, pa, rb, pb, npa, npb), E[c + 1]);
+                Hp[c], score2<SLOW>(qw[(c + 1) * WF2_THREADS], selT, c + 1, selN, ra, pa, rb, pb, npa, npb), E[c + 1]);
         const uint32_t h = __vimax_s16x2_relu(m0, f);  // H = max(M0, F)
         // row-maximum key per job: (H << 8) | (255 - column); selector bytes: column, H_A, column, H_B
         const uint32_t kk = prmt(h, cw[c >> 2], (uint32_t)((4 + (c & 3)) * 0x101 + 0x2000));
@@ -214,12 +212,16 @@ __device__ Out2 pass2(const Lane2<L, C> &W, const uint8_t *const t[2], const int
     bool done_a = tlen[0] <= 0, done_b = tlen[1] <= 0;
     uint32_t send_h = 0u, send_f = 0u, send_key = 0u;
     uint32_t hprev = 0u;  // (H_A, H_B) of row i-1 at the column left of this lane's first
-    uint32_t tn[2] = {0u, 0u};
+    // target codes of rows i + 1 and i + 2: each load is issued two rows before its use, so a
+    // miss on a new target sector has two steps of the warp's work to arrive
+    uint32_t tn[2] = {0u, 0u}, tn2[2] = {0u, 0u};
     {
-        const int i0 = -k;
 #pragma unroll
-        for (int h = 0; h < 2; ++h)
+        for (int h = 0; h < 2; ++h) {
+            const int i0 = -k, i1 = 1 - k;
             if (i0 >= 0 && i0 < tlen[h]) tn[h] = (TMAP && i0 <= te0[h]) ? t[h][te0[h] - i0] : t[h][i0];
+            if (i1 >= 0 && i1 < tlen[h]) tn2[h] = (TMAP && i1 <= te0[h]) ? t[h][te0[h] - i1] : t[h][i1];
+        }
     }
     for (int s = 0; s < steps; ++s) {
         const uint32_t rh = __shfl_up_sync(0xffffffffu, send_h, 1, L) * W.nf;
@@ -228,10 +230,12 @@ __device__ Out2 pass2(const Lane2<L, C> &W, const uint8_t *const t[2], const int
         const int i = s - k;
         const uint32_t tca = tn[0], tcb = tn[1];
         {
-            const int in = i + 1;
+            const int in = i + 2;
 #pragma unroll
-            for (int h = 0; h < 2; ++h)
-                if ((unsigned)in < (unsigned)tlen[h]) tn[h] = (TMAP && in <= te0[h]) ? t[h][te0[h] - in] : t[h][in];
+            for (int h = 0; h < 2; ++h) {
+                tn[h] = tn2[h];
+                if ((unsigned)in < (unsigned)tlen[h]) tn2[h] = (TMAP && in <= te0[h]) ? t[h][te0[h] - in] : t[h][in];
+            }
         }
         const bool live_a = !done_a && (unsigned)i < (unsigned)tlen[0];
         const bool live_b = !done_b && (unsigned)i < (unsigned)tlen[1];
@@ -245,9 +249,9 @@ __device__ Out2 pass2(const Lane2<L, C> &W, const uint8_t *const t[2], const int
                 if (live_a) bad |= tca >= (uint32_t)m;
                 if (live_b) bad |= tcb >= (uint32_t)m;
                 const uint32_t selN = (live_a && tca >= 4u ? 0x54u : 0x10u) | (live_b && tcb >= 4u ? 0x7600u : 0x3200u);
-                row2<C, SYM, true>(W.qa, W.qb, W.cw, Hp, E, f, key, hprev, selT, g, selN, ra, pa, rb, pb, npa, npb);
+                row2<C, SYM, true>(W.qw, W.cw, Hp, E, f, key, hprev, selT, g, selN, ra, pa, rb, pb, npa, npb);
             } else {
-                row2<C, SYM, false>(W.qa, W.qb, W.cw, Hp, E, f, key, hprev, selT, g, 0u, 0, 0, 0, 0, 0u, 0u);
+                row2<C, SYM, false>(W.qw, W.cw, Hp, E, f, key, hprev, selT, g, 0u, 0, 0, 0, 0, 0u, 0u);
             }
             send_h = Hp[C - 1];
             send_f = f;
@@ -323,10 +327,52 @@ __device__ inline void peaks_scan(const uint16_t *rk, int nrows, int minsc, int 
     if (has && (lr < lo || lr > hi) && ls > score2) { score2 = ls; te2 = lr; }
 }
 
+// One job's fields as a phase of the kernel uses them; inactive: an empty job.
+struct JobView {
+    const uint8_t *q, *t;
+    int qlen, tlen, qpad, minsc, endsc;
+    uint16_t *rk;  // row-maximum keys, 2 bytes a row, in the job's tracker scratch (4 * tlen + 16 bytes)
+};
+
+__device__ __forceinline__ JobView job_view(const volatile bwacuda_dev_rescue_job *jobs, uint32_t jid, bool act,
+                                            const uint8_t *seq, uint2 *scratch, const uint64_t *scratch_off, int mode,
+                                            int minsc_all, int lanes_fixed, int max_sc)
+{
+    JobView v;
+    uint64_t q_off = 0, t_off = 0, s_off = 0;
+    int qlen = 0, tlen = 0, jminsc = 0, jendsc = 0;
+    if (act) {
+        const volatile bwacuda_dev_rescue_job &J = jobs[jid];
+        q_off = J.q_off;
+        t_off = J.t_off;
+        qlen = J.qlen;
+        tlen = J.tlen;
+        jminsc = J.minsc;
+        jendsc = J.endsc;
+        s_off = scratch_off[jid];
+    }
+    v.q = seq + q_off;
+    v.t = seq + t_off;
+    v.qlen = qlen;
+    v.tlen = tlen;
+    const int ln = lanes_fixed ? lanes_fixed : (qlen * max_sc < 250 ? 16 : 8);
+    v.qpad = act ? ceil_to(qlen, ln) : 0;
+    v.minsc = mode == 2 ? jminsc : minsc_all;
+    v.endsc = mode == 2 ? jendsc : 0x7fffffff;
+    v.rk = reinterpret_cast<uint16_t *>(scratch + s_off);
+    return v;
+}
+
 // One group of L lanes per pair of jobs (positions 2p and 2p+1 of the launch); a half whose job
 // does not qualify (job_ok) stays idle and is left to the other rescue kernels.
+// Blocks per SM the register budget aims at (two warps a block): 8 (128 registers, four warps a
+// scheduler) up to 12 columns a lane, 6 (168 registers, three) up to 20, and no cap above, where
+// a cap would spill.
+template <int C>
+constexpr int wf2_min_blocks() { return C <= 12 ? 8 : (C <= 20 ? 6 : 1); }
+
 template <int L, int C, bool SYM>
-__global__ void __launch_bounds__(64)
+__global__ void __launch_bounds__(WF2_THREADS, wf2_min_blocks<C>())
 rescue_wf2_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_rescue_job *__restrict__ jobs,
                   const uint32_t *__restrict__ order, uint32_t n, const __grid_constant__ Scoring sc, int mode,
                   int lanes_fixed, int minsc_all, int npen, uint2 *__restrict__ scratch,
@@ -334,62 +380,67 @@ rescue_wf2_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_rescue_job 
                   bwacuda_fwd_result *__restrict__ out_fwd, uint32_t *__restrict__ err)
 {
     __shared__ uint32_t qp_s[8];
+    __shared__ uint2 qw_s[C * WF2_THREADS];
     build_qprof(qp_s, sc, npen);
     __syncthreads();
     const uint32_t pair = (blockIdx.x * blockDim.x + threadIdx.x) / L;
     Lane2<L, C> W;
     W.k = threadIdx.x % L;
+    W.qw = qw_s + threadIdx.x;
     W.nf = W.k != 0 ? 1u : 0u;
     const bool last = W.k == L - 1;
     bool act[2];
     uint32_t jid[2] = {0u, 0u};
-    bwacuda_dev_rescue_job J[2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         const uint32_t pos = 2 * pair + h;
         act[h] = pos < n;
-        J[h].q_off = 0; J[h].t_off = 0; J[h].qlen = 0; J[h].tlen = 0; J[h].minsc = 0; J[h].endsc = 0;
         if (act[h]) {
             jid[h] = order ? order[pos] : pos;
-            J[h] = jobs[jid[h]];
-            act[h] = job_ok(J[h].qlen, J[h].tlen, sc.max_sc, lanes_fixed, L * C);
+            const bwacuda_dev_rescue_job &J = jobs[jid[h]];
+            act[h] = job_ok(J.qlen, J.tlen, sc.max_sc, lanes_fixed, L * C);
         }
     }
-    const uint8_t *q[2], *t[2];
-    int qlen[2], tlen[2], qpad[2], minsc[2], endsc[2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        q[h] = seq + J[h].q_off;
-        t[h] = seq + J[h].t_off;
-        qlen[h] = act[h] ? J[h].qlen : 0;
-        tlen[h] = act[h] ? J[h].tlen : 0;
-        const int ln = lanes_fixed ? lanes_fixed : (J[h].qlen * sc.max_sc < 250 ? 16 : 8);
-        qpad[h] = act[h] ? ceil_to(J[h].qlen, ln) : 0;
-        minsc[h] = mode == 2 ? J[h].minsc : minsc_all;
-        endsc[h] = mode == 2 ? J[h].endsc : 0x7fffffff;
-    }
+    // The job records are read again for each phase (volatile reads, cached in L2) instead of
+    // being held in registers across the forward pass: the pass's register budget sets how many
+    // warps an SM holds.
+    const volatile bwacuda_dev_rescue_job *vjobs = jobs;
     bool bad = false;
     const Gap2 g = gap2(sc);
-    // row-maximum keys, 2 bytes a row, in the job's tracker scratch (4 * tlen + 16 bytes)
-    uint16_t *rk[2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) rk[h] = reinterpret_cast<uint16_t *>(scratch + (act[h] ? scratch_off[jid[h]] : 0));
-    load_query2<L, C>(W, qp_s, q[0], qlen[0], qpad[0], q[1], qlen[1], qpad[1], false, 0, 0, sc.m, bad);
-    const int te0z[2] = {0, 0};
-    const Out2 fw = pass2<L, C, SYM, false>(W, t, tlen, te0z, g, npen, sc.m, mode == 2, endsc, rk, qlen, qpad, bad);
-    __syncwarp();  // the last lane's key stores before the scans of lanes L - 1 (job A) and L - 2 (job B)
+    Out2 fw;
     int score2[2] = {-1, -1}, te2[2] = {-1, -1};
+    {
+        const uint8_t *t[2];
+        int qlen[2], tlen[2], qpad[2], endsc[2];
+        uint16_t *rk[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const JobView v = job_view(vjobs, jid[h], act[h], seq, scratch, scratch_off, mode, minsc_all, lanes_fixed,
+                                       sc.max_sc);
+            load_query2_half<L, C>(W, qp_s, v.q, v.qlen, v.qpad, false, 0, h, sc.m, bad);
+            t[h] = v.t;
+            qlen[h] = v.qlen;
+            tlen[h] = v.tlen;
+            qpad[h] = v.qpad;
+            endsc[h] = v.endsc;
+            rk[h] = v.rk;
+        }
+        const int te0z[2] = {0, 0};
+        fw = pass2<L, C, SYM, false>(W, t, tlen, te0z, g, npen, sc.m, mode == 2, endsc, rk, qlen, qpad, bad);
+    }
+    __syncwarp();  // the last lane's key stores before the scans of lanes L - 1 (job A) and L - 2 (job B)
     {
         // lane L - 1 scans job A, lane L - 2 job B (selects, not a dynamic index, keep this in registers)
         const bool b = !last;
         const bool a_h = b ? act[1] : act[0];
         const int sc_h = b ? fw.score[1] : fw.score[0], te_h = b ? fw.te[1] : fw.te[0];
-        const int end_h = b ? endsc[1] : endsc[0];
         int s2 = -1, t2 = -1;
         if ((last || W.k == L - 2) && a_h) {
+            const JobView v = job_view(vjobs, b ? jid[1] : jid[0], true, seq, scratch, scratch_off, mode, minsc_all,
+                                       lanes_fixed, sc.max_sc);
             // a forward pass that stopped (mode 2, score reached endsc) recorded rows up to te
-            const int nrows = mode == 2 && sc_h >= (end_h > 1 ? end_h : 1) ? te_h + 1 : (b ? tlen[1] : tlen[0]);
-            peaks_scan(b ? rk[1] : rk[0], nrows, b ? minsc[1] : minsc[0], sc_h, te_h, sc.max_sc, s2, t2);
+            const int nrows = mode == 2 && sc_h >= (v.endsc > 1 ? v.endsc : 1) ? te_h + 1 : v.tlen;
+            peaks_scan(v.rk, nrows, v.minsc, sc_h, te_h, sc.max_sc, s2, t2);
         }
         // job B's result to the last lane, which writes both
         score2[0] = s2;
@@ -409,23 +460,28 @@ rescue_wf2_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_rescue_job 
         }
     } else {
         bool rev[2];
+        const uint8_t *t[2];
         int rq[2], rqpad[2], rt[2], te0[2], stopsc[2];
+        uint16_t *rk[2];
+        __syncwarp();  // the scans' reads of the keys before the reverse pass rewrites them
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-            rev[h] = act[h] && fw.score[h] >= minsc[h] && fw.qe[h] >= 0 && fw.qe[h] < J[h].qlen;
+            const JobView v = job_view(vjobs, jid[h], act[h], seq, scratch, scratch_off, mode, minsc_all, lanes_fixed,
+                                       sc.max_sc);
+            rev[h] = act[h] && fw.score[h] >= v.minsc && fw.qe[h] >= 0 && fw.qe[h] < v.qlen;
             rq[h] = rev[h] ? fw.qe[h] + 1 : 0;
             // reverse-pass padding: batched_ksw_align2 recomputes the width from qe + 1, the
             // scalar form keeps the forward one
-            const int ln = lanes_fixed ? lanes_fixed : (J[h].qlen * sc.max_sc < 250 ? 16 : 8);
+            const int ln = lanes_fixed ? lanes_fixed : (v.qlen * sc.max_sc < 250 ? 16 : 8);
             const int rl = mode == 0 ? (rq[h] * sc.max_sc < 250 ? 16 : 8) : ln;
             rqpad[h] = rev[h] ? ceil_to(rq[h], rl) : 0;
-            rt[h] = rev[h] ? (mode == 0 ? fw.te[h] + 1 : J[h].tlen) : 0;
+            rt[h] = rev[h] ? (mode == 0 ? fw.te[h] + 1 : v.tlen) : 0;
             te0[h] = fw.te[h];
             stopsc[h] = fw.score[h];
+            t[h] = v.t;
+            rk[h] = v.rk;
+            load_query2_half<L, C>(W, qp_s, v.q, rq[h], rqpad[h], true, fw.qe[h], h, sc.m, bad);
         }
-        load_query2<L, C>(W, qp_s, q[0], rq[0], rqpad[0], q[1], rq[1], rqpad[1], true, fw.qe[0], fw.qe[1], sc.m,
-                          bad);
-        __syncwarp();  // the scans' reads of the keys before the reverse pass rewrites them
         const Out2 rv = pass2<L, C, SYM, true>(W, t, rt, te0, g, npen, sc.m, true, stopsc, rk, rq, rqpad, bad);
         if (last) {
 #pragma unroll
@@ -450,7 +506,7 @@ cudaError_t launch_wf2(const RescueLaunch &Lr, int npen)
 {
     // two-warp blocks: residency is register-bound, and small blocks let an SM hold every warp its
     // register file fits
-    const uint32_t threads = 64;
+    const uint32_t threads = WF2_THREADS;
     const uint64_t total = (uint64_t)((Lr.n + 1) / 2) * L;
     const uint32_t grid = (uint32_t)((total + threads - 1) / threads);
     if (grid == 0) return cudaSuccess;
