@@ -54,6 +54,12 @@ __device__ __forceinline__ uint32_t opaque(uint32_t k)
     return k;
 }
 
+// Pulls the 32-byte sector holding p into L2 (no register result, no wait).
+__device__ __forceinline__ void prefetch_l2(const void *p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // PTX prmt in its generic mode: a selector nibble with bit 3 set replicates the
 // sign of the selected byte (the __byte_perm intrinsic ignores that bit).
 __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel)

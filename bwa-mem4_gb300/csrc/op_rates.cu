@@ -16,8 +16,10 @@ namespace {
 constexpr int CHAINS = 8;
 constexpr int UNROLL = 16;
 
+// One operation of chain value a; nb is the neighbouring chain's value.  The two idempotent forms
+// (a max of two, an and-or) take nb as an operand so that no two steps of a chain fold into one.
 template <int OP>
-__device__ __forceinline__ uint32_t op(uint32_t a, uint32_t b, uint32_t c)
+__device__ __forceinline__ uint32_t op(uint32_t a, uint32_t nb, uint32_t b, uint32_t c)
 {
     if constexpr (OP == BWACUDA_OPR_VIADDMAX_S32) return (uint32_t)__viaddmax_s32((int)a, (int)b, (int)c);
     if constexpr (OP == BWACUDA_OPR_VIADDMAX_S32_RELU) return (uint32_t)__viaddmax_s32_relu((int)a, (int)b, (int)c);
@@ -26,7 +28,7 @@ __device__ __forceinline__ uint32_t op(uint32_t a, uint32_t b, uint32_t c)
     if constexpr (OP == BWACUDA_OPR_VIADDMIN_S16X2) return __viaddmin_s16x2(a, b, c);
     if constexpr (OP == BWACUDA_OPR_VIMAX3_S16X2) return __vimax3_s16x2(a, b, c);
     if constexpr (OP == BWACUDA_OPR_VIMAX3_U16X2) return __vimax3_u16x2(a, b, c);
-    if constexpr (OP == BWACUDA_OPR_VIMAX_S16X2_RELU) return __vimax_s16x2_relu(a, b);
+    if constexpr (OP == BWACUDA_OPR_VIMAX_S16X2_RELU) return __vimax_s16x2_relu(a, nb);
     if constexpr (OP == BWACUDA_OPR_VIMAX3_S32) return (uint32_t)__vimax3_s32((int)a, (int)b, (int)c);
     if constexpr (OP == BWACUDA_OPR_PRMT) return prmt(a, b, c);
     if constexpr (OP == BWACUDA_OPR_C_ADD_MAX) {
@@ -34,7 +36,8 @@ __device__ __forceinline__ uint32_t op(uint32_t a, uint32_t b, uint32_t c)
         return (uint32_t)(x > (int)c ? x : (int)c);
     }
     if constexpr (OP == BWACUDA_OPR_IMAD) return a * b + c;
-    if constexpr (OP == BWACUDA_OPR_LOP3) return (a & b) | c;
+    if constexpr (OP == BWACUDA_OPR_LOP3) return (a & b) | nb;
+    (void)nb;
     return a;
 }
 
@@ -48,7 +51,7 @@ __global__ void __launch_bounds__(256) op_rate_kernel(int iters, uint32_t b, uin
 #pragma unroll
         for (int u = 0; u < UNROLL; ++u) {
 #pragma unroll
-            for (int k = 0; k < CHAINS; ++k) a[k] = op<OP>(a[k], b, c);
+            for (int k = 0; k < CHAINS; ++k) a[k] = op<OP>(a[k], a[(k + 1) % CHAINS], b, c);
         }
     }
     uint32_t s = 0;

@@ -229,6 +229,13 @@ __device__ Out2 pass2(const Lane2<L, C> &W, const uint8_t *const t[2], const int
         uint32_t key = __shfl_up_sync(0xffffffffu, send_key, 1, L) * W.nf;
         const int i = s - k;
         const uint32_t tca = tn[0], tcb = tn[1];
+        if ((s & 15) == 0 && k == 0) {  // every 16 rows, the group's first lane pulls row i + 64 into L2
+            const int ip = i + 64;
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                if ((unsigned)ip < (unsigned)tlen[h])
+                    prefetch_l2(t[h] + ((TMAP && ip <= te0[h]) ? te0[h] - ip : ip));
+        }
         {
             const int in = i + 2;
 #pragma unroll
@@ -309,12 +316,24 @@ __device__ inline void peaks_scan(const uint16_t *rk, int nrows, int minsc, int 
     const int hw = (score + max_sc - 1) / max_sc, lo = te - hw, hi = te + hw;
     bool has = false;
     int ls = 0, lr = 0;
+    // words of four rows, four words in flight (the scan is one lane's serial walk: its loads,
+    // not its arithmetic, set its time); a word whose four maxima are all below minsc is skipped
     const uint2 *p = reinterpret_cast<const uint2 *>(rk);
-    for (int r0 = 0; r0 < nrows; r0 += 4) {
-        const uint2 v4 = p[r0 >> 2];
+    const int nw = (nrows + 3) >> 2;
+    const uint2 z = make_uint2(0u, 0u);
+    uint2 b0 = nw > 0 ? p[0] : z, b1 = nw > 1 ? p[1] : z, b2 = nw > 2 ? p[2] : z, b3 = nw > 3 ? p[3] : z;
+    const uint32_t kmin = (uint32_t)(minsc > 0 ? minsc : 0) << 8;
+    for (int wi = 0; wi < nw; ++wi) {
+        const uint2 v4 = b0;
+        b0 = b1;
+        b1 = b2;
+        b2 = b3;
+        b3 = wi + 4 < nw ? p[wi + 4] : z;
+        const uint32_t mx = __vimax3_u16x2(v4.x, v4.y, 0u);
+        if (max(mx & 0xffffu, mx >> 16) < kmin && minsc > 0) continue;
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            const int r = r0 + u;
+            const int r = 4 * wi + u;
             const uint32_t w = u < 2 ? v4.x : v4.y;
             const int v = (int)((w >> (16 * (u & 1) + 8)) & 0xffu);
             if (r >= nrows || v < minsc) continue;
@@ -366,10 +385,10 @@ __device__ __forceinline__ JobView job_view(const volatile bwacuda_dev_rescue_jo
 // One group of L lanes per pair of jobs (positions 2p and 2p+1 of the launch); a half whose job
 // does not qualify (job_ok) stays idle and is left to the other rescue kernels.
 // Blocks per SM the register budget aims at (two warps a block): 8 (128 registers, four warps a
-// scheduler) up to 12 columns a lane, 6 (168 registers, three) up to 20, and no cap above, where
+// scheduler) up to 12 columns a lane, 6 (168 registers, three) up to 24, and no cap above, where
 // a cap would spill.
 template <int C>
-constexpr int wf2_min_blocks() { return C <= 12 ? 8 : (C <= 20 ? 6 : 1); }
+constexpr int wf2_min_blocks() { return C <= 12 ? 8 : (C <= 24 ? 6 : 1); }
 
 template <int L, int C, bool SYM>
 __global__ void __launch_bounds__(WF2_THREADS, wf2_min_blocks<C>())
