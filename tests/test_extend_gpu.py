@@ -515,6 +515,39 @@ def test_ungapped_prefilter_on_reference_streams(ugctx):
                      ei, w, eb, zd, path=(B.PATH_BATCHED, B.GATHER_AUTO), what=f"gate {key}")
 
 
+def test_ungapped_prefilter_edges(ugctx):
+    # the fast path at its edges: queries of 1-300 bases, exact diagonals past 128 columns
+    # (settled), mismatches before and after column 127 (only the former can settle), N in
+    # either sequence, targets shorter than the query, h0 of 0 to 2, and batch sizes that end
+    # inside a warp
+    rng = np.random.default_rng(77)
+    qs, ts, h0s = [], [], []
+    for k in range(2500):
+        ql = int(rng.integers(1, 301))
+        t = rng.integers(0, 4, ql + int(rng.integers(0, 40))).astype(np.uint8)
+        q = t[:ql].copy()
+        kind = k % 7
+        if kind in (1, 2):  # 1-3 mismatches anywhere
+            for c in rng.integers(0, ql, int(rng.integers(1, 4))):
+                q[c] = (q[c] + 1) % 4
+        elif kind == 3 and ql > 130:  # one mismatch past column 127
+            c = int(rng.integers(128, ql))
+            q[c] = (q[c] + 1) % 4
+        elif kind == 4:  # an N in the query or the target's diagonal
+            c = int(rng.integers(0, ql))
+            if rng.random() < 0.5:
+                q[c] = 4
+            else:
+                t[c] = 4
+        elif kind == 5:  # target shorter than the query
+            t = t[:max(0, ql - int(rng.integers(1, 5)))]
+        qs.append(q)
+        ts.append(t)
+        h0s.append(int(rng.integers(0, 3)) if kind == 6 else int(rng.integers(1, 60)))
+    for n in (2500, 2497, 33, 1):
+        _check_batch(ugctx, qs[:n], ts[:n], h0s[:n], path=(B.PATH_BATCHED, B.GATHER_AUTO), what=f"ungapped edges {n}")
+
+
 @pytest.mark.parametrize("cfg,n", [(1, 20000), (2, 200000), (3, 60000)])
 def test_ungapped_prefilter_on_workloads(ugctx, cfg, n):
     js = B.synth_ext(cfg, n, seed=30 + cfg)
