@@ -535,6 +535,17 @@ def long_query_config(B, ctx, st, stream, timed, world, m=20000, seed=7000):
             "value": rows[best]["value"], "unit": "GCUPS", "best": best, "runs": rows}
 
 
+def alu_roofline(gcups, ops_per_cell, peak_g, lanes_per_op):
+    """The integer-ALU roofline of a DP path: achieved = GCUPS x the minimal fused operation count
+    of a cell; peak = the measured ALU instruction rate x the operations one instruction does at
+    the width the cells need (2 for 16-bit lanes: one DPX instruction updates two cells)."""
+    achieved = gcups * ops_per_cell
+    peak = peak_g * lanes_per_op
+    return {"bound": "alu", "ops_per_cell": ops_per_cell, "lanes_per_op": lanes_per_op,
+            "achieved": round(achieved, 1), "peak": round(peak, 1), "unit": "Gop/s",
+            "frac": round(achieved / peak, 4), "frac_32bit_lanes": round(achieved / peak_g, 4)}
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -1044,7 +1055,6 @@ def main():
     mhz = clocks["sm_mhz"] or pk.get("sm_max_mhz", 2070.0)
     peak_nominal = int_peak_gops(nsm, mhz)
     peak_g = ctx.measure_alu_peak()  # fused add-max instructions per second, measured on this GPU now
-    achieved = gcups_b / world * OPS_PER_CELL
     line = {
         "metric": METRIC, "value": round(gcups_b, 2), "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_b / args.steps, 3), "higher_is_better": True,
@@ -1061,17 +1071,17 @@ def main():
         "plain_equals_batched": same,
         "gpu_launches": int(launches),
         "clocks": clocks,
-        "roofline": {"bound": "alu", "achieved": round(achieved, 1), "peak": round(peak_g, 1), "unit": "Gop/s",
-                     "frac": round(achieved / peak_g, 4),
-                     "traffic": int(DRAM_BYTES_PER_JOB * n),
-                     "traffic_unit": "bytes per step (ncu capture of all bucket kernels, scaled by jobs)",
-                     "peak_nominal": round(peak_nominal, 1),
-                     "note": f"integer ops = GCUPS x {OPS_PER_CELL} ops/cell (minimal fused count) over the whole step "
-                             "(the persistent extension kernels hold ~95% of its device time); peak = "
-                             "bwacuda_measure_alu_peak (a chain-free __viaddmax_s32 loop on every SM, measured in this "
-                             f"run); peak_nominal = {nsm} SMs x 64 ALU lanes x median SM clock. The {kind} peaks file "
-                             "has HBM and bf16 figures only; this path touches ~0.05 B of HBM per cell and no tensor "
-                             "core"},
+        "roofline": dict(alu_roofline(gcups_b / world, OPS_PER_CELL, peak_g, 2),
+                         traffic=int(DRAM_BYTES_PER_JOB * n),
+                         traffic_unit="bytes per step (ncu capture of all bucket kernels, scaled by jobs)",
+                         peak_nominal=round(2 * peak_nominal, 1),
+                         note=f"integer ops = GCUPS x {OPS_PER_CELL} ops/cell (minimal fused count) over the whole step "
+                              "(the persistent extension kernels hold ~95% of its device time); the read-pair cells "
+                              "fit 16-bit lanes, where one DPX instruction does two operations, so peak = 2 x "
+                              "bwacuda_measure_alu_peak (a chain-free __viaddmax_s32 loop on every SM, measured in this "
+                              "run; frac_32bit_lanes divides by the single-lane peak instead); peak_nominal = 2 x "
+                              f"{nsm} SMs x 64 ALU lanes x median SM clock. The {kind} peaks file has HBM and bf16 "
+                              "figures only; this path touches ~0.05 B of HBM per cell and no tensor core"),
     }
     if e2e:
         line["e2e"] = e2e
@@ -1083,21 +1093,14 @@ def main():
         line["configs"] = other_configs(args, B, ctx, st, barrier, max_over_ranks, world, rank)
         # the rescue kernel against the same measured ALU peak, at the reference's minimal fused
         # count for a rescue cell (10: max(0, Hd + s), max3, E and F updates, max / argmax)
-        rsc = line["configs"].get("rescue")
-        if rsc:
-            rsc["roofline"] = {"bound": "alu", "ops_per_cell": RESCUE_OPS_PER_CELL,
-                               "achieved": round(rsc["value"] / world * RESCUE_OPS_PER_CELL, 1),
-                               "peak": round(peak_g, 1), "unit": "Gop/s",
-                               "frac": round(rsc["value"] / world * RESCUE_OPS_PER_CELL / peak_g, 4)}
-        for key, opc, note in (("cigar_stage", GLOBAL_OPS_PER_CELL, "the whole host-buffer stage (gather, DP, "
-                                "traceback, CIGAR compaction) over its wall time"),
-                               ("long_queries", OPS_PER_CELL, "the group-per-job kernel on the device")):
+        for key, opc, lanes, note in (
+                ("rescue", RESCUE_OPS_PER_CELL, 2, "byte-range scores: the paired kernel's 16-bit lanes"),
+                ("cigar_stage", GLOBAL_OPS_PER_CELL, 2, "the whole host-buffer stage (gather, DP, traceback, CIGAR "
+                 "compaction) over its wall time; 16-bit lanes (every job of the workload fits them)"),
+                ("long_queries", OPS_PER_CELL, 1, "the group-per-job kernel on the device, 32-bit cells")):
             cfg = line["configs"].get(key)
             if cfg:
-                cfg["roofline"] = {"bound": "alu", "ops_per_cell": opc,
-                                   "achieved": round(cfg["value"] / world * opc, 1), "peak": round(peak_g, 1),
-                                   "unit": "Gop/s", "frac": round(cfg["value"] / world * opc / peak_g, 4),
-                                   "note": note}
+                cfg["roofline"] = dict(alu_roofline(cfg["value"] / world, opc, peak_g, lanes), note=note)
     if not args.no_serve and world == 1:
         rates = [float(r) for r in args.serve_rates.split(",") if r]
         line["served"] = serve_bench(B, rates, args.serve_requests, tuning=ctx.tuning())

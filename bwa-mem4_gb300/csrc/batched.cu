@@ -257,7 +257,6 @@ static cudaError_t enqueue_batched(bwacuda_ctx *c, BatchBufs &bb, const uint8_t 
     L.seq = d_seq;
     L.jobs = d_jobs;
     L.order = static_cast<const uint32_t *>(bb.idx_out.p);
-    L.njobs = (uint32_t)n;
     L.P = P;
     L.out = d_out;
     L.err = err ? err : reinterpret_cast<uint32_t *>(c->d_misc.p);

@@ -44,16 +44,6 @@ constexpr uint32_t ERR_SCRATCH = 4u;   // tracker scratch overflow (never expect
 __host__ __device__ inline uint32_t prof_lo(const Scoring &s, int tc) { return s.prof[tc][0]; }
 __host__ __device__ inline uint32_t prof_hi(const Scoring &s, int tc) { return s.prof[tc][1]; }
 
-// A constant the compiler cannot see through (an empty asm rewrites it): x * opaque(k)
-// stays an integer multiply, which issues on the FMA pipe, where a known power of two would
-// become a shift on the ALU pipe -- the pipe the DP kernels are bound by.  Call it once,
-// outside the loops.
-__device__ __forceinline__ uint32_t opaque(uint32_t k)
-{
-    asm("" : "+r"(k));
-    return k;
-}
-
 // Pulls the 32-byte sector holding p into L2 (no register result, no wait).
 __device__ __forceinline__ void prefetch_l2(const void *p)
 {

@@ -407,9 +407,6 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
     const uint32_t ne_del2 = (uint32_t)(-e_del & 0xffff) * 0x10001u;
     const uint32_t ne_ins2 = (uint32_t)(-e_ins & 0xffff) * 0x10001u;
     const uint32_t fsel2 = 0x8000u | ((uint32_t)(-e_ins & 0xffff) << 16);
-    // multipliers for the FMA pipe: the zero-diagonal guard's hd << 7 and the second query
-    // half-word's selector (qv >> 16 as the high word of qv * 2^16)
-    const uint32_t k128 = opaque(128u), k64k = opaque(0x10000u);
     for (int i = 0; i < tlen; ++i) {
         uint32_t tc = ts.next();
         bad |= tc >= (uint32_t)m;
@@ -451,7 +448,7 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
                 // M = hd ? hd + s : 0, as min(hd + s, 128 hd): hd <= 255 and s >= -128, so
                 // the minimum is hd + s whenever hd >= 1 and <= 0 when hd == 0, and a
                 // non-positive M acts as 0 below (E, F >= 0)
-                const uint32_t M2 = __viaddmin_s16x2(hd2, s2, hd2 * k128);
+                const uint32_t M2 = __viaddmin_s16x2(hd2, s2, hd2 << 7);
                 const uint32_t ti2 = __viaddmax_s16x2_relu(M2, noe_ins2, 0u);  // max(M - oe_ins, 0)
                 const uint32_t td2 = SYM ? ti2 : __viaddmax_s16x2_relu(M2, noe_del2, 0u);  // max(M - oe_del, 0)
                 const uint32_t en2 = __viaddmax_s16x2(e2, ne_del2, td2);       // E(i+1, .)
@@ -474,7 +471,7 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
                     const uint32_t qv = qn;
                     qn = qw[((j >> 2) + 1) * TB];  // j + 4 <= qlen < qcap: inside the query words
                     const uint32_t h2a = pair(j, qv);
-                    const uint32_t h2b = pair(j + 2, __umulhi(qv, k64k));
+                    const uint32_t h2b = pair(j + 2, qv >> 16);
                     rowkey.quad(h2a, h2b, j);
                 }
             }
@@ -608,8 +605,6 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_i16p(uint2 *__restrict
     const uint32_t ne_del2 = (uint32_t)(-e_del & 0xffff) * 0x10001u;
     const uint32_t ne_ins2 = (uint32_t)(-e_ins & 0xffff) * 0x10001u;
     const uint32_t fsel2 = 0x8000u | ((uint32_t)(-e_ins & 0xffff) << 16);
-    // multipliers for the FMA pipe (the guard's 32767 * min(hd, 1), qv >> 16 as a high word)
-    const uint32_t k7fff = opaque(0x7fffu), k64k = opaque(0x10000u);
     for (int i = 0; i < tlen; ++i) {
         uint32_t tc = tnext;
         if (i + 1 < tlen) tnext = t[i + 1];
@@ -649,7 +644,7 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_i16p(uint2 *__restrict
                 const uint32_t hd2 = wv.x, e2 = wv.y;
                 // M = hd ? hd + s : 0, as min(hd + s, 32767 * min(hd, 1)): every path score
                 // is < 32768 here, and a non-positive M acts as 0 below (E, F >= 0)
-                const uint32_t g2 = __viaddmin_u16x2(hd2, 0u, 0x00010001u) * k7fff;
+                const uint32_t g2 = __viaddmin_u16x2(hd2, 0u, 0x00010001u) * 0x7fffu;
                 const uint32_t M2 = __viaddmin_s16x2(hd2, s2, g2);
                 const uint32_t ti2 = __viaddmax_s16x2_relu(M2, noe_ins2, 0u);
                 const uint32_t td2 = SYM ? ti2 : __viaddmax_s16x2_relu(M2, noe_del2, 0u);
@@ -671,7 +666,7 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_i16p(uint2 *__restrict
                     const uint32_t qv = qn;
                     qn = qw[((j >> 2) + 1) * TB];  // j + 4 <= qlen < qcap: inside the query words
                     pair(j, qv);
-                    pair(j + 2, __umulhi(qv, k64k));
+                    pair(j + 2, qv >> 16);
                 }
             }
             if (j + 1 < end) {

@@ -113,7 +113,9 @@ __device__ __forceinline__ uint32_t lower_bound16(const uint16_t *a, uint32_t n,
 }
 
 // Bucket b covers sorted keys [key_lo, key_hi]; writes its [start, end) and
-// clears its work counter.
+// clears its work counter.  This kernel is the only writer of the bounds, and a lower bound over
+// the n sorted keys lies in [0, n], so no persistent kernel reading them (in a stream launch or a
+// graph replay, whose capture is keyed on the same n) can index past the order and job arrays.
 __global__ void ext_bucket_bounds_kernel(const uint16_t *__restrict__ keys, uint32_t n,
                                          const ExtBucketDef *__restrict__ defs, int nb,
                                          uint32_t *__restrict__ table)

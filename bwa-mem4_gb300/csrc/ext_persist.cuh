@@ -21,7 +21,7 @@ template <class F, int TB, int GRAB>
 __global__ void __launch_bounds__(TB)
 ext_persist_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *__restrict__ jobs,
                    const uint32_t *__restrict__ order, uint32_t *__restrict__ table,
-                   const __grid_constant__ ExtParams P, int qcap, uint32_t njobs, bwacuda_ext_result *__restrict__ out,
+                   const __grid_constant__ ExtParams P, int qcap, bwacuda_ext_result *__restrict__ out,
                    uint32_t *__restrict__ err, unsigned long long *__restrict__ cells_total)
 {
     using CellT = typename F::T;
@@ -30,9 +30,7 @@ ext_persist_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *_
     const int tid = threadIdx.x, lane = tid & 31;
     CellT *cell = reinterpret_cast<CellT *>(smem_raw) + tid;
     uint32_t *qw = reinterpret_cast<uint32_t *>(reinterpret_cast<CellT *>(smem_raw) + (size_t)qcap * TB) + tid;
-    // the bucket bounds are device-written (ext_bucket_bounds_kernel); clamped to the launch's
-    // job count so no value of them can send a warp past the order and job arrays
-    const uint32_t stop = min(table[1], njobs), start = min(table[0], stop);
+    const uint32_t start = table[0], stop = table[1];
     uint32_t *counter = table + 2;
     unsigned long long ncells = 0;
     for (;;) {
@@ -45,10 +43,6 @@ ext_persist_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *_
         const uint32_t k = base + 32u * (uint32_t)g + lane;
         if (k < stop) {
             const uint32_t jid = order[k];
-            if (jid >= njobs) {
-                atomicOr(err, ERR_RANGE);
-                continue;
-            }
             const bwacuda_dev_ext_job J = jobs[jid];
             const bool fits = WIDE || ext_fits_i16(J.qlen, J.tlen, J.h0, P.sc.max_sc);
             if (J.qlen < 0 || J.qlen + 1 > qcap || !fits) {
@@ -73,9 +67,8 @@ template <int TB, int GRAB, bool W16>
 __global__ void __launch_bounds__(TB)
 ext_persist_pair_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *__restrict__ jobs,
                         const uint32_t *__restrict__ order, uint32_t *__restrict__ table,
-                        const __grid_constant__ ExtParams P, int qcap, uint32_t njobs,
-                        bwacuda_ext_result *__restrict__ out, uint32_t *__restrict__ err,
-                        unsigned long long *__restrict__ cells_total)
+                        const __grid_constant__ ExtParams P, int qcap, bwacuda_ext_result *__restrict__ out,
+                        uint32_t *__restrict__ err, unsigned long long *__restrict__ cells_total)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int tid = threadIdx.x, lane = tid & 31;
@@ -83,9 +76,7 @@ ext_persist_pair_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_j
     uint32_t *cellw = reinterpret_cast<uint32_t *>(smem_raw) + tid;
     uint2 *cell2 = reinterpret_cast<uint2 *>(smem_raw) + tid;
     uint32_t *qw = reinterpret_cast<uint32_t *>(smem_raw) + cpairs * (W16 ? 2 : 1) * TB + tid;
-    // the bucket bounds are device-written (ext_bucket_bounds_kernel); clamped to the launch's
-    // job count so no value of them can send a warp past the order and job arrays
-    const uint32_t stop = min(table[1], njobs), start = min(table[0], stop);
+    const uint32_t start = table[0], stop = table[1];
     uint32_t *counter = table + 2;
     const bool sym = P.sc.o_del + P.sc.e_del == P.sc.o_ins + P.sc.e_ins;
     unsigned long long ncells = 0;
@@ -99,10 +90,6 @@ ext_persist_pair_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_j
         const uint32_t k = base + 32u * (uint32_t)g + lane;
         if (k < stop) {
             const uint32_t jid = order[k];
-            if (jid >= njobs) {
-                atomicOr(err, ERR_RANGE);
-                continue;
-            }
             const bwacuda_dev_ext_job J = jobs[jid];
             const bool fits = W16 ? ext_fits_i16(J.qlen, J.tlen, J.h0, P.sc.max_sc)
                                   : ext_fits_u8(J.qlen, J.tlen, J.h0, P.sc.max_sc);
@@ -168,7 +155,7 @@ cudaError_t launch_persist_tb(const PersistLaunch &L, const ExtBucketDef &d, uin
     int per_sm = 0;
     if ((e = persist_blocks_per_sm(kern, TB, smem, L, per_sm)) != cudaSuccess) return e;
     const int grid = per_sm * nsm;
-    kern<<<grid, TB, smem, L.stream>>>(L.seq, L.jobs, L.order, table, L.P, d.qcap, L.njobs, L.out, L.err, L.cells);
+    kern<<<grid, TB, smem, L.stream>>>(L.seq, L.jobs, L.order, table, L.P, d.qcap, L.out, L.err, L.cells);
     return cudaGetLastError();
 }
 
@@ -189,8 +176,7 @@ cudaError_t launch_persist_pair_tb(const PersistLaunch &L, const ExtBucketDef &d
     if (e != cudaSuccess) return e;
     int per_sm = 0;
     if ((e = persist_blocks_per_sm(kern, TB, smem, L, per_sm)) != cudaSuccess) return e;
-    kern<<<per_sm * nsm, TB, smem, L.stream>>>(L.seq, L.jobs, L.order, table, L.P, d.qcap, L.njobs, L.out, L.err,
-                                               L.cells);
+    kern<<<per_sm * nsm, TB, smem, L.stream>>>(L.seq, L.jobs, L.order, table, L.P, d.qcap, L.out, L.err, L.cells);
     return cudaGetLastError();
 }
 

@@ -26,7 +26,6 @@ struct PersistLaunch {
     const uint8_t *seq;
     const bwacuda_dev_ext_job *jobs;
     const uint32_t *order;  // sorted job indices
-    uint32_t njobs;         // jobs of the launch sequence: bounds every sorted position and index
     ExtParams P;
     bwacuda_ext_result *out;
     uint32_t *err;

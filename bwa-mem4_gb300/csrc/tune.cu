@@ -139,8 +139,9 @@ extern "C" int bwacuda_autotune_extend(bwacuda_ctx *c, const uint8_t *d_seq, con
         P.zdrop = zdrop;
         P.ug = ungapped_rule(c, scp->m, scp->mat, scp->o_del, scp->e_del, scp->o_ins, scp->e_ins);
         const bwacuda_stats saved = c->stats;
+        // candidates run as the calls they tune do: replayed graphs when the context uses them
+        // (each shape is captured on its untimed first run), plain stream launches otherwise
         const bool graphs = c->use_graphs;
-        c->use_graphs = false;
         auto run = [&]() {
             return extend_device_batched(c, d_seq, static_cast<const bwacuda_dev_ext_job *>(jp), count, P,
                                          static_cast<bwacuda_ext_result *>(dout.p), s);

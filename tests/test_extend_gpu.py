@@ -518,8 +518,8 @@ def test_ungapped_prefilter_on_reference_streams(ugctx):
 def test_ungapped_prefilter_edges(ugctx):
     # the fast path at its edges: queries of 1-300 bases, exact diagonals past 128 columns
     # (settled), mismatches before and after column 127 (only the former can settle), N in
-    # either sequence, targets shorter than the query, h0 of 0 to 2, and batch sizes that end
-    # inside a warp
+    # either sequence, targets shorter than the query, h0 of 1 or 2 (runs that die on the first
+    # mismatch), and batch sizes that end inside a warp
     rng = np.random.default_rng(77)
     qs, ts, h0s = [], [], []
     for k in range(2500):
@@ -543,7 +543,7 @@ def test_ungapped_prefilter_edges(ugctx):
             t = t[:max(0, ql - int(rng.integers(1, 5)))]
         qs.append(q)
         ts.append(t)
-        h0s.append(int(rng.integers(0, 3)) if kind == 6 else int(rng.integers(1, 60)))
+        h0s.append(int(rng.integers(1, 3)) if kind == 6 else int(rng.integers(1, 60)))
     for n in (2500, 2497, 33, 1):
         _check_batch(ugctx, qs[:n], ts[:n], h0s[:n], path=(B.PATH_BATCHED, B.GATHER_AUTO), what=f"ungapped edges {n}")
 
