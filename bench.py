@@ -1084,6 +1084,21 @@ def main():
                               "figures only; this path touches ~0.05 B of HBM per cell and no tensor core"),
     }
     if e2e:
+        # the host link's roofline: the bytes a step moves over NVLink-C2C at the measured rates
+        # (device loads from host memory for the inputs, device stores for the results; the two
+        # directions overlap), for the full-DP call and for the production flow (ungapped on)
+        link = ctx.measure_host_link(1 << 30)
+        hb, db = e2e["h2d_bytes_per_step"], e2e["d2h_bytes_per_step"]
+        floor_ms = max(hb / (link["device_read_gbs"] * 1e6), db / (link["device_write_gbs"] * 1e6))
+        e2e["link_roofline"] = {
+            "bound": "host link", "unit": "GB/s", "measured": {k: round(v, 1) for k, v in link.items()},
+            "bytes_per_step": hb + db, "floor_ms": round(floor_ms, 2),
+            "achieved": round((hb + db) / (e2e["ms_per_step"] * 1e6), 1),
+            "frac_of_floor": round(floor_ms / e2e["ms_per_step"], 4),
+            "ungapped_route": {"ms_per_step": ug_route["ms_per_step"] if ug_route else None,
+                               "frac_of_floor": round(floor_ms / ug_route["ms_per_step"], 4) if ug_route else None},
+            "note": "bwacuda_measure_host_link over 1 GiB of pinned host memory in this run; floor = max(inputs / "
+                    "device read rate, results / device write rate)"}
         line["e2e"] = e2e
     if ug:
         line["ungapped_prefilter"] = ug

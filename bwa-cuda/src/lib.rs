@@ -293,6 +293,8 @@ pub mod ffi {
         pub fn bwacuda_reset_stats(ctx: *mut bwacuda_ctx) -> c_int;
         pub fn bwacuda_measure_alu_peak(ctx: *mut bwacuda_ctx, gops: *mut f64) -> c_int;
         pub fn bwacuda_measure_op_rate(ctx: *mut bwacuda_ctx, op: c_int, gops: *mut f64) -> c_int;
+        pub fn bwacuda_measure_host_link(ctx: *mut bwacuda_ctx, bytes: usize, read_gbs: *mut f64,
+                                         copy_gbs: *mut f64, write_gbs: *mut f64) -> c_int;
         pub fn bwacuda_get_tuning(ctx: *mut bwacuda_ctx, out: *mut bwacuda_tuning) -> c_int;
         pub fn bwacuda_autotune_extend(ctx: *mut bwacuda_ctx, d_seq: *const u8, d_jobs: *const bwacuda_dev_ext_job,
                                        n: usize, sc: *const bwacuda_scoring, end_bonus: c_int, zdrop: c_int,

@@ -88,7 +88,8 @@ EXPORTS = ("bwacuda_ctx_create", "bwacuda_ctx_destroy", "bwacuda_set_option", "b
            "bwacuda_server_stats", "bwacuda_measure_alu_peak", "bwacuda_get_tuning", "bwacuda_autotune_extend",
            "bwacuda_autotune_rescue", "bwacuda_ksw_global2_batch", "bwacuda_extend_batch_retry",
            "bwacuda_extend_retry_device", "bwacuda_ref_set", "bwacuda_mate_rescue_windows",
-           "bwacuda_server_submit_mixed", "bwacuda_server_cells", "bwacuda_measure_op_rate")
+           "bwacuda_server_submit_mixed", "bwacuda_server_cells", "bwacuda_measure_op_rate",
+           "bwacuda_measure_host_link")
 
 # bwacuda_measure_op_rate operations, in header order
 OP_RATE_NAMES = ("viaddmax_s32", "viaddmax_s32_relu", "viaddmax_s16x2", "viaddmax_s16x2_relu", "viaddmin_s16x2",
@@ -118,6 +119,8 @@ def lib():
     L.bwacuda_ctx_create.argtypes = [I, C.POINTER(vp)]
     L.bwacuda_measure_alu_peak.argtypes = [vp, C.POINTER(C.c_double)]
     L.bwacuda_measure_op_rate.argtypes = [vp, I, C.POINTER(C.c_double)]
+    L.bwacuda_measure_host_link.argtypes = [vp, C.c_size_t, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                            C.POINTER(C.c_double)]
     L.bwacuda_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.bwacuda_ksw_global2_batch.argtypes = [vp, vp, sz, I, vp, I, I, I, I, vp, vp, vp, sz]
     L.bwacuda_ref_set.argtypes = [vp, vp, C.c_int64, vp, vp, C.c_int32]
@@ -669,6 +672,14 @@ class Context:
             self._check(lib().bwacuda_measure_op_rate(self.h, k, C.byref(g)), "bwacuda_measure_op_rate")
             out[name] = g.value
         return out
+
+    def measure_host_link(self, nbytes: int = 1 << 30) -> dict:
+        """Measured host-link bandwidth (GB/s): device reads of pinned host memory, the copy
+        engine's host-to-device copy, device writes to pinned host memory."""
+        r, cp, w = C.c_double(), C.c_double(), C.c_double()
+        self._check(lib().bwacuda_measure_host_link(self.h, nbytes, C.byref(r), C.byref(cp), C.byref(w)),
+                    "bwacuda_measure_host_link")
+        return {"device_read_gbs": r.value, "copy_h2d_gbs": cp.value, "device_write_gbs": w.value}
 
     def measure_alu_peak(self) -> float:
         """Measured integer ALU-pipe rate of the device, 1e9 fused add-max ops per second."""

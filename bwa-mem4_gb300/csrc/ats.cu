@@ -68,9 +68,13 @@ __device__ __forceinline__ bool job_ok(const bwacuda_ext_job &J)
 // covering word outside the slice lie in the same page as bytes of the slice,
 // so the widened reads touch only mapped memory; in HBM they land in the
 // slice's own reserve.
+// The lengths kernel is the only reader of the caller's job array: it leaves each job's fields in
+// its device descriptor (the slice addresses, for now, in q_off / t_off; an invalid job empty)
+// for the gather, so the array crosses the host link once.
 __global__ void __launch_bounds__(ATS_THREADS) ats_lengths_kernel(const bwacuda_ext_job *__restrict__ hjobs,
                                                                   uint32_t n, BinRule br,
-                                   uint64_t *__restrict__ sizes, uint32_t *__restrict__ flags)
+                                   uint64_t *__restrict__ sizes, uint32_t *__restrict__ flags,
+                                   bwacuda_dev_ext_job *__restrict__ djobs)
 {
     uint32_t bad = 0, bins[3] = {0, 0, 0};
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
@@ -80,6 +84,14 @@ __global__ void __launch_bounds__(ATS_THREADS) ats_lengths_kernel(const bwacuda_
         if (ok) bins[bin_label(br, J.qlen, J.tlen, J.h0)]++;
         // reserve, in bytes (a multiple of 16, so every job's base stays aligned)
         sizes[k] = ok ? 16ull * (slice_words(J.query, J.qlen) + slice_words(J.target, J.tlen)) : 0u;
+        bwacuda_dev_ext_job D;
+        D.q_off = reinterpret_cast<uint64_t>(J.query);
+        D.t_off = reinterpret_cast<uint64_t>(J.target);
+        D.qlen = ok ? J.qlen : 0;
+        D.tlen = ok ? J.tlen : 0;
+        D.h0 = ok ? J.h0 : 1;
+        D.w = 0;
+        djobs[k] = D;
     }
     // every thread of the warp reaches this point
     bad = __reduce_or_sync(0xffffffffu, bad);
@@ -95,12 +107,11 @@ __global__ void __launch_bounds__(ATS_THREADS) ats_lengths_kernel(const bwacuda_
     }
 }
 
-// A warp takes 32 consecutive jobs: lane i loads job i's descriptor (one
-// coalesced read of the caller's array) and writes its device descriptor; then
-// the warp copies all 32 jobs' words as one flat list (warp_gather_slices).  An
-// invalid job becomes an empty one (qlen = tlen = 0, h0 = 1); the call then fails.
-__global__ void __launch_bounds__(ATS_THREADS, 8) ats_gather_kernel(const bwacuda_ext_job *__restrict__ hjobs,
-                                                                    uint32_t n, const uint64_t *__restrict__ offs,
+// A warp takes 32 consecutive jobs: lane i reads job i's fields from the descriptor the lengths
+// kernel left (HBM) and completes it with the job's offsets in the sequence buffer; then the warp
+// copies all 32 jobs' words as one flat list (warp_gather_slices).  An invalid job is an empty one
+// (qlen = tlen = 0, h0 = 1); the call then fails.
+__global__ void __launch_bounds__(ATS_THREADS, 8) ats_gather_kernel(uint32_t n, const uint64_t *__restrict__ offs,
                                                                     int w, uint8_t *__restrict__ seq,
                                                                     bwacuda_dev_ext_job *__restrict__ djobs)
 {
@@ -112,19 +123,14 @@ __global__ void __launch_bounds__(ATS_THREADS, 8) ats_gather_kernel(const bwacud
         uint64_t qa = 0, ta = 0, base = 0;
         uint32_t qw = 0, tw = 0;
         if (k < n) {
-            const bwacuda_ext_job J = hjobs[k];
-            const bool ok = job_ok(J);
+            bwacuda_dev_ext_job D = djobs[k];
             base = offs[k];
-            qa = reinterpret_cast<uint64_t>(J.query);
-            ta = reinterpret_cast<uint64_t>(J.target);
-            qw = ok ? slice_words(J.query, J.qlen) : 0u;
-            tw = ok ? slice_words(J.target, J.tlen) : 0u;
-            bwacuda_dev_ext_job D;
+            qa = D.q_off;  // the slice addresses, as the lengths kernel left them
+            ta = D.t_off;
+            qw = slice_words(reinterpret_cast<const uint8_t *>(qa), D.qlen);
+            tw = slice_words(reinterpret_cast<const uint8_t *>(ta), D.tlen);
             D.q_off = base + (qa & 15);
             D.t_off = base + 16ull * qw + (ta & 15);
-            D.qlen = ok ? J.qlen : 0;
-            D.tlen = ok ? J.tlen : 0;
-            D.h0 = ok ? J.h0 : 1;
             D.w = w;
             djobs[k] = D;
         }
@@ -245,7 +251,8 @@ cudaError_t ats_gather_chunk(bwacuda_ctx *c, AtsChunk &R, const bwacuda_ext_job 
     if ((e = cudaMemsetAsync(sizes + cn, 0, 8, g)) != cudaSuccess) return e;
     const uint32_t grid = (uint32_t)std::min<size_t>((cn + ATS_THREADS - 1) / ATS_THREADS,
                                                      (size_t)batched_nsm(c) * ATS_BLOCKS_PER_SM);
-    ats_lengths_kernel<<<grid, ATS_THREADS, 0, g>>>(hj, (uint32_t)cn, br, sizes, flags);
+    ats_lengths_kernel<<<grid, ATS_THREADS, 0, g>>>(hj, (uint32_t)cn, br, sizes, flags,
+                                                    static_cast<bwacuda_dev_ext_job *>(R.djobs.p));
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = cub::DeviceScan::ExclusiveSum(R.scan_tmp.p, scan_bytes, sizes, offs, (int)cn + 1, g)) != cudaSuccess)
         return e;
@@ -253,7 +260,7 @@ cudaError_t ats_gather_chunk(bwacuda_ctx *c, AtsChunk &R, const bwacuda_ext_job 
     if ((e = cudaStreamSynchronize(g)) != cudaSuccess) return e;
     const uint64_t total = *static_cast<const uint64_t *>(R.h_total.p);
     if ((e = R.seq.ensure(total + 16)) != cudaSuccess) return e;
-    ats_gather_kernel<<<grid, ATS_THREADS, 0, g>>>(hj, (uint32_t)cn, offs, w, static_cast<uint8_t *>(R.seq.p),
+    ats_gather_kernel<<<grid, ATS_THREADS, 0, g>>>((uint32_t)cn, offs, w, static_cast<uint8_t *>(R.seq.p),
                                                    static_cast<bwacuda_dev_ext_job *>(R.djobs.p));
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     return cudaEventRecord(R.gathered, g);
@@ -312,7 +319,8 @@ int ats_gather_ext(bwacuda_ctx *c, const bwacuda_ext_job *hj, size_t n, int w, D
     const int nsm = batched_nsm(c);
     const uint32_t grid = (uint32_t)std::min<size_t>((n + ATS_THREADS - 1) / ATS_THREADS, (size_t)nsm * 16);
     BinRule br{0, 0, 0};
-    ats_lengths_kernel<<<grid, ATS_THREADS, 0, s>>>(hj, (uint32_t)n, br, sizes, flags);
+    ats_lengths_kernel<<<grid, ATS_THREADS, 0, s>>>(hj, (uint32_t)n, br, sizes, flags,
+                                                    static_cast<bwacuda_dev_ext_job *>(djobs.p));
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
     if ((e = cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, sizes, offs, (int)n + 1, s)) != cudaSuccess)
         return cuda_status(e);
@@ -322,7 +330,7 @@ int ats_gather_ext(bwacuda_ctx *c, const bwacuda_ext_job *hj, size_t n, int w, D
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_status(e);
     if (static_cast<uint32_t>(h[1]) & ERR_INPUT) return BWACUDA_EINVAL;
     if ((e = seq.ensure(h[0] + 16)) != cudaSuccess) return cuda_status(e);
-    ats_gather_kernel<<<grid, ATS_THREADS, 0, s>>>(hj, (uint32_t)n, offs, w, static_cast<uint8_t *>(seq.p),
+    ats_gather_kernel<<<grid, ATS_THREADS, 0, s>>>((uint32_t)n, offs, w, static_cast<uint8_t *>(seq.p),
                                                    static_cast<bwacuda_dev_ext_job *>(djobs.p));
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
     c->stats.kernel_launches += 4;

@@ -99,7 +99,7 @@ struct bwacuda_ctx {
     int tune_candidates = 0;        // last autotune call
     double tuned_ext_gcups = 0.0;   // best candidates' rates on their samples
     double tuned_rescue_gcups = 0.0;
-    size_t chunk_jobs = 262144;
+    size_t chunk_jobs = 1048576;
     size_t dev_piece = size_t(1) << 30;  // jobs per launch sequence of a device-resident call
     int host_gather = BWACUDA_GATHER_AUTO;
     bool pageable_access = false;  // the device reads pageable host memory (host page tables)

@@ -100,9 +100,12 @@ typedef struct bwacuda_ctx bwacuda_ctx;
 #define BWACUDA_OPT_EXT_PATH 1
 #define BWACUDA_PATH_PLAIN 0   /* one launch per chunk, jobs in caller order */
 #define BWACUDA_PATH_BATCHED 1 /* length-bucketed, persistent, graph-replayed (default) */
-/* Jobs per device chunk (pipelining granularity of the host-buffer calls; default 262144).
- * Device-gather extension calls ramp up to it from 65536 jobs, doubling chunk by chunk;
- * bwacuda_ksw_global2_batch takes 4 x this many jobs per chunk, at most 1,048,576. */
+/* Jobs per device chunk (pipelining granularity of the host-buffer calls; default 1048576:
+ * smaller chunks cost each length bucket's tail once more per chunk, which dominates when most
+ * jobs are settled before the DP -- 23.1 against 16.1 ms per 8.4M read-pair jobs at 262144 with
+ * BWACUDA_OPT_UNGAPPED).  Device-gather extension calls ramp up to it from 65536 jobs, doubling
+ * chunk by chunk; bwacuda_ksw_global2_batch takes 4 x this many jobs per chunk, at most
+ * 1,048,576. */
 #define BWACUDA_OPT_CHUNK_JOBS 2
 /* Batched device calls: replay a captured CUDA graph (1, default) or enqueue every call (0). */
 #define BWACUDA_OPT_GRAPHS 3
@@ -422,6 +425,14 @@ int bwacuda_measure_alu_peak(bwacuda_ctx *ctx, double *gops);
 #define BWACUDA_OPR_LOP3 12               /* (a & b) | c */
 #define BWACUDA_OPR_COUNT 13
 int bwacuda_measure_op_rate(bwacuda_ctx *ctx, int op, double *gops);
+
+/* Host-link bandwidth in GB/s (1e9 bytes/s) over `bytes` (1 MiB .. 16 GiB) of pinned host memory:
+ * the device reading it with 16-byte loads (the device-gather route's access), the copy engine's
+ * host-to-device copy, and the device writing it (the host-buffer calls' result stores).  The
+ * bytes a host-buffer call moves over these rates bound its end-to-end time.  Allocates and frees
+ * its buffers. */
+int bwacuda_measure_host_link(bwacuda_ctx *ctx, size_t bytes, double *read_gbs, double *copy_gbs,
+                              double *write_gbs);
 
 /* ------------------------------------------------------------------------
  * Autotuner.  No counterpart in the reference (its NEON kernels have fixed

@@ -156,7 +156,7 @@ def test_chunked_pipeline_boundaries(ctx):
                 got = ctx.extend_batch(js.take(idx), w=int(wv))
                 assert np.array_equal(got, want[idx])
     finally:
-        ctx.set_option(B.OPT_CHUNK_JOBS, 262144)
+        ctx.set_option(B.OPT_CHUNK_JOBS, 1 << 20)
         ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_AUTO)
 
 
@@ -445,7 +445,7 @@ def test_invalid_job_in_a_later_chunk(ctx, path):
         got = ctx.extend_batch(js)
         assert np.array_equal(got, want)
     finally:
-        ctx.set_option(B.OPT_CHUNK_JOBS, 262144)
+        ctx.set_option(B.OPT_CHUNK_JOBS, 1 << 20)
         ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_AUTO)
 
 
@@ -470,7 +470,7 @@ def test_device_gather_equals_host_packing(ctx):
                 runs[(gather, chunk)] = (out, {k: st[k] for k in ("ext_jobs", "ext_cells", "ext_bin_u8",
                                                                   "ext_bin_i16", "ext_bin_i32")})
     finally:
-        ctx.set_option(B.OPT_CHUNK_JOBS, 262144)
+        ctx.set_option(B.OPT_CHUNK_JOBS, 1 << 20)
         ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_AUTO)
     want, _ = oracle.extend_batch(sub)
     for key, (out, st) in runs.items():

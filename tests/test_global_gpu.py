@@ -154,7 +154,7 @@ def test_many_chunks(gctx):
     try:
         _check(gctx, js)
     finally:
-        gctx.set_option(B.OPT_CHUNK_JOBS, 262144)
+        gctx.set_option(B.OPT_CHUNK_JOBS, 1 << 20)
 
 
 def test_short_buffer_reports_sizes(gctx):

@@ -20,3 +20,12 @@ def test_op_rates(ctx):
     assert all(v > 0 for v in rates.values())
     for name in ("viaddmax_s32", "viaddmax_s16x2", "viaddmax_s16x2_relu", "vimax3_s16x2", "vimax3_u16x2"):
         assert 0.8 * peak < rates[name] < 1.25 * peak, (name, rates[name], peak)
+
+
+def test_host_link(ctx):
+    # the link the host-buffer calls use: every rate positive and below a generous physical bound
+    r = ctx.measure_host_link(64 << 20)
+    assert set(r) == {"device_read_gbs", "copy_h2d_gbs", "device_write_gbs"}
+    assert all(0 < v < 2000 for v in r.values()), r
+    with pytest.raises(B.BwaCudaError):
+        ctx.measure_host_link(1000)  # below 1 MiB
