@@ -561,3 +561,28 @@ def test_ungapped_prefilter_on_workloads(ugctx, cfg, n):
         ugctx.reset_stats()
         ugctx.extend_batch(js, w=100) if len(np.unique(js.w)) == 1 else None
         assert ugctx.stats()["ext_cells"] < cells // 4
+
+
+@pytest.mark.parametrize("gather", [B.GATHER_DEVICE, B.GATHER_HOST])
+@pytest.mark.parametrize("offset", [0, 4, 8, 12])
+def test_output_array_alignment(ctx, gather, offset):
+    # the caller's result array at every 4-byte alignment, an odd job count, both host-buffer
+    # routes: nothing written outside the array
+    import ctypes as C
+
+    js = B.synth_ext(2, 70001, seed=81)
+    want, _ = oracle.extend_batch(js)
+    jobs = B.Context._host_jobs(js, B.EXT_JOB)
+    raw = np.zeros(len(js) * B.EXT_RES.itemsize + 64, np.uint8)
+    base = (-raw.ctypes.data) % 16 + offset
+    out = np.frombuffer(raw.data, dtype=B.EXT_RES, count=len(js), offset=base)
+    mat = oracle.scmat()
+    ctx.set_option(B.OPT_HOST_GATHER, gather)
+    try:
+        rc = B.lib().bwacuda_extend_batch(ctx.h, C.c_void_p(jobs.ctypes.data), len(js), 5, C.c_void_p(mat.ctypes.data),
+                                          6, 1, 6, 1, 100, 5, 100, C.c_void_p(out.ctypes.data))
+    finally:
+        ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_AUTO)
+    assert rc == B.OK
+    assert np.array_equal(out, want)
+    assert not raw[:base].any() and not raw[base + len(js) * B.EXT_RES.itemsize:].any()
