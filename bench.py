@@ -80,7 +80,8 @@ def parse():
                                        "global", "windows", "retry", "serve", "op-rates"],
                     help="profiling case: run the small workload twice through one path, no timing")
     ap.add_argument("--lanes", type=int, default=8, help="rescue case: wavefront lanes per job")
-    ap.add_argument("--pair", type=int, default=0, help="rescue case: two byte-range jobs per wavefront group")
+    ap.add_argument("--pair", type=int, default=0, choices=[0, 1, 4, 8, 16],
+                    help="rescue case: lanes of a group holding two byte-range jobs (0: one job per group)")
     ap.add_argument("--rescue-kernel", choices=["auto", "tpj"], default="auto",
                     help="rescue case: the wavefronts where the jobs fit (auto) or thread-per-job for all")
     ap.add_argument("--gaps", default="6,1,6,1", help="extension cases: o_del,e_del,o_ins,e_ins")

@@ -306,8 +306,8 @@ extern "C" int bwacuda_set_option(bwacuda_ctx *c, int option, int64_t value)
         c->rescue_lanes = (int)value;
         return BWACUDA_OK;
     case BWACUDA_OPT_RESCUE_PAIR:
-        if (value != 0 && value != 1) return BWACUDA_EINVAL;
-        c->rescue_pair = value != 0;
+        if (value != 0 && value != 1 && value != 4 && value != 8 && value != 16) return BWACUDA_EINVAL;
+        c->rescue_pair = value == 1 ? 4 : (int)value;
         return BWACUDA_OK;
     case BWACUDA_OPT_LONG_QLEN:
         if (value < 0 || value > (1 << 30)) return BWACUDA_EINVAL;
@@ -703,7 +703,7 @@ cudaError_t rescue_narrow_launch(bwacuda_ctx *c, const RescueLaunch &L)
         if (!c->rescue_pair) return rescue_wf_launch(L, L.qcap, c->rescue_lanes);
         // jobs whose values fit a byte: two per group; the rest in the 32-bit wavefront
         int cols = 0;
-        cudaError_t e = rescue_wf2_launch(L, L.qcap, c->rescue_lanes == 16 ? 16 : 8, &cols);
+        cudaError_t e = rescue_wf2_launch(L, L.qcap, c->rescue_pair, &cols);
         if (e != cudaSuccess) return e;
         RescueLaunch R = L;
         R.pair_cols = cols;

@@ -110,7 +110,7 @@ __host__ __device__ inline bool rescue_pair_job_ok(int qlen, int tlen, int max_s
 
 cudaError_t rescue_tpj_launch(const RescueLaunch &L, bool wide);
 cudaError_t rescue_wf_launch(const RescueLaunch &L, int qcap, int lanes);  // lanes per job: 8, 16 or 32
-// The paired wavefront (two jobs per group of 8 or 16 lanes) over the jobs rescue_pair_job_ok
+// The paired wavefront (two jobs per group of 4, 8 or 16 lanes) over the jobs rescue_pair_job_ok
 // admits at its column count; *cols receives that count (0: no launch, the matrix or the
 // queries do not suit it).
 cudaError_t rescue_wf2_launch(const RescueLaunch &L, int qcap, int lanes, int *cols);

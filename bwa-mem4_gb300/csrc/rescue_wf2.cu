@@ -1,5 +1,5 @@
 // rescue_wf2.cu -- launches of the paired register wavefront (rescue_wf2.cuh): two rescue jobs
-// per group of 8 or 16 lanes, one in each 16-bit lane of the registers.  This unit builds the
+// per group of 4, 8 or 16 lanes, one in each 16-bit lane of the registers.  This unit builds the
 // kernels of scorings whose gap opens agree (o_del + e_del == o_ins + e_ins, bwa's default);
 // rescue_wf2a.cu the others.
 #include "rescue_wf2.cuh"
@@ -56,8 +56,12 @@ cudaError_t rescue_wf2_launch(const RescueLaunch &Lr, int qcap, int lanes, int *
     int need = qcap - 16;
     if (need < 16) need = 16;
     if (need > 256) need = 256;
-    const int L = lanes == 16 ? 16 : 8;
-    const int c = L == 16 ? pick_c(wf2::C16, 16, need) : pick_c(wf2::C8, 8, need);
+    int L = lanes == 16 ? 16 : (lanes == 4 ? 4 : 8);
+    int c = L == 16 ? pick_c(wf2::C16, 16, need) : (L == 4 ? pick_c(wf2::C4, 4, need) : pick_c(wf2::C8, 8, need));
+    if (c == 0 && L == 4) {  // queries past 4-lane groups' columns: 8-lane groups
+        L = 8;
+        c = pick_c(wf2::C8, 8, need);
+    }
     if (c == 0) return cudaSuccess;
     *cols = L * c;
     const bool sym = Lr.sc.o_del + Lr.sc.e_del == Lr.sc.o_ins + Lr.sc.e_ins;

@@ -382,11 +382,12 @@ __device__ __forceinline__ JobView job_view(const volatile bwacuda_dev_rescue_jo
     return v;
 }
 
-// One group of L lanes per pair of jobs (positions 2p and 2p+1 of the launch); a half whose job
+// One group of L lanes (4, 8 or 16) per pair of jobs (positions 2p and 2p+1 of the launch); a half whose job
 // does not qualify (job_ok) stays idle and is left to the other rescue kernels.
 // Blocks per SM the register budget aims at (two warps a block): 8 (128 registers, four warps a
 // scheduler) up to 12 columns a lane, 6 (168 registers, three) up to 24, and no cap above, where
-// a cap would spill.
+// a cap would spill (40 columns a lane at 247 registers and two warps a scheduler: 2761 GCUPS on
+// the rescue windows, against 2316 capped at 168 with spills and 2564 for 20 columns at 168).
 template <int C>
 constexpr int wf2_min_blocks() { return C <= 12 ? 8 : (C <= 24 ? 6 : 1); }
 
@@ -535,13 +536,26 @@ cudaError_t launch_wf2(const RescueLaunch &Lr, int npen)
     return cudaGetLastError();
 }
 
-// Column counts built per lane count (L * C covers queries padded to 256 columns).
+// Column counts built per lane count (L * C covers queries padded to 256 columns; 4-lane
+// groups to 192: their 48 columns a lane already hold every register).
+constexpr int C4[] = {8, 16, 24, 32, 40, 48};
 constexpr int C8[] = {4, 8, 12, 16, 20, 24, 32};
 constexpr int C16[] = {4, 6, 8, 10, 12, 16};
 
 template <bool SYM>
 cudaError_t launch_shape(const RescueLaunch &Lr, int lanes, int c, int npen)
 {
+    if (lanes == 4) {
+        switch (c) {
+        case 8: return launch_wf2<4, 8, SYM>(Lr, npen);
+        case 16: return launch_wf2<4, 16, SYM>(Lr, npen);
+        case 24: return launch_wf2<4, 24, SYM>(Lr, npen);
+        case 32: return launch_wf2<4, 32, SYM>(Lr, npen);
+        case 40: return launch_wf2<4, 40, SYM>(Lr, npen);
+        case 48: return launch_wf2<4, 48, SYM>(Lr, npen);
+        default: return cudaErrorInvalidValue;
+        }
+    }
     if (lanes == 16) {
         switch (c) {
         case 4: return launch_wf2<16, 4, SYM>(Lr, npen);

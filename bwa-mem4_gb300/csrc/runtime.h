@@ -93,7 +93,7 @@ struct bwacuda_ctx {
     bool use_graphs = true;
     int rescue_kernel = BWACUDA_RESCUE_AUTO;
     int rescue_lanes = 16;  // lanes per job of the register wavefront (8, 16, 32)
-    bool rescue_pair = false;  // two byte-range jobs per wavefront group (rescue_wf2.cuh)
+    int rescue_pair = 0;  // lanes of a group holding two byte-range jobs (rescue_wf2.cuh): 4, 8, 16; 0 off
     bool ungapped = false;  // ungapped-diagonal fast path on the batched extension path
     int long_lanes = 16;    // lanes per job of the group-per-job extension kernel (8, 16, 32)
     int tune_candidates = 0;        // last autotune call

@@ -108,7 +108,7 @@ extern "C" int bwacuda_get_tuning(bwacuda_ctx *c, bwacuda_tuning *out)
     const int lq = batched_get_long(c);
     out->long_qlen = lq == INT_MAX ? 0 : lq;
     out->long_lanes = c->long_lanes;
-    out->rescue_pair = c->rescue_pair ? 1 : 0;
+    out->rescue_pair = c->rescue_pair;
     out->reserved = 0;
     return BWACUDA_OK;
 }
@@ -275,7 +275,7 @@ extern "C" int bwacuda_autotune_rescue(bwacuda_ctx *c, const uint8_t *d_seq, con
         if (e != cudaSuccess) { tmp.release(); dout.release(); dcells.release(); return cuda_status(e); }
         const bwacuda_stats saved = c->stats;
         const int kern0 = c->rescue_kernel, lanes0 = c->rescue_lanes;
-        const bool pair0 = c->rescue_pair;
+        const int pair0 = c->rescue_pair;
         auto run = [&]() {
             return ksw_align2_device_locked(c, d_seq, static_cast<const bwacuda_dev_rescue_job *>(jp), count, scp,
                                             minsc, max_sc, 0, 0, static_cast<bwacuda_rescue_result *>(dout.p), s);
@@ -284,9 +284,11 @@ extern "C" int bwacuda_autotune_rescue(bwacuda_ctx *c, const uint8_t *d_seq, con
         uint64_t dummy = 0;
         int rc = run();
         if (!rc) rc = collect_device_status(c, s, &dummy);
-        struct Cand { int kernel, lanes; bool pair; } cands[] = {
-            {BWACUDA_RESCUE_AUTO, 8, false}, {BWACUDA_RESCUE_AUTO, 16, false}, {BWACUDA_RESCUE_AUTO, 32, false},
-            {BWACUDA_RESCUE_TPJ, 16, false}, {BWACUDA_RESCUE_AUTO, 8, true}, {BWACUDA_RESCUE_AUTO, 16, true}};
+        // the paired candidates keep the 32-bit wavefront at 8 lanes for the jobs they leave
+        struct Cand { int kernel, lanes, pair; } cands[] = {
+            {BWACUDA_RESCUE_AUTO, 8, 0}, {BWACUDA_RESCUE_AUTO, 16, 0}, {BWACUDA_RESCUE_AUTO, 32, 0},
+            {BWACUDA_RESCUE_TPJ, 16, 0}, {BWACUDA_RESCUE_AUTO, 8, 4}, {BWACUDA_RESCUE_AUTO, 8, 8},
+            {BWACUDA_RESCUE_AUTO, 8, 16}};
         double best_ms = 0;
         Cand best = {kern0, lanes0, pair0};
         int ncand = 0;

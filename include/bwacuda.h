@@ -152,11 +152,11 @@ typedef struct bwacuda_ctx bwacuda_ctx;
 #define BWACUDA_OPT_LONG_QLEN 12
 /* Lanes per job of the group-per-job extension kernel: 8, 16 (default) or 32. */
 #define BWACUDA_OPT_LONG_LANES 13
-/* Mate rescue, register wavefront: 1 = jobs whose every value fits a byte
+/* Mate rescue, register wavefront: 4, 8 or 16 = jobs whose every value fits a byte
  * (min(qlen, tlen) * max_sc <= 255, padded query <= 256 columns, bwa-shaped matrix) run two
- * per group of 8 or 16 lanes, one in each 16-bit lane of the DPX instructions; the others
- * stay in the 32-bit wavefront.  0 (default before tuning) = one job per group.  Results never
- * depend on it. */
+ * per group of that many lanes, one in each 16-bit lane of the DPX instructions (4 lanes: the
+ * most columns per lane); the others stay in the 32-bit wavefront.  1 = 4.  0 (default before
+ * tuning) = one job per group.  Results never depend on it. */
 #define BWACUDA_OPT_RESCUE_PAIR 14
 
 int bwacuda_ctx_create(int device, bwacuda_ctx **out);
@@ -454,7 +454,8 @@ typedef struct {
     int32_t long_qlen;      /* batched extension: buckets from this query length up use the group-per-job
                                kernel (0: only the open-ended buckets, queries beyond the thread-per-job rows) */
     int32_t long_lanes;     /* lanes per job of the group-per-job kernel: 8, 16 or 32 */
-    int32_t rescue_pair;    /* 1: byte-range rescue jobs two per wavefront group (BWACUDA_OPT_RESCUE_PAIR) */
+    int32_t rescue_pair;    /* lanes of a group holding two byte-range rescue jobs, 4, 8 or 16 (0: off;
+                               BWACUDA_OPT_RESCUE_PAIR) */
     int32_t reserved;
 } bwacuda_tuning;
 

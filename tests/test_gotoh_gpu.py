@@ -16,7 +16,8 @@ pytestmark = pytest.mark.gpu
 
 KERNELS = [pytest.param((B.RESCUE_AUTO, 16, 0), id="wavefront16"), pytest.param((B.RESCUE_AUTO, 8, 0), id="wavefront8"),
            pytest.param((B.RESCUE_AUTO, 32, 0), id="wavefront32"), pytest.param((B.RESCUE_TPJ, 16, 0), id="tpj"),
-           pytest.param((B.RESCUE_AUTO, 8, 1), id="paired8"), pytest.param((B.RESCUE_AUTO, 16, 1), id="paired16")]
+           pytest.param((B.RESCUE_AUTO, 8, 4), id="paired4"), pytest.param((B.RESCUE_AUTO, 8, 8), id="paired8"),
+           pytest.param((B.RESCUE_AUTO, 16, 16), id="paired16")]
 SCORINGS = [(1, 4, 6, 1), (2, 3, 5, 2)]
 
 

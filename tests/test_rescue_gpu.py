@@ -12,7 +12,8 @@ pytestmark = pytest.mark.gpu
 # (kernel family, lanes per job of the register wavefront)
 KERNELS = [pytest.param((B.RESCUE_AUTO, 16, 0), id="wavefront16"), pytest.param((B.RESCUE_AUTO, 8, 0), id="wavefront8"),
            pytest.param((B.RESCUE_AUTO, 32, 0), id="wavefront32"), pytest.param((B.RESCUE_TPJ, 16, 0), id="tpj"),
-           pytest.param((B.RESCUE_AUTO, 8, 1), id="paired8"), pytest.param((B.RESCUE_AUTO, 16, 1), id="paired16")]
+           pytest.param((B.RESCUE_AUTO, 8, 4), id="paired4"), pytest.param((B.RESCUE_AUTO, 8, 8), id="paired8"),
+           pytest.param((B.RESCUE_AUTO, 16, 16), id="paired16")]
 
 
 @pytest.fixture(params=KERNELS)
@@ -162,11 +163,12 @@ def test_autotune_rescue_keeps_results(ctx):
     d_out = torch.zeros(len(js) * 28, dtype=torch.uint8, device="cuda")
     try:
         t = ctx.autotune_rescue(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), minsc=20, max_sc=1, sample=8192)
-        # the 32-bit wavefront at 8/16/32 lanes, thread-per-job, the paired wavefront at 8/16 lanes
-        assert t["candidates"] == 6 and t["rescue_gcups"] > 0
+        # the 32-bit wavefront at 8/16/32 lanes, thread-per-job, the paired wavefront in groups of
+        # 4/8/16 lanes
+        assert t["candidates"] == 7 and t["rescue_gcups"] > 0
         assert (t["rescue_kernel"], t["rescue_lanes"], t["rescue_pair"]) in {
             (B.RESCUE_AUTO, 8, 0), (B.RESCUE_AUTO, 16, 0), (B.RESCUE_AUTO, 32, 0), (B.RESCUE_TPJ, 16, 0),
-            (B.RESCUE_AUTO, 8, 1), (B.RESCUE_AUTO, 16, 1)}
+            (B.RESCUE_AUTO, 8, 4), (B.RESCUE_AUTO, 8, 8), (B.RESCUE_AUTO, 8, 16)}
         ctx.ksw_align2_device(d_seq.data_ptr(), d_jobs.data_ptr(), len(js), d_out.data_ptr(), minsc=20, max_sc=1)
         ctx.sync()
         assert np.array_equal(d_out.cpu().numpy().view(B.ALN_RES), want)
@@ -199,14 +201,14 @@ def _pair_mix(seed, n):
     return pairs
 
 
-@pytest.mark.parametrize("lanes", [8, 16])
+@pytest.mark.parametrize("lanes", [4, 8, 16])
 @pytest.mark.parametrize("scoring", [(1, 4, 6, 1), (2, 3, 5, 2)])
 def test_paired_wavefront_limits(ctx, lanes, scoring):
     a, b, o, e = scoring
     mat = oracle.scmat(a, b)
     js = _js(_pair_mix(100 + lanes + a, 3001))  # odd: the last pair has one job
-    ctx.set_option(B.OPT_RESCUE_PAIR, 1)
-    ctx.set_option(B.OPT_RESCUE_LANES, lanes)
+    ctx.set_option(B.OPT_RESCUE_PAIR, lanes)
+    ctx.set_option(B.OPT_RESCUE_LANES, 16 if lanes == 16 else 8)
     try:
         for mode in (0, 1):
             want, _ = oracle.align2_batch(js, mat, o, e, o, e, 19 * a, a, mode=mode)
@@ -231,7 +233,7 @@ def test_paired_wavefront_other_matrices(ctx):
     odd_row[20 + 1] = -2  # mat[4][1]: the N row is no longer one value
     asym = oracle.scmat(1, 4).copy()
     asym[1], asym[5 + 2], asym[10 + 3] = -3, -2, -1  # mat[0][1], mat[1][2], mat[2][3]
-    ctx.set_option(B.OPT_RESCUE_PAIR, 1)
+    ctx.set_option(B.OPT_RESCUE_PAIR, 1)  # 1: groups of 4 lanes
     ctx.set_option(B.OPT_RESCUE_LANES, 8)
     try:
         for mat in (odd, odd_row, asym):
