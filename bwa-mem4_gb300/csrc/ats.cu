@@ -3,17 +3,19 @@
 // On Grace-Blackwell the GPU reads and writes pageable host memory through the
 // host's page tables (cudaDevAttrPageableMemoryAccess), over NVLink-C2C.  So
 // bwacuda_extend_batch hands the caller's job array to the device as it is:
-//   1. a length kernel reads the jobs, validates them and writes per-job sizes
+//   1. a length kernel reads the jobs (the only read of the job array), validates
+//      them, writes per-job sizes and leaves each job in its device descriptor
 //      (and counts the bwa-mem bin labels for the statistics);
 //   2. a device scan turns sizes into HBM offsets;
 //   3. a gather kernel copies every query and target slice from host memory
-//      into one HBM buffer and writes the device descriptors;
+//      into one HBM buffer and completes the device descriptors;
 //   4. the batched extension runs (sort, buckets, persistent kernels);
 //   5. a scatter kernel stores the results straight into the caller's out[].
-// The host only launches.  Steps 1-3 of every chunk run back to back on one
-// high-priority gather stream (one chunk reads host memory at a time: the link is
-// the shared resource); steps 4-5 run on two alternating extension streams, each
-// chunk's extension waiting only for its own gather.  A ring of ATS_RING chunk
+// The host only launches.  Steps 1-2 of chunk k+1 run on a plan stream while
+// chunk k's gather (step 3) runs on the high-priority gather stream, so the
+// gathers follow one another on the host link (the shared resource); steps 4-5
+// run on two alternating extension streams, each chunk's extension waiting only
+// for its own gather.  A ring of ATS_RING chunk
 // buffers lets the gathers run ahead of the extensions; one 8-byte readback per
 // chunk (its byte total) sizes the chunk's sequence buffer.  While a chunk is in
 // flight the persistent bucket kernels leave one small block's worth of registers
@@ -149,6 +151,7 @@ __global__ void __launch_bounds__(ATS_THREADS) ats_scatter_kernel(const uint32_t
 struct AtsChunk {
     DevBuf sizes, offs, scan_tmp, seq, djobs, dout, flags;
     HostBuf h_total, h_flags;
+    cudaEvent_t planned = nullptr;   // lengths, offsets and the byte total are in (plan stream)
     cudaEvent_t gathered = nullptr;  // sequence buffer and descriptors are in HBM
     cudaEvent_t done = nullptr;      // results stored, flags read back
     bool busy = false;
@@ -158,22 +161,26 @@ struct AtsChunk {
 
 struct AtsState {
     AtsChunk ring[ATS_RING];
-    cudaStream_t gstream = nullptr;  // lengths, scans, gathers (highest priority)
+    cudaStream_t gstream = nullptr;  // gathers (highest priority)
+    cudaStream_t pstream = nullptr;  // the next chunk's lengths and offsets, beside the current gather
 };
 
 void ats_release(bwacuda_ctx *c)
 {
     if (!c->ats) return;
     if (c->ats->gstream) cudaStreamSynchronize(c->ats->gstream);
+    if (c->ats->pstream) cudaStreamSynchronize(c->ats->pstream);
     for (auto &r : c->ats->ring) {
         if (r.done) cudaEventSynchronize(r.done);
         r.sizes.release(); r.offs.release(); r.scan_tmp.release(); r.seq.release();
         r.djobs.release(); r.dout.release(); r.flags.release();
         r.h_total.release(); r.h_flags.release();
+        if (r.planned) cudaEventDestroy(r.planned);
         if (r.gathered) cudaEventDestroy(r.gathered);
         if (r.done) cudaEventDestroy(r.done);
     }
     if (c->ats->gstream) cudaStreamDestroy(c->ats->gstream);
+    if (c->ats->pstream) cudaStreamDestroy(c->ats->pstream);
     delete c->ats;
     c->ats = nullptr;
 }
@@ -188,7 +195,9 @@ int ats_init(bwacuda_ctx *c)
     int lo_prio = 0, hi_prio = 0;
     cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&A->gstream, cudaStreamNonBlocking, hi_prio);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&A->pstream, cudaStreamNonBlocking, hi_prio);
     for (auto &r : A->ring) {
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r.planned, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r.gathered, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r.done, cudaEventDisableTiming);
     }
@@ -225,13 +234,12 @@ int ats_retire(bwacuda_ctx *c, AtsChunk &R, uint32_t *input_flags)
     return BWACUDA_OK;
 }
 
-// Steps 1-3 of a chunk on the gather stream: lengths and validation, the offset
-// scan, the byte total read back (the host waits for it: it sizes the sequence
-// buffer, and the gather stream holds nothing else), then the gather.
-cudaError_t ats_gather_chunk(bwacuda_ctx *c, AtsChunk &R, const bwacuda_ext_job *hj, size_t cn, const BinRule &br,
-                             int w)
+// Steps 1-2 of a chunk on the plan stream: lengths and validation (the only read of the
+// caller's job array: each job lands in its device descriptor), the offset scan, the byte total
+// back to the host.  Enqueued while the previous chunk's gather runs.
+cudaError_t ats_plan_chunk(bwacuda_ctx *c, AtsChunk &R, const bwacuda_ext_job *hj, size_t cn, const BinRule &br)
 {
-    cudaStream_t g = c->ats->gstream;
+    cudaStream_t p = c->ats->pstream;
     cudaError_t e;
     size_t scan_bytes = 0;
     if ((e = cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, (const uint64_t *)nullptr, (uint64_t *)nullptr,
@@ -247,20 +255,33 @@ cudaError_t ats_gather_chunk(bwacuda_ctx *c, AtsChunk &R, const bwacuda_ext_job 
     if ((e = R.h_flags.ensure(ATS_FLAG_BYTES)) != cudaSuccess) return e;
     uint64_t *sizes = static_cast<uint64_t *>(R.sizes.p), *offs = static_cast<uint64_t *>(R.offs.p);
     uint32_t *flags = static_cast<uint32_t *>(R.flags.p);
-    if ((e = cudaMemsetAsync(flags, 0, ATS_FLAG_BYTES, g)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(sizes + cn, 0, 8, g)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(flags, 0, ATS_FLAG_BYTES, p)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(sizes + cn, 0, 8, p)) != cudaSuccess) return e;
     const uint32_t grid = (uint32_t)std::min<size_t>((cn + ATS_THREADS - 1) / ATS_THREADS,
                                                      (size_t)batched_nsm(c) * ATS_BLOCKS_PER_SM);
-    ats_lengths_kernel<<<grid, ATS_THREADS, 0, g>>>(hj, (uint32_t)cn, br, sizes, flags,
+    ats_lengths_kernel<<<grid, ATS_THREADS, 0, p>>>(hj, (uint32_t)cn, br, sizes, flags,
                                                     static_cast<bwacuda_dev_ext_job *>(R.djobs.p));
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    if ((e = cub::DeviceScan::ExclusiveSum(R.scan_tmp.p, scan_bytes, sizes, offs, (int)cn + 1, g)) != cudaSuccess)
+    if ((e = cub::DeviceScan::ExclusiveSum(R.scan_tmp.p, scan_bytes, sizes, offs, (int)cn + 1, p)) != cudaSuccess)
         return e;
-    if ((e = cudaMemcpyAsync(R.h_total.p, offs + cn, 8, cudaMemcpyDeviceToHost, g)) != cudaSuccess) return e;
-    if ((e = cudaStreamSynchronize(g)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(R.h_total.p, offs + cn, 8, cudaMemcpyDeviceToHost, p)) != cudaSuccess) return e;
+    return cudaEventRecord(R.planned, p);
+}
+
+// Step 3 on the gather stream, once the chunk is planned: the host reads the byte total (it
+// sizes the sequence buffer), then the gather.
+cudaError_t ats_gather_chunk(bwacuda_ctx *c, AtsChunk &R, size_t cn, int w)
+{
+    cudaStream_t g = c->ats->gstream;
+    cudaError_t e;
+    if ((e = cudaEventSynchronize(R.planned)) != cudaSuccess) return e;
     const uint64_t total = *static_cast<const uint64_t *>(R.h_total.p);
     if ((e = R.seq.ensure(total + 16)) != cudaSuccess) return e;
-    ats_gather_kernel<<<grid, ATS_THREADS, 0, g>>>((uint32_t)cn, offs, w, static_cast<uint8_t *>(R.seq.p),
+    if ((e = cudaStreamWaitEvent(g, R.planned, 0)) != cudaSuccess) return e;
+    const uint32_t grid = (uint32_t)std::min<size_t>((cn + ATS_THREADS - 1) / ATS_THREADS,
+                                                     (size_t)batched_nsm(c) * ATS_BLOCKS_PER_SM);
+    ats_gather_kernel<<<grid, ATS_THREADS, 0, g>>>((uint32_t)cn, static_cast<const uint64_t *>(R.offs.p), w,
+                                                   static_cast<uint8_t *>(R.seq.p),
                                                    static_cast<bwacuda_dev_ext_job *>(R.djobs.p));
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     return cudaEventRecord(R.gathered, g);
@@ -348,16 +369,25 @@ int extend_batch_ats(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int 
     const BinRule br = bin_rule(m, mat);
     const size_t CH = std::min(c->chunk_jobs, ATS_MAX_CHUNK);
     uint32_t input_flags = 0;
+    // chunks ramp up from 64k jobs, doubling: the extension starts after a short gather, and each
+    // gather (about 2.5x faster than the extension of as many jobs) ends before the extension of
+    // the chunks ahead of it.  Chunk k+1 is planned (its lengths and offsets) while chunk k is
+    // gathered, so the gathers follow one another on the host link.
+    auto chunk_len = [&](size_t k, size_t c0) {
+        return std::min(std::min(CH, (size_t)65536 << (k < 16 ? k : 16)), n - c0);
+    };
+    {
+        AtsChunk &R0 = c->ats->ring[0];
+        if ((rc = ats_retire(c, R0, &input_flags)) == BWACUDA_OK) {
+            const cudaError_t e = ats_plan_chunk(c, R0, jobs, chunk_len(0, 0), br);
+            if (e != cudaSuccess) rc = cuda_status(e);
+        }
+    }
     size_t k = 0;
     for (size_t c0 = 0, cn = 0; c0 < n && rc == BWACUDA_OK; c0 += cn, ++k) {
-        // chunks ramp up from 64k jobs, doubling: the extension starts after a short gather, and
-        // each gather (about 2.5x faster than the extension of as many jobs) ends before the
-        // extension of the chunks ahead of it
-        const size_t ramp = std::min(CH, (size_t)65536 << (k < 16 ? k : 16));
-        cn = std::min(ramp, n - c0);
+        cn = chunk_len(k, c0);
         AtsChunk &R = c->ats->ring[k % ATS_RING];
-        if ((rc = ats_retire(c, R, &input_flags)) != BWACUDA_OK) break;
-        cudaError_t e = ats_gather_chunk(c, R, jobs + c0, cn, br, w);
+        cudaError_t e = ats_gather_chunk(c, R, cn, w);
         if (e == cudaSuccess) e = ats_extend_chunk(c, R, (int)(k & 1), cn, P, out + c0);
         if (e != cudaSuccess) {
             rc = cuda_status(e);
@@ -365,12 +395,22 @@ int extend_batch_ats(bwacuda_ctx *c, const bwacuda_ext_job *jobs, size_t n, int 
         }
         R.busy = true;
         c->stats.kernel_launches += 3 + 3 + (uint64_t)batched_bucket_count(c);
+        const size_t c1 = c0 + cn;
+        if (c1 < n) {
+            AtsChunk &R1 = c->ats->ring[(k + 1) % ATS_RING];
+            if ((rc = ats_retire(c, R1, &input_flags)) != BWACUDA_OK) break;
+            if ((e = ats_plan_chunk(c, R1, jobs + c1, chunk_len(k + 1, c1), br)) != cudaSuccess) {
+                rc = cuda_status(e);
+                break;
+            }
+        }
     }
     for (auto &R : c->ats->ring) {
         const int r2 = ats_retire(c, R, &input_flags);
         if (!rc) rc = r2;
     }
     if (rc != BWACUDA_OK) {  // a failed enqueue may leave work behind on the streams
+        cudaStreamSynchronize(c->ats->pstream);
         cudaStreamSynchronize(c->ats->gstream);
         cudaStreamSynchronize(c->slot[0].stream);
         cudaStreamSynchronize(c->slot[1].stream);
