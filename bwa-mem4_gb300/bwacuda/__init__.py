@@ -23,7 +23,7 @@ RESCUE_AUTO, RESCUE_TPJ = 0, 1
 OPT_HOST_GATHER = 6
 GATHER_AUTO, GATHER_HOST, GATHER_DEVICE = 0, 1, 2
 OPT_GRAB, OPT_BUCKET_STEP, OPT_RESCUE_LANES, OPT_UNGAPPED, OPT_DEVICE_PIECE = 7, 8, 9, 10, 11
-OPT_LONG_QLEN, OPT_LONG_LANES, OPT_RESCUE_PAIR = 12, 13, 14
+OPT_LONG_QLEN, OPT_LONG_LANES, OPT_RESCUE_PAIR, OPT_LONG_SLIDE = 12, 13, 14, 15
 PATH_PLAIN, PATH_BATCHED = 0, 1
 INT_MAX = 2**31 - 1
 

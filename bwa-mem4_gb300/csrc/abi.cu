@@ -316,6 +316,9 @@ extern "C" int bwacuda_set_option(bwacuda_ctx *c, int option, int64_t value)
     case BWACUDA_OPT_LONG_LANES:
         if (value != 8 && value != 16 && value != 32) return BWACUDA_EINVAL;
         return batched_set_long_lanes(c, (int)value);
+    case BWACUDA_OPT_LONG_SLIDE:
+        if (value < 0 || value > 2) return BWACUDA_EINVAL;
+        return batched_set_long_slide(c, (int)value);
     case BWACUDA_OPT_DEVICE_PIECE:
         if (value < 1 || value > ((int64_t)1 << 30)) return BWACUDA_EINVAL;
         c->dev_piece = (size_t)value;

@@ -179,6 +179,19 @@ int batched_set_long_lanes(bwacuda_ctx *c, int lanes)
     return BWACUDA_OK;
 }
 
+// Window kernel on the open-ended buckets: 0 off, 1 on buckets of a warp of jobs per SM or
+// more, 2 always; a new value invalidates captured graphs.
+int batched_set_long_slide(bwacuda_ctx *c, int mode)
+{
+    int rc = batched_init(c);
+    if (rc) return rc;
+    if (c->long_slide != mode) {
+        c->long_slide = mode;
+        c->batched->gen++;
+    }
+    return BWACUDA_OK;
+}
+
 void batched_get_tuning(bwacuda_ctx *c, int *tb, int *grab, int *step)
 {
     BatchedState *B = c->batched;
@@ -240,12 +253,19 @@ static cudaError_t enqueue_batched(bwacuda_ctx *c, BatchBufs &bb, const uint8_t 
     X.sm_regs = B->sm_regs;
     X.sm_threads = B->sm_threads;
     X.stream = bb.fan[0];
+    // the open-ended buckets of the 8- and 16-bit classes run the thread-per-job window kernel
+    // first (bands up to bwa-mem's default 100; wider ones stay with the group kernel), on
+    // buckets of at least a warp of jobs per SM unless BWACUDA_OPT_LONG_SLIDE forces it
+    const int slide_wc = c->long_slide && lanes ? ext_slide_window_for_band(100) : 0;
+    X.slide_min = c->long_slide == 2 ? 0u : (uint32_t)B->nsm * 32u;
     bool long16 = false, long32 = false;
     for (int b = B->nb - 1; b >= 0; --b) {
         if (B->defs[b].kernel != 1) continue;
         uint32_t *tab = static_cast<uint32_t *>(bb.table.p) + 4 * b;
         X.bounds = tab;
         X.counter = tab + 2;
+        X.slide_counter = tab + 3;
+        X.slide_wc = B->defs[b].qhi == EXT_QHI_OPEN ? slide_wc : 0;
         const bool w32 = B->defs[b].cls == 2;
         if ((e = ext_long_launch(X, w32, B->nsm)) != cudaSuccess) return e;
         long16 |= !w32;
@@ -332,7 +352,7 @@ void batched_set_reserve(BatchBufs *bb, int regs, int threads)
 BatchBufs *batched_slot_bufs(bwacuda_ctx *c, int slot) { return &c->batched->bufs[slot & 1]; }
 int batched_nsm(bwacuda_ctx *c) { return c->batched->nsm; }
 // Launches of the bucket stage: one per bucket and the two deferred group-per-job launches.
-int batched_bucket_count(bwacuda_ctx *c) { return c->batched->nb + 2; }
+int batched_bucket_count(bwacuda_ctx *c) { return c->batched->nb + 2 + (c->long_slide ? 2 : 0); }
 
 static cudaError_t bufs_streams(BatchBufs &bb)
 {

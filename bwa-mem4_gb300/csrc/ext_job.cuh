@@ -331,6 +331,16 @@ struct U8Keys {
             v = (uint32_t)pair_rowkey((int32_t)v, h2, jj);
         }
     }
+    // quad with its key bytes given (kk = bytes k, k + 1 with k = jj / 2)
+    __device__ __forceinline__ void quad_kk(uint32_t h2a, uint32_t h2b, uint32_t kk, int jj)
+    {
+        if (K16) {
+            v = __vimax3_u16x2(v, prmt(kk, h2a, 0x6040u), prmt(kk, h2b, 0x6141u));
+        } else {
+            v = (uint32_t)pair_rowkey((int32_t)v, h2a, jj);
+            v = (uint32_t)pair_rowkey((int32_t)v, h2b, jj + 2);
+        }
+    }
     // two consecutive pairs at columns jj..jj+3 (jj even)
     __device__ __forceinline__ void quad(uint32_t h2a, uint32_t h2b, int jj)
     {
@@ -439,9 +449,12 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
             // columns j, j+1 of one word as 16x2 lanes.  F runs through the lanes too:
             // fv holds F(i, j) in its high half, h1v holds H(i, j-1) in its high half.
             uint32_t fv = (uint32_t)f << 16, h1v = (uint32_t)h1 << 16;
-            auto pair = [&](int jj, uint32_t sel) {
+            // cw: the cell word of the current pair (running pointer: constant offsets, no
+            // per-pair index arithmetic)
+            uint32_t *cw = cellw + (j >> 1) * TB;
+            auto pair_at = [&](int off, uint32_t sel) {
                 const uint32_t wv = wn;
-                wn = cellw[((jj >> 1) + 1) * TB];  // spare word keeps this in bounds
+                wn = cw[off + TB];  // spare word keeps this in bounds
                 const uint32_t s2 = prmt(plo, phi, sel);   // (s_j, s_j+1)
                 const uint32_t hd2 = prmt(wv, 0u, 0x4240u);  // (H(i-1,j-1), H(i-1,j))
                 const uint32_t e2 = prmt(wv, 0u, 0x4341u);   // (E(i,j), E(i,j+1))
@@ -455,28 +468,34 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_u8p(uint32_t *__restri
                 const uint32_t f2 = f_pair(fv, ti2, fsel2, ne_ins2);            // (F(i,j), F(i,j+1))
                 const uint32_t h2 = __vimax3_s16x2(M2, e2, f2);  // (H(i,j), H(i,j+1))
                 // stored bytes: H(i,j-1), E(i+1,j), H(i,j), E(i+1,j+1)
-                cellw[(jj >> 1) * TB] = prmt(prmt(h1v, h2, 0x0042u), en2, 0x6140u);
+                cw[off] = prmt(prmt(h1v, h2, 0x0042u), en2, 0x6140u);
                 h1v = h2;
                 return h2;
             };
             // one pair to reach a query-word boundary, then whole words (four columns) with
             // the next word loaded one step ahead, then a last pair
             if ((j & 2) && j + 1 < end) {
-                rowkey.pair(pair(j, qw[(j >> 2) * TB] >> 16), j);
+                rowkey.pair(pair_at(0, qw[(j >> 2) * TB] >> 16), j);
                 j += 2;
+                cw += TB;
             }
             if (j + 3 < end) {
-                uint32_t qn = qw[(j >> 2) * TB];
+                const uint32_t *qp = qw + (j >> 2) * TB;
+                uint32_t qn = qp[0];
+                uint32_t kk = (uint32_t)(j >> 1) * 0x0101u + 0x0100u;  // key column bytes of the quad
                 for (; j + 3 < end; j += 4) {
                     const uint32_t qv = qn;
-                    qn = qw[((j >> 2) + 1) * TB];  // j + 4 <= qlen < qcap: inside the query words
-                    const uint32_t h2a = pair(j, qv);
-                    const uint32_t h2b = pair(j + 2, qv >> 16);
-                    rowkey.quad(h2a, h2b, j);
+                    qp += TB;
+                    qn = qp[0];  // j + 4 <= qlen < qcap: inside the query words
+                    const uint32_t h2a = pair_at(0, qv);
+                    const uint32_t h2b = pair_at(TB, qv >> 16);
+                    cw += 2 * TB;
+                    rowkey.quad_kk(h2a, h2b, kk, j);
+                    kk += 0x0202u;
                 }
             }
             if (j + 1 < end) {
-                rowkey.pair(pair(j, qw[(j >> 2) * TB] >> ((j & 2) * 8)), j);
+                rowkey.pair(pair_at(0, qw[(j >> 2) * TB] >> ((j & 2) * 8)), j);
                 j += 2;
             }
             f = (int)(fv >> 16);
@@ -637,9 +656,11 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_i16p(uint2 *__restrict
             }
             uint2 wn = cell2[(j >> 1) * TB];  // j <= end <= qlen: allocated
             uint32_t fv = (uint32_t)f << 16, h1v = (uint32_t)h1 << 16;
-            auto pair = [&](int jj, uint32_t sel) {
+            // cw: the pair word of the current pair (running pointer, as in the 8-bit form)
+            uint2 *cw = cell2 + (j >> 1) * TB;
+            auto pair_at = [&](int off, uint32_t sel, int jj) {
                 const uint2 wv = wn;
-                wn = cell2[((jj >> 1) + 1) * TB];  // spare pair keeps this in bounds
+                wn = cw[off + TB];  // spare pair keeps this in bounds
                 const uint32_t s2 = prmt(plo, phi, sel);  // (s_j, s_j+1)
                 const uint32_t hd2 = wv.x, e2 = wv.y;
                 // M = hd ? hd + s : 0, as min(hd + s, 32767 * min(hd, 1)): every path score
@@ -652,25 +673,29 @@ __device__ __forceinline__ bwacuda_ext_result ext_run_job_i16p(uint2 *__restrict
                 const uint32_t f2 = f_pair(fv, ti2, fsel2, ne_ins2);
                 const uint32_t h2 = __vimax3_s16x2(M2, e2, f2);
                 // stored: H(i,j-1), H(i,j) and E(i+1,j), E(i+1,j+1)
-                cell2[(jj >> 1) * TB] = make_uint2(prmt(h1v, h2, 0x5432u), en2);
+                cw[off] = make_uint2(prmt(h1v, h2, 0x5432u), en2);
                 h1v = h2;
                 rowkey = pair_rowkey(rowkey, h2, jj);
             };
             if ((j & 2) && j + 1 < end) {
-                pair(j, qw[(j >> 2) * TB] >> 16);
+                pair_at(0, qw[(j >> 2) * TB] >> 16, j);
                 j += 2;
+                cw += TB;
             }
             if (j + 3 < end) {
-                uint32_t qn = qw[(j >> 2) * TB];
+                const uint32_t *qp = qw + (j >> 2) * TB;
+                uint32_t qn = qp[0];
                 for (; j + 3 < end; j += 4) {
                     const uint32_t qv = qn;
-                    qn = qw[((j >> 2) + 1) * TB];  // j + 4 <= qlen < qcap: inside the query words
-                    pair(j, qv);
-                    pair(j + 2, qv >> 16);
+                    qp += TB;
+                    qn = qp[0];  // j + 4 <= qlen < qcap: inside the query words
+                    pair_at(0, qv, j);
+                    pair_at(TB, qv >> 16, j + 2);
+                    cw += 2 * TB;
                 }
             }
             if (j + 1 < end) {
-                pair(j, qw[(j >> 2) * TB] >> ((j & 2) * 8));
+                pair_at(0, qw[(j >> 2) * TB] >> ((j & 2) * 8), j);
                 j += 2;
             }
             f = (int)(fv >> 16);

@@ -45,8 +45,8 @@ cudaError_t launch_first(const ExtLongLaunch &X, int nsm)
         per_sm = std::max(1, std::min(per_sm, std::min(cap_r, cap_t)));
     }
     kern<<<per_sm * nsm, XL_BLOCK, smem, X.stream>>>(X.seq, X.jobs, X.order, X.bounds, X.counter, X.njobs,
-                                                    X.min_qlen, ring, X.defer, X.defer_count, X.P, X.out, X.err,
-                                                    X.cells);
+                                                    X.min_qlen, ring, X.defer, X.defer_count, W32 ? 0 : X.slide_wc,
+                                                    X.slide_min, X.P, X.out, X.err, X.cells);
     return cudaGetLastError();
 }
 
@@ -70,7 +70,7 @@ cudaError_t launch_deferred(const ExtLongLaunch &X, const uint32_t *dbounds, uin
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32, smem)) != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidValue;
     kern<<<per_sm * nsm, 32, smem, X.stream>>>(X.seq, X.jobs, X.defer, dbounds, dcounter, X.njobs, 0, R, nullptr,
-                                              nullptr, X.P, X.out, X.err, X.cells);
+                                              nullptr, 0, 0u, X.P, X.out, X.err, X.cells);
     return cudaGetLastError();
 }
 
@@ -78,7 +78,14 @@ cudaError_t launch_deferred(const ExtLongLaunch &X, const uint32_t *dbounds, uin
 
 cudaError_t ext_long_launch(const ExtLongLaunch &X, bool w32, int nsm)
 {
-    return w32 ? launch_first_lanes<true>(X, nsm) : launch_first_lanes<false>(X, nsm);
+    if (w32) return launch_first_lanes<true>(X, nsm);
+    // the window kernel first (it exits at once when the bucket is below slide_min jobs); the
+    // group kernel then runs the jobs it left
+    if (X.slide_wc > 0) {
+        const cudaError_t e = ext_slide_launch(X, nsm);
+        if (e != cudaSuccess) return e;
+    }
+    return launch_first_lanes<false>(X, nsm);
 }
 
 cudaError_t ext_long_deferred_launch(const ExtLongLaunch &X, bool w32, uint32_t *work, int nsm)

@@ -109,6 +109,26 @@ __host__ __device__ inline bool ring_fits(int qlen, int w, int R)
     return (long long)qlen + 1 <= R || 2LL * w + 3 <= R;
 }
 
+// The thread-per-job window kernel (ext_slide.cu): a job's row lives in a window of wc
+// columns that moves right SLIDE_K columns at a time.  A row touches at most columns
+// [i - w - 1, i + w + 4], and the window starts at most SLIDE_K - 1 columns left of i - w - 1,
+// so it holds every band of 2w + 5 + SLIDE_K <= wc columns, and every query of qlen + 4 <= wc
+// columns without moving.
+constexpr int SLIDE_K = 64;
+
+__host__ __device__ inline bool slide_fits(int qlen, int w, int wc)
+{
+    return (long long)qlen + 4 <= wc || 2LL * w + 5 + SLIDE_K <= wc;
+}
+
+// Whether the window kernel takes a 16-bit job of a bucket of `count` jobs: it is enabled for
+// the launch (wc > 0), the bucket holds at least slide_min jobs and the job's band fits.  The
+// group-per-job kernel leaves exactly these jobs to it.
+__host__ __device__ inline bool slide_takes(int qlen, int w, int wc, uint32_t count, uint32_t slide_min)
+{
+    return wc > 0 && count >= slide_min && slide_fits(qlen, w, wc);
+}
+
 template <int L>
 __device__ __forceinline__ int group_max(int v)
 {
@@ -135,15 +155,16 @@ __device__ __forceinline__ int group_min(int v)
 
 // Jobs come from order[bounds[0] .. bounds[1]) (order nullptr: the identity; bounds nullptr:
 // [0, njobs)), taken G = 32 / L at a time per warp from *counter.  A job is this launch's if
-// its cell class is W32's and qlen >= min_qlen; one whose band needs a larger ring than
-// ring_cols goes to defer[] (count in *defer_count), or fails the call when defer is nullptr.
+// its cell class is W32's, qlen >= min_qlen and the window kernel does not take it
+// (slide_takes with slide_wc, slide_min); one whose band needs a larger ring than ring_cols
+// goes to defer[] (count in *defer_count), or fails the call when defer is nullptr.
 template <bool W32, int L, int C>
 __global__ void __launch_bounds__(128)
 ext_long_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *__restrict__ jobs,
                 const uint32_t *__restrict__ order, const uint32_t *__restrict__ bounds,
                 uint32_t *__restrict__ counter, uint32_t njobs, int min_qlen, int ring_cols,
-                uint32_t *__restrict__ defer, uint32_t *__restrict__ defer_count,
-                const __grid_constant__ ExtParams P, bwacuda_ext_result *__restrict__ out,
+                uint32_t *__restrict__ defer, uint32_t *__restrict__ defer_count, int slide_wc,
+                uint32_t slide_min, const __grid_constant__ ExtParams P, bwacuda_ext_result *__restrict__ out,
                 uint32_t *__restrict__ err, unsigned long long *__restrict__ cells_total)
 {
     constexpr int G = 32 / L;  // jobs per warp
@@ -198,6 +219,9 @@ ext_long_kernel(const uint8_t *__restrict__ seq, const bwacuda_dev_ext_job *__re
         int w = 0;
         if (active) {
             w = clamp_band(J.w < 0 ? 0 : J.w, J.qlen, P.sc.max_sc, P.end_bonus, o_ins, e_ins, o_del, e_del);
+            if (!W32 && slide_takes(J.qlen, w, slide_wc, stop - start, slide_min)) active = false;
+        }
+        if (active) {
             if (!ring_fits(J.qlen, w, ring_cols)) {
                 if (k == 0) {
                     if (defer) {

@@ -29,13 +29,16 @@ __device__ __forceinline__ uint32_t ext_cell_class(const bwacuda_dev_ext_job &J,
 }
 
 // 16-bit sort key: cell class (at least min_cls), query length descending
-// (clamped at 1023), target length descending in 32-row steps.
+// (clamped at 1023), target length descending in 32-row steps (1024-row steps for the
+// queries of 1023 bases or more, whose rows the open-ended buckets' kernels run longest
+// first).  Within a bucket the order sets only which jobs run together, never a result.
 __device__ __forceinline__ uint16_t ext_sort_key(const bwacuda_dev_ext_job &J, int max_sc, uint32_t min_cls)
 {
     uint32_t cls = ext_cell_class(J, max_sc);
     cls = cls > min_cls ? cls : min_cls;
     const uint32_t ql = J.qlen < 0 ? 0u : (J.qlen > 1023 ? 1023u : (uint32_t)J.qlen);
-    const uint32_t tb = J.tlen < 0 ? 0u : ((uint32_t)J.tlen >> 5 > 15u ? 15u : (uint32_t)J.tlen >> 5);
+    const uint32_t tsh = ql == 1023u ? 10u : 5u;
+    const uint32_t tb = J.tlen < 0 ? 0u : ((uint32_t)J.tlen >> tsh > 15u ? 15u : (uint32_t)J.tlen >> tsh);
     return (uint16_t)((cls << 14) | ((1023u - ql) << 4) | (15u - tb));
 }
 
@@ -130,6 +133,7 @@ __global__ void ext_bucket_bounds_kernel(const uint16_t *__restrict__ keys, uint
     table[b * 4 + 0] = lower_bound16(keys, n, key_lo);
     table[b * 4 + 1] = lower_bound16(keys, n, key_hi + 1);
     table[b * 4 + 2] = 0;  // work counter
+    table[b * 4 + 3] = 0;  // work counter of the window kernel (open-ended buckets)
 }
 
 }  // namespace
@@ -171,7 +175,7 @@ int ext_bucket_defs(ExtBucketDef *defs, int max_defs, int step, int long_qlo)
             ExtBucketDef d;
             d.cls = cls;
             d.qlo = lo;
-            d.qhi = 1 << 30;
+            d.qhi = EXT_QHI_OPEN;
             d.qcap = cls == 0 ? (int)ext_tpj_smem_limit_qcap(false) : max_qcap_of_class(cls);
             d.kernel = 1;  // any query length
             defs[nb++] = d;

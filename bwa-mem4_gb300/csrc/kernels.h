@@ -61,11 +61,21 @@ struct ExtLongLaunch {
     unsigned long long *cells;
     uint32_t *defer;         // njobs entries: jobs set aside for the deferred launch
     uint32_t *defer_count;   // work + XL_WORK_DCOUNT
+    // thread-per-job window kernel (ext_slide.cu) ahead of the group kernel on 16-bit jobs:
+    // window columns (0: off), the fewest jobs [start, stop) must hold for it to run, and its
+    // zeroed work counter
+    int slide_wc = 0;
+    uint32_t slide_min = 0;
+    uint32_t *slide_counter = nullptr;
     int reserve_regs = 0, reserve_threads = 0, sm_regs = 65536, sm_threads = 2048;
     cudaStream_t stream;
 };
 
 cudaError_t ext_long_launch(const ExtLongLaunch &X, bool w32, int nsm);
+// The window kernel alone (ext_long_launch runs it ahead of the group kernel when slide_wc > 0).
+cudaError_t ext_slide_launch(const ExtLongLaunch &X, int nsm);
+// Window columns for clamped bands up to w.
+int ext_slide_window_for_band(int w);
 cudaError_t ext_long_deferred_launch(const ExtLongLaunch &X, bool w32, uint32_t *work, int nsm);
 // First-launch ring for bands up to w (XL_RING_MIN .. XL_RING_FIRST_MAX columns).
 int ext_long_ring_for_band(int w);

@@ -21,6 +21,7 @@ struct ExtBucketDef {
 };
 
 constexpr int EXT_MAX_BUCKETS = 64;  // one thread each in the bucket-bounds kernel
+constexpr int32_t EXT_QHI_OPEN = 1 << 30;  // qhi of a class's open-ended last bucket
 
 struct PersistLaunch {
     const uint8_t *seq;

@@ -96,6 +96,7 @@ struct bwacuda_ctx {
     int rescue_pair = 0;  // lanes of a group holding two byte-range jobs (rescue_wf2.cuh): 4, 8, 16; 0 off
     bool ungapped = false;  // ungapped-diagonal fast path on the batched extension path
     int long_lanes = 16;    // lanes per job of the group-per-job extension kernel (8, 16, 32)
+    int long_slide = 1;     // thread-per-job window kernel on the open-ended buckets: 0 off, 1 auto, 2 always
     int tune_candidates = 0;        // last autotune call
     double tuned_ext_gcups = 0.0;   // best candidates' rates on their samples
     double tuned_rescue_gcups = 0.0;
@@ -149,6 +150,7 @@ void batched_get_tuning(bwacuda_ctx *c, int *tb, int *grab, int *step);
 int batched_set_long(bwacuda_ctx *c, int long_qlo);
 int batched_get_long(bwacuda_ctx *c);
 int batched_set_long_lanes(bwacuda_ctx *c, int lanes);
+int batched_set_long_slide(bwacuda_ctx *c, int mode);
 
 struct BatchBufs;
 int batched_prepare(bwacuda_ctx *c);

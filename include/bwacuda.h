@@ -158,6 +158,13 @@ typedef struct bwacuda_ctx bwacuda_ctx;
  * most columns per lane); the others stay in the 32-bit wavefront.  1 = 4.  0 (default before
  * tuning) = one job per group.  Results never depend on it. */
 #define BWACUDA_OPT_RESCUE_PAIR 14
+/* Batched extension, the open-ended query-length buckets (queries too long for a thread's
+ * shared-memory row): 1 (default) = a thread-per-job kernel holding each job's row in a window
+ * of the band that slides along the query runs the jobs of bands up to 101 columns when the
+ * bucket holds at least 32 jobs per SM, the group-per-job kernel the rest; 2 = the window
+ * kernel whatever the bucket's size; 0 = the group-per-job kernel only.  Results never depend
+ * on it. */
+#define BWACUDA_OPT_LONG_SLIDE 15
 
 int bwacuda_ctx_create(int device, bwacuda_ctx **out);
 void bwacuda_ctx_destroy(bwacuda_ctx *ctx);

@@ -71,19 +71,35 @@ def _mix(long_js, short_n, seed, w):
     return B.JobSet.from_lists([qs[i] for i in perm], [ts[i] for i in perm], h0[perm], w)
 
 
-ROUTES = [pytest.param((B.PATH_PLAIN, B.GATHER_AUTO), id="plain"),
-          pytest.param((B.PATH_BATCHED, B.GATHER_HOST), id="batched-hostpack"),
-          pytest.param((B.PATH_BATCHED, B.GATHER_DEVICE), id="batched-devgather")]
+# (path, gather route, window-kernel mode): mode 2 runs the thread-per-job window kernel
+# (csrc/ext_slide.cu) on every open-ended bucket however few jobs it holds; mode 1 (the default)
+# leaves buckets under 32 jobs per SM, every bucket of these small cases, to the group kernel
+ROUTES = [pytest.param((B.PATH_PLAIN, B.GATHER_AUTO, 1), id="plain"),
+          pytest.param((B.PATH_BATCHED, B.GATHER_HOST, 1), id="batched-hostpack"),
+          pytest.param((B.PATH_BATCHED, B.GATHER_DEVICE, 1), id="batched-devgather"),
+          pytest.param((B.PATH_BATCHED, B.GATHER_HOST, 2), id="batched-hostpack-window"),
+          pytest.param((B.PATH_BATCHED, B.GATHER_DEVICE, 2), id="batched-devgather-window")]
 
 
 @pytest.fixture(params=ROUTES)
 def rctx(ctx, request):
-    path, gather = request.param
+    path, gather, slide = request.param
     ctx.set_option(B.OPT_EXT_PATH, path)
     ctx.set_option(B.OPT_HOST_GATHER, gather)
+    ctx.set_option(B.OPT_LONG_SLIDE, slide)
     yield ctx
     ctx.set_option(B.OPT_EXT_PATH, B.PATH_BATCHED)
     ctx.set_option(B.OPT_HOST_GATHER, B.GATHER_AUTO)
+    ctx.set_option(B.OPT_LONG_SLIDE, 1)
+
+
+@pytest.fixture
+def wctx(ctx):
+    """Batched path with the window kernel on every open-ended bucket."""
+    ctx.set_option(B.OPT_EXT_PATH, B.PATH_BATCHED)
+    ctx.set_option(B.OPT_LONG_SLIDE, 2)
+    yield ctx
+    ctx.set_option(B.OPT_LONG_SLIDE, 1)
 
 
 def _check(ctx, js, w, mat=None, **kw):
@@ -135,6 +151,75 @@ def test_other_scorings(rctx):
     js = long_jobs(16, 1000, 3000, 100, seed=9)
     _check(rctx, js, 100, mat, o_del=5, e_del=2, o_ins=4, e_ins=3, end_bonus=0, zdrop=40)
     _check(rctx, js, 100, mat, o_del=5, e_del=2, o_ins=4, e_ins=3, end_bonus=7, zdrop=0)
+
+
+@pytest.mark.parametrize("w", [99, 100, 101, 102, 140])
+def test_window_kernel_band_limit(wctx, w):
+    # bands up to 101 columns run in the window kernel's 272-column window (2w + 5 + 64 <= 272),
+    # wider ones in the group kernel beside it
+    js = long_jobs(40, 1030, 6000, w, seed=40 + w)
+    _check(wctx, js, w)
+
+
+def test_window_kernel_row_minus1_beyond_window(wctx):
+    # h0 ~ 20000: row -1 stays positive for thousands of columns, so every column that enters
+    # the window on the right carries a nonzero row -1 value
+    js = long_jobs(24, 2000, 6000, 100, seed=50, h0=(19000, 23000))
+    _check(wctx, js, 100)
+    _check(wctx, js, 100, zdrop=0)
+
+
+def test_window_kernel_target_lengths(wctx):
+    # targets much longer than the query (rows past the query's end empty the band) and much
+    # shorter (the 8-bit class's open-ended bucket), with the query-code check past the band
+    rng = np.random.default_rng(51)
+    qs, ts, h0s = [], [], []
+    for k in range(30):
+        ql = int(rng.integers(1100, 3000))
+        tl = ql * 3 if k % 2 == 0 else int(rng.integers(30, 400))
+        t = rng.integers(0, 4, max(tl, ql)).astype(np.uint8)
+        q = _mutate(rng, t, ql)
+        qs.append(q)
+        ts.append(t[:tl])
+        h0s.append(int(rng.integers(5, 90)))
+    js = B.JobSet.from_lists(qs, ts, h0s, 100)
+    _check(wctx, js, 100)
+    _check(wctx, js, 100, end_bonus=0, zdrop=30)
+
+
+def test_window_kernel_cells_and_asymmetric_gaps(wctx):
+    js = long_jobs(30, 1030, 5000, 100, seed=52)
+    wctx.reset_stats()
+    got = wctx.extend_batch(js, w=100)
+    want, cells = oracle.extend_batch(js)
+    assert np.array_equal(got, want)
+    assert wctx.stats()["ext_cells"] == cells
+    mat = oracle.scmat(1, 4)
+    _check(wctx, js, 100, mat, o_del=6, e_del=1, o_ins=4, e_ins=2, zdrop=60)
+
+
+def test_window_kernel_auto_threshold(ctx):
+    # default mode: a bucket of at least 32 jobs per SM runs in the window kernel, a smaller one
+    # in the group kernel; results are the same either way
+    ctx.set_option(B.OPT_EXT_PATH, B.PATH_BATCHED)
+    rng = np.random.default_rng(53)
+    n = 5200
+    ql = rng.integers(1030, 1300, n)
+    tl = ql + rng.integers(0, 200, n)
+    ts = [rng.integers(0, 4, int(x)).astype(np.uint8) for x in tl]
+    qs = []
+    for k in range(n):  # substitutions at 1%, an error-dense tail on every fourth job
+        q = ts[k][:ql[k]].copy()
+        rate = np.where(np.arange(ql[k]) > ql[k] // 2, 0.3 if k % 4 == 0 else 0.01, 0.01)
+        mask = rng.random(ql[k]) < rate
+        q[mask] = (q[mask] + rng.integers(1, 4, int(mask.sum()))) % 4
+        qs.append(q)
+    js = B.JobSet.from_lists(qs, ts, rng.integers(20, 60, n), 100)
+    want, _ = oracle.extend_batch(js)
+    got = ctx.extend_batch(js, w=100)
+    assert np.array_equal(got, want)
+    head = js.take(np.arange(300))
+    assert np.array_equal(ctx.extend_batch(head, w=100), want[:300])
 
 
 @pytest.mark.parametrize("path", [B.PATH_PLAIN, B.PATH_BATCHED])
