@@ -86,6 +86,8 @@ def parse():
                     help="rescue case: the wavefronts where the jobs fit (auto) or thread-per-job for all")
     ap.add_argument("--gaps", default="6,1,6,1", help="extension cases: o_del,e_del,o_ins,e_ins")
     ap.add_argument("--ungapped", type=int, default=0, help="extension cases: the ungapped pre-pass on (1)")
+    ap.add_argument("--persist-block", type=int, default=0,
+                    help="extension cases: threads per block of the persistent kernels (0: the library's default)")
     ap.add_argument("--h0-add", type=int, default=0,
                     help="extension cases: add this to every h0 (300 moves read pairs into the 16-bit cell class)")
     return ap.parse_args()
@@ -756,6 +758,8 @@ def run_case(args):
         od, ed, oi, ei = (int(x) for x in args.gaps.split(","))
         sc = ctx.scoring(o_del=od, e_del=ed, o_ins=oi, e_ins=ei)
         ctx.set_option(B.OPT_UNGAPPED, args.ungapped)
+        if args.persist_block:
+            ctx.set_option(B.OPT_PERSIST_BLOCK, args.persist_block)
         d_seq = torch.from_numpy(js.seq).cuda()
         d_jobs = torch.from_numpy(js.dev_ext_jobs().view(np.uint8)).cuda()
         d_out = torch.zeros(len(js) * 24, dtype=torch.uint8, device="cuda")
@@ -982,13 +986,16 @@ def main():
             barrier()
             t0 = time.perf_counter()
             esteps = max(1, min(args.steps, 10))
+            call_ms = []
             for _ in range(esteps):
+                tc = time.perf_counter()
                 call()
+                call_ms.append(round((time.perf_counter() - tc) * 1e3, 2))
             barrier()
             et = max_over_ranks(time.perf_counter() - t0)
             ste = ctx.stats()
             r = {"value": round(ste["ext_cells"] / esteps * world / (et / esteps) / 1e9, 2), "unit": "GCUPS",
-                 "ms_per_step": round(et / esteps * 1e3, 2),
+                 "ms_per_step": round(et / esteps * 1e3, 2), "call_ms": call_ms,
                  "bit_identical_to_device_path": bool(np.array_equal(host_out, batched_out))}
             if ste["h2d_bytes"]:
                 r["h2d_bytes_per_step"] = int(ste["h2d_bytes"] / esteps)
@@ -1015,7 +1022,9 @@ def main():
         best = "device-gather" if "device-gather" in routes else "host-pack"
         e2e = dict(routes[best])
         e2e["route"] = best
-        e2e["routes"] = {k: {"value": v["value"], "ms_per_step": v["ms_per_step"]} for k, v in routes.items()}
+        e2e["routes"] = {k: {"value": v["value"], "ms_per_step": v["ms_per_step"], "call_ms": v["call_ms"]}
+                         for k, v in routes.items()}
+        e2e.pop("call_ms", None)
         ug_e2e_eq = round(cells_step * world / (ug_route["ms_per_step"] / 1e3) / 1e9, 2)
 
     # the reference's ungapped-diagonal fast path (opt-in): same results, most clean read-pair

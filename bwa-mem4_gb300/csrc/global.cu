@@ -359,53 +359,6 @@ __device__ __forceinline__ uint32_t glb_cell(int hd, int &e, int &f, int s, int 
     return d;
 }
 
-// Direction bytes of one row, kept at offset column - (beg & ~1) so column pairs land on
-// even offsets: 16-bit units gather into words, four words make a 16-byte store.
-struct GlbRowBytes {
-    uint4 *zr;
-    uint32_t cur = 0, w0 = 0, w1 = 0, w2 = 0, w3 = 0;
-    int last = -1;  // offset of the last byte put, -1: none
-    __device__ __forceinline__ void put(int off, uint32_t v, int nbytes)
-    {
-        cur |= v << (8 * (off & 3));
-        last = off + nbytes - 1;
-        if ((last & 3) == 3) flush_word();
-    }
-    __device__ __forceinline__ void flush_word()
-    {
-        const int g = (last >> 2) & 3;
-        w0 = g == 0 ? cur : w0;
-        w1 = g == 1 ? cur : w1;
-        w2 = g == 2 ? cur : w2;
-        w3 = g == 3 ? cur : w3;
-        cur = 0;
-        if (g == 3) {
-            zr[last >> 4] = make_uint4(w0, w1, w2, w3);
-            w0 = w1 = w2 = w3 = 0;
-        }
-    }
-    // the row's open word and group, then zero groups up to ngroups
-    __device__ __forceinline__ void finish(int ngroups)
-    {
-        int next = 0;
-        if (last >= 0) {
-            if ((last & 3) != 3) flush_word_partial();
-            if ((last & 15) != 15) zr[last >> 4] = make_uint4(w0, w1, w2, w3);
-            next = (last >> 4) + 1;
-        }
-        for (int g = next; g < ngroups; ++g) zr[g] = make_uint4(0u, 0u, 0u, 0u);
-    }
-    __device__ __forceinline__ void flush_word_partial()
-    {
-        const int g = (last >> 2) & 3;
-        w0 = g == 0 ? cur : w0;
-        w1 = g == 1 ? cur : w1;
-        w2 = g == 2 ? cur : w2;
-        w3 = g == 3 ? cur : w3;
-        cur = 0;
-    }
-};
-
 // ksw_global2 on 16-bit pair cells (jobs that pass global_narrow): two columns per lane
 // operation, direction bits from the DPX max-with-predicate instructions.  Slot x of the
 // band (x = column mod B2, B2 the band slots rounded up to even) is lane x & 1 of pair word
@@ -504,12 +457,24 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
         bad |= tc >= (uint32_t)sc.m;
         tc = tc < (uint32_t)sc.m ? tc : (uint32_t)PAD_CODE;
         const uint32_t plo = sc.prof[tc & 7u][0], phi = sc.prof[tc & 7u][1];
-        GlbRowBytes zb;
-        zb.zr = reinterpret_cast<uint4 *>(zj + (size_t)i * zrow);
-        const int base_off = beg & ~1;
+        // Direction bytes of the row at offset column - (beg & ~1): 4-byte words from word 0,
+        // kept as a group of four (g0..g3, the newest in g3) and stored 16 bytes at a time.
+        uint4 *zr = reinterpret_cast<uint4 *>(zj + (size_t)i * zrow);
+        uint32_t g0 = 0, g1 = 0, g2 = 0, g3 = 0;
+        int nw = 0;  // words emitted so far
+        auto emit = [&](uint32_t word) {
+            g0 = g1;
+            g1 = g2;
+            g2 = g3;
+            g3 = word;
+            if ((nw & 3) == 3) zr[nw >> 2] = make_uint4(g0, g1, g2, g3);
+            ++nw;
+        };
+        uint32_t part = 0;  // the open word: its low half (or the odd first column's byte 1)
+        bool open = false;
         int j = beg;
         int xj = xbeg;  // slot of column j
-        if (j < end && (j & 1)) {  // odd first column: the high lanes of its pair
+        if (j < end && (j & 1)) {  // odd first column (offset 1): the high lanes of its pair
             const int x = xj;
             uint2 cw = cell2[(size_t)(x >> 1) * TB];
             int e = (int)cw.y >> 16, h;
@@ -520,23 +485,20 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
             cw.y = (cw.y & 0xffffu) | ((uint32_t)e << 16);
             cell2[(size_t)(x >> 1) * TB] = cw;
             h1 = h;
-            zb.put(j - base_off, d, 1);
+            part = d << 8;
+            open = true;
             ++j;
             if (++xj == B2) xj = 0;
         }
-        if (j + 1 < end) {
+        const int npairs = j < end ? (end - j) >> 1 : 0;
+        if (npairs > 0) {
             // F(i, j) in fv's high lane, H(i, j-1) in h1v's high lane
             uint32_t fv = (uint32_t)f << 16, h1v = (uint32_t)h1 << 16;
-            int p = xj >> 1;
-            uint2 wn = cell2[(size_t)p * TB];
-            uint32_t qn = qsel(j >> 1);
-            for (; j + 1 < end; j += 2) {
-                const uint2 cw = wn;
-                const uint32_t sel = qn;
-                const int pc = p;
-                if (++p == P2) p = 0;
-                wn = cell2[(size_t)p * TB];               // a row's columns use distinct slots
-                qn = qsel((j >> 1) + 1);                  // j / 2 + 1 <= (qlen + 1) / 2: allocated
+            const int p0 = xj >> 1;
+            // one column pair: cp its pair word (read, then overwritten), sel its selector;
+            // returns the two direction bytes
+            auto pair_dir = [&](uint2 *cp, uint32_t sel) -> uint32_t {
+                const uint2 cw = *cp;
                 const uint32_t s2 = prmt(plo, phi, sel);  // (s_j, s_j+1)
                 const uint32_t M2 = __viaddmax_s16x2(cw.x, s2, MIN2);  // H(i-1, .-1) + s
                 bool pm_hi, pm_lo, ph_hi, ph_lo, pf_hi, pf_lo, pe_hi, pe_lo;
@@ -553,15 +515,73 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
                 const uint32_t ttd2 = __viaddmax_s16x2(M2, noe_del2, MIN2);         // M - oe_del
                 const uint32_t E2m = __viaddmax_s16x2(cw.y, ne_del2, MIN2);
                 const uint32_t En2 = __vibmax_s16x2(ttd2, E2m, &pe_hi, &pe_lo);     // open >= extend
-                cell2[(size_t)pc * TB] = make_uint2(prmt(h1v, H2, 0x5432u), En2);
+                *cp = make_uint2(prmt(h1v, H2, 0x5432u), En2);
                 h1v = H2;
                 const uint32_t dlo = (ph_lo ? (pm_lo ? 0u : 1u) : 2u) | (pe_lo ? 0u : 4u) | (pf_lo ? 0u : 32u);
                 const uint32_t dhi = (ph_hi ? (pm_hi ? 0u : 1u) : 2u) | (pe_hi ? 0u : 4u) | (pf_hi ? 0u : 32u);
-                zb.put(j - base_off, dlo | (dhi << 8), 2);
+                return dlo | (dhi << 8);
+            };
+            // the row's pairs k = 0 .. npairs-1 take slots p0 + k, wrapping once at P2 (kw pairs
+            // before the wrap): straight runs of running pointers, no per-pair wrap test
+            const int kw = P2 - p0 < npairs ? P2 - p0 : npairs;
+            uint2 *cp = cell2 + (size_t)p0 * TB;
+            int k = 0;
+            const uint8_t *q1p = qs1 + (size_t)(j >> 1) * TB;
+            const uint16_t *q2p = qs2 + (size_t)(j >> 1) * TB;
+            auto next_sel = [&]() -> uint32_t {
+                uint32_t s;
+                if (Q4) {
+                    s = glb_q4_sel(*q1p);
+                    q1p += TB;
+                } else {
+                    s = *q2p;
+                    q2p += TB;
+                }
+                return s;
+            };
+            auto advance = [&]() {
+                cp += TB;
+                if (++k == kw) cp = cell2;
+            };
+            if (open) {  // a pair at offset 2 closes word 0
+                const uint32_t v = pair_dir(cp, next_sel());
+                emit(part | (v << 16));
+                part = 0;
+                open = false;
+                advance();
             }
+            // word-aligned pairs two at a time; the pair pointers of a step that straddles the
+            // wrap come apart
+            while (k + 2 <= npairs) {
+                const int run = (k < kw ? kw : npairs) - k;  // pairs before the wrap or the end
+                if (run >= 2) {
+                    const int steps = run >> 1;
+                    for (int s = 0; s < steps; ++s) {
+                        const uint32_t va = pair_dir(cp, next_sel());
+                        const uint32_t vb = pair_dir(cp + TB, next_sel());
+                        emit(va | (vb << 16));
+                        cp += 2 * TB;
+                    }
+                    k += 2 * steps;
+                    if (k == kw) cp = cell2;
+                } else {  // one pair left before the wrap: its partner is slot 0
+                    const uint32_t va = pair_dir(cp, next_sel());
+                    const uint32_t vb = pair_dir(cell2, next_sel());
+                    emit(va | (vb << 16));
+                    k += 2;
+                    cp = cell2 + TB;
+                }
+            }
+            if (k < npairs) {  // a last pair: the low half of an open word
+                part = pair_dir(cp, next_sel());
+                open = true;
+                advance();
+            }
+            j += 2 * npairs;
+            const int pe = p0 + npairs;
+            xj = 2 * (pe >= P2 ? pe - P2 : pe);
             f = (int)fv >> 16;
             h1 = (int)h1v >> 16;
-            xj = 2 * p;
         }
         if (j < end) {  // even last column: the low lanes of its pair
             const int x = xj;
@@ -575,7 +595,8 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
             cw.y = (cw.y & 0xffff0000u) | ((uint32_t)e & 0xffffu);
             cell2[(size_t)(x >> 1) * TB] = cw;
             h1 = h;
-            zb.put(j - base_off, d, 1);
+            part |= open ? d << 16 : d;  // offset even: byte 2 after an open pair, else byte 0
+            open = true;
             ++j;
         }
         {   // sentinel slot of column end: H(i, end-1), E unreachable
@@ -586,7 +607,10 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
                                  (cw.y & 0xffff0000u) | ((uint32_t)NEG & 0xffffu));
             cell2[(size_t)(x >> 1) * TB] = cw;
         }
-        zb.finish(ngroups);
+        // the open word, the rest of its group as zeros, then zero groups up to ngroups
+        if (open) emit(part);
+        while (nw & 3) emit(0u);
+        for (int g = nw >> 2; g < ngroups; ++g) zr[g] = make_uint4(0u, 0u, 0u, 0u);
         ncells += (unsigned long long)(end > beg ? end - beg : 0);
     }
     const int end_last = tlen > 0 ? (tlen + w < qlen ? tlen + w : qlen) : -1;
