@@ -981,7 +981,8 @@ def main():
         def timed_route(gather):
             ctx.set_option(B.OPT_HOST_GATHER, gather)
             host_out[:] = 0
-            call()  # warm-up (staging allocation)
+            for _ in range(max(1, args.warmup)):  # warm-up (staging allocation, first touches)
+                call()
             ctx.reset_stats()
             barrier()
             t0 = time.perf_counter()
