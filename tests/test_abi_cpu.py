@@ -73,5 +73,5 @@ def test_header_constants_match_binding():
         if hasattr(B, name):
             assert getattr(B, name) == val, name
     for name in ("OPT_EXT_PATH", "OPT_CHUNK_JOBS", "OPT_GRAPHS", "OPT_PERSIST_BLOCK", "OPT_RESCUE_KERNEL",
-                 "OPT_HOST_GATHER", "OPT_GRAB", "OPT_BUCKET_STEP", "OPT_RESCUE_LANES", "OPT_UNGAPPED", "OPT_DEVICE_PIECE", "OPT_LONG_QLEN", "OPT_LONG_LANES", "OPT_RESCUE_PAIR", "GATHER_AUTO", "GATHER_HOST", "GATHER_DEVICE", "PATH_PLAIN", "PATH_BATCHED"):
+                 "OPT_HOST_GATHER", "OPT_GRAB", "OPT_BUCKET_STEP", "OPT_RESCUE_LANES", "OPT_UNGAPPED", "OPT_DEVICE_PIECE", "OPT_LONG_QLEN", "OPT_LONG_LANES", "OPT_RESCUE_PAIR", "OPT_LONG_SLIDE", "GATHER_AUTO", "GATHER_HOST", "GATHER_DEVICE", "PATH_PLAIN", "PATH_BATCHED"):
         assert getattr(B, name) == defs[name], name

@@ -198,6 +198,15 @@ def test_window_kernel_cells_and_asymmetric_gaps(wctx):
     _check(wctx, js, 100, mat, o_del=6, e_del=1, o_ins=4, e_ins=2, zdrop=60)
 
 
+def test_window_kernel_option_values(ctx):
+    for bad in (-1, 3):
+        with pytest.raises(B.BwaCudaError) as e:
+            ctx.set_option(B.OPT_LONG_SLIDE, bad)
+        assert e.value.code == B.EINVAL
+    for ok in (0, 2, 1):
+        ctx.set_option(B.OPT_LONG_SLIDE, ok)
+
+
 def test_window_kernel_auto_threshold(ctx):
     # default mode: a bucket of at least 32 jobs per SM runs in the window kernel, a smaller one
     # in the group kernel; results are the same either way
