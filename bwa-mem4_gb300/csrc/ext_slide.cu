@@ -181,8 +181,32 @@ __device__ __forceinline__ bwacuda_ext_result slide_job(uint2 *__restrict__ cell
                     for (int u = 0; u < 8; ++u) wv[u] = cw[u * TB];
 #pragma unroll
                     for (int u = 0; u < 4; ++u) qv[u] = qp[u * TB];
+                    // phase by phase over the eight pairs (the same operations per pair as
+                    // cell_pair): a warp alone on its scheduler issues in order, so independent
+                    // instructions go back to back and only F chains from pair to pair
+                    uint32_t M2[8], ti2[8], en2[8], f2[8], h2[8];
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) cell_pair(wv[u], qv[u >> 1] >> ((u & 1) * 16), u * TB, j + 2 * u);
+                    for (int u = 0; u < 8; ++u) {
+                        const uint32_t s2 = prmt(plo, phi, qv[u >> 1] >> ((u & 1) * 16));
+                        const uint32_t g2 = __viaddmin_u16x2(wv[u].x, 0u, 0x00010001u) * 0x7fffu;
+                        M2[u] = __viaddmin_s16x2(wv[u].x, s2, g2);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) ti2[u] = __viaddmax_s16x2_relu(M2[u], noe_ins2, 0u);
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const uint32_t td2 = SYM ? ti2[u] : __viaddmax_s16x2_relu(M2[u], noe_del2, 0u);
+                        en2[u] = __viaddmax_s16x2(wv[u].y, ne_del2, td2);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) f2[u] = f_pair(fv, ti2[u], fsel2, ne_ins2);
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) h2[u] = __vimax3_s16x2(M2[u], wv[u].y, f2[u]);
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) cw[u * TB] = make_uint2(prmt(u == 0 ? h1v : h2[u - 1], h2[u], 0x5432u), en2[u]);
+                    h1v = h2[7];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) rowkey = pair_rowkey(rowkey, h2[u], j + 2 * u);
                     cw += 8 * TB;
                     qp += 4 * TB;
                 }
