@@ -521,6 +521,52 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
                 const uint32_t dhi = (ph_hi ? (pm_hi ? 0u : 1u) : 2u) | (pe_hi ? 0u : 4u) | (pf_hi ? 0u : 32u);
                 return dlo | (dhi << 8);
             };
+            // two consecutive column pairs (pair words pa, pb; selectors sa, sb) with the same
+            // operations as pair_dir, ordered so both pairs' independent work comes first and
+            // only F chains from a to b; returns the four direction bytes
+            auto pair2_dir = [&](uint2 *pa, uint2 *pb, uint32_t sa, uint32_t sb) -> uint32_t {
+                const uint2 ca = *pa, cb = *pb;
+                const uint32_t M2a = __viaddmax_s16x2(ca.x, prmt(plo, phi, sa), MIN2);
+                const uint32_t M2b = __viaddmax_s16x2(cb.x, prmt(plo, phi, sb), MIN2);
+                const uint32_t tti2a = __viaddmax_s16x2(M2a, noe_ins2, MIN2);
+                const uint32_t tti2b = __viaddmax_s16x2(M2b, noe_ins2, MIN2);
+                const uint32_t ttd2a = __viaddmax_s16x2(M2a, noe_del2, MIN2);
+                const uint32_t ttd2b = __viaddmax_s16x2(M2b, noe_del2, MIN2);
+                const uint32_t E2ma = __viaddmax_s16x2(ca.y, ne_del2, MIN2);
+                const uint32_t E2mb = __viaddmax_s16x2(cb.y, ne_del2, MIN2);
+                uint32_t v = 0;
+                uint32_t H2a;
+                {
+                    bool pm_hi, pm_lo, ph_hi, ph_lo, pf_hi, pf_lo, pe_hi, pe_lo;
+                    const uint32_t ME2 = __vibmax_s16x2(M2a, ca.y, &pm_hi, &pm_lo);
+                    const uint32_t En2 = __vibmax_s16x2(ttd2a, E2ma, &pe_hi, &pe_lo);
+                    const uint32_t X = prmt(fv, tti2a, 0x5432u);
+                    const uint32_t fvm = __viaddmax_s16x2(fv, ne_ins2, MIN2);
+                    const uint32_t F2 = __viaddmax_s16x2(X, 0u, prmt(MIN2, fvm, 0x7610u));
+                    H2a = __vibmax_s16x2(ME2, F2, &ph_hi, &ph_lo);
+                    fv = __vibmax_s16x2(tti2a, __viaddmax_s16x2(F2, ne_ins2, MIN2), &pf_hi, &pf_lo);
+                    *pa = make_uint2(prmt(h1v, H2a, 0x5432u), En2);
+                    const uint32_t dlo = (ph_lo ? (pm_lo ? 0u : 1u) : 2u) | (pe_lo ? 0u : 4u) | (pf_lo ? 0u : 32u);
+                    const uint32_t dhi = (ph_hi ? (pm_hi ? 0u : 1u) : 2u) | (pe_hi ? 0u : 4u) | (pf_hi ? 0u : 32u);
+                    v = dlo | (dhi << 8);
+                }
+                {
+                    bool pm_hi, pm_lo, ph_hi, ph_lo, pf_hi, pf_lo, pe_hi, pe_lo;
+                    const uint32_t ME2 = __vibmax_s16x2(M2b, cb.y, &pm_hi, &pm_lo);
+                    const uint32_t En2 = __vibmax_s16x2(ttd2b, E2mb, &pe_hi, &pe_lo);
+                    const uint32_t X = prmt(fv, tti2b, 0x5432u);
+                    const uint32_t fvm = __viaddmax_s16x2(fv, ne_ins2, MIN2);
+                    const uint32_t F2 = __viaddmax_s16x2(X, 0u, prmt(MIN2, fvm, 0x7610u));
+                    const uint32_t H2b = __vibmax_s16x2(ME2, F2, &ph_hi, &ph_lo);
+                    fv = __vibmax_s16x2(tti2b, __viaddmax_s16x2(F2, ne_ins2, MIN2), &pf_hi, &pf_lo);
+                    *pb = make_uint2(prmt(H2a, H2b, 0x5432u), En2);
+                    h1v = H2b;
+                    const uint32_t dlo = (ph_lo ? (pm_lo ? 0u : 1u) : 2u) | (pe_lo ? 0u : 4u) | (pf_lo ? 0u : 32u);
+                    const uint32_t dhi = (ph_hi ? (pm_hi ? 0u : 1u) : 2u) | (pe_hi ? 0u : 4u) | (pf_hi ? 0u : 32u);
+                    v |= (dlo | (dhi << 8)) << 16;
+                }
+                return v;
+            };
             // the row's pairs k = 0 .. npairs-1 take slots p0 + k, wrapping once at P2 (kw pairs
             // before the wrap): straight runs of running pointers, no per-pair wrap test
             const int kw = P2 - p0 < npairs ? P2 - p0 : npairs;
@@ -557,9 +603,9 @@ global_pair_kernel(const uint8_t *__restrict__ seq, const GlobalDevJob *__restri
                 if (run >= 2) {
                     const int steps = run >> 1;
                     for (int s = 0; s < steps; ++s) {
-                        const uint32_t va = pair_dir(cp, next_sel());
-                        const uint32_t vb = pair_dir(cp + TB, next_sel());
-                        emit(va | (vb << 16));
+                        const uint32_t sa = next_sel();
+                        const uint32_t sb = next_sel();
+                        emit(pair2_dir(cp, cp + TB, sa, sb));
                         cp += 2 * TB;
                     }
                     k += 2 * steps;
